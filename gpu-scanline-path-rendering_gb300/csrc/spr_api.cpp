@@ -1,0 +1,579 @@
+// spr_api.cpp -- the C ABI of include/spr.h: handle lifetime, scene upload
+// (addVg + unifyCurveVertexOrder), per-frame orchestration of the CUDA
+// stages (rasterizeImpl), read-back, PNG output, element counts, step timing
+// and stage dumps.
+//
+// Device memory: the scene lives in per-handle buffers written once by
+// spr_set_scene; every per-frame array is a grow-only buffer of the handle
+// (the role of the reference's 256 MB bump arena, cuda_cached_allocator.h),
+// so steady-state frames allocate nothing.  The frame reads back three
+// counts to size its work (fragments, merged fragments + spans, resolve
+// pairs); everything else stays on the device.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/spr.h"
+#include "spr_internal.h"
+
+namespace spr {
+int write_png_rgba(const char *path, const uint8_t *rgba, int w, int h);
+}
+
+using namespace spr;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T *as() const {
+        return static_cast<T *>(p);
+    }
+};
+
+int ensure(DevBuf &b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return SPR_OK;
+    b.release();
+    size_t want = bytes + bytes / 4;
+    want = (want + 255) & ~(size_t)255;
+    if (cudaMalloc(&b.p, want) != cudaSuccess) {
+        cudaGetLastError();
+        b.p = nullptr;
+        return SPR_ERR_OUT_OF_MEMORY;
+    }
+    b.bytes = want;
+    return SPR_OK;
+}
+
+int cuda_status() {
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) return SPR_OK;
+    if (e == cudaErrorMemoryAllocation) return SPR_ERR_OUT_OF_MEMORY;
+    return SPR_ERR_CUDA;
+}
+
+int bits_for(uint64_t v) {  // number of bits needed to hold values 0..v
+    int b = 0;
+    while (v) {
+        ++b;
+        v >>= 1;
+    }
+    return b;
+}
+
+const char *kStepNames[] = {"transform", "intersect_count", "intersect_emit_fragment", "sort", "scan_mark",
+                            "stencil",   "resolve_bin",     "resolve"};
+constexpr int kSteps = 8;
+
+}  // namespace
+
+struct spr_handle {
+    spr_config cfg{};
+    float m[16];
+    // tables
+    DevBuf mask_table;
+    int table_samples = 0;
+    DevBuf rtables;
+    // scene
+    bool has_scene = false;
+    uint32_t P = 0, C = 0, V = 0;
+    DevBuf vertex, vpid, curves, rule, fill, affine;
+    bool has_affine = false;
+    // frame buffers
+    DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
+        wn_scan, draw, heads, flags_tmp, merged, tiles, pair_off, pkey[2], pval[2], bins, image, counters, dump_tmp;
+    uint64_t *skey_sorted = nullptr;
+    uint32_t *perm_sorted = nullptr;
+    // host staging
+    FrameCounters *h_counters = nullptr;
+    uint32_t *h_u32 = nullptr;
+    // last frame
+    spr_element_number en{};
+    int64_t nf = 0, nm = 0, ns = 0, npairs = 0;
+    bool frame_valid = false;
+    int frame_W = 0, frame_H = 0, frame_S = 8;
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[kSteps + 1] = {};
+    double step_ms[kSteps] = {};
+};
+
+namespace {
+
+int validate_config(const spr_config *c) {
+    if (c->width < 1 || c->height < 1 || c->width > 4096 || c->height > 4096) return SPR_ERR_INVALID_ARG;
+    if (c->samples != 8 && c->samples != 32) return SPR_ERR_INVALID_ARG;
+    return SPR_OK;
+}
+
+int build_tables(spr_handle *h) {
+    if (h->table_samples == h->cfg.samples) return SPR_OK;
+    const int words = h->cfg.samples / 8;
+    std::vector<uint32_t> t((size_t)65536 * words);
+    build_mask_table(h->cfg.samples, t.data());
+    int st = ensure(h->mask_table, t.size() * 4);
+    if (st) return st;
+    if (cudaMemcpy(h->mask_table.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) return cuda_status();
+    h->table_samples = h->cfg.samples;
+    return SPR_OK;
+}
+
+FrameArgs make_args(const spr_handle *h) {
+    FrameArgs a;
+    a.W = h->cfg.width;
+    a.H = h->cfg.height;
+    a.S = h->cfg.samples;
+    a.ms_output = h->cfg.ms_output;
+    a.srgb = h->cfg.srgb;
+    a.P = (int)h->P;
+    a.C = (int)h->C;
+    a.V = (int)h->V;
+    std::memcpy(a.m, h->m, sizeof(a.m));
+    a.vertex = h->vertex.as<float2>();
+    a.vertex_pid = h->vpid.as<uint32_t>();
+    a.affine = h->has_affine ? h->affine.as<float>() : nullptr;
+    a.curves = h->curves.as<CurveDesc>();
+    a.fill_rule = h->rule.as<uint8_t>();
+    a.fill_rgba = h->fill.as<uint32_t>();
+    a.mask_table = h->mask_table.as<uint32_t>();
+    a.rtables = h->rtables.as<ResolveTables>();
+    return a;
+}
+
+int validate_scene(const spr_scene_view *v) {
+    if (!v) return SPR_ERR_INVALID_ARG;
+    if ((v->n_vertices && (!v->vertex || !v->vertex_path_id)) ||
+        (v->n_curves && (!v->curve_vertex_pos || !v->curve_type || !v->curve_path_id)) ||
+        (v->n_paths && (!v->path_fill_rule || !v->path_fill_rgba)))
+        return SPR_ERR_INVALID_ARG;
+    if (v->n_vertices > (1u << 30) || v->n_curves > (1u << 30) || v->n_paths > (1u << 30))
+        return SPR_ERR_INVALID_SCENE;
+    uint32_t last = 0;
+    for (uint32_t i = 0; i < v->n_curves; ++i) {
+        const int t = v->curve_type[i];
+        if (t != SPR_CURVE_LINEAR && t != SPR_CURVE_QUADRATIC && t != SPR_CURVE_CUBIC && t != SPR_CURVE_RATIONAL)
+            return SPR_ERR_INVALID_SCENE;
+        if (t == SPR_CURVE_RATIONAL && !v->curve_arc_w) return SPR_ERR_INVALID_SCENE;
+        if ((uint64_t)v->curve_vertex_pos[i] + (uint64_t)(t & 7) > v->n_vertices) return SPR_ERR_INVALID_SCENE;
+        const uint32_t p = v->curve_path_id[i];
+        if (p >= v->n_paths || p < last) return SPR_ERR_INVALID_SCENE;
+        last = p;
+    }
+    for (uint32_t i = 0; i < v->n_vertices; ++i)
+        if (v->vertex_path_id[i] >= v->n_paths) return SPR_ERR_INVALID_SCENE;
+    return SPR_OK;
+}
+
+template <class T>
+int upload(DevBuf &b, const T *src, size_t n) {
+    int st = ensure(b, n * sizeof(T));
+    if (st) return st;
+    if (n && cudaMemcpy(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return cuda_status();
+    return SPR_OK;
+}
+
+void rec(spr_handle *h, int i, cudaStream_t s) {
+    if (h->timing) cudaEventRecord(h->ev[i], s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int spr_create(const spr_config *config, spr_handle **out) {
+    if (!config || !out) return SPR_ERR_INVALID_ARG;
+    *out = nullptr;
+    int st = validate_config(config);
+    if (st) return st;
+    if (cudaSetDevice(config->device) != cudaSuccess) return cuda_status();
+    spr_handle *h = new (std::nothrow) spr_handle();
+    if (!h) return SPR_ERR_OUT_OF_MEMORY;
+    h->cfg = *config;
+    for (int i = 0; i < 16; ++i) h->m[i] = (i % 5 == 0) ? 1.f : 0.f;
+    st = build_tables(h);
+    if (!st) {
+        ResolveTables rt;
+        build_resolve_tables(&rt);
+        st = upload(h->rtables, &rt, 1);
+    }
+    if (!st) st = ensure(h->counters, sizeof(FrameCounters));
+    if (!st && cudaMallocHost((void **)&h->h_counters, sizeof(FrameCounters)) != cudaSuccess) st = cuda_status();
+    if (!st && cudaMallocHost((void **)&h->h_u32, 64) != cudaSuccess) st = cuda_status();
+    if (st) {
+        spr_destroy(h);
+        return st;
+    }
+    *out = h;
+    return SPR_OK;
+}
+
+int spr_destroy(spr_handle *h) {
+    if (!h) return SPR_OK;
+    cudaSetDevice(h->cfg.device);
+    DevBuf *bufs[] = {&h->mask_table, &h->rtables, &h->vertex,   &h->vpid,      &h->curves,  &h->rule,
+                      &h->fill,       &h->affine,  &h->tvert,    &h->pflags,    &h->pvis,    &h->counts,
+                      &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
+                      &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
+                      &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
+                      &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
+                      &h->image,      &h->counters, &h->dump_tmp};
+    for (DevBuf *b : bufs) b->release();
+    if (h->h_counters) cudaFreeHost(h->h_counters);
+    if (h->h_u32) cudaFreeHost(h->h_u32);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
+    delete h;
+    return SPR_OK;
+}
+
+int spr_resize(spr_handle *h, int32_t width, int32_t height) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    spr_config c = h->cfg;
+    c.width = width;
+    c.height = height;
+    int st = validate_config(&c);
+    if (st) return st;
+    h->cfg = c;
+    h->frame_valid = false;
+    return SPR_OK;
+}
+
+int spr_set_samples(spr_handle *h, int32_t samples) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    if (samples != 8 && samples != 32) return SPR_ERR_INVALID_ARG;
+    cudaSetDevice(h->cfg.device);
+    h->cfg.samples = samples;
+    h->frame_valid = false;
+    return build_tables(h);
+}
+
+int spr_set_multisample_output(spr_handle *h, int32_t enable) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    h->cfg.ms_output = enable ? 1 : 0;
+    return SPR_OK;
+}
+
+int spr_enable_srgb_correction(spr_handle *h, int32_t enable) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    h->cfg.srgb = enable ? 1 : 0;
+    return SPR_OK;
+}
+
+int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    int st = validate_scene(v);
+    if (st) return st;
+    cudaSetDevice(h->cfg.device);
+    h->has_scene = false;
+    h->frame_valid = false;
+    const uint32_t P = v->n_paths, C = v->n_curves, V = v->n_vertices;
+    // unifyCurveVertexOrder (ras_base.cpp:523-569): reverse a curve unless
+    // (y_first, x_first) < (y_last, x_last) comparing float bit patterns.
+    std::vector<float> vert(v->vertex, v->vertex + 2 * (size_t)V);
+    std::vector<CurveDesc> cd(C);
+    for (uint32_t i = 0; i < C; ++i) {
+        const int type = v->curve_type[i];
+        const int vn = type & 7;
+        const uint32_t p = v->curve_vertex_pos[i];
+        uint32_t bxf, byf, bxl, byl;
+        std::memcpy(&bxf, &vert[2 * p], 4);
+        std::memcpy(&byf, &vert[2 * p + 1], 4);
+        std::memcpy(&bxl, &vert[2 * (p + vn - 1)], 4);
+        std::memcpy(&byl, &vert[2 * (p + vn - 1) + 1], 4);
+        uint32_t rev = 0;
+        if (!(byf < byl || (byf == byl && bxf < bxl))) {
+            rev = 1;
+            for (int k = 0; k < vn / 2; ++k) {
+                std::swap(vert[2 * (p + k)], vert[2 * (p + vn - k - 1)]);
+                std::swap(vert[2 * (p + k) + 1], vert[2 * (p + vn - k - 1) + 1]);
+            }
+        }
+        cd[i].vpos = p;
+        cd[i].pid = v->curve_path_id[i];
+        cd[i].w = type == SPR_CURVE_RATIONAL ? v->curve_arc_w[i] : 0.f;
+        cd[i].type = (uint32_t)type | (rev << 8);
+    }
+    if ((st = upload(h->vertex, vert.data(), vert.size()))) return st;
+    if ((st = upload(h->vpid, v->vertex_path_id, V))) return st;
+    if ((st = upload(h->curves, cd.data(), C))) return st;
+    if ((st = upload(h->rule, v->path_fill_rule, P))) return st;
+    if ((st = upload(h->fill, v->path_fill_rgba, P))) return st;
+    h->has_affine = v->path_affine != nullptr;
+    if (h->has_affine && (st = upload(h->affine, v->path_affine, 6 * (size_t)P))) return st;
+    h->P = P;
+    h->C = C;
+    h->V = V;
+    h->has_scene = true;
+    return SPR_OK;
+}
+
+int spr_set_transform(spr_handle *h, const float m[16]) {
+    if (!h || !m) return SPR_ERR_INVALID_ARG;
+    std::memcpy(h->m, m, sizeof(h->m));
+    return SPR_OK;
+}
+
+int spr_render(spr_handle *h, void *stream) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    if (!h->has_scene) return SPR_ERR_NO_SCENE;
+    cudaSetDevice(h->cfg.device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int st = build_tables(h);
+    if (st) return st;
+    h->frame_valid = false;
+    const FrameArgs a = make_args(h);
+    const int W = a.W, H = a.H, WORDS = a.S / 8;
+    if (h->timing) {
+        for (auto &e : h->ev)
+            if (!e) cudaEventCreate(&e);
+    }
+    // stage 3: transform + visibility
+    if ((st = ensure(h->tvert, sizeof(float2) * h->V)) || (st = ensure(h->pflags, 4 * (size_t)h->P)) ||
+        (st = ensure(h->pvis, h->P)) || (st = ensure(h->counts, 4 * (size_t)h->C + 4)) ||
+        (st = ensure(h->offsets, 4 * ((size_t)h->C + 1))) ||
+        (st = ensure(h->scan_tmp, 4 * (size_t)scan_tmp_words(std::max<int64_t>(h->C, 1)))) ||
+        (st = ensure(h->image, 4 * (size_t)W * H)))
+        return st;
+    rec(h, 0, s);
+    launch_transform(a, h->tvert.as<float2>(), h->pflags.as<uint32_t>(), h->pvis.as<uint8_t>(), s);
+    rec(h, 1, s);
+    // stages 4-5: monotone pieces, entry counts, exclusive scan
+    launch_curve_count(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->counts.as<uint32_t>(), s);
+    scan_exclusive_u32(h->counts.as<uint32_t>(), h->offsets.as<uint32_t>(), h->C, h->scan_tmp.as<uint32_t>(), s);
+    cudaMemcpyAsync(h->h_u32, h->offsets.as<uint32_t>() + h->C, 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+    if ((st = cuda_status())) return st;
+    const int64_t nf = h->h_u32[0];
+    if (nf > INT32_MAX) return SPR_ERR_CAPACITY_EXCEEDED;
+    h->nf = nf;
+    h->en.path = (int32_t)h->P;
+    h->en.curve = (int32_t)h->C;
+    h->en.vertex = (int32_t)h->V;
+    h->en.curve_fragment = (int32_t)nf;
+    h->en.merged_fragment = 0;
+    h->en.span = 0;
+    h->nm = h->ns = h->npairs = 0;
+    const int ntx = (W + 31) / 32, nrows = (H + 1) / 2;
+    const int64_t nbins = (int64_t)ntx * nrows;
+    if ((st = ensure(h->bins, 8 * (size_t)nbins))) return st;
+    uint32_t *bin_start = h->bins.as<uint32_t>(), *bin_end = bin_start + nbins;
+    if (nf == 0) {
+        cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
+        for (int i = 2; i <= 6; ++i) rec(h, i, s);
+        launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(), s);
+        rec(h, 7, s);
+        rec(h, 8, s);
+        h->frame_valid = true;
+        h->frame_W = W;
+        h->frame_H = H;
+        h->frame_S = a.S;
+        return cuda_status();
+    }
+    // stages 6-7: entries, fragments, boundary masks
+    if ((st = ensure(h->entries, 8 * (size_t)nf)) || (st = ensure(h->key, 4 * (size_t)nf)) ||
+        (st = ensure(h->pidw, 4 * (size_t)nf)) || (st = ensure(h->wn, (size_t)nf)) ||
+        (st = ensure(h->mask, 4 * (size_t)WORDS * nf)) || (st = ensure(h->skey[0], 8 * (size_t)nf)) ||
+        (st = ensure(h->skey[1], 8 * (size_t)nf)) || (st = ensure(h->sval[0], 4 * (size_t)nf)) ||
+        (st = ensure(h->sval[1], 4 * (size_t)nf)) || (st = ensure(h->sort_tmp, 4 * (size_t)radix_tmp_words(nf))) ||
+        (st = ensure(h->wn_scan, (size_t)nf)) || (st = ensure(h->draw, 16 * 2 * (size_t)nf)) ||
+        (st = ensure(h->heads, 4 * (size_t)nf)) || (st = ensure(h->flags_tmp, 4 * (size_t)flags_tmp_words(nf))) ||
+        (st = ensure(h->merged, 4 * (size_t)WORDS * nf)))
+        return st;
+    rec(h, 2, s);
+    launch_curve_emit(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->offsets.as<uint32_t>(), h->entries.as<int2>(),
+                      s);
+    launch_fragment(a, h->tvert.as<float2>(), h->entries.as<int2>(), nf, h->key.as<int32_t>(), h->pidw.as<uint32_t>(),
+                    h->wn.as<int8_t>(), h->mask.as<uint32_t>(), h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), s);
+    rec(h, 3, s);
+    // stage 8: stable sort by (path, cell key)
+    const int key_bits = 24 + bits_for(h->P ? h->P - 1 : 0);
+    const bool alt = radix_sort<uint64_t>(h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(),
+                                          h->skey[1].as<uint64_t>(), h->sval[1].as<uint32_t>(), nf, key_bits,
+                                          h->sort_tmp.as<uint32_t>(), s);
+    h->skey_sorted = alt ? h->skey[1].as<uint64_t>() : h->skey[0].as<uint64_t>();
+    h->perm_sorted = alt ? h->sval[1].as<uint32_t>() : h->sval[0].as<uint32_t>();
+    rec(h, 4, s);
+    // stages 9-12, 14: winding scan, marks, draw list
+    cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);
+    launch_scan_mark(a, nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
+                     h->draw.as<int4>(), h->heads.as<uint32_t>(), h->counters.as<FrameCounters>(),
+                     h->flags_tmp.as<uint32_t>(), s);
+    cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+    if ((st = cuda_status())) return st;
+    h->nm = h->h_counters->n_merged;
+    h->ns = h->h_counters->n_span;
+    h->en.merged_fragment = (int32_t)h->nm;
+    h->en.span = (int32_t)h->ns;
+    rec(h, 5, s);
+    // stage 13: merged sample masks
+    launch_stencil(a, nf, h->nm, h->skey_sorted, h->perm_sorted, h->pidw.as<uint32_t>(), h->mask.as<uint32_t>(),
+                   h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), s);
+    rec(h, 6, s);
+    // stage 15: bin draw items by (cell row, 32-column tile), resolve
+    const int64_t items = h->nm + h->ns;
+    if ((st = ensure(h->tiles, 4 * ((size_t)items + 1))) || (st = ensure(h->pair_off, 4 * ((size_t)items + 1))))
+        return st;
+    if ((st = ensure(h->scan_tmp, 4 * (size_t)scan_tmp_words(std::max<int64_t>({items, (int64_t)h->C, 1}))))) return st;
+    launch_item_tiles(a, h->draw.as<int4>(), items, h->tiles.as<uint32_t>(), s);
+    scan_exclusive_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), items, h->scan_tmp.as<uint32_t>(), s);
+    cudaMemcpyAsync(h->h_u32, h->pair_off.as<uint32_t>() + items, 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+    const int64_t npairs = h->h_u32[0];
+    h->npairs = npairs;
+    if ((st = ensure(h->pkey[0], 4 * (size_t)npairs)) || (st = ensure(h->pkey[1], 4 * (size_t)npairs)) ||
+        (st = ensure(h->pval[0], 4 * (size_t)npairs)) || (st = ensure(h->pval[1], 4 * (size_t)npairs)) ||
+        (st = ensure(h->sort_tmp, 4 * (size_t)std::max(radix_tmp_words(npairs), radix_tmp_words(nf)))))
+        return st;
+    launch_emit_pairs(a, h->draw.as<int4>(), items, h->pair_off.as<uint32_t>(), h->pkey[0].as<uint32_t>(),
+                      h->pval[0].as<uint32_t>(), s);
+    const bool palt = radix_sort<uint32_t>(h->pkey[0].as<uint32_t>(), h->pval[0].as<uint32_t>(),
+                                           h->pkey[1].as<uint32_t>(), h->pval[1].as<uint32_t>(), npairs,
+                                           std::max(bits_for((uint64_t)nbins - 1), 1), h->sort_tmp.as<uint32_t>(), s);
+    const uint32_t *pk = palt ? h->pkey[1].as<uint32_t>() : h->pkey[0].as<uint32_t>();
+    const uint32_t *pv = palt ? h->pval[1].as<uint32_t>() : h->pval[0].as<uint32_t>();
+    cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
+    launch_bin_bounds(pk, npairs, bin_start, bin_end, s);
+    rec(h, 7, s);
+    launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end, h->image.as<uint32_t>(), s);
+    rec(h, 8, s);
+    if ((st = cuda_status())) return st;
+    if (h->timing) {
+        cudaEventSynchronize(h->ev[8]);
+        for (int i = 0; i < kSteps; ++i) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]);
+            h->step_ms[i] = ms;
+        }
+    }
+    h->frame_valid = true;
+    h->frame_W = W;
+    h->frame_H = H;
+    h->frame_S = a.S;
+    return SPR_OK;
+}
+
+int spr_image_device_ptr(spr_handle *h, void **out) {
+    if (!h || !out) return SPR_ERR_INVALID_ARG;
+    if (!h->frame_valid) return SPR_ERR_NO_SCENE;
+    *out = h->image.p;
+    return SPR_OK;
+}
+
+int spr_read_image(spr_handle *h, uint8_t *host_rgba, void *stream) {
+    if (!h || !host_rgba) return SPR_ERR_INVALID_ARG;
+    if (!h->frame_valid) return SPR_ERR_NO_SCENE;
+    cudaSetDevice(h->cfg.device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t bytes = 4 * (size_t)h->frame_W * h->frame_H;
+    if (cudaMemcpyAsync(host_rgba, h->image.p, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return cuda_status();
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+    return SPR_OK;
+}
+
+int spr_save_png(spr_handle *h, const char *path) {
+    if (!h || !path) return SPR_ERR_INVALID_ARG;
+    if (!h->frame_valid) return SPR_ERR_NO_SCENE;
+    const int W = h->frame_W, Hh = h->frame_H;
+    std::vector<uint8_t> img((size_t)W * Hh * 4), flip((size_t)W * Hh * 4);
+    int st = spr_read_image(h, img.data(), nullptr);
+    if (st) return st;
+    // saveOutputToFile (ras_base.cpp:1221-1277): vertical flip, alpha = 255.
+    for (int y = 0; y < Hh; ++y) std::memcpy(&flip[(size_t)y * W * 4], &img[(size_t)(Hh - 1 - y) * W * 4], (size_t)W * 4);
+    for (size_t i = 3; i < flip.size(); i += 4) flip[i] = 255;
+    return write_png_rgba(path, flip.data(), W, Hh) ? SPR_ERR_INVALID_ARG : SPR_OK;
+}
+
+int spr_get_counts(spr_handle *h, spr_element_number *out) {
+    if (!h || !out) return SPR_ERR_INVALID_ARG;
+    *out = h->en;
+    return SPR_OK;
+}
+
+int spr_enable_step_timing(spr_handle *h, int32_t enable) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    h->timing = enable != 0;
+    return SPR_OK;
+}
+
+int spr_step_timing(spr_handle *h, double *ms, int32_t capacity, int32_t *n_out) {
+    if (!h || !n_out) return SPR_ERR_INVALID_ARG;
+    *n_out = kSteps;
+    if (ms)
+        for (int i = 0; i < kSteps && i < capacity; ++i) ms[i] = h->step_ms[i];
+    return SPR_OK;
+}
+
+const char *spr_step_name(int32_t i) { return (i >= 0 && i < kSteps) ? kStepNames[i] : nullptr; }
+
+int spr_debug_dump(spr_handle *h, int32_t stage, void *dst, size_t capacity, size_t *needed) {
+    if (!h || !needed) return SPR_ERR_INVALID_ARG;
+    if (!h->frame_valid) return SPR_ERR_NO_SCENE;
+    cudaSetDevice(h->cfg.device);
+    const int64_t nf = h->nf;
+    const int WORDS = h->frame_S / 8;
+    const void *src = nullptr;
+    size_t bytes = 0;
+    switch (stage) {
+    case SPR_STAGE_TVERTEX: src = h->tvert.p; bytes = 8 * (size_t)h->V; break;
+    case SPR_STAGE_PATH_VISIBLE: src = h->pvis.p; bytes = h->P; break;
+    case SPR_STAGE_CURVE_COUNT: src = h->counts.p; bytes = 4 * (size_t)h->C; break;
+    case SPR_STAGE_INTERSECTION: src = h->entries.p; bytes = 8 * (size_t)nf; break;
+    case SPR_STAGE_FRAG_KEY: src = h->key.p; bytes = 4 * (size_t)nf; break;
+    case SPR_STAGE_FRAG_PID: src = h->pidw.p; bytes = 4 * (size_t)nf; break;
+    case SPR_STAGE_FRAG_WN: src = h->wn.p; bytes = (size_t)nf; break;
+    case SPR_STAGE_FRAG_MASK: src = h->mask.p; bytes = 4 * (size_t)WORDS * nf; break;
+    case SPR_STAGE_SORT_PERM: src = h->perm_sorted; bytes = 4 * (size_t)nf; break;
+    case SPR_STAGE_SORT_KEY: {
+        bytes = 4 * (size_t)nf;
+        if (nf) {
+            int st = ensure(h->dump_tmp, bytes);
+            if (st) return st;
+            launch_decode_keys(h->skey_sorted, nf, (h->frame_H + 1) / 2, h->dump_tmp.as<int32_t>(), nullptr);
+            src = h->dump_tmp.p;
+        }
+        break;
+    }
+    case SPR_STAGE_WN_SCAN: src = h->wn_scan.p; bytes = (size_t)nf; break;
+    case SPR_STAGE_MERGED_MASK: src = h->merged.p; bytes = 4 * (size_t)WORDS * h->nm; break;
+    case SPR_STAGE_DRAW_LIST: src = h->draw.p; bytes = 16 * (size_t)(h->nm + h->ns); break;
+    case SPR_STAGE_IMAGE: src = h->image.p; bytes = 4 * (size_t)h->frame_W * h->frame_H; break;
+    default: return SPR_ERR_INVALID_ARG;
+    }
+    *needed = bytes;
+    if (!dst) return SPR_OK;  // size query
+    if (capacity < bytes) return SPR_ERR_INVALID_ARG;
+    if (bytes && cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) return cuda_status();
+    return SPR_OK;
+}
+
+const char *spr_status_string(int32_t status) {
+    switch (status) {
+    case SPR_OK: return "ok";
+    case SPR_ERR_INVALID_ARG: return "invalid argument";
+    case SPR_ERR_INVALID_SCENE: return "invalid scene";
+    case SPR_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case SPR_ERR_CAPACITY_EXCEEDED: return "capacity exceeded";
+    case SPR_ERR_TIMEOUT: return "bounded device wait timed out";
+    case SPR_ERR_CUDA: return "CUDA error";
+    case SPR_ERR_NO_SCENE: return "no scene / no frame";
+    case SPR_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+}  // extern "C"

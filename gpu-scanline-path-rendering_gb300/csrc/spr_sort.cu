@@ -1,0 +1,235 @@
+// spr_sort.cu -- device-wide exclusive scan and stable LSD radix sort.
+//
+// Both are reduce-then-scan designs: every kernel reads its own tile and
+// global prefixes come from a separate small scan, so no thread block ever
+// waits on another one (no spin loops anywhere).  The radix scatter ranks
+// keys stably inside a tile with warp-level __match_any_sync and per-warp
+// digit counters, so equal keys keep their input order across the whole
+// array (the segmented sort of the reference is stable).
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "spr_internal.h"
+
+namespace spr {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+constexpr int kRadixThreads = 256;
+constexpr int kRadixWarps = kRadixThreads / 32;
+constexpr int kRadixItems = 16;  // per lane
+constexpr int kRadixTile = kRadixThreads * kRadixItems;
+constexpr int kRadixWarpSpan = 32 * kRadixItems;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+// Exclusive block scan of one value per thread; returns the prefix and the
+// block total through *total.
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *smem_warp, uint32_t *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int W = THREADS / 32;
+    uint32_t inc = warp_incl_scan(v);
+    if (lane == 31) smem_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = lane < W ? smem_warp[lane] : 0u;
+        uint32_t ti = warp_incl_scan(t);
+        if (lane < W) smem_warp[lane] = ti - t;
+        if (lane == W - 1) smem_warp[W] = ti;
+    }
+    __syncthreads();
+    uint32_t r = smem_warp[warp] + inc - v;
+    *total = smem_warp[W];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_scan_reduce(const uint32_t *__restrict__ in, int64_t n, uint32_t *__restrict__ tile_sums) {
+    __shared__ uint32_t sw[kScanThreads / 32 + 1];
+    const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + k;
+        if (i < n) s += in[i];
+    }
+    uint32_t total;
+    block_excl_scan<kScanThreads>(s, sw, &total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of tile sums in place by one block; tile_sums[n] = total.
+__global__ void k_scan_tiles(uint32_t *tile_sums, int64_t n) {
+    __shared__ uint32_t sw[1024 / 32 + 1];
+    uint32_t carry = 0;
+    for (int64_t b = 0; b < n; b += 1024) {
+        int64_t i = b + threadIdx.x;
+        uint32_t v = i < n ? tile_sums[i] : 0u;
+        uint32_t total;
+        uint32_t p = block_excl_scan<1024>(v, sw, &total);
+        if (i < n) tile_sums[i] = carry + p;
+        carry += total;
+    }
+    if (threadIdx.x == 0) tile_sums[n] = carry;
+}
+
+__global__ void k_scan_down(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, int64_t n,
+                            const uint32_t *__restrict__ tile_sums, int64_t ntiles) {
+    __shared__ uint32_t sw[kScanThreads / 32 + 1];
+    const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + k;
+        v[k] = i < n ? in[i] : 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t p = block_excl_scan<kScanThreads>(s, sw, &total) + tile_sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + k;
+        if (i < n) out[i] = p;
+        p += v[k];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = tile_sums[ntiles];
+}
+
+template <class K>
+__global__ void k_radix_hist(const K *__restrict__ keys, int64_t n, int shift, uint32_t *__restrict__ counts,
+                             int64_t ntiles) {
+    __shared__ uint32_t hist[256];
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * kRadixTile;
+#pragma unroll 4
+    for (int k = 0; k < kRadixItems; ++k) {
+        int64_t i = base + (int64_t)k * kRadixThreads + threadIdx.x;
+        if (i < n) atomicAdd(&hist[(uint32_t)(keys[i] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    counts[(int64_t)threadIdx.x * ntiles + blockIdx.x] = hist[threadIdx.x];
+}
+
+template <class K>
+__global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const K *__restrict__ keys,
+                                                                  const uint32_t *__restrict__ vals, int64_t n,
+                                                                  int shift, const uint32_t *__restrict__ offsets,
+                                                                  int64_t ntiles, K *__restrict__ keys_out,
+                                                                  uint32_t *__restrict__ vals_out) {
+    __shared__ uint32_t whist[kRadixWarps][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&whist[0][0])[i] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * kRadixTile + (int64_t)warp * kRadixWarpSpan;
+    K kk[kRadixItems];
+    uint32_t vv[kRadixItems];
+    uint32_t rank[kRadixItems];
+#pragma unroll
+    for (int r = 0; r < kRadixItems; ++r) {
+        int64_t i = base + r * 32 + lane;
+        bool valid = i < n;
+        kk[r] = valid ? keys[i] : (K)0;
+        vv[r] = valid ? vals[i] : 0u;
+        uint32_t d = valid ? ((uint32_t)(kk[r] >> shift) & 0xFFu) : (256u + lane);
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t before = __popc(peers & ((1u << lane) - 1u));
+        uint32_t cur = valid ? whist[warp][d] : 0u;
+        __syncwarp();
+        if (valid && before == 0) whist[warp][d] = cur + __popc(peers);
+        __syncwarp();
+        rank[r] = cur + before;
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;  // one digit per thread
+        uint32_t acc = offsets[(int64_t)d * ntiles + blockIdx.x];
+#pragma unroll
+        for (int w = 0; w < kRadixWarps; ++w) {
+            uint32_t c = whist[w][d];
+            whist[w][d] = acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRadixItems; ++r) {
+        int64_t i = base + r * 32 + lane;
+        if (i < n) {
+            uint32_t d = (uint32_t)(kk[r] >> shift) & 0xFFu;
+            uint32_t pos = whist[warp][d] + rank[r];
+            keys_out[pos] = kk[r];
+            vals_out[pos] = vv[r];
+        }
+    }
+}
+
+}  // namespace
+
+int64_t scan_tmp_words(int64_t n) { return (n + kScanTile - 1) / kScanTile + 2; }
+
+void scan_exclusive_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp, cudaStream_t s) {
+    int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    if (ntiles == 0) {
+        cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
+        return;
+    }
+    k_scan_reduce<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tmp);
+    k_scan_tiles<<<1, 1024, 0, s>>>(tmp, ntiles);
+    k_scan_down<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, out, n, tmp, ntiles);
+}
+
+void scan_tiles_inplace(uint32_t *a, int64_t n, cudaStream_t s) { k_scan_tiles<<<1, 1024, 0, s>>>(a, n); }
+
+int64_t radix_tiles(int64_t n) { return (n + kRadixTile - 1) / kRadixTile; }
+
+int64_t radix_tmp_words(int64_t n) {
+    int64_t c = 256 * radix_tiles(n);
+    return 2 * (c + 1) + scan_tmp_words(c) + 64;
+}
+
+template <class K>
+bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_t n, int key_bits, uint32_t *tmp,
+                cudaStream_t s) {
+    if (n <= 1) return false;
+    const int64_t ntiles = radix_tiles(n);
+    const int64_t c = 256 * ntiles;
+    uint32_t *counts = tmp;
+    uint32_t *offsets = tmp + (c + 1);
+    uint32_t *scan_tmp = tmp + 2 * (c + 1);
+    bool alt = false;
+    for (int shift = 0; shift < key_bits; shift += 8) {
+        const K *ki = alt ? keys_alt : keys;
+        const uint32_t *vi = alt ? vals_alt : vals;
+        K *ko = alt ? keys : keys_alt;
+        uint32_t *vo = alt ? vals : vals_alt;
+        k_radix_hist<K><<<(unsigned)ntiles, kRadixThreads, 0, s>>>(ki, n, shift, counts, ntiles);
+        scan_exclusive_u32(counts, offsets, c, scan_tmp, s);
+        k_radix_scatter<K><<<(unsigned)ntiles, kRadixThreads, 0, s>>>(ki, vi, n, shift, offsets, ntiles, ko, vo);
+        alt = !alt;
+    }
+    return alt;
+}
+
+template bool radix_sort<uint64_t>(uint64_t *, uint32_t *, uint64_t *, uint32_t *, int64_t, int, uint32_t *,
+                                   cudaStream_t);
+template bool radix_sort<uint32_t>(uint32_t *, uint32_t *, uint32_t *, uint32_t *, int64_t, int, uint32_t *,
+                                   cudaStream_t);
+
+}  // namespace spr

@@ -1,0 +1,313 @@
+"""Python mirror of the renderer's C ABI (include/spr.h).
+
+The class :class:`VGRasterizer` mirrors the reference plugin interface
+``RasterizerBase::VGRasterizer`` (gpu-scanline/src/rasterizer/shared/
+ras_base.h:133-378): ``addVg`` -> :meth:`VGRasterizer.add_vg`,
+``setInputTransform`` -> :meth:`set_input_transform`, ``rasterize`` ->
+:meth:`rasterize`, ``elementNumber`` -> :meth:`element_number`,
+``saveOutputToFile`` -> :meth:`save_output_to_file`, ``setSamples`` /
+``setMultisampleOutput`` / ``enableSRGBCorrection`` and step timing.  Errors
+come back from the library as status codes and are raised here as
+:class:`SprError`.
+
+The binding loads the in-tree ``libspr.so`` built by ``build.py``; it never
+falls back to another implementation.  Host-only entry points (the scene
+generator, validation) work without a GPU; everything that renders needs one.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import pathlib
+
+import numpy as np
+
+PKG_DIR = pathlib.Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "libspr.so"
+
+# ---- status codes (enum spr_status) ---------------------------------------
+OK = 0
+ERR_INVALID_ARG = 1
+ERR_INVALID_SCENE = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_CAPACITY_EXCEEDED = 4
+ERR_TIMEOUT = 5
+ERR_CUDA = 6
+ERR_NO_SCENE = 7
+ERR_UNSUPPORTED = 8
+
+# ---- curve types / fill rules / stages / scene kinds -----------------------
+CURVE_LINEAR, CURVE_QUADRATIC, CURVE_CUBIC, CURVE_RATIONAL = 0x02, 0x03, 0x04, 0x13
+FILL_NONZERO, FILL_EVEN_ODD = 0, 1
+SCENE_RANDOM, SCENE_MIXED, SCENE_CUBICS = 0, 1, 2
+
+STAGES = [
+    "TVERTEX", "PATH_VISIBLE", "CURVE_COUNT", "INTERSECTION", "FRAG_KEY", "FRAG_PID", "FRAG_WN",
+    "FRAG_MASK", "SORT_PERM", "SORT_KEY", "WN_SCAN", "MERGED_MASK", "DRAW_LIST", "IMAGE",
+]
+STAGE = {n: i for i, n in enumerate(STAGES)}
+STAGE_DTYPE = {
+    "TVERTEX": np.float32, "PATH_VISIBLE": np.uint8, "CURVE_COUNT": np.int32,
+    "INTERSECTION": np.int32, "FRAG_KEY": np.int32, "FRAG_PID": np.uint32, "FRAG_WN": np.int8,
+    "FRAG_MASK": np.uint32, "SORT_PERM": np.int32, "SORT_KEY": np.int32, "WN_SCAN": np.int8,
+    "MERGED_MASK": np.uint32, "DRAW_LIST": np.int32, "IMAGE": np.uint8,
+}
+
+
+class SprError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: status {status}" if what else f"status {status}")
+
+
+class SceneView(C.Structure):
+    _fields_ = [
+        ("n_paths", C.c_uint32), ("n_curves", C.c_uint32), ("n_vertices", C.c_uint32),
+        ("vertex", C.c_void_p), ("vertex_path_id", C.c_void_p), ("curve_vertex_pos", C.c_void_p),
+        ("curve_type", C.c_void_p), ("curve_path_id", C.c_void_p), ("curve_arc_w", C.c_void_p),
+        ("path_fill_rule", C.c_void_p), ("path_fill_rgba", C.c_void_p), ("path_affine", C.c_void_p),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("samples", C.c_int32),
+                ("ms_output", C.c_int32), ("srgb", C.c_int32), ("device", C.c_int32)]
+
+
+class ElementNumber(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in
+                ("path", "curve", "vertex", "curve_fragment", "merged_fragment", "span")]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class SceneSpec(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("seed", C.c_uint64), ("width", C.c_int32),
+                ("height", C.c_int32), ("n_paths", C.c_int32), ("n_large", C.c_int32),
+                ("seg_min", C.c_int32), ("seg_max", C.c_int32), ("with_rational", C.c_int32),
+                ("with_affine", C.c_int32)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libspr.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with build.py "
+                               "(python -c 'import __graft_entry__ as g; g.build()')")
+        L = C.CDLL(str(LIB_PATH))
+        vp, i32, sz = C.c_void_p, C.c_int32, C.c_size_t
+        L.spr_create.argtypes = [C.POINTER(Config), C.POINTER(vp)]
+        L.spr_destroy.argtypes = [vp]
+        L.spr_resize.argtypes = [vp, i32, i32]
+        L.spr_set_samples.argtypes = [vp, i32]
+        L.spr_set_multisample_output.argtypes = [vp, i32]
+        L.spr_enable_srgb_correction.argtypes = [vp, i32]
+        L.spr_set_scene.argtypes = [vp, C.POINTER(SceneView)]
+        L.spr_set_transform.argtypes = [vp, C.POINTER(C.c_float)]
+        L.spr_render.argtypes = [vp, vp]
+        L.spr_image_device_ptr.argtypes = [vp, C.POINTER(vp)]
+        L.spr_read_image.argtypes = [vp, vp, vp]
+        L.spr_save_png.argtypes = [vp, C.c_char_p]
+        L.spr_get_counts.argtypes = [vp, C.POINTER(ElementNumber)]
+        L.spr_enable_step_timing.argtypes = [vp, i32]
+        L.spr_step_timing.argtypes = [vp, C.POINTER(C.c_double), i32, C.POINTER(i32)]
+        L.spr_step_name.argtypes = [i32]
+        L.spr_step_name.restype = C.c_char_p
+        L.spr_debug_dump.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
+        L.spr_status_string.argtypes = [i32]
+        L.spr_status_string.restype = C.c_char_p
+        L.spr_scene_generate.argtypes = [C.POINTER(SceneSpec), C.POINTER(vp)]
+        L.spr_scene_view_of.argtypes = [vp, C.POINTER(SceneView)]
+        L.spr_scene_free.argtypes = [vp]
+        L.spr_scene_free.restype = None
+        _lib = L
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != OK:
+        msg = lib().spr_status_string(status).decode()
+        raise SprError(status, f"{what} ({msg})" if what else msg)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class Scene:
+    """A host scene in the reference's SoA layout (numpy arrays).
+
+    Construct from arrays, or with :meth:`generate` from a seeded synthetic
+    spec.  :meth:`view` returns the C view (the arrays stay owned here).
+    """
+
+    FIELDS = ("vertex", "vertex_path_id", "curve_vertex_pos", "curve_type", "curve_path_id",
+              "curve_arc_w", "path_fill_rule", "path_fill_rgba", "path_affine")
+
+    def __init__(self, vertex, vertex_path_id, curve_vertex_pos, curve_type, curve_path_id,
+                 curve_arc_w, path_fill_rule, path_fill_rgba, path_affine=None):
+        self.vertex = np.ascontiguousarray(vertex, dtype=np.float32).reshape(-1, 2)
+        self.vertex_path_id = np.ascontiguousarray(vertex_path_id, dtype=np.uint32)
+        self.curve_vertex_pos = np.ascontiguousarray(curve_vertex_pos, dtype=np.uint32)
+        self.curve_type = np.ascontiguousarray(curve_type, dtype=np.uint8)
+        self.curve_path_id = np.ascontiguousarray(curve_path_id, dtype=np.uint32)
+        self.curve_arc_w = np.ascontiguousarray(curve_arc_w, dtype=np.float32)
+        self.path_fill_rule = np.ascontiguousarray(path_fill_rule, dtype=np.uint8)
+        self.path_fill_rgba = np.ascontiguousarray(path_fill_rgba, dtype=np.uint32)
+        self.path_affine = (None if path_affine is None else
+                            np.ascontiguousarray(path_affine, dtype=np.float32).reshape(-1, 6))
+
+    @property
+    def n_paths(self):
+        return len(self.path_fill_rule)
+
+    @property
+    def n_curves(self):
+        return len(self.curve_type)
+
+    @property
+    def n_vertices(self):
+        return len(self.vertex)
+
+    def view(self) -> SceneView:
+        return SceneView(self.n_paths, self.n_curves, self.n_vertices, _ptr(self.vertex),
+                         _ptr(self.vertex_path_id), _ptr(self.curve_vertex_pos),
+                         _ptr(self.curve_type), _ptr(self.curve_path_id), _ptr(self.curve_arc_w),
+                         _ptr(self.path_fill_rule), _ptr(self.path_fill_rgba),
+                         _ptr(self.path_affine))
+
+    def copy(self) -> "Scene":
+        return Scene(*[None if getattr(self, f) is None else getattr(self, f).copy()
+                       for f in self.FIELDS])
+
+    @classmethod
+    def generate(cls, kind=SCENE_RANDOM, seed=1, width=512, height=512, n_paths=64, n_large=0,
+                 seg_min=8, seg_max=32, with_rational=False, with_affine=False) -> "Scene":
+        spec = SceneSpec(kind, seed, width, height, n_paths, n_large, seg_min, seg_max,
+                         int(with_rational), int(with_affine))
+        h = C.c_void_p()
+        check(lib().spr_scene_generate(C.byref(spec), C.byref(h)), "spr_scene_generate")
+        try:
+            v = SceneView()
+            check(lib().spr_scene_view_of(h, C.byref(v)), "spr_scene_view_of")
+
+            def arr(p, n, dt):
+                if not p or n == 0:
+                    return np.zeros(n, dtype=dt)
+                return np.ctypeslib.as_array(C.cast(p, C.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                             (n,)).copy()
+            s = cls(arr(v.vertex, 2 * v.n_vertices, np.float32),
+                    arr(v.vertex_path_id, v.n_vertices, np.uint32),
+                    arr(v.curve_vertex_pos, v.n_curves, np.uint32),
+                    arr(v.curve_type, v.n_curves, np.uint8),
+                    arr(v.curve_path_id, v.n_curves, np.uint32),
+                    arr(v.curve_arc_w, v.n_curves, np.float32),
+                    arr(v.path_fill_rule, v.n_paths, np.uint8),
+                    arr(v.path_fill_rgba, v.n_paths, np.uint32),
+                    None if not v.path_affine else arr(v.path_affine, 6 * v.n_paths, np.float32))
+        finally:
+            lib().spr_scene_free(h)
+        return s
+
+
+class VGRasterizer:
+    """Mirror of RasterizerBase::VGRasterizer over the C ABI."""
+
+    def __init__(self, width=512, height=512, samples=8, ms_output=True, srgb=True, device=0):
+        cfg = Config(width, height, samples, int(ms_output), int(srgb), device)
+        h = C.c_void_p()
+        check(lib().spr_create(C.byref(cfg), C.byref(h)), "spr_create")
+        self._h = h
+        self.width, self.height, self.samples = width, height, samples
+        self._scene = None
+
+    def close(self):
+        if self._h:
+            lib().spr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- configuration -------------------------------------------------------
+    def resize_output_buffer(self, width, height):
+        check(lib().spr_resize(self._h, width, height), "spr_resize")
+        self.width, self.height = width, height
+
+    def set_samples(self, s):
+        check(lib().spr_set_samples(self._h, s), "spr_set_samples")
+        self.samples = s
+
+    def set_multisample_output(self, f):
+        check(lib().spr_set_multisample_output(self._h, int(f)), "spr_set_multisample_output")
+
+    def enable_srgb_correction(self, f=True):
+        check(lib().spr_enable_srgb_correction(self._h, int(f)), "spr_enable_srgb_correction")
+
+    # -- scene and frame -----------------------------------------------------
+    def add_vg(self, scene: Scene):
+        v = scene.view()
+        check(lib().spr_set_scene(self._h, C.byref(v)), "spr_set_scene")
+        self._scene = scene
+
+    def set_input_transform(self, m):
+        m = np.ascontiguousarray(m, dtype=np.float32).reshape(16)
+        check(lib().spr_set_transform(self._h, m.ctypes.data_as(C.POINTER(C.c_float))),
+              "spr_set_transform")
+
+    def rasterize(self, stream=None):
+        check(lib().spr_render(self._h, stream), "spr_render")
+
+    def image_device_ptr(self) -> int:
+        p = C.c_void_p()
+        check(lib().spr_image_device_ptr(self._h, C.byref(p)), "spr_image_device_ptr")
+        return p.value or 0
+
+    def read_image(self, out=None, stream=None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.height, self.width, 4), dtype=np.uint8)
+        check(lib().spr_read_image(self._h, out.ctypes.data, stream), "spr_read_image")
+        return out
+
+    def save_output_to_file(self, path):
+        check(lib().spr_save_png(self._h, os.fsencode(str(path))), "spr_save_png")
+
+    def element_number(self) -> dict:
+        e = ElementNumber()
+        check(lib().spr_get_counts(self._h, C.byref(e)), "spr_get_counts")
+        return e.as_dict()
+
+    def enable_step_timing(self, f=True):
+        check(lib().spr_enable_step_timing(self._h, int(f)), "spr_enable_step_timing")
+
+    def step_timing(self) -> dict:
+        buf = (C.c_double * 64)()
+        n = C.c_int32()
+        check(lib().spr_step_timing(self._h, buf, 64, C.byref(n)), "spr_step_timing")
+        return {lib().spr_step_name(i).decode(): buf[i] for i in range(n.value)}
+
+    def dump(self, stage) -> np.ndarray:
+        sid = STAGE[stage] if isinstance(stage, str) else int(stage)
+        name = STAGES[sid]
+        need = C.c_size_t()
+        check(lib().spr_debug_dump(self._h, sid, None, 0, C.byref(need)), f"spr_debug_dump({name})")
+        dt = np.dtype(STAGE_DTYPE[name])
+        out = np.empty(need.value // dt.itemsize, dtype=dt)
+        if need.value:
+            check(lib().spr_debug_dump(self._h, sid, out.ctypes.data, need.value, C.byref(need)),
+                  f"spr_debug_dump({name})")
+        return out

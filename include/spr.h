@@ -1,0 +1,255 @@
+/*
+ * spr.h -- C ABI of the GB300-native scanline path renderer.
+ *
+ * This header is the drop-in boundary for the reference's rasterizer plugin
+ * interface, the abstract C++ class RasterizerBase::VGRasterizer
+ * (gpu-scanline/src/rasterizer/shared/ras_base.h:133-378) created through
+ * createRasterizer(PM_Cut_Mask_Comb_Scanline)
+ * (gpu-scanline/src/rasterizer/shared/ras_factory.h:18-34).  Every entry point
+ * below names the reference member it replaces.  The signatures use plain C
+ * types only (no CUDA, no torch): a CUDA stream is passed as `void *`
+ * (a cudaStream_t, NULL = the legacy default stream).
+ *
+ * Differences from the reference boundary, by design:
+ *   - errors are returned as status codes instead of C++ exceptions;
+ *   - saving the output never calls exit() (ras_base.cpp:1276);
+ *   - there is no OpenGL: the output is an RGBA8 image in device memory that
+ *     the caller can read back or write to a PNG file.
+ */
+#ifndef SPR_H_
+#define SPR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum spr_status {
+    SPR_OK = 0,
+    SPR_ERR_INVALID_ARG = 1,       /* bad pointer, size or option            */
+    SPR_ERR_INVALID_SCENE = 2,     /* bad curve type, index or path order    */
+    SPR_ERR_OUT_OF_MEMORY = 3,     /* device allocation failed               */
+    SPR_ERR_CAPACITY_EXCEEDED = 4, /* a fixed-capacity buffer overflowed     */
+    SPR_ERR_TIMEOUT = 5,           /* a bounded device wait gave up          */
+    SPR_ERR_CUDA = 6,              /* any other CUDA runtime error           */
+    SPR_ERR_NO_SCENE = 7,          /* render called before spr_set_scene     */
+    SPR_ERR_UNSUPPORTED = 8        /* option not supported by this build     */
+};
+
+/* ---- scene model ------------------------------------------------------- */
+/* Curve type codes; the low 3 bits are the control-point count
+ * (gpu-scanline/src/bezier_curve_type.h:6-18). */
+enum spr_curve_type {
+    SPR_CURVE_LINEAR = 0x02,
+    SPR_CURVE_QUADRATIC = 0x03,
+    SPR_CURVE_CUBIC = 0x04,
+    SPR_CURVE_RATIONAL = 0x13
+};
+
+/* Fill rules (gpu-scanline/src/vg_container.h:43-46). */
+enum spr_fill_rule { SPR_FILL_NONZERO = 0, SPR_FILL_EVEN_ODD = 1 };
+
+/*
+ * Flat structure-of-arrays scene, the same layout as the reference's
+ * VGInputCurveDataPack / VGInputPathDataPack (ras_base.h:34-112) filled by
+ * addVg (ras_base.cpp:70-382).  All pointers are HOST pointers.
+ *
+ *   vertex            float2[n_vertices] (x, y interleaved).  Vertices are not
+ *                     shared: curve i owns (curve_type[i] & 7) consecutive
+ *                     vertices starting at curve_vertex_pos[i].
+ *   vertex_path_id    uint32[n_vertices], path of each vertex.
+ *   curve_vertex_pos  uint32[n_curves].
+ *   curve_type        uint8[n_curves], one of spr_curve_type.
+ *   curve_path_id     uint32[n_curves], non-decreasing (curves are grouped
+ *                     by path, in painter's order).
+ *   curve_arc_w       float[n_curves], middle weight of rational curves
+ *                     (ignored for other types); may be NULL if the scene has
+ *                     no rational curve.
+ *   path_fill_rule    uint8[n_paths], spr_fill_rule.
+ *   path_fill_rgba    uint32[n_paths], solid colour r | g<<8 | b<<16 | a<<24.
+ *                     A colour with a = 0 is stored as 0 (ras_base.cpp:148-152).
+ *   path_affine       optional float[6 * n_paths]: per-path affine
+ *                     (a, b, c, d, e, f): x' = a*x + c*y + e, y' = b*x + d*y + f,
+ *                     applied before the global transform.  NULL = identity.
+ *                     (The reference bakes path transforms into vertices in
+ *                     its loader, rvg.cpp:400-431; here it is a device-side
+ *                     stage so that it can be differentiated.)
+ */
+typedef struct spr_scene_view {
+    uint32_t n_paths;
+    uint32_t n_curves;
+    uint32_t n_vertices;
+    const float *vertex;
+    const uint32_t *vertex_path_id;
+    const uint32_t *curve_vertex_pos;
+    const uint8_t *curve_type;
+    const uint32_t *curve_path_id;
+    const float *curve_arc_w;
+    const uint8_t *path_fill_rule;
+    const uint32_t *path_fill_rgba;
+    const float *path_affine;
+} spr_scene_view;
+
+/* ---- renderer configuration ------------------------------------------- */
+/*
+ * width, height : output buffer size, 1..4096 each (resizeOutputBuffer,
+ *                 ras_base.cpp:396-402; the reference caps its buffers at
+ *                 4096, ras_define.h:17-20).
+ * samples       : samples per pixel, 8 or 32 (setSamples).
+ * ms_output     : 1 = per-sample coverage resolve (the reference's
+ *                 multisample GL output, setMultisampleOutput); 0 = one colour
+ *                 per pixel with alpha scaled by coverage.
+ * srgb          : 1 = sRGB-correct blending (enableSRGBCorrection).
+ * device        : CUDA device ordinal.
+ */
+typedef struct spr_config {
+    int32_t width;
+    int32_t height;
+    int32_t samples;
+    int32_t ms_output;
+    int32_t srgb;
+    int32_t device;
+} spr_config;
+
+/* Element counts of the last frame (ElementNumber, ras_base.h:124-131). */
+typedef struct spr_element_number {
+    int32_t path;
+    int32_t curve;
+    int32_t vertex;
+    int32_t curve_fragment;
+    int32_t merged_fragment;
+    int32_t span;
+} spr_element_number;
+
+typedef struct spr_handle spr_handle;
+
+/* ---- lifetime ---------------------------------------------------------- */
+/* createRasterizer + VGRasterizer::init (ras_factory.h:18-34,
+ * ras_cut_mask_comb_scanline.cpp:31-45): builds the sample pattern and the
+ * half-plane mask table and uploads them to the device. */
+int spr_create(const spr_config *config, spr_handle **out);
+/* VGRasterizer::uninit / destructor. Accepts NULL. */
+int spr_destroy(spr_handle *h);
+
+/* resizeOutputBuffer (ras_base.cpp:396-402). */
+int spr_resize(spr_handle *h, int32_t width, int32_t height);
+/* setSamples (ras_base.h:185); 8 or 32.  Rebuilds the device tables. */
+int spr_set_samples(spr_handle *h, int32_t samples);
+/* setMultisampleOutput (ras_base.h:186). */
+int spr_set_multisample_output(spr_handle *h, int32_t enable);
+/* enableSRGBCorrection (ras_base.h:179). */
+int spr_enable_srgb_correction(spr_handle *h, int32_t enable);
+
+/* ---- scene -------------------------------------------------------------- */
+/* addVg + unifyCurveVertexOrder (ras_base.cpp:70-382, 523-569;
+ * ras_cut_mask_comb_scanline.cpp:224-229).  Validates the scene, reverses
+ * curves so that each runs "upward" by float bit pattern, and copies it to
+ * the device.  The host arrays are not referenced after the call returns. */
+int spr_set_scene(spr_handle *h, const spr_scene_view *scene);
+
+/* setInputTransform (ras_base.cpp:576-583): a row-major 4x4 matrix applied to
+ * (x, y, 0, 1) followed by the reference's perspective fold (cu:36-105). */
+int spr_set_transform(spr_handle *h, const float m[16]);
+
+/* ---- frame -------------------------------------------------------------- */
+/* rasterize / rasterizeImpl (ras_base.cpp:1131-1195, cu:879-1453): runs the
+ * whole pipeline on `stream` and leaves an RGBA8 image (row y = scene
+ * y in [y, y+1), row-major, 4*width bytes per row) in device memory.  Returns
+ * after the work is enqueued; the element counts are read back once per frame
+ * to size the work buffers. */
+int spr_render(spr_handle *h, void *stream);
+
+/* Device pointer of the image written by the last spr_render. */
+int spr_image_device_ptr(spr_handle *h, void **out);
+
+/* Copies the last image to host memory (4*width*height bytes) and
+ * synchronizes the stream. */
+int spr_read_image(spr_handle *h, uint8_t *host_rgba, void *stream);
+
+/* saveOutputToFile (ras_base.cpp:1221-1277) without the exit(0): writes the
+ * last image as a PNG, flipped vertically and with alpha forced to 255 like
+ * the reference. */
+int spr_save_png(spr_handle *h, const char *path);
+
+/* elementNumber (ras_base.h:203). */
+int spr_get_counts(spr_handle *h, spr_element_number *out);
+
+/* enableStepTiming / stepTiming (ras_base.h:182-183, ras_base.cpp:1205-1218):
+ * when enabled, spr_render records CUDA events between its stages and
+ * spr_step_timing returns the per-stage milliseconds of the last frame. */
+int spr_enable_step_timing(spr_handle *h, int32_t enable);
+int spr_step_timing(spr_handle *h, double *ms, int32_t capacity, int32_t *n_out);
+/* Name of step i of spr_step_timing (static string, NULL if out of range). */
+const char *spr_step_name(int32_t i);
+
+/* ---- stage dumps (parity testing) -------------------------------------- */
+enum spr_stage {
+    SPR_STAGE_TVERTEX = 0,       /* float2[n_vertices] transformed vertices          */
+    SPR_STAGE_PATH_VISIBLE = 1,  /* uint8[n_paths], 1 = path passes PATH_VISIBLE     */
+    SPR_STAGE_CURVE_COUNT = 2,   /* int32[n_curves] intersection entries per curve   */
+    SPR_STAGE_INTERSECTION = 3,  /* int2[n_fragments] (curve id, t bits | flags)     */
+    SPR_STAGE_FRAG_KEY = 4,      /* int32[n_fragments] cell key yx, raw order        */
+    SPR_STAGE_FRAG_PID = 5,      /* uint32[n_fragments] path id | winding change<<30 */
+    SPR_STAGE_FRAG_WN = 6,       /* int8[n_fragments] scanline winding, raw order    */
+    SPR_STAGE_FRAG_MASK = 7,     /* uint32[n_fragments * samples/8] boundary masks   */
+    SPR_STAGE_SORT_PERM = 8,     /* int32[n_fragments] sorted position -> raw index  */
+    SPR_STAGE_SORT_KEY = 9,      /* int32[n_fragments] sorted keys                   */
+    SPR_STAGE_WN_SCAN = 10,      /* int8[n_fragments] exclusive winding scan, sorted */
+    SPR_STAGE_MERGED_MASK = 11,  /* uint32[merged * samples/8] final sample masks    */
+    SPR_STAGE_DRAW_LIST = 12,    /* int4[merged + span] draw items                   */
+    SPR_STAGE_IMAGE = 13,        /* uint8[4 * width * height]                        */
+    SPR_STAGE_COUNT_ = 14
+};
+
+/* Copies stage `stage` of the last frame to host memory.  *needed receives
+ * the size in bytes; nothing is copied if capacity is smaller. */
+int spr_debug_dump(spr_handle *h, int32_t stage, void *host_dst, size_t capacity,
+                   size_t *needed);
+
+/* Human-readable text for a status code (static string). */
+const char *spr_status_string(int32_t status);
+
+/* ---- synthetic scenes ---------------------------------------------------- */
+/*
+ * Seeded synthetic scene generator standing in for the reference's MPVG .rvg
+ * inputs, which are not available.  kind:
+ *   SPR_SCENE_RANDOM  : n_paths closed paths of seg_min..seg_max segments,
+ *                       40% line / 30% quadratic / 30% cubic, control points
+ *                       uniform in the viewport, RGB U[0,1], alpha U[0.5,1],
+ *                       fill rule 50/50 (the small plain-path scene).
+ *   SPR_SCENE_MIXED   : glyph-like small paths plus large closed bands
+ *                       spanning the viewport (the large plain-path scene);
+ *                       n_paths = glyphs, n_large = large paths.
+ *   SPR_SCENE_CUBICS  : n_paths closed paths of seg_min..seg_max cubic
+ *                       segments (the differentiable-render scene).
+ */
+enum spr_scene_kind { SPR_SCENE_RANDOM = 0, SPR_SCENE_MIXED = 1, SPR_SCENE_CUBICS = 2 };
+
+typedef struct spr_scene_spec {
+    int32_t kind;
+    uint64_t seed;
+    int32_t width;
+    int32_t height;
+    int32_t n_paths;
+    int32_t n_large;
+    int32_t seg_min;
+    int32_t seg_max;
+    int32_t with_rational; /* 1 = replace 10% of quadratics with rational quadratics */
+    int32_t with_affine;   /* 1 = emit per-path affine transforms (glyphs)          */
+} spr_scene_spec;
+
+typedef struct spr_scene spr_scene;
+
+int spr_scene_generate(const spr_scene_spec *spec, spr_scene **out);
+/* The view stays valid until spr_scene_free. */
+int spr_scene_view_of(const spr_scene *s, spr_scene_view *view);
+void spr_scene_free(spr_scene *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPR_H_ */

@@ -1,0 +1,62 @@
+/*
+ * spr_oracle.h -- CPU restatement of the reference's comb-scanline fill
+ * pipeline.  TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and
+ * the cpu_baseline / reference legs of bench.py use it as the checker.  The
+ * product library (libspr) never links or calls it.
+ */
+#ifndef SPR_ORACLE_H_
+#define SPR_ORACLE_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../include/spr.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_config {
+    int32_t width;
+    int32_t height;
+    int32_t samples;   /* 8 or 32 */
+    int32_t ms_output; /* 1 = per-sample resolve */
+    int32_t srgb;      /* 1 = sRGB blending */
+    int32_t threads;   /* host threads; <= 0 = all hardware threads */
+    int32_t has_transform;
+    float transform[16]; /* row-major 4x4, used when has_transform */
+    int32_t stop_after;  /* run stages up to and including this spr_stage id (-1 = all) */
+} orc_config;
+
+typedef struct orc_result orc_result;
+
+/* Runs the pipeline on a host scene.  Returns SPR_OK or an spr_status. */
+int orc_run(const spr_scene_view *scene, const orc_config *cfg, orc_result **out);
+/* Pointer/size of stage `stage` (spr_stage ids); valid until orc_free. */
+int orc_get(const orc_result *r, int32_t stage, const void **ptr, size_t *bytes);
+int orc_counts(const orc_result *r, spr_element_number *out);
+/* Wall-clock milliseconds spent in each spr_stage of the last run. */
+int orc_stage_ms(const orc_result *r, double *ms, int32_t capacity);
+void orc_free(orc_result *r);
+
+/* Tables shared by the stages, exposed for table-level tests:
+ *   sample positions in the 2x2-pixel cell, float2[4*samples]
+ *   (index k*samples + i = sample i of pixel k, k = px.x*2 + px.y);
+ *   the 256x256 half-plane mask table, uint32[65536 * samples/8];
+ *   sRGB decode LUT float[256], encode thresholds float[255],
+ *   encode bin base uint8[4096]. */
+int orc_sample_positions(int32_t samples, float *out);
+int orc_mask_table(int32_t samples, uint32_t *out);
+int orc_srgb_tables(float *decode256, float *thresholds255, uint8_t *bins4096);
+
+/* Single-call helpers of the mask math for property tests. */
+int orc_fetch_pixel_table(int32_t samples, float p0x, float p0y, float p1x, float p1y,
+                          uint32_t *out_words);
+int orc_vertical_mask(int32_t samples, float y, uint32_t *out_words);
+int orc_vertical_mask2(int32_t samples, float y0, float y1, uint32_t *out_words);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

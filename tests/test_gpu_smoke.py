@@ -1,0 +1,14 @@
+"""End-to-end parity of the CUDA path against the CPU oracle on small scenes."""
+import numpy as np
+import pytest
+
+import oracle
+import spr
+
+pytestmark = pytest.mark.gpu
+
+
+def test_smoke():
+    import __graft_entry__
+
+    __graft_entry__.smoke()
