@@ -1,0 +1,389 @@
+#!/usr/bin/env python3
+"""Benchmark of the plain forward scanline fill path.
+
+Workload: the large plain-path scene -- 2048x2048 RGBA8, 32 samples per
+pixel, multisample sRGB resolve, 15,000 glyph-like paths (10-40 quadratic /
+cubic segments, 8-64 px box, per-path affine scale 0.5-4 and rotation) and
+5,000 large paths (50-500 mixed segments spanning up to the viewport),
+painter's-order alpha blending, from one seed (synthetic: the reference's
+MPVG documents are not available).  One step = one frame through the C ABI
+(spr_render) with the scene resident on the device.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU oracle -- the C++ restatement of the
+reference pipeline (its own GPU code needs OpenGL, unavailable on this machine)
+-- on all host threads, each step a 2048x512 band of the same scene.
+Multi-GPU runs are independent replicas (the path has no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+for p in (ROOT / "gpu-scanline-path-rendering_gb300", ROOT / "oracle", ROOT):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+METRIC = "Mpix/s & ms/frame vs CPU oracle; batched scenes/s and fwd+bwd ms vs plain GPU path"
+UNIT = "Mpix/s"
+WORKLOAD = dict(kind=1, seed=20261203, width=2048, height=2048, n_paths=15000, n_large=5000,
+                seg_min=10, seg_max=40, with_rational=False, with_affine=True)
+SAMPLES, MS_OUTPUT, SRGB = 32, True, True
+BAND = (896, 256)  # CPU sample: rows 896..1151
+L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
+
+
+def workload_config(extra=None):
+    c = {"workload": "plain forward, large scene: 2048x2048 RGBA8, 32 spp ms sRGB, "
+                     "15000 glyph-like + 5000 large paths",
+         "width": WORKLOAD["width"], "height": WORKLOAD["height"], "samples": SAMPLES,
+         "ms_output": MS_OUTPUT, "srgb": SRGB, "glyph_paths": WORKLOAD["n_paths"],
+         "large_paths": WORKLOAD["n_large"], "seed": WORKLOAD["seed"],
+         "l2": "flushed (512 MB write) before every timed step; per-frame buffers exceed L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def make_scene():
+    import spr
+
+    w = WORKLOAD
+    return spr.Scene.generate(w["kind"], seed=w["seed"], width=w["width"], height=w["height"],
+                              n_paths=w["n_paths"], n_large=w["n_large"], seg_min=w["seg_min"],
+                              seg_max=w["seg_max"], with_rational=w["with_rational"],
+                              with_affine=w["with_affine"])
+
+
+def band_transform(y0):
+    import numpy as np
+
+    m = np.eye(4, dtype=np.float32)
+    m[1, 3] = -float(y0)
+    return m
+
+
+# ---------------------------------------------------------------- clocks --
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (every 200 ms)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------- byte accounting --
+def step_bytes(counts, npairs, V, C, P, W, H, S, affine):
+    """Algorithmic bytes of each timed step (one read of every input, one
+    write of every output, per frame)."""
+    nf, nm, ns = counts["curve_fragment"], counts["merged_fragment"], counts["span"]
+    mb = S // 2  # mask bytes per 2x2 cell
+    nbins = ((W + 31) // 32) * ((H + 1) // 2)
+    return {
+        "transform": V * 20 + P * 5 + (24 * P if affine else 0),
+        "intersect_count": C * 16 + V * 8 + P + C * 12,
+        "intersect_emit_fragment": C * 16 + V * 8 + nf * 16 + nf * (4 + 4 + 1 + mb + 8 + 4),
+        "sort": nf * 12 * 2,
+        "scan_mark": nf * 15 + (nm + ns) * 16 + nm * 4,
+        "stencil": nm * 13 + nf * (16 + mb) + nm * mb,
+        "resolve_bin": (nm + ns) * 24 + npairs * 32,
+        "resolve": npairs * 20 + nm * mb + nbins * 8 + W * H * 4,
+    }
+
+
+def frame_alg_bytes(counts, V, C, P, W, H, S):
+    """Frame-level algorithmic bytes B_alg of the plain path."""
+    nf, nm, ns = counts["curve_fragment"], counts["merged_fragment"], counts["span"]
+    return (8 * V + 14 * C + 5 * P + nf * (2 * 8 + 2 * (9 + S // 2) + 2 * 8) + nm * (2 * (S // 2))
+            + (nm + ns) * 2 * 16 + 4 * W * H)
+
+
+def read_traffic(kernel):
+    """Per-unit DRAM traffic of `kernel` from the committed ncu summary
+    (profiles/roofline.md, rows `| kernel | dram bytes per unit | unit |`)."""
+    f = ROOT / "profiles" / "roofline.md"
+    if not f.exists():
+        return None, None
+    for line in f.read_text().splitlines():
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) >= 3 and cells[0] == kernel:
+            try:
+                return float(cells[1]), cells[2]
+            except ValueError:
+                return None, None
+    return None, None
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------- CPU arm --
+def cpu_sample(scene, steps=1, warmup=0, threads=0):
+    """Oracle on the band sample; returns (Mpix/s, mean ms, cores)."""
+    import oracle
+
+    cores = threads or os.cpu_count()
+    y0, bh = BAND
+    W = WORKLOAD["width"]
+    tf = band_transform(y0)
+    for _ in range(warmup):
+        oracle.time_run(scene, W, bh, SAMPLES, MS_OUTPUT, SRGB, threads=cores, transform=tf)
+    ms = []
+    for _ in range(steps):
+        t, _ = oracle.time_run(scene, W, bh, SAMPLES, MS_OUTPUT, SRGB, threads=cores, transform=tf)
+        ms.append(t)
+    mean = sum(ms) / len(ms)
+    return W * bh / (mean / 1e3) / 1e6, mean, cores
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    scene = make_scene()
+    value, mean_ms, cores = cpu_sample(scene, steps=args.steps, warmup=args.warmup)
+    y0, bh = BAND
+    sample = (f"rows {y0}..{y0 + bh - 1} (a {WORKLOAD['width']}x{bh} band) of the 2048x2048 scene "
+              f"per step, all stages, {cores} threads")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": workload_config({"sample": sample}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm --
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import spr
+
+    if not spr.LIB_PATH.exists():
+        import __graft_entry__
+
+        __graft_entry__.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    scene = make_scene()
+    r = spr.VGRasterizer(W, H, samples=SAMPLES, ms_output=MS_OUTPUT, srgb=SRGB, device=local_rank)
+    r.add_vg(scene)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    for _ in range(args.warmup):
+        r.rasterize(sp)
+    torch.cuda.synchronize(dev)
+    counts = r.element_number()
+    stats = r.frame_stats()
+    launches = stats["kernel_launches"]
+
+    # ---- timed region: device-resident scene, one frame per step
+    r.enable_step_timing(True)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    frame_ms, steps = [], {}
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.rasterize(sp)
+        e1.record(stream)
+        e1.synchronize()
+        frame_ms.append(e0.elapsed_time(e1))
+        for k, v in r.step_timing().items():
+            steps.setdefault(k, []).append(v)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    clk = clocks.stop()
+    r.enable_step_timing(False)
+    ms = sum(frame_ms) / len(frame_ms)
+    ms_max = allreduce_max(ms, world)
+    value = world * W * H / (ms_max / 1e3) / 1e6
+
+    # ---- end to end through the C ABI with host buffers: scene H2D (pinned),
+    #      render, image D2H (pinned), every step
+    pinned = [torch.from_numpy(getattr(scene, f)).pin_memory() if getattr(scene, f) is not None else None
+              for f in spr.Scene.FIELDS]
+    host_scene = spr.Scene(*[p.numpy() if p is not None else None for p in pinned])
+    img = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
+    bi = sum(getattr(host_scene, f).nbytes for f in spr.Scene.FIELDS if getattr(host_scene, f) is not None)
+    bo = img.numel()
+    for _ in range(1):
+        r.add_vg(host_scene)
+        r.rasterize(sp)
+        r.read_image(img.numpy(), sp)
+    e2e_ms = []
+    barrier(world)
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r.add_vg(host_scene)
+        r.rasterize(sp)
+        r.read_image(img.numpy(), sp)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e = sum(e2e_ms) / len(e2e_ms)
+    e2e_max = allreduce_max(e2e, world)
+    e2e_value = world * W * H / (e2e_max / 1e3) / 1e6
+
+    if rank != 0:
+        return
+    # ---- roofline of the dominant step
+    step_mean = {k: sum(v) / len(v) for k, v in steps.items()}
+    dom = max(step_mean, key=step_mean.get)
+    npairs = stats["resolve_pairs"]
+    sb = step_bytes(counts, npairs, scene.n_vertices, scene.n_curves, scene.n_paths, W, H, SAMPLES,
+                    scene.path_affine is not None)
+    peak, peak_kind = peaks()
+    achieved = sb[dom] / (step_mean[dom] / 1e3) / 1e9
+    per_unit, unit_name = read_traffic(dom)
+    units = {"fragment": counts["curve_fragment"], "pixel": W * H}.get(unit_name or "", None)
+    traffic = per_unit * units if (per_unit is not None and units) else None
+    frame_bytes = frame_alg_bytes(counts, scene.n_vertices, scene.n_curves, scene.n_paths, W, H, SAMPLES)
+
+    cpu_value, cpu_ms, cores = cpu_sample(scene, steps=1, warmup=0)
+    y0, bh = BAND
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config({"counts": counts, "resolve_pairs": npairs,
+                                   "host_syncs_per_frame": stats["host_syncs"],
+                                   "device_bytes": stats["device_bytes"]}),
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_max, "h2d_bytes_per_step": bi,
+                "d2h_bytes_per_step": bo},
+        "gpu_launches": launches * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "alg_bytes": sb[dom], "ms": step_mean[dom]},
+        "frame_roofline": {"alg_bytes": frame_bytes, "achieved": frame_bytes / (ms_max / 1e3) / 1e9,
+                           "frac": frame_bytes / (ms_max / 1e3) / 1e9 / peak, "unit": "GB/s"},
+        "step_ms": step_mean,
+        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"rows {y0}..{y0 + bh - 1} (a {W}x{bh} band) of the same scene, "
+                                   f"one frame, all stages, {cores} threads",
+                         "ms": cpu_ms},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------- distributed --
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group(backend="nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

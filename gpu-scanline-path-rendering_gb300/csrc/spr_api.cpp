@@ -105,6 +105,7 @@ struct spr_handle {
     spr_element_number en{};
     int64_t nf = 0, nm = 0, ns = 0, npairs = 0;
     bool frame_valid = false;
+    int launches = 0, host_syncs = 0;
     int frame_W = 0, frame_H = 0, frame_S = 8;
     // timing
     bool timing = false;
@@ -335,6 +336,8 @@ int spr_render(spr_handle *h, void *stream) {
     int st = build_tables(h);
     if (st) return st;
     h->frame_valid = false;
+    int L = 0;  // kernels launched by this frame
+    h->host_syncs = 0;
     const FrameArgs a = make_args(h);
     const int W = a.W, H = a.H, WORDS = a.S / 8;
     if (h->timing) {
@@ -349,12 +352,13 @@ int spr_render(spr_handle *h, void *stream) {
         (st = ensure(h->image, 4 * (size_t)W * H)))
         return st;
     rec(h, 0, s);
-    launch_transform(a, h->tvert.as<float2>(), h->pflags.as<uint32_t>(), h->pvis.as<uint8_t>(), s);
+    L += launch_transform(a, h->tvert.as<float2>(), h->pflags.as<uint32_t>(), h->pvis.as<uint8_t>(), s);
     rec(h, 1, s);
     // stages 4-5: monotone pieces, entry counts, exclusive scan
-    launch_curve_count(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->counts.as<uint32_t>(), s);
-    scan_exclusive_u32(h->counts.as<uint32_t>(), h->offsets.as<uint32_t>(), h->C, h->scan_tmp.as<uint32_t>(), s);
+    L += launch_curve_count(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->counts.as<uint32_t>(), s);
+    L += scan_exclusive_u32(h->counts.as<uint32_t>(), h->offsets.as<uint32_t>(), h->C, h->scan_tmp.as<uint32_t>(), s);
     cudaMemcpyAsync(h->h_u32, h->offsets.as<uint32_t>() + h->C, 4, cudaMemcpyDeviceToHost, s);
+    ++h->host_syncs;
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
     if ((st = cuda_status())) return st;
     const int64_t nf = h->h_u32[0];
@@ -374,9 +378,10 @@ int spr_render(spr_handle *h, void *stream) {
     if (nf == 0) {
         cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
         for (int i = 2; i <= 6; ++i) rec(h, i, s);
-        launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(), s);
+        L += launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(), s);
         rec(h, 7, s);
         rec(h, 8, s);
+        h->launches = L;
         h->frame_valid = true;
         h->frame_W = W;
         h->frame_H = H;
@@ -394,25 +399,28 @@ int spr_render(spr_handle *h, void *stream) {
         (st = ensure(h->merged, 4 * (size_t)WORDS * nf)))
         return st;
     rec(h, 2, s);
-    launch_curve_emit(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->offsets.as<uint32_t>(), h->entries.as<int2>(),
+    L += launch_curve_emit(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->offsets.as<uint32_t>(), h->entries.as<int2>(),
                       s);
-    launch_fragment(a, h->tvert.as<float2>(), h->entries.as<int2>(), nf, h->key.as<int32_t>(), h->pidw.as<uint32_t>(),
+    L += launch_fragment(a, h->tvert.as<float2>(), h->entries.as<int2>(), nf, h->key.as<int32_t>(), h->pidw.as<uint32_t>(),
                     h->wn.as<int8_t>(), h->mask.as<uint32_t>(), h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), s);
     rec(h, 3, s);
     // stage 8: stable sort by (path, cell key)
     const int key_bits = 24 + bits_for(h->P ? h->P - 1 : 0);
+    int rl = 0;
     const bool alt = radix_sort<uint64_t>(h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(),
                                           h->skey[1].as<uint64_t>(), h->sval[1].as<uint32_t>(), nf, key_bits,
-                                          h->sort_tmp.as<uint32_t>(), s);
+                                          h->sort_tmp.as<uint32_t>(), s, &rl);
+    L += rl;
     h->skey_sorted = alt ? h->skey[1].as<uint64_t>() : h->skey[0].as<uint64_t>();
     h->perm_sorted = alt ? h->sval[1].as<uint32_t>() : h->sval[0].as<uint32_t>();
     rec(h, 4, s);
     // stages 9-12, 14: winding scan, marks, draw list
     cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);
-    launch_scan_mark(a, nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
+    L += launch_scan_mark(a, nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
                      h->draw.as<int4>(), h->heads.as<uint32_t>(), h->counters.as<FrameCounters>(),
                      h->flags_tmp.as<uint32_t>(), s);
     cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
+    ++h->host_syncs;
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
     if ((st = cuda_status())) return st;
     h->nm = h->h_counters->n_merged;
@@ -421,7 +429,7 @@ int spr_render(spr_handle *h, void *stream) {
     h->en.span = (int32_t)h->ns;
     rec(h, 5, s);
     // stage 13: merged sample masks
-    launch_stencil(a, nf, h->nm, h->skey_sorted, h->perm_sorted, h->pidw.as<uint32_t>(), h->mask.as<uint32_t>(),
+    L += launch_stencil(a, nf, h->nm, h->skey_sorted, h->perm_sorted, h->pidw.as<uint32_t>(), h->mask.as<uint32_t>(),
                    h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), s);
     rec(h, 6, s);
     // stage 15: bin draw items by (cell row, 32-column tile), resolve
@@ -429,9 +437,10 @@ int spr_render(spr_handle *h, void *stream) {
     if ((st = ensure(h->tiles, 4 * ((size_t)items + 1))) || (st = ensure(h->pair_off, 4 * ((size_t)items + 1))))
         return st;
     if ((st = ensure(h->scan_tmp, 4 * (size_t)scan_tmp_words(std::max<int64_t>({items, (int64_t)h->C, 1}))))) return st;
-    launch_item_tiles(a, h->draw.as<int4>(), items, h->tiles.as<uint32_t>(), s);
-    scan_exclusive_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), items, h->scan_tmp.as<uint32_t>(), s);
+    L += launch_item_tiles(a, h->draw.as<int4>(), items, h->tiles.as<uint32_t>(), s);
+    L += scan_exclusive_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), items, h->scan_tmp.as<uint32_t>(), s);
     cudaMemcpyAsync(h->h_u32, h->pair_off.as<uint32_t>() + items, 4, cudaMemcpyDeviceToHost, s);
+    ++h->host_syncs;
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
     const int64_t npairs = h->h_u32[0];
     h->npairs = npairs;
@@ -439,17 +448,19 @@ int spr_render(spr_handle *h, void *stream) {
         (st = ensure(h->pval[0], 4 * (size_t)npairs)) || (st = ensure(h->pval[1], 4 * (size_t)npairs)) ||
         (st = ensure(h->sort_tmp, 4 * (size_t)std::max(radix_tmp_words(npairs), radix_tmp_words(nf)))))
         return st;
-    launch_emit_pairs(a, h->draw.as<int4>(), items, h->pair_off.as<uint32_t>(), h->pkey[0].as<uint32_t>(),
+    L += launch_emit_pairs(a, h->draw.as<int4>(), items, h->pair_off.as<uint32_t>(), h->pkey[0].as<uint32_t>(),
                       h->pval[0].as<uint32_t>(), s);
     const bool palt = radix_sort<uint32_t>(h->pkey[0].as<uint32_t>(), h->pval[0].as<uint32_t>(),
                                            h->pkey[1].as<uint32_t>(), h->pval[1].as<uint32_t>(), npairs,
-                                           std::max(bits_for((uint64_t)nbins - 1), 1), h->sort_tmp.as<uint32_t>(), s);
+                                           std::max(bits_for((uint64_t)nbins - 1), 1), h->sort_tmp.as<uint32_t>(), s,
+                                           &rl);
+    L += rl;
     const uint32_t *pk = palt ? h->pkey[1].as<uint32_t>() : h->pkey[0].as<uint32_t>();
     const uint32_t *pv = palt ? h->pval[1].as<uint32_t>() : h->pval[0].as<uint32_t>();
     cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
-    launch_bin_bounds(pk, npairs, bin_start, bin_end, s);
+    L += launch_bin_bounds(pk, npairs, bin_start, bin_end, s);
     rec(h, 7, s);
-    launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end, h->image.as<uint32_t>(), s);
+    L += launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end, h->image.as<uint32_t>(), s);
     rec(h, 8, s);
     if ((st = cuda_status())) return st;
     if (h->timing) {
@@ -460,6 +471,7 @@ int spr_render(spr_handle *h, void *stream) {
             h->step_ms[i] = ms;
         }
     }
+    h->launches = L;
     h->frame_valid = true;
     h->frame_W = W;
     h->frame_H = H;
@@ -481,6 +493,7 @@ int spr_read_image(spr_handle *h, uint8_t *host_rgba, void *stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t bytes = 4 * (size_t)h->frame_W * h->frame_H;
     if (cudaMemcpyAsync(host_rgba, h->image.p, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return cuda_status();
+    ++h->host_syncs;
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
     return SPR_OK;
 }
@@ -515,6 +528,24 @@ int spr_step_timing(spr_handle *h, double *ms, int32_t capacity, int32_t *n_out)
     *n_out = kSteps;
     if (ms)
         for (int i = 0; i < kSteps && i < capacity; ++i) ms[i] = h->step_ms[i];
+    return SPR_OK;
+}
+
+int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
+    if (!h || !out) return SPR_ERR_INVALID_ARG;
+    out->kernel_launches = h->launches;
+    out->host_syncs = h->host_syncs;
+    out->resolve_pairs = h->npairs;
+    size_t total = 0;
+    const DevBuf *bufs[] = {&h->mask_table, &h->rtables, &h->vertex,   &h->vpid,      &h->curves,  &h->rule,
+                            &h->fill,       &h->affine,  &h->tvert,    &h->pflags,    &h->pvis,    &h->counts,
+                            &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
+                            &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
+                            &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
+                            &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
+                            &h->image,      &h->counters, &h->dump_tmp};
+    for (const DevBuf *b : bufs) total += b->bytes;
+    out->device_bytes = (int64_t)total;
     return SPR_OK;
 }
 
@@ -559,6 +590,22 @@ int spr_debug_dump(spr_handle *h, int32_t stage, void *dst, size_t capacity, siz
     if (capacity < bytes) return SPR_ERR_INVALID_ARG;
     if (bytes && cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) return cuda_status();
     return SPR_OK;
+}
+
+int spr_selftest(spr_handle *h, int64_t *srgb_encode_mismatches) {
+    if (!h || !srgb_encode_mismatches) return SPR_ERR_INVALID_ARG;
+    cudaSetDevice(h->cfg.device);
+    DevBuf bad;
+    int st = ensure(bad, 8);
+    if (st) return st;
+    cudaMemset(bad.p, 0, 8);
+    launch_selftest_encode(h->rtables.as<ResolveTables>(), bad.as<unsigned long long>(), nullptr);
+    unsigned long long n = 0;
+    cudaMemcpy(&n, bad.p, 8, cudaMemcpyDeviceToHost);
+    bad.release();
+    st = cuda_status();
+    *srgb_encode_mismatches = (int64_t)n;
+    return st;
 }
 
 const char *spr_status_string(int32_t status) {

@@ -44,18 +44,19 @@ void build_resolve_tables(ResolveTables *t);
 // ---- scan / sort (spr_sort.cu) ----------------------------------------------------
 int64_t scan_tmp_words(int64_t n);
 // out[0..n) = exclusive prefix sums of in, out[n] = total.
-void scan_exclusive_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp, cudaStream_t s);
+int scan_exclusive_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp, cudaStream_t s);
 // In-place exclusive scan of a short array by one block; a[n] = total.
-void scan_tiles_inplace(uint32_t *a, int64_t n, cudaStream_t s);
+int scan_tiles_inplace(uint32_t *a, int64_t n, cudaStream_t s);
 int64_t radix_tiles(int64_t n);
 int64_t radix_tmp_words(int64_t n);
 // Stable LSD sort on bits [0, key_bits); returns true when the result is in
 // the *_alt buffers.
+// *launches receives the number of kernels launched.
 template <class K>
 bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_t n, int key_bits, uint32_t *tmp,
-                cudaStream_t s);
+                cudaStream_t s, int *launches);
 
-// ---- pipeline kernels (spr_kernels.cu) -----------------------------------------
+// ---- pipeline kernels (spr_kernels.cu); each launcher returns its kernel count --
 struct FrameArgs {
     int W, H, S, ms_output, srgb;
     int P, C, V;
@@ -71,32 +72,33 @@ struct FrameArgs {
     const ResolveTables *rtables;
 };
 
-void launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible,
+int launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible,
                       cudaStream_t s);
-void launch_curve_count(const FrameArgs &a, const float2 *tvert, const uint8_t *path_visible, uint32_t *counts,
+int launch_curve_count(const FrameArgs &a, const float2 *tvert, const uint8_t *path_visible, uint32_t *counts,
                         cudaStream_t s);
-void launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *path_visible,
+int launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *path_visible,
                        const uint32_t *offsets, int2 *entries, cudaStream_t s);
-void launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t nf, int32_t *key,
+int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t nf, int32_t *key,
                      uint32_t *pidw, int8_t *wn, uint32_t *mask, uint64_t *sort_key, uint32_t *sort_val,
                      cudaStream_t s);
 int64_t flags_tmp_words(int64_t nf);
 // Winding scan, merged-fragment / span marks, draw list and merged heads.
-void launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
+int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
                       int8_t *wn_scan, int4 *draw, uint32_t *heads, FrameCounters *counters, uint32_t *tmp,
                       cudaStream_t s);
-void launch_stencil(const FrameArgs &a, int64_t nf, int64_t n_merged, const uint64_t *skey, const uint32_t *perm,
+int launch_stencil(const FrameArgs &a, int64_t nf, int64_t n_merged, const uint64_t *skey, const uint32_t *perm,
                     const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan, const uint32_t *heads,
                     uint32_t *merged_mask, cudaStream_t s);
-void launch_item_tiles(const FrameArgs &a, const int4 *draw, int64_t n_items, uint32_t *tile_counts,
+int launch_item_tiles(const FrameArgs &a, const int4 *draw, int64_t n_items, uint32_t *tile_counts,
                        cudaStream_t s);
-void launch_emit_pairs(const FrameArgs &a, const int4 *draw, int64_t n_items, const uint32_t *pair_offsets,
+int launch_emit_pairs(const FrameArgs &a, const int4 *draw, int64_t n_items, const uint32_t *pair_offsets,
                        uint32_t *pair_key, uint32_t *pair_val, cudaStream_t s);
-void launch_bin_bounds(const uint32_t *pair_key, int64_t n_pairs, uint32_t *bin_start, uint32_t *bin_end,
+int launch_bin_bounds(const uint32_t *pair_key, int64_t n_pairs, uint32_t *bin_start, uint32_t *bin_end,
                        cudaStream_t s);
-void launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_mask, const uint32_t *pair_val,
+int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_mask, const uint32_t *pair_val,
                     const uint32_t *bin_start, const uint32_t *bin_end, uint32_t *image, cudaStream_t s);
-void launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s);
-void launch_decode_keys(const uint64_t *skey, int64_t nf, int nrows, int32_t *out, cudaStream_t s);
+int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s);
+int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cudaStream_t s);
+int launch_decode_keys(const uint64_t *skey, int64_t nf, int nrows, int32_t *out, cudaStream_t s);
 
 }  // namespace spr

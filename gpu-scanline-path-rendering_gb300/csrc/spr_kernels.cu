@@ -636,51 +636,190 @@ __global__ void k_bin_bounds(const uint32_t *__restrict__ key, int64_t n, uint32
     if (i == n - 1 || key[i + 1] != k) end[k] = (uint32_t)(i + 1);
 }
 
+// Shared-memory tables of the resolve.  The sRGB decode table is replicated
+// once per lane (entry k of lane l at k * 32 + l) so that the data-dependent
+// lookups of a warp never collide in a bank.
 struct SmemTables {
-    float dec[256];
-    float lin[256];
+    float dec32[256 * 32];
     float th[256];
-    uint8_t bin[4096];
 };
 
+__device__ __forceinline__ float lin8(uint32_t k) { return (float)k * (1.f / 255.f); }
+
+// Position of the r-th (0-based) set bit of m; requires r < popc(m).
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const uint32_t lo = m & ((1u << w) - 1u);
+        const int c = __popc(lo);
+        if (r >= c) {
+            r -= c;
+            m >>= w;
+            pos += w;
+        } else {
+            m = lo;
+        }
+    }
+    return pos;
+}
+
+// Blend results are finite and never -0 (products and sums of non-negative
+// values), so the hardware min/max give the same clamp as fmin_r/fmax_r.
+__device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.f), 1.f); }
+
 __device__ __forceinline__ uint32_t enc_lin(float v) {
-    const float c = fmin_r(fmax_r(v, 0.f), 1.f);
+    const float c = clamp01(v);
     return (uint32_t)cvt_rzi(c * 255.f + 0.5f);
 }
-__device__ __forceinline__ uint32_t enc_srgb(const SmemTables &t, float v) {
-    const float c = fmin_r(fmax_r(v, 0.f), 1.f);
-    const int b = min(cvt_rzi(c * 4096.f), 4095);
-    uint32_t k = t.bin[b];
-    if (k < 255 && c >= t.th[k]) ++k;
-    return k;
+
+// sRGB encode: the number of thresholds t[k] (the linear value at which the
+// 8-bit code steps from k to k+1) that are <= v.  A closed-form estimate
+// (within one code of the answer) is corrected by exact comparisons against
+// the thresholds, so the result is exactly the table definition.
+__device__ __forceinline__ uint32_t enc_srgb(const float *__restrict__ th, float v) {
+    const float c = clamp01(v);
+    const float e = c <= 0.0031308f ? c * 12.92f : 1.055f * __powf(c, 1.f / 2.4f) - 0.055f;
+    int k = min(max(__float2int_rn(e * 255.f), 0), 255);
+    // th[-1] = -inf and th[255] = +inf are implied by the clamps below
+    const float lo = th[max(k - 1, 0)], hi = th[k];
+    if (k > 0 && c < lo) return (uint32_t)(k - 1);
+    if (k < 255 && c >= hi) return (uint32_t)(k + 1);
+    return (uint32_t)k;
 }
 
 template <bool SRGB>
-__device__ __forceinline__ uint32_t blend_sample(const SmemTables &t, uint32_t dv, float sr, float sg, float sb, float a,
-                                                 float om) {
-    const float dr = t.dec[dv & 0xFF], dg = t.dec[(dv >> 8) & 0xFF], db = t.dec[(dv >> 16) & 0xFF];
-    const float da = t.lin[dv >> 24];
+__device__ __forceinline__ float dec8(const SmemTables &t, uint32_t k, int lane) {
+    if constexpr (SRGB) return t.dec32[k * 32 + lane];
+    else return lin8(k);
+}
+
+template <bool SRGB>
+__device__ __forceinline__ uint32_t enc8(const SmemTables &t, float v) {
+    if constexpr (SRGB) return enc_srgb(t.th, v);
+    else return enc_lin(v);
+}
+
+template <bool SRGB>
+__device__ __forceinline__ uint32_t blend_sample(const SmemTables &t, int lane, uint32_t dv, float sr, float sg,
+                                                 float sb, float a, float om) {
+    const float dr = dec8<SRGB>(t, dv & 0xFF, lane), dg = dec8<SRGB>(t, (dv >> 8) & 0xFF, lane),
+                db = dec8<SRGB>(t, (dv >> 16) & 0xFF, lane);
+    const float da = lin8(dv >> 24);
     const float orr = sr * a + dr * om;
     const float og = sg * a + dg * om;
     const float ob = sb * a + db * om;
     const float oa = a * a + da * om;
-    uint32_t er, eg, eb;
-    if (SRGB) {
-        er = enc_srgb(t, orr);
-        eg = enc_srgb(t, og);
-        eb = enc_srgb(t, ob);
-    } else {
-        er = enc_lin(orr);
-        eg = enc_lin(og);
-        eb = enc_lin(ob);
-    }
-    return er | (eg << 8) | (eb << 16) | (enc_lin(oa) << 24);
+    return enc8<SRGB>(t, orr) | (enc8<SRGB>(t, og) << 8) | (enc8<SRGB>(t, ob) << 16) | (enc_lin(oa) << 24);
 }
 
-// One warp per bin of (cell row, 32 pixel columns); lane = pixel column,
-// two pixel rows each.  Items of the bin are applied in draw-list order to
-// the per-sample RGBA8 state kept in shared memory, then every pixel is
-// averaged over its samples.
+// ---- resolve state -----------------------------------------------------
+// A bin is 2 pixel rows x 32 columns = 64 pixels, pixel p = row * 32 + col.
+// Each pixel keeps its samples as a short list of (sample mask, RGBA8 colour)
+// entries whose masks partition the pixel's samples: equal colours are merged
+// after every blend, so a pixel typically holds 1-3 entries and a blend costs
+// one evaluation per entry instead of one per sample.  A 32-sample pixel that
+// would need more than 16 entries switches to an explicit 32-sample array in
+// the same storage (count = kFull) and switches back once it has 16 or fewer
+// distinct colours.  Every sample still gets exactly the value the
+// per-sample rule gives.
+constexpr uint8_t kFull = 0xFF;
+
+template <int CAP>
+struct BinState {
+    uint32_t emask[CAP][64];
+    uint32_t ecol[CAP][64];
+    uint8_t cnt[64];
+    unsigned long long bm[32];  // pixel bitmap of each staged item
+    int4 it[32];
+    uint4 mm[32];
+};
+
+__device__ __forceinline__ unsigned long long span_bits(int c0, int c1, int rows) {
+    if (c1 <= c0) return 0ull;
+    const uint32_t hi = c1 >= 32 ? 0xFFFFFFFFu : ((1u << c1) - 1u);
+    const uint32_t r = hi & ~((1u << c0) - 1u);
+    return (unsigned long long)r | (rows > 1 ? ((unsigned long long)r << 32) : 0ull);
+}
+
+// Index of the r-th set bit of a 64-bit word.
+__device__ __forceinline__ int nth_set_bit64(unsigned long long m, int r) {
+    const uint32_t lo = (uint32_t)m;
+    const int c = __popc(lo);
+    return r < c ? nth_set_bit(lo, r) : 32 + nth_set_bit((uint32_t)(m >> 32), r - c);
+}
+
+template <int CAP>
+__device__ __forceinline__ uint32_t &full_sample(BinState<CAP> &w, int p, int s) {
+    return s < 16 ? w.ecol[s][p] : w.emask[s - 16][p];
+}
+
+// Entries -> explicit 32 samples (32-sample pixels only).
+template <int CAP>
+__device__ void to_full(BinState<CAP> &w, int p) {
+    if constexpr (CAP == 16) {
+        const int n = w.cnt[p];
+        uint32_t em[16], ec[16];
+        for (int j = 0; j < n; ++j) em[j] = w.emask[j][p], ec[j] = w.ecol[j][p];
+        for (int smp = 0; smp < 32; ++smp) {
+            uint32_t v = 0;
+            for (int j = 0; j < n; ++j)
+                if ((em[j] >> smp) & 1u) v = ec[j];
+            full_sample(w, p, smp) = v;
+        }
+        w.cnt[p] = kFull;
+    }
+}
+
+// Explicit samples -> entries when at most CAP distinct colours remain.
+template <int CAP>
+__device__ void try_compress(BinState<CAP> &w, int p) {
+    if constexpr (CAP == 16) {
+        uint32_t v[32];
+        for (int smp = 0; smp < 32; ++smp) v[smp] = full_sample(w, p, smp);
+        uint32_t col[16], msk[16];
+        int n = 0;
+        for (int smp = 0; smp < 32; ++smp) {
+            int j = 0;
+            while (j < n && col[j] != v[smp]) ++j;
+            if (j == n) {
+                if (n == 16) return;  // stays explicit
+                col[n] = v[smp];
+                msk[n] = 0u;
+                ++n;
+            }
+            msk[j] |= 1u << smp;
+        }
+        for (int j = 0; j < n; ++j) w.emask[j][p] = msk[j], w.ecol[j][p] = col[j];
+        w.cnt[p] = (uint8_t)n;
+    }
+}
+
+// Merges entries of equal colour.
+template <int CAP>
+__device__ __forceinline__ void dedup(BinState<CAP> &w, int p) {
+    int n = w.cnt[p];
+    for (int j = 1; j < n; ++j) {
+        const uint32_t cj = w.ecol[j][p];
+        for (int i = 0; i < j; ++i) {
+            if (w.ecol[i][p] == cj) {
+                w.emask[i][p] |= w.emask[j][p];
+                --n;
+                w.emask[j][p] = w.emask[n][p];
+                w.ecol[j][p] = w.ecol[n][p];
+                --j;
+                break;
+            }
+        }
+    }
+    w.cnt[p] = (uint8_t)n;
+}
+
+// One warp per bin of (cell row, 32 pixel columns).  Items (merged fragments
+// and spans, in draw-list order) are taken in batches whose pixel sets are
+// pairwise disjoint, so each batch is applied with one lane per covered
+// pixel and no ordering conflicts; then every pixel is averaged over its
+// samples with an exact fixed-point sum.
 template <int S, bool MS, bool SRGB>
 __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
                                                                  const uint32_t *__restrict__ merged,
@@ -688,102 +827,198 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                                                                  const uint32_t *__restrict__ bstart,
                                                                  const uint32_t *__restrict__ bend,
                                                                  uint32_t *__restrict__ image) {
-    constexpr int SPP = MS ? S : 1;
+    constexpr int CAP = MS ? (S == 32 ? 16 : 8) : 1;
+    constexpr uint32_t ALL = MS ? (S == 32 ? 0xFFFFFFFFu : 0xFFu) : 1u;
+    constexpr int MW = S / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemTables &T = *reinterpret_cast<SmemTables *>(smem_raw);
-    int4 *stage = reinterpret_cast<int4 *>(smem_raw + sizeof(SmemTables));
-    uint32_t *state = reinterpret_cast<uint32_t *>(smem_raw + sizeof(SmemTables) + kResolveWarps * 32 * sizeof(int4));
     {
         const ResolveTables *rt = a.rtables;
-        for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-            T.dec[i] = SRGB ? rt->srgb_dec[i] : rt->lin_dec[i];
-            T.lin[i] = rt->lin_dec[i];
-            T.th[i] = rt->threshold[i];
-        }
-        for (int i = threadIdx.x; i < 4096; i += blockDim.x) T.bin[i] = rt->bin[i];
+        if constexpr (SRGB)
+            for (int i = threadIdx.x; i < 256 * 32; i += blockDim.x) T.dec32[i] = rt->srgb_dec[i >> 5];
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) T.th[i] = rt->threshold[i];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    BinState<CAP> &w = reinterpret_cast<BinState<CAP> *>(smem_raw + sizeof(SmemTables))[warp];
     const int ntx = (a.W + kTileW - 1) / kTileW;
     const int nrows = (a.H + 1) / 2;
     const int64_t b = (int64_t)blockIdx.x * kResolveWarps + warp;
     if (b >= (int64_t)ntx * nrows) return;
     const int row = (int)(b / ntx), tile = (int)(b % ntx);
-    const int px = tile * kTileW + lane;
+    const int tx0 = tile * kTileW;
     const int y0 = row * 2;
-    int4 *st = stage + warp * 32;
-    uint32_t *ws = state + warp * 2 * SPP * 32;
+    const int cols = min(kTileW, a.W - tx0);  // valid columns of this bin
+    const int rows = min(2, a.H - y0);        // valid pixel rows
 #pragma unroll
-    for (int py = 0; py < 2; ++py)
-        for (int s = 0; s < SPP; ++s) ws[(py * SPP + s) * 32 + lane] = 0xFFFFFFFFu;
+    for (int h = 0; h < 2; ++h) {
+        const int p = lane + 32 * h;
+        w.cnt[p] = 1;
+        w.emask[0][p] = ALL;
+        w.ecol[0][p] = 0xFFFFFFFFu;
+    }
     const uint32_t beg = bstart[b], fin = bend[b];
-    const float *dec = T.dec;
     for (uint32_t base = beg; base < fin; base += 32) {
-        if (base + lane < fin) st[lane] = draw[pval[base + lane]];
         __syncwarp();
         const int cnt = (int)min(32u, fin - base);
-        for (int q = 0; q < cnt; ++q) {
-            const int4 it = st[q];
-            const int x = (int)((uint32_t)it.x & 0xFFFFu);
-            if (px < x || px >= x + it.y || px >= a.W) continue;
-            const uint32_t c = (uint32_t)it.z;
-            const float sr = dec[c & 0xFF], sg = dec[(c >> 8) & 0xFF], sb = dec[(c >> 16) & 0xFF];
-            const float sa = T.lin[c >> 24];
-#pragma unroll
-            for (int py = 0; py < 2; ++py) {
-                if (y0 + py >= a.H) continue;
-                uint32_t m = 0xFFFFFFFFu;
-                if (it.w != 0) {
-                    const int k = (px - x) * 2 + py;
-                    if (S == 8)
-                        m = (__ldg(merged + (it.w - 1)) >> (8 * k)) & 0xFFu;
-                    else
-                        m = __ldg(merged + (int64_t)(it.w - 1) * 4 + k);
-                }
-                uint32_t *pst = ws + py * SPP * 32 + lane;
-                if (MS) {
-                    if (S == 8) m &= 0xFFu;
-                    const float om = 1.f - sa;
-                    while (m) {
-                        const int s = __ffs(m) - 1;
-                        m &= m - 1;
-                        pst[s * 32] = blend_sample<SRGB>(T, pst[s * 32], sr, sg, sb, sa, om);
-                    }
-                } else {
-                    const int cntb = __popc(S == 8 ? (m & 0xFFu) : m);
-                    const float aa = sa * ((float)cntb / (float)S);
-                    pst[0] = blend_sample<SRGB>(T, pst[0], sr, sg, sb, aa, 1.f - aa);
-                }
+        if (lane < cnt) {
+            const int4 it = draw[pval[base + lane]];
+            w.it[lane] = it;
+            const int x = (int)((uint32_t)it.x & 0xFFFFu) - tx0;
+            unsigned long long bm;
+            if (it.w != 0) {
+                if constexpr (MW == 4)
+                    w.mm[lane] = __ldg(reinterpret_cast<const uint4 *>(merged) + (it.w - 1));
+                else
+                    w.mm[lane] = make_uint4(__ldg(merged + (it.w - 1)), 0u, 0u, 0u);
+                bm = span_bits(max(x, 0), min(x + 2, cols), rows);
+            } else {
+                bm = span_bits(max(x, 0), min(x + it.y, cols), rows);
             }
+            w.bm[lane] = bm;
         }
         __syncwarp();
+        int q0 = 0;
+        while (q0 < cnt) {
+            // batch [q0, q1): items with pairwise disjoint pixel sets
+            unsigned long long acc = 0ull;
+            int q1 = q0;
+            while (q1 < cnt && (acc & w.bm[q1]) == 0ull) acc |= w.bm[q1++];
+            const int npix = __popcll(acc);
+            for (int r = lane; r < npix; r += 32) {
+                const int p = nth_set_bit64(acc, r);
+                int q = q0;
+                while (!((w.bm[q] >> p) & 1ull)) ++q;
+                const int4 it = w.it[q];
+                const uint32_t c = (uint32_t)it.z;
+                const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
+                            sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
+                const float sa = lin8(c >> 24);
+                int n = w.cnt[p];
+                if (it.w != 0) {
+                    // merged fragment: this pixel's sample mask
+                    const int k = ((p & 31) + tx0 - (int)((uint32_t)it.x & 0xFFFFu)) * 2 + (p >> 5);
+                    const uint4 mm = w.mm[q];
+                    uint32_t m;
+                    if constexpr (MW == 4)
+                        m = k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w));
+                    else
+                        m = (mm.x >> (8 * k)) & 0xFFu;
+                    if (m == 0u) continue;
+                    if constexpr (!MS) {
+                        const float aa = sa * ((float)__popc(m) / (float)S);
+                        w.ecol[0][p] = blend_sample<SRGB>(T, lane, w.ecol[0][p], sr, sg, sb, aa, 1.f - aa);
+                        continue;
+                    } else {
+                        const float om = 1.f - sa;
+                        if (n != kFull) {
+                            int splits = 0;
+                            for (int j = 0; j < n; ++j) {
+                                const uint32_t em = w.emask[j][p];
+                                splits += ((em & m) != 0u && (em & ~m) != 0u) ? 1 : 0;
+                            }
+                            if (n + splits > CAP) {
+                                to_full(w, p);
+                                n = kFull;
+                            }
+                        }
+                        if (n == kFull) {
+                            if constexpr (CAP == 16) {
+                                for (uint32_t mk = m; mk; mk &= mk - 1u) {
+                                    uint32_t &v = full_sample(w, p, __ffs(mk) - 1);
+                                    v = blend_sample<SRGB>(T, lane, v, sr, sg, sb, sa, om);
+                                }
+                                try_compress(w, p);
+                            }
+                        } else {
+                            int nn = n;
+                            for (int j = 0; j < n; ++j) {
+                                const uint32_t em = w.emask[j][p];
+                                const uint32_t in = em & m;
+                                if (!in) continue;
+                                const uint32_t nc = blend_sample<SRGB>(T, lane, w.ecol[j][p], sr, sg, sb, sa, om);
+                                if (in == em) {
+                                    w.ecol[j][p] = nc;
+                                } else {
+                                    w.emask[j][p] = em & ~m;
+                                    w.emask[nn][p] = in;
+                                    w.ecol[nn][p] = nc;
+                                    ++nn;
+                                }
+                            }
+                            w.cnt[p] = (uint8_t)nn;
+                            dedup(w, p);
+                        }
+                    }
+                } else {
+                    // span: every sample of the pixel
+                    const float om = 1.f - sa;
+                    if (n == kFull) {
+                        if constexpr (CAP == 16) {
+                            for (int smp = 0; smp < 32; ++smp) {
+                                uint32_t &v = full_sample(w, p, smp);
+                                v = blend_sample<SRGB>(T, lane, v, sr, sg, sb, sa, om);
+                            }
+                            try_compress(w, p);
+                        }
+                    } else {
+                        for (int j = 0; j < n; ++j)
+                            w.ecol[j][p] = blend_sample<SRGB>(T, lane, w.ecol[j][p], sr, sg, sb, sa, om);
+                        if (n > 1) dedup(w, p);
+                    }
+                }
+            }
+            __syncwarp();
+            q0 = q1;
+        }
     }
-    if (px >= a.W) return;
+    __syncwarp();
+    if (lane >= cols) return;
+    const double scale = 1.0 / (68719476736.0 * (double)(MS ? S : 1));
 #pragma unroll
     for (int py = 0; py < 2; ++py) {
-        const int yy = y0 + py;
-        if (yy >= a.H) continue;
-        const uint32_t *pst = ws + py * SPP * 32 + lane;
-        float ar = 0.f, ag = 0.f, ab = 0.f, aa = 0.f;
-        for (int s = 0; s < SPP; ++s) {
-            const uint32_t v = pst[s * 32];
-            ar += dec[v & 0xFF];
-            ag += dec[(v >> 8) & 0xFF];
-            ab += dec[(v >> 16) & 0xFF];
-            aa += T.lin[v >> 24];
+        if (py >= rows) continue;
+        const int p = py * 32 + lane;
+        long long ir = 0, ig = 0, ib = 0, ia = 0;
+        const int n = w.cnt[p];
+        auto add = [&](uint32_t v, int weight) {
+            ir += (long long)weight * (long long)(dec8<SRGB>(T, v & 0xFF, lane) * 68719476736.0f);
+            ig += (long long)weight * (long long)(dec8<SRGB>(T, (v >> 8) & 0xFF, lane) * 68719476736.0f);
+            ib += (long long)weight * (long long)(dec8<SRGB>(T, (v >> 16) & 0xFF, lane) * 68719476736.0f);
+            ia += (long long)weight * (long long)(lin8(v >> 24) * 68719476736.0f);
+        };
+        if (n == kFull) {
+            if constexpr (CAP == 16)
+                for (int smp = 0; smp < 32; ++smp) add(full_sample(w, p, smp), 1);
+        } else {
+            for (int j = 0; j < n; ++j) add(w.ecol[j][p], __popc(w.emask[j][p]));
         }
-        const float n = (float)SPP;
-        ar /= n;
-        ag /= n;
-        ab /= n;
-        aa /= n;
-        uint32_t out;
-        if (SRGB)
-            out = enc_srgb(T, ar) | (enc_srgb(T, ag) << 8) | (enc_srgb(T, ab) << 16) | (enc_lin(aa) << 24);
-        else
-            out = enc_lin(ar) | (enc_lin(ag) << 8) | (enc_lin(ab) << 16) | (enc_lin(aa) << 24);
-        image[(int64_t)yy * a.W + px] = out;
+        const float ar = (float)((double)ir * scale), ag = (float)((double)ig * scale);
+        const float ab = (float)((double)ib * scale), aa = (float)((double)ia * scale);
+        const uint32_t out = enc8<SRGB>(T, ar) | (enc8<SRGB>(T, ag) << 8) | (enc8<SRGB>(T, ab) << 16) |
+                             (enc_lin(aa) << 24);
+        image[(int64_t)(y0 + py) * a.W + tx0 + lane] = out;
     }
+}
+
+// Exhaustive check of enc_srgb against the table definition (bins + one
+// threshold step) over every float bit pattern in [lo, hi).
+__global__ void k_selftest_encode(const ResolveTables *__restrict__ rt, uint32_t lo, uint32_t hi,
+                                  unsigned long long *__restrict__ bad) {
+    __shared__ float th[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) th[i] = rt->threshold[i];
+    __syncthreads();
+    unsigned long long local = 0;
+    for (uint64_t u = lo + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < hi;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        const float v = __uint_as_float((uint32_t)u);
+        const float c = fmin_r(fmax_r(v, 0.f), 1.f);
+        const int bb = min(cvt_rzi(c * 4096.f), 4095);
+        uint32_t k = rt->bin[bb];
+        if (k < 255 && c >= th[k]) ++k;
+        if (enc_srgb(th, v) != k) ++local;
+    }
+    if (local) atomicAdd(bad, local);
 }
 
 __global__ void k_fill(uint32_t *image, int64_t n, uint32_t v) {
@@ -799,9 +1034,8 @@ __global__ void k_decode_keys(const uint64_t *__restrict__ skey, int64_t n, int 
 template <int S, bool MS, bool SRGB>
 void resolve_variant(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
                      const uint32_t *bstart, const uint32_t *bend, uint32_t *image, cudaStream_t s) {
-    constexpr int SPP = MS ? S : 1;
-    const size_t smem = sizeof(SmemTables) + kResolveWarps * 32 * sizeof(int4) +
-                        (size_t)kResolveWarps * 2 * SPP * 32 * sizeof(uint32_t);
+    constexpr int CAP = MS ? (S == 32 ? 16 : 8) : 1;
+    const size_t smem = sizeof(SmemTables) + (size_t)kResolveWarps * sizeof(BinState<CAP>);
     cudaFuncSetAttribute(k_resolve<S, MS, SRGB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int64_t nbins = (int64_t)((a.W + kTileW - 1) / kTileW) * ((a.H + 1) / 2);
     k_resolve<S, MS, SRGB><<<grid_for(nbins, kResolveWarps), kResolveWarps * 32, smem, s>>>(a, draw, merged, pval,
@@ -810,34 +1044,41 @@ void resolve_variant(const FrameArgs &a, const int4 *draw, const uint32_t *merge
 
 }  // namespace
 
-void launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible, cudaStream_t s) {
+int launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible, cudaStream_t s) {
     cudaMemsetAsync(path_flags, 0, sizeof(uint32_t) * (size_t)a.P, s);
-    if (a.V > 0) k_transform<<<grid_for(a.V), kThreads, 0, s>>>(a, tvert, path_flags);
-    if (a.P > 0) k_path_visible<<<grid_for(a.P), kThreads, 0, s>>>(a.P, path_flags, path_visible);
+    int n = 0;
+    if (a.V > 0) k_transform<<<grid_for(a.V), kThreads, 0, s>>>(a, tvert, path_flags), ++n;
+    if (a.P > 0) k_path_visible<<<grid_for(a.P), kThreads, 0, s>>>(a.P, path_flags, path_visible), ++n;
+    return n;
 }
 
-void launch_curve_count(const FrameArgs &a, const float2 *tvert, const uint8_t *vis, uint32_t *counts, cudaStream_t s) {
-    if (a.C > 0) k_curve_count<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, counts);
+int launch_curve_count(const FrameArgs &a, const float2 *tvert, const uint8_t *vis, uint32_t *counts, cudaStream_t s) {
+    if (a.C <= 0) return 0;
+    k_curve_count<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, counts);
+    return 1;
 }
 
-void launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *vis, const uint32_t *offsets,
+int launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *vis, const uint32_t *offsets,
                        int2 *entries, cudaStream_t s) {
-    if (a.C > 0) k_curve_emit<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, offsets, entries);
+    if (a.C <= 0) return 0;
+    k_curve_emit<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, offsets, entries);
+    return 1;
 }
 
-void launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t nf, int32_t *key,
+int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t nf, int32_t *key,
                      uint32_t *pidw, int8_t *wn, uint32_t *mask, uint64_t *sort_key, uint32_t *sort_val,
                      cudaStream_t s) {
-    if (nf <= 0) return;
+    if (nf <= 0) return 0;
     if (a.S == 8)
         k_fragment<8><<<grid_for(nf), kThreads, 0, s>>>(a, tvert, entries, nf, key, pidw, wn, mask, sort_key, sort_val);
     else
         k_fragment<32><<<grid_for(nf), kThreads, 0, s>>>(a, tvert, entries, nf, key, pidw, wn, mask, sort_key, sort_val);
+    return 1;
 }
 
 int64_t flags_tmp_words(int64_t nf) { return 2 * ((nf + kFlagTile - 1) / kFlagTile + 2); }
 
-void launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
+int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
                       int8_t *wn_scan, int4 *draw, uint32_t *heads, FrameCounters *counters, uint32_t *tmp,
                       cudaStream_t s) {
     const int64_t ntiles = (nf + kFlagTile - 1) / kFlagTile;
@@ -849,32 +1090,40 @@ void launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, cons
     scan_tiles_inplace(s0, ntiles, s);
     scan_tiles_inplace(s1, ntiles, s);
     k_flags_down<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(a, nf, ntiles, skey, wn_scan, s0, s1, draw, heads, counters);
+    return 8;
 }
 
-void launch_stencil(const FrameArgs &a, int64_t nf, int64_t nm, const uint64_t *skey, const uint32_t *perm,
+int launch_stencil(const FrameArgs &a, int64_t nf, int64_t nm, const uint64_t *skey, const uint32_t *perm,
                     const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan, const uint32_t *heads,
                     uint32_t *merged, cudaStream_t s) {
-    if (nm <= 0) return;
+    if (nm <= 0) return 0;
     if (a.S == 8)
         k_stencil<8><<<grid_for(nm), kThreads, 0, s>>>(a, nf, nm, skey, perm, pidw, mask, wn_scan, heads, merged);
     else
         k_stencil<32><<<grid_for(nm), kThreads, 0, s>>>(a, nf, nm, skey, perm, pidw, mask, wn_scan, heads, merged);
+    return 1;
 }
 
-void launch_item_tiles(const FrameArgs &a, const int4 *draw, int64_t n, uint32_t *cnt, cudaStream_t s) {
-    if (n > 0) k_item_tiles<<<grid_for(n), kThreads, 0, s>>>(a, draw, n, cnt);
+int launch_item_tiles(const FrameArgs &a, const int4 *draw, int64_t n, uint32_t *cnt, cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_item_tiles<<<grid_for(n), kThreads, 0, s>>>(a, draw, n, cnt);
+    return 1;
 }
 
-void launch_emit_pairs(const FrameArgs &a, const int4 *draw, int64_t n, const uint32_t *offs, uint32_t *pkey,
+int launch_emit_pairs(const FrameArgs &a, const int4 *draw, int64_t n, const uint32_t *offs, uint32_t *pkey,
                        uint32_t *pval, cudaStream_t s) {
-    if (n > 0) k_emit_pairs<<<grid_for(n), kThreads, 0, s>>>(a, draw, n, offs, pkey, pval);
+    if (n <= 0) return 0;
+    k_emit_pairs<<<grid_for(n), kThreads, 0, s>>>(a, draw, n, offs, pkey, pval);
+    return 1;
 }
 
-void launch_bin_bounds(const uint32_t *key, int64_t n, uint32_t *start, uint32_t *end, cudaStream_t s) {
-    if (n > 0) k_bin_bounds<<<grid_for(n), kThreads, 0, s>>>(key, n, start, end);
+int launch_bin_bounds(const uint32_t *key, int64_t n, uint32_t *start, uint32_t *end, cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_bin_bounds<<<grid_for(n), kThreads, 0, s>>>(key, n, start, end);
+    return 1;
 }
 
-void launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
+int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
                     const uint32_t *bstart, const uint32_t *bend, uint32_t *image, cudaStream_t s) {
     const bool ms = a.ms_output != 0, srgb = a.srgb != 0;
     if (a.S == 8) {
@@ -888,14 +1137,26 @@ void launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged
         else if (srgb) resolve_variant<32, false, true>(a, draw, merged, pval, bstart, bend, image, s);
         else resolve_variant<32, false, false>(a, draw, merged, pval, bstart, bend, image, s);
     }
+    return 1;
 }
 
-void launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s) {
-    if (n > 0) k_fill<<<grid_for(n), kThreads, 0, s>>>(image, n, value);
+int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cudaStream_t s) {
+    // non-negative floats up to and a little beyond 1.0, plus the negative zero
+    k_selftest_encode<<<4 * 152, 256, 0, s>>>(rt, 0u, 0x3F800100u, bad);
+    k_selftest_encode<<<1, 256, 0, s>>>(rt, 0x80000000u, 0x80000100u, bad);
+    return 2;
 }
 
-void launch_decode_keys(const uint64_t *skey, int64_t n, int nrows, int32_t *out, cudaStream_t s) {
-    if (n > 0) k_decode_keys<<<grid_for(n), kThreads, 0, s>>>(skey, n, nrows, out);
+int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_fill<<<grid_for(n), kThreads, 0, s>>>(image, n, value);
+    return 1;
+}
+
+int launch_decode_keys(const uint64_t *skey, int64_t n, int nrows, int32_t *out, cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_decode_keys<<<grid_for(n), kThreads, 0, s>>>(skey, n, nrows, out);
+    return 1;
 }
 
 }  // namespace spr

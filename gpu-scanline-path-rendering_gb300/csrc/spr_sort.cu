@@ -184,18 +184,22 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const K *__rest
 
 int64_t scan_tmp_words(int64_t n) { return (n + kScanTile - 1) / kScanTile + 2; }
 
-void scan_exclusive_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp, cudaStream_t s) {
+int scan_exclusive_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp, cudaStream_t s) {
     int64_t ntiles = (n + kScanTile - 1) / kScanTile;
     if (ntiles == 0) {
         cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
-        return;
+        return 0;
     }
     k_scan_reduce<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tmp);
     k_scan_tiles<<<1, 1024, 0, s>>>(tmp, ntiles);
     k_scan_down<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, out, n, tmp, ntiles);
+    return 3;
 }
 
-void scan_tiles_inplace(uint32_t *a, int64_t n, cudaStream_t s) { k_scan_tiles<<<1, 1024, 0, s>>>(a, n); }
+int scan_tiles_inplace(uint32_t *a, int64_t n, cudaStream_t s) {
+    k_scan_tiles<<<1, 1024, 0, s>>>(a, n);
+    return 1;
+}
 
 int64_t radix_tiles(int64_t n) { return (n + kRadixTile - 1) / kRadixTile; }
 
@@ -206,7 +210,8 @@ int64_t radix_tmp_words(int64_t n) {
 
 template <class K>
 bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_t n, int key_bits, uint32_t *tmp,
-                cudaStream_t s) {
+                cudaStream_t s, int *launches) {
+    *launches = 0;
     if (n <= 1) return false;
     const int64_t ntiles = radix_tiles(n);
     const int64_t c = 256 * ntiles;
@@ -220,7 +225,7 @@ bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_
         K *ko = alt ? keys : keys_alt;
         uint32_t *vo = alt ? vals : vals_alt;
         k_radix_hist<K><<<(unsigned)ntiles, kRadixThreads, 0, s>>>(ki, n, shift, counts, ntiles);
-        scan_exclusive_u32(counts, offsets, c, scan_tmp, s);
+        *launches += 2 + scan_exclusive_u32(counts, offsets, c, scan_tmp, s);
         k_radix_scatter<K><<<(unsigned)ntiles, kRadixThreads, 0, s>>>(ki, vi, n, shift, offsets, ntiles, ko, vo);
         alt = !alt;
     }
@@ -228,8 +233,8 @@ bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_
 }
 
 template bool radix_sort<uint64_t>(uint64_t *, uint32_t *, uint64_t *, uint32_t *, int64_t, int, uint32_t *,
-                                   cudaStream_t);
+                                   cudaStream_t, int *);
 template bool radix_sort<uint32_t>(uint32_t *, uint32_t *, uint32_t *, uint32_t *, int64_t, int, uint32_t *,
-                                   cudaStream_t);
+                                   cudaStream_t, int *);
 
 }  // namespace spr

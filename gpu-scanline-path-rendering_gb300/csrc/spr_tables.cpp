@@ -101,7 +101,7 @@ void build_resolve_tables(ResolveTables *t) {
     std::memset(t, 0, sizeof(*t));
     for (int k = 0; k < 256; ++k) {
         t->srgb_dec[k] = (float)s2l(k / 255.0);
-        t->lin_dec[k] = (float)(k / 255.0);
+        t->lin_dec[k] = (float)k * (1.f / 255.f);
     }
     for (int k = 0; k < 255; ++k) t->threshold[k] = (float)s2l((k + 0.5) / 255.0);
     t->threshold[255] = 2.f;

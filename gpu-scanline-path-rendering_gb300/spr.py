@@ -82,6 +82,11 @@ class ElementNumber(C.Structure):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
 
 
+class FrameStats(C.Structure):
+    _fields_ = [("kernel_launches", C.c_int32), ("host_syncs", C.c_int32),
+                ("resolve_pairs", C.c_int64), ("device_bytes", C.c_int64)]
+
+
 class SceneSpec(C.Structure):
     _fields_ = [("kind", C.c_int32), ("seed", C.c_uint64), ("width", C.c_int32),
                 ("height", C.c_int32), ("n_paths", C.c_int32), ("n_large", C.c_int32),
@@ -116,9 +121,11 @@ def lib() -> C.CDLL:
         L.spr_get_counts.argtypes = [vp, C.POINTER(ElementNumber)]
         L.spr_enable_step_timing.argtypes = [vp, i32]
         L.spr_step_timing.argtypes = [vp, C.POINTER(C.c_double), i32, C.POINTER(i32)]
+        L.spr_get_frame_stats.argtypes = [vp, C.POINTER(FrameStats)]
         L.spr_step_name.argtypes = [i32]
         L.spr_step_name.restype = C.c_char_p
         L.spr_debug_dump.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
+        L.spr_selftest.argtypes = [vp, C.POINTER(C.c_int64)]
         L.spr_status_string.argtypes = [i32]
         L.spr_status_string.restype = C.c_char_p
         L.spr_scene_generate.argtypes = [C.POINTER(SceneSpec), C.POINTER(vp)]
@@ -299,6 +306,16 @@ class VGRasterizer:
         n = C.c_int32()
         check(lib().spr_step_timing(self._h, buf, 64, C.byref(n)), "spr_step_timing")
         return {lib().spr_step_name(i).decode(): buf[i] for i in range(n.value)}
+
+    def frame_stats(self) -> dict:
+        st = FrameStats()
+        check(lib().spr_get_frame_stats(self._h, C.byref(st)), "spr_get_frame_stats")
+        return {n: int(getattr(st, n)) for n, _ in FrameStats._fields_}
+
+    def selftest(self) -> dict:
+        n = C.c_int64()
+        check(lib().spr_selftest(self._h, C.byref(n)), "spr_selftest")
+        return {"srgb_encode_mismatches": int(n.value)}
 
     def dump(self, stage) -> np.ndarray:
         sid = STAGE[stage] if isinstance(stage, str) else int(stage)

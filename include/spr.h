@@ -182,6 +182,14 @@ int spr_get_counts(spr_handle *h, spr_element_number *out);
  * spr_step_timing returns the per-stage milliseconds of the last frame. */
 int spr_enable_step_timing(spr_handle *h, int32_t enable);
 int spr_step_timing(spr_handle *h, double *ms, int32_t capacity, int32_t *n_out);
+/* Work statistics of the last spr_render. */
+typedef struct spr_frame_stats {
+    int32_t kernel_launches; /* CUDA kernels launched by the frame          */
+    int32_t host_syncs;      /* stream synchronizations inside the frame    */
+    int64_t resolve_pairs;   /* (draw item, 32-column tile) pairs resolved  */
+    int64_t device_bytes;    /* device memory held by the handle            */
+} spr_frame_stats;
+int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out);
 /* Name of step i of spr_step_timing (static string, NULL if out of range). */
 const char *spr_step_name(int32_t i);
 
@@ -208,6 +216,11 @@ enum spr_stage {
  * the size in bytes; nothing is copied if capacity is smaller. */
 int spr_debug_dump(spr_handle *h, int32_t stage, void *host_dst, size_t capacity,
                    size_t *needed);
+
+/* Device self-test of the resolve arithmetic: counts the float inputs in
+ * [0, 1] (and slightly beyond) whose closed-form-then-corrected sRGB encode
+ * differs from the threshold-table definition (expected 0). */
+int spr_selftest(spr_handle *h, int64_t *srgb_encode_mismatches);
 
 /* Human-readable text for a status code (static string). */
 const char *spr_status_string(int32_t status);

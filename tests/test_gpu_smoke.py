@@ -12,3 +12,8 @@ def test_smoke():
     import __graft_entry__
 
     __graft_entry__.smoke()
+
+
+def test_srgb_encode_selftest():
+    with spr.VGRasterizer(64, 64, samples=8) as r:
+        assert r.selftest()["srgb_encode_mismatches"] == 0
