@@ -730,23 +730,18 @@ struct BinState {
     uint32_t emask[CAP][64];
     uint32_t ecol[CAP][64];
     uint8_t cnt[64];
-    unsigned long long bm[32];  // pixel bitmap of each staged item
+    uint32_t cm[32];  // column mask of each staged item
     int4 it[32];
     uint4 mm[32];
+    uint32_t task[64];  // packed (pixel, entry, item) blend tasks of one chunk
+    uint32_t tres[64];  // their results
 };
 
-__device__ __forceinline__ unsigned long long span_bits(int c0, int c1, int rows) {
-    if (c1 <= c0) return 0ull;
+// Columns [c0, c1) of a bin as a bit mask.
+__device__ __forceinline__ uint32_t col_bits(int c0, int c1) {
+    if (c1 <= c0) return 0u;
     const uint32_t hi = c1 >= 32 ? 0xFFFFFFFFu : ((1u << c1) - 1u);
-    const uint32_t r = hi & ~((1u << c0) - 1u);
-    return (unsigned long long)r | (rows > 1 ? ((unsigned long long)r << 32) : 0ull);
-}
-
-// Index of the r-th set bit of a 64-bit word.
-__device__ __forceinline__ int nth_set_bit64(unsigned long long m, int r) {
-    const uint32_t lo = (uint32_t)m;
-    const int c = __popc(lo);
-    return r < c ? nth_set_bit(lo, r) : 32 + nth_set_bit((uint32_t)(m >> 32), r - c);
+    return hi & ~((1u << c0) - 1u);
 }
 
 template <int CAP>
@@ -815,10 +810,11 @@ __device__ __forceinline__ void dedup(BinState<CAP> &w, int p) {
     w.cnt[p] = (uint8_t)n;
 }
 
-// One warp per bin of (cell row, 32 pixel columns).  Items (merged fragments
-// and spans, in draw-list order) are taken in batches whose pixel sets are
-// pairwise disjoint, so each batch is applied with one lane per covered
-// pixel and no ordering conflicts; then every pixel is averaged over its
+// One warp per bin of (cell row, 32 pixel columns), lane = column (both pixel
+// rows).  Every item covers both rows of its columns, so items (merged
+// fragments and spans, in draw-list order) are taken in batches whose column
+// sets are pairwise disjoint and each batch is applied in one step, each
+// lane updating its own two pixels; then every pixel is averaged over its
 // samples with an exact fixed-point sum.
 template <int S, bool MS, bool SRGB>
 __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
@@ -865,106 +861,170 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
             const int4 it = draw[pval[base + lane]];
             w.it[lane] = it;
             const int x = (int)((uint32_t)it.x & 0xFFFFu) - tx0;
-            unsigned long long bm;
+            uint32_t cm;
             if (it.w != 0) {
                 if constexpr (MW == 4)
                     w.mm[lane] = __ldg(reinterpret_cast<const uint4 *>(merged) + (it.w - 1));
                 else
                     w.mm[lane] = make_uint4(__ldg(merged + (it.w - 1)), 0u, 0u, 0u);
-                bm = span_bits(max(x, 0), min(x + 2, cols), rows);
+                cm = col_bits(max(x, 0), min(x + 2, cols));
             } else {
-                bm = span_bits(max(x, 0), min(x + it.y, cols), rows);
+                cm = col_bits(max(x, 0), min(x + it.y, cols));
             }
-            w.bm[lane] = bm;
+            w.cm[lane] = cm;
         }
         __syncwarp();
         int q0 = 0;
         while (q0 < cnt) {
-            // batch [q0, q1): items with pairwise disjoint pixel sets
-            unsigned long long acc = 0ull;
+            // batch [q0, q1): items with pairwise disjoint column sets; lane =
+            // column, owning pixels p0 = lane and p1 = 32 + lane
+            uint32_t acc = 0u;
             int q1 = q0;
-            while (q1 < cnt && (acc & w.bm[q1]) == 0ull) acc |= w.bm[q1++];
-            const int npix = __popcll(acc);
-            for (int r = lane; r < npix; r += 32) {
-                const int p = nth_set_bit64(acc, r);
-                int q = q0;
-                while (!((w.bm[q] >> p) & 1ull)) ++q;
+            while (q1 < cnt && (acc & w.cm[q1]) == 0u) acc |= w.cm[q1++];
+            int q = -1;
+            uint32_t msk[2] = {0u, 0u};  // sample mask per row (ALL for spans)
+            int n0[2] = {0, 0};          // entry counts before this batch
+            bool frag = false;
+            if ((acc >> lane) & 1u) {
+                q = q0;
+                while (!((w.cm[q] >> lane) & 1u)) ++q;
                 const int4 it = w.it[q];
-                const uint32_t c = (uint32_t)it.z;
-                const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
-                            sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
-                const float sa = lin8(c >> 24);
-                int n = w.cnt[p];
-                if (it.w != 0) {
-                    // merged fragment: this pixel's sample mask
-                    const int k = ((p & 31) + tx0 - (int)((uint32_t)it.x & 0xFFFFu)) * 2 + (p >> 5);
-                    const uint4 mm = w.mm[q];
-                    uint32_t m;
-                    if constexpr (MW == 4)
-                        m = k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w));
-                    else
-                        m = (mm.x >> (8 * k)) & 0xFFu;
-                    if (m == 0u) continue;
-                    if constexpr (!MS) {
-                        const float aa = sa * ((float)__popc(m) / (float)S);
-                        w.ecol[0][p] = blend_sample<SRGB>(T, lane, w.ecol[0][p], sr, sg, sb, aa, 1.f - aa);
-                        continue;
-                    } else {
-                        const float om = 1.f - sa;
-                        if (n != kFull) {
-                            int splits = 0;
-                            for (int j = 0; j < n; ++j) {
-                                const uint32_t em = w.emask[j][p];
-                                splits += ((em & m) != 0u && (em & ~m) != 0u) ? 1 : 0;
-                            }
-                            if (n + splits > CAP) {
-                                to_full(w, p);
-                                n = kFull;
-                            }
+                frag = it.w != 0;
+                const int dx = lane + tx0 - (int)((uint32_t)it.x & 0xFFFFu);
+                const uint4 mm = w.mm[q];
+#pragma unroll
+                for (int py = 0; py < 2; ++py) {
+                    if (py >= rows) break;
+                    const int p = py * 32 + lane;
+                    uint32_t m = ALL;
+                    if (frag) {
+                        const int k = dx * 2 + py;
+                        if constexpr (MW == 4)
+                            m = k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w));
+                        else
+                            m = (mm.x >> (8 * k)) & 0xFFu;
+                        if constexpr (!MS) m = m ? ALL : 0u;
+                    }
+                    msk[py] = m;
+                    int n = w.cnt[p];
+                    if (m != 0u && n != kFull && frag && MS) {
+                        int splits = 0;
+                        for (int j = 0; j < n; ++j) {
+                            const uint32_t em = w.emask[j][p];
+                            splits += ((em & m) != 0u && (em & ~m) != 0u) ? 1 : 0;
                         }
-                        if (n == kFull) {
-                            if constexpr (CAP == 16) {
-                                for (uint32_t mk = m; mk; mk &= mk - 1u) {
-                                    uint32_t &v = full_sample(w, p, __ffs(mk) - 1);
-                                    v = blend_sample<SRGB>(T, lane, v, sr, sg, sb, sa, om);
-                                }
-                                try_compress(w, p);
-                            }
-                        } else {
-                            int nn = n;
-                            for (int j = 0; j < n; ++j) {
-                                const uint32_t em = w.emask[j][p];
-                                const uint32_t in = em & m;
-                                if (!in) continue;
-                                const uint32_t nc = blend_sample<SRGB>(T, lane, w.ecol[j][p], sr, sg, sb, sa, om);
+                        if (n + splits > CAP) {
+                            to_full(w, p);
+                            n = kFull;
+                        }
+                    }
+                    n0[py] = n;
+                }
+            }
+            // phase A: the entries of this lane's pixels that the batch blends
+            // (a snapshot: splits below rewrite entry masks)
+            uint32_t tj[2] = {0u, 0u};
+#pragma unroll
+            for (int py = 0; py < 2; ++py) {
+                if (msk[py] == 0u || n0[py] == kFull) continue;
+                const int p = py * 32 + lane;
+                for (int j = 0; j < n0[py]; ++j) tj[py] |= (w.emask[j][p] & msk[py]) != 0u ? (1u << j) : 0u;
+            }
+            const int ntask = __popc(tj[0]) + __popc(tj[1]);
+            int off = ntask;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, off, o);
+                if (lane >= o) off += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, off, 31);
+            off -= ntask;
+            for (int cb = 0; cb < total; cb += 64) {
+                const int ce = min(cb + 64, total);
+                // write this lane's tasks that fall in [cb, ce)
+                if (off < ce && off + ntask > cb) {
+                    int t = off;
+#pragma unroll
+                    for (int py = 0; py < 2; ++py) {
+                        const int p = py * 32 + lane;
+                        for (uint32_t bits = tj[py]; bits; bits &= bits - 1u) {
+                            const int j = __ffs(bits) - 1;
+                            if (t >= cb && t < ce) w.task[t - cb] = (uint32_t)p | ((uint32_t)j << 6) | ((uint32_t)q << 11);
+                            ++t;
+                        }
+                    }
+                }
+                __syncwarp();
+                // phase B: all lanes blend
+                for (int t = lane; t < ce - cb; t += 32) {
+                    const uint32_t tk = w.task[t];
+                    const int p = (int)(tk & 63u), j = (int)((tk >> 6) & 31u), tq = (int)(tk >> 11);
+                    const int4 it = w.it[tq];
+                    const uint32_t c = (uint32_t)it.z;
+                    const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
+                                sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
+                    float sa = lin8(c >> 24);
+                    if constexpr (!MS) {
+                        if (it.w != 0) {
+                            const int k = ((p & 31) + tx0 - (int)((uint32_t)it.x & 0xFFFFu)) * 2 + (p >> 5);
+                            const uint4 mm = w.mm[tq];
+                            const uint32_t m = MW == 4 ? (k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w)))
+                                                       : ((mm.x >> (8 * k)) & 0xFFu);
+                            sa = sa * ((float)__popc(m) / (float)S);
+                        }
+                    }
+                    w.tres[t] = blend_sample<SRGB>(T, lane, w.ecol[j][p], sr, sg, sb, sa, 1.f - sa);
+                }
+                __syncwarp();
+                // phase C: owners apply their results
+                if (off < ce && off + ntask > cb) {
+                    int t = off;
+#pragma unroll
+                    for (int py = 0; py < 2; ++py) {
+                        const int p = py * 32 + lane;
+                        const uint32_t m = msk[py];
+                        for (uint32_t bits = tj[py]; bits; bits &= bits - 1u) {
+                            const int j = __ffs(bits) - 1;
+                            const uint32_t em = w.emask[j][p];
+                            const uint32_t in = em & m;
+                            if (t >= cb && t < ce) {
+                                const uint32_t nc = w.tres[t - cb];
                                 if (in == em) {
                                     w.ecol[j][p] = nc;
                                 } else {
+                                    const int nn = w.cnt[p];
                                     w.emask[j][p] = em & ~m;
                                     w.emask[nn][p] = in;
                                     w.ecol[nn][p] = nc;
-                                    ++nn;
+                                    w.cnt[p] = (uint8_t)(nn + 1);
                                 }
                             }
-                            w.cnt[p] = (uint8_t)nn;
-                            dedup(w, p);
+                            ++t;
                         }
                     }
-                } else {
-                    // span: every sample of the pixel
-                    const float om = 1.f - sa;
-                    if (n == kFull) {
+                }
+                __syncwarp();
+            }
+            // explicit-sample pixels (rare), then merge equal colours
+            if (q >= 0) {
+#pragma unroll
+                for (int py = 0; py < 2; ++py) {
+                    if (msk[py] == 0u) continue;
+                    const int p = py * 32 + lane;
+                    if (n0[py] == kFull) {
                         if constexpr (CAP == 16) {
-                            for (int smp = 0; smp < 32; ++smp) {
-                                uint32_t &v = full_sample(w, p, smp);
+                            const uint32_t c = (uint32_t)w.it[q].z;
+                            const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
+                                        sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
+                            const float sa = lin8(c >> 24), om = 1.f - sa;
+                            for (uint32_t mk = msk[py]; mk; mk &= mk - 1u) {
+                                uint32_t &v = full_sample(w, p, __ffs(mk) - 1);
                                 v = blend_sample<SRGB>(T, lane, v, sr, sg, sb, sa, om);
                             }
                             try_compress(w, p);
                         }
-                    } else {
-                        for (int j = 0; j < n; ++j)
-                            w.ecol[j][p] = blend_sample<SRGB>(T, lane, w.ecol[j][p], sr, sg, sb, sa, om);
-                        if (n > 1) dedup(w, p);
+                    } else if (w.cnt[p] > 1) {
+                        dedup(w, p);
                     }
                 }
             }
