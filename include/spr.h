@@ -222,6 +222,30 @@ int spr_debug_dump(spr_handle *h, int32_t stage, void *host_dst, size_t capacity
  * differs from the threshold-table definition (expected 0). */
 int spr_selftest(spr_handle *h, int64_t *srgb_encode_mismatches);
 
+/*
+ * Allocation-free exclusive scan.  No counterpart in the reference: it is an
+ * extra entry point for callers that cannot allocate device memory, such as
+ * plugin hosts that hand out all device memory from their own pools and
+ * real-time loops that must not call cudaMalloc / cudaFree (those calls can
+ * block on or synchronize the whole device).
+ *
+ * Writes d_offsets[i] = d_counts[0] + ... + d_counts[i-1] for i in [0, n]
+ * (d_offsets holds n + 1 values; d_offsets[n] is the total), the scan that
+ * turns per-curve intersection counts into entry offsets.  Both pointers are
+ * device memory owned by the caller; the work is enqueued on `stream` (a
+ * cudaStream_t, NULL = legacy default stream) on the current device.
+ *
+ * Its scratch is a fixed 64 KB array compiled into the library, which every
+ * GPU that loads the library holds until the process exits.  Limit:
+ * n <= 33,554,432 (16384 tiles of 2048 counts); larger n returns
+ * SPR_ERR_CAPACITY_EXCEEDED and launches nothing.  The first call on each
+ * device looks up the array's device address with that device current; make
+ * that first call before any stream capture.  All calls on a device share
+ * the one array, so calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialized by the caller.
+ */
+int spr_scan_offsets_noalloc(const uint32_t *d_counts, uint32_t *d_offsets, int64_t n, void *stream);
+
 /* Human-readable text for a status code (static string). */
 const char *spr_status_string(int32_t status);
 
