@@ -322,6 +322,8 @@ int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     return SPR_OK;
 }
 
+int spr_validate_scene(const spr_scene_view *scene) { return validate_scene(scene); }
+
 int spr_set_transform(spr_handle *h, const float m[16]) {
     if (!h || !m) return SPR_ERR_INVALID_ARG;
     std::memcpy(h->m, m, sizeof(h->m));

@@ -646,24 +646,6 @@ struct SmemTables {
 
 __device__ __forceinline__ float lin8(uint32_t k) { return (float)k * (1.f / 255.f); }
 
-// Position of the r-th (0-based) set bit of m; requires r < popc(m).
-__device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
-    int pos = 0;
-#pragma unroll
-    for (int w = 16; w >= 1; w >>= 1) {
-        const uint32_t lo = m & ((1u << w) - 1u);
-        const int c = __popc(lo);
-        if (r >= c) {
-            r -= c;
-            m >>= w;
-            pos += w;
-        } else {
-            m = lo;
-        }
-    }
-    return pos;
-}
-
 // Blend results are finite and never -0 (products and sums of non-negative
 // values), so the hardware min/max give the same clamp as fmin_r/fmax_r.
 __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.f), 1.f); }

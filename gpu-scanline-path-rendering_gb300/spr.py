@@ -114,6 +114,7 @@ def lib() -> C.CDLL:
         L.spr_enable_srgb_correction.argtypes = [vp, i32]
         L.spr_set_scene.argtypes = [vp, C.POINTER(SceneView)]
         L.spr_set_transform.argtypes = [vp, C.POINTER(C.c_float)]
+        L.spr_validate_scene.argtypes = [C.POINTER(SceneView)]
         L.spr_render.argtypes = [vp, vp]
         L.spr_image_device_ptr.argtypes = [vp, C.POINTER(vp)]
         L.spr_read_image.argtypes = [vp, vp, vp]
@@ -187,6 +188,11 @@ class Scene:
                          _ptr(self.curve_type), _ptr(self.curve_path_id), _ptr(self.curve_arc_w),
                          _ptr(self.path_fill_rule), _ptr(self.path_fill_rgba),
                          _ptr(self.path_affine))
+
+    def validate(self) -> int:
+        """Host-side scene checks of spr_set_scene; returns the status code."""
+        v = self.view()
+        return lib().spr_validate_scene(C.byref(v))
 
     def copy(self) -> "Scene":
         return Scene(*[None if getattr(self, f) is None else getattr(self, f).copy()

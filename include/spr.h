@@ -150,6 +150,12 @@ int spr_enable_srgb_correction(spr_handle *h, int32_t enable);
  * the device.  The host arrays are not referenced after the call returns. */
 int spr_set_scene(spr_handle *h, const spr_scene_view *scene);
 
+/* The checks spr_set_scene makes, on the host only (no device needed):
+ * curve types, control-point ranges, path ids in range and non-decreasing
+ * along the curves, vertex path ids in range.  Returns SPR_OK,
+ * SPR_ERR_INVALID_ARG (missing array) or SPR_ERR_INVALID_SCENE. */
+int spr_validate_scene(const spr_scene_view *scene);
+
 /* setInputTransform (ras_base.cpp:576-583): a row-major 4x4 matrix applied to
  * (x, y, 0, 1) followed by the reference's perspective fold (cu:36-105). */
 int spr_set_transform(spr_handle *h, const float m[16]);

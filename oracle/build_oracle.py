@@ -58,7 +58,8 @@ def build_ref(force=False):
     outdir = HERE / "_ref"
     outdir.mkdir(exist_ok=True)
     out = outdir / "libref.so"
-    srcs = [HERE / "ref" / "ref_driver.cpp", HERE / "ref" / "ref_shim.h"]
+    srcs = [HERE / "ref" / "ref_driver.cpp", HERE / "ref" / "ref_shim.h",
+            HERE / "ref" / "shim_include" / "mochimazui" / "glpp.h"]
     if force or _stale(out, srcs):
         cuda_inc = "/usr/local/cuda/include"
         _run([CXX, *FLAGS, "-w", "-I", str(HERE / "ref" / "shim_include"), "-I", str(HERE / "ref"),

@@ -52,6 +52,7 @@ def lib() -> C.CDLL:
         L.orc_fetch_pixel_table.argtypes = [C.c_int32, f, f, f, f, vp]
         L.orc_vertical_mask.argtypes = [C.c_int32, f, vp]
         L.orc_vertical_mask2.argtypes = [C.c_int32, f, f, vp]
+        L.orc_fetch_table_selftest.argtypes = [C.c_int32, C.c_int32, vp]
         _lib = L
     return _lib
 
@@ -71,6 +72,7 @@ def ref() -> C.CDLL:
         L.ref_fetch_pixel_table.argtypes = [i32, vp, f, f, f, f, vp]
         L.ref_vertical_mask.argtypes = [i32, f, vp]
         L.ref_vertical_mask2.argtypes = [i32, f, f, vp]
+        L.ref_sample_positions.argtypes = [i32, vp]
         _ref = L
     return _ref
 
@@ -174,6 +176,12 @@ def fetch_pixel_table(samples, p0, p1) -> np.ndarray:
     return out
 
 
+def fetch_table_selftest(samples, res=33) -> np.ndarray:
+    hist = np.zeros(33, np.int64)
+    lib().orc_fetch_table_selftest(samples, res, hist.ctypes.data)
+    return hist
+
+
 def vertical_mask(samples, y) -> np.ndarray:
     out = np.zeros(samples // 8, np.uint32)
     lib().orc_vertical_mask(samples, y, out.ctypes.data)
@@ -207,6 +215,13 @@ def ref_intersections(scene: "spr.Scene", tvertex: np.ndarray, visible: np.ndarr
     entries = np.zeros((max(nf, 1), 2), np.int32)
     L.ref_emit(*args, offs.ctypes.data, tcut.ctypes.data, ncut.ctypes.data, nf, entries.ctypes.data)
     return counts, entries[:nf]
+
+
+def ref_sample_positions(samples) -> np.ndarray:
+    """Pixel sample pattern from the reference's vg_sample_position."""
+    out = np.zeros((samples, 2), np.float32)
+    ref().ref_sample_positions(samples, out.ctypes.data)
+    return out
 
 
 def ref_mask_table(samples8_cell: np.ndarray, samples32_cell: np.ndarray):

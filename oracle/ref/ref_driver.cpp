@@ -1,8 +1,9 @@
 // ref_driver.cpp -- host driver around the reference's own device code,
 // compiled in place from the reference tree (see build_oracle.py): the
-// intersection kernels of ras_cut.h (k_make_intersection_0/1) and the mask
+// intersection kernels of ras_cut.h (k_make_intersection_0/1), the mask
 // helpers of ras_qm_mask.h (makeTable, fetchPixelTable, fetchVerticalTable,
-// fetchVerticalTable2).  Each "kernel launch" is a loop that sets blockIdx.x
+// fetchVerticalTable2) and the sample pattern of ras_qm_mask.cu
+// (vg_sample_position).  Each "kernel launch" is a loop that sets blockIdx.x
 // and calls the kernel body once per thread index.
 //
 // TEST INFRASTRUCTURE ONLY: the result is a cross-check of the oracle and is
@@ -29,6 +30,7 @@ RefDim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1}, gridD
 #define LAUNCH(kernel, N, NT, args) ((void)0)
 #include "ras_cut.h"
 #include "ras_qm_mask.h"
+#include "ras_qm_mask.cu"  // vg_sample_position; its GL query is stubbed
 
 using namespace Mochimazui;
 
@@ -104,6 +106,16 @@ int ref_fetch_pixel_table(int samples, const int32_t *table, float p0x, float p0
     out4[2] = r.z;
     out4[3] = r.w;
     return 0;
+}
+
+// vg_sample_position (ras_qm_mask.cu:118-175): the pixel sample pattern.
+int ref_sample_positions(int samples, float *out_xy) {
+    std::vector<float2> v = QM_Mask_Sample_Position::vg_sample_position(samples);
+    for (size_t i = 0; i < v.size(); ++i) {
+        out_xy[2 * i] = v[i].x;
+        out_xy[2 * i + 1] = v[i].y;
+    }
+    return (int)v.size();
 }
 
 int ref_vertical_mask(int samples, float y, int32_t *out4) {

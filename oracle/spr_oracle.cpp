@@ -1350,6 +1350,51 @@ extern "C" int orc_fetch_pixel_table(int32_t samples, float p0x, float p0y, floa
     return SPR_OK;
 }
 
+// testFetchTable_8 / _32 (ras_qm_mask.h:601-713, disabled in the reference):
+// every segment between two points of a res x res lattice of the unit cell
+// (P0.y != P1.y), table fetch against the exact "sample right of segment"
+// test; hist[k] counts segments whose worst pixel word differs in k bits.
+extern "C" int orc_fetch_table_selftest(int32_t samples, int32_t res, int64_t *hist33) {
+    if ((samples != 8 && samples != 32) || res < 2 || !hist33) return SPR_ERR_INVALID_ARG;
+    std::vector<uint32_t> t = build_mask_table(samples);
+    std::vector<F2> cs = cell_samples(samples);
+    const int words = samples / 8;
+    for (int i = 0; i < 33; ++i) hist33[i] = 0;
+    const float step = 1.f / (res - 1.f);
+    for (int p1 = 0; p1 < res * res; ++p1)
+        for (int p0 = 0; p0 < res * res; ++p0) {
+            const int y0 = p0 / res, x0 = p0 - y0 * res, y1 = p1 / res, x1 = p1 - y1 * res;
+            if (y0 == y1) continue;
+            F2 P0{step * (float)x0, step * (float)y0}, P1{step * (float)x1, step * (float)y1};
+            uint32_t got[4];
+            fetch_pixel_table(t.data(), words, P0, P1, got);
+            int worst = 0;
+            if (samples == 8) {
+                uint32_t acc = 0;
+                for (int j = 0; j < 4; ++j) {
+                    uint32_t d = 0;
+                    for (int k = 0; k < 8; ++k) {
+                        F2 P = cs[j * 8 + k];
+                        if (P.x > (P.y - P0.y) / (P1.y - P0.y) * (P1.x - P0.x) + P0.x) d |= 1u << k;
+                    }
+                    acc |= d << (8 * j);
+                }
+                worst = __builtin_popcount(got[0] ^ acc);
+            } else {
+                for (int j = 0; j < 4; ++j) {
+                    uint32_t d = 0;
+                    for (int k = 0; k < 32; ++k) {
+                        F2 P = cs[j * 32 + k];
+                        if (P.x > (P.y - P0.y) / (P1.y - P0.y) * (P1.x - P0.x) + P0.x) d |= 1u << k;
+                    }
+                    worst = std::max(worst, __builtin_popcount(got[j] ^ d));
+                }
+            }
+            hist33[worst]++;
+        }
+    return SPR_OK;
+}
+
 extern "C" int orc_vertical_mask(int32_t samples, float y, uint32_t *out_words) {
     if ((samples != 8 && samples != 32) || !out_words) return SPR_ERR_INVALID_ARG;
     uint32_t tmp[4];

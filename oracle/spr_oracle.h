@@ -53,6 +53,9 @@ int orc_srgb_tables(float *decode256, float *thresholds255, uint8_t *bins4096);
 int orc_fetch_pixel_table(int32_t samples, float p0x, float p0y, float p1x, float p1y,
                           uint32_t *out_words);
 int orc_vertical_mask(int32_t samples, float y, uint32_t *out_words);
+/* The reference's table self-test over a res x res lattice; hist33[k] =
+ * number of segments whose worst 32-bit word differs in k bits. */
+int orc_fetch_table_selftest(int32_t samples, int32_t res, int64_t *hist33);
 int orc_vertical_mask2(int32_t samples, float y0, float y1, uint32_t *out_words);
 
 #ifdef __cplusplus

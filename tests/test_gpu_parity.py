@@ -1,0 +1,234 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Integer and bit-pattern stages must match exactly: intersection counts and
+entries, cell keys, path ids with winding changes, scanline winding numbers,
+boundary sample masks, the sort permutation, scanned winding numbers, merged
+sample masks and the draw list.  The RGBA8 image is allowed +-1 per channel
+(the resolve arithmetic is identical on both sides, so in practice it is
+exact and the tests report the maximum difference).
+"""
+import pathlib
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+import oracle
+import spr
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+EXACT = ["TVERTEX", "PATH_VISIBLE", "CURVE_COUNT", "INTERSECTION", "FRAG_KEY", "FRAG_PID", "FRAG_WN",
+         "FRAG_MASK", "SORT_PERM", "SORT_KEY", "WN_SCAN", "MERGED_MASK", "DRAW_LIST"]
+IMAGE_TOL = 1  # RGBA8 per-channel tolerance
+
+
+def render(scene, W, H, samples=8, ms=True, srgb=True, transform=None):
+    r = spr.VGRasterizer(W, H, samples=samples, ms_output=ms, srgb=srgb)
+    if transform is not None:
+        r.set_input_transform(transform)
+    r.add_vg(scene)
+    r.rasterize()
+    return r
+
+
+def check_parity(scene, W, H, samples=8, ms=True, srgb=True, transform=None):
+    ref = oracle.run(scene, W, H, samples=samples, ms_output=ms, srgb=srgb, transform=transform)
+    with render(scene, W, H, samples, ms, srgb, transform) as r:
+        assert r.element_number() == ref.counts
+        for st in EXACT:
+            got, exp = r.dump(st), ref[st]
+            assert got.shape == exp.shape, st
+            assert np.array_equal(got.view(np.uint8), exp.view(np.uint8)), st
+        img = r.read_image()
+        diff = np.abs(img.astype(np.int16) - ref["IMAGE"].reshape(H, W, 4).astype(np.int16)).max()
+        assert diff <= IMAGE_TOL
+        return ref.counts, int(diff)
+
+
+def load_golden(name):
+    d = np.load(GOLDEN / f"scene_{name}.npz")
+    fields = {f: d[f] for f in spr.Scene.FIELDS if f in d.files}
+    tf = d["transform"] if bool(d["has_transform"]) else None
+    return spr.Scene(**fields), int(d["width"]), int(d["height"]), tf, d["ref_counts"], d["ref_entries"]
+
+
+@pytest.mark.parametrize("name", ["random", "cubics", "mixed", "oddsize", "handmade"])
+@pytest.mark.parametrize("samples", [8, 32])
+def test_golden_scenes(name, samples):
+    scene, W, H, tf, counts, entries = load_golden(name)
+    check_parity(scene, W, H, samples=samples, transform=tf)
+    with render(scene, W, H, samples, transform=tf) as r:  # against the reference's own kernels
+        assert np.array_equal(r.dump("CURVE_COUNT"), counts)
+        assert np.array_equal(r.dump("INTERSECTION").reshape(-1, 2), entries)
+
+
+@pytest.mark.parametrize("samples", [8, 32])
+@pytest.mark.parametrize("ms", [True, False])
+@pytest.mark.parametrize("srgb", [True, False])
+def test_mode_matrix(samples, ms, srgb):
+    scene = spr.Scene.generate(spr.SCENE_RANDOM, seed=21, width=256, height=192, n_paths=24, seg_min=6,
+                               seg_max=20, with_rational=True)
+    check_parity(scene, 256, 192, samples, ms, srgb)
+
+
+@pytest.mark.parametrize("kind,size,n,nl", [(spr.SCENE_RANDOM, 512, 64, 0), (spr.SCENE_MIXED, 768, 900, 60),
+                                            (spr.SCENE_CUBICS, 640, 48, 0)])
+def test_scene_families(kind, size, n, nl):
+    scene = spr.Scene.generate(kind, seed=31, width=size, height=size, n_paths=n, n_large=nl,
+                               seg_min=8 if kind != spr.SCENE_CUBICS else 16,
+                               seg_max=32 if kind != spr.SCENE_CUBICS else 64, with_rational=True,
+                               with_affine=kind == spr.SCENE_MIXED)
+    check_parity(scene, size, size, samples=32)
+
+
+def test_transforms():
+    scene = spr.Scene.generate(spr.SCENE_MIXED, seed=41, width=400, height=300, n_paths=200, n_large=10,
+                               with_affine=True)
+    a = np.float32(0.4)
+    rot = np.array([[np.cos(a) * 1.3, -np.sin(a), 0, 40], [np.sin(a), np.cos(a) * 0.8, 0, -30], [0, 0, 1, 0],
+                    [0.0003, -0.0002, 0, 1]], np.float32)
+    check_parity(scene, 400, 300, samples=8, transform=rot)
+    zoom = np.diag([3.0, 3.0, 1.0, 1.0]).astype(np.float32)
+    zoom[0, 3], zoom[1, 3] = -300, -250
+    check_parity(scene, 400, 300, samples=32, transform=zoom)
+
+
+@pytest.mark.parametrize("W,H", [(1, 1), (3, 5), (4096, 8), (8, 4096), (257, 129)])
+def test_sizes(W, H):
+    scene = spr.Scene.generate(spr.SCENE_RANDOM, seed=51, width=W, height=H, n_paths=6, seg_min=3, seg_max=8)
+    check_parity(scene, W, H, samples=8)
+
+
+def test_empty_and_invisible_scenes():
+    empty = spr.Scene(np.zeros((0, 2), np.float32), [], [], [], [], [], [], [])
+    with render(empty, 64, 48) as r:
+        assert r.element_number()["curve_fragment"] == 0
+        assert np.all(r.read_image() == 255)
+    far = spr.Scene.generate(spr.SCENE_RANDOM, seed=52, width=100, height=100, n_paths=5, seg_min=3, seg_max=6)
+    far.vertex[:, 0] += 5000.0
+    counts, _ = check_parity(far, 100, 100, samples=8)
+    assert counts["curve_fragment"] == 0
+
+
+def test_huge_coordinates_and_degenerate_curves():
+    s = spr.Scene.generate(spr.SCENE_RANDOM, seed=53, width=200, height=200, n_paths=10, seg_min=4, seg_max=10)
+    s.vertex[s.vertex_path_id == 1] *= 1.0e4
+    s.vertex[s.vertex_path_id == 2] = s.vertex[s.vertex_path_id == 2][0]  # every point equal
+    s.vertex[s.vertex_path_id == 3] = np.round(s.vertex[s.vertex_path_id == 3])  # on the pixel grid
+    check_parity(s, 200, 200, samples=32)
+
+
+def test_errors_leave_the_handle_usable():
+    s = spr.Scene.generate(spr.SCENE_RANDOM, seed=54, width=64, height=64, n_paths=4, seg_min=3, seg_max=5)
+    with spr.VGRasterizer(64, 64, samples=8) as r:
+        with pytest.raises(spr.SprError) as e:
+            r.rasterize()
+        assert e.value.status == spr.ERR_NO_SCENE
+        with pytest.raises(spr.SprError) as e:
+            r.dump("IMAGE")
+        assert e.value.status == spr.ERR_NO_SCENE
+        bad = s.copy()
+        bad.curve_type[0] = 9
+        with pytest.raises(spr.SprError) as e:
+            r.add_vg(bad)
+        assert e.value.status == spr.ERR_INVALID_SCENE
+        with pytest.raises(spr.SprError):
+            r.resize_output_buffer(0, 10)
+        r.add_vg(s)
+        r.rasterize()
+        assert r.element_number()["curve_fragment"] > 0
+
+
+def test_determinism_resize_and_samples():
+    s = spr.Scene.generate(spr.SCENE_MIXED, seed=55, width=300, height=300, n_paths=150, n_large=8,
+                           with_affine=True)
+    with render(s, 300, 300, samples=32) as r:
+        a = r.read_image().copy()
+        r.rasterize()
+        assert np.array_equal(a, r.read_image())
+        r.set_samples(8)
+        r.rasterize()
+        ref8 = oracle.run(s, 300, 300, samples=8)
+        assert np.array_equal(r.read_image().reshape(-1), ref8["IMAGE"])
+        r.resize_output_buffer(160, 120)
+        r.rasterize()
+        ref = oracle.run(s, 160, 120, samples=8)
+        assert np.array_equal(r.read_image().reshape(-1), ref["IMAGE"])
+        assert np.array_equal(r.dump("MERGED_MASK"), ref["MERGED_MASK"])
+
+
+def _read_png(path):
+    data = pathlib.Path(path).read_bytes()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, w = 8, b"", 0
+    while pos < len(data):
+        n, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        crc = struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0]
+        assert crc == zlib.crc32(typ + body) & 0xFFFFFFFF
+        if typ == b"IHDR":
+            w, h = struct.unpack(">II", body[:8])
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + n
+    raw = zlib.decompress(idat)
+    rows = [raw[y * (4 * w + 1) + 1:(y + 1) * (4 * w + 1)] for y in range(h)]
+    return np.frombuffer(b"".join(rows), np.uint8).reshape(h, w, 4)
+
+
+def test_save_png_flips_and_forces_alpha(tmp_path):
+    s = spr.Scene.generate(spr.SCENE_RANDOM, seed=56, width=90, height=70, n_paths=8, seg_min=3, seg_max=9)
+    with render(s, 90, 70) as r:
+        img = r.read_image()
+        r.save_output_to_file(tmp_path / "out.png")
+    png = _read_png(tmp_path / "out.png")
+    exp = img[::-1].copy()
+    exp[..., 3] = 255
+    assert np.array_equal(png, exp)
+
+
+def test_step_timing_and_stats():
+    s = spr.Scene.generate(spr.SCENE_RANDOM, seed=57, width=256, height=256, n_paths=20, seg_min=5, seg_max=12)
+    with spr.VGRasterizer(256, 256, samples=8) as r:
+        r.add_vg(s)
+        r.enable_step_timing(True)
+        r.rasterize()
+        t = r.step_timing()
+        assert set(t) >= {"transform", "sort", "resolve"} and all(v >= 0 for v in t.values())
+        st = r.frame_stats()
+        assert st["kernel_launches"] > 10 and st["host_syncs"] == 3 and st["device_bytes"] > 0
+
+
+def test_benchmark_scene_band():
+    """A 2048x256 band of the benchmark scene (all 20,000 paths), exact."""
+    import bench
+
+    scene = bench.make_scene()
+    y0, bh = bench.BAND
+    counts, diff = check_parity(scene, 2048, bh, samples=32, transform=bench.band_transform(y0))
+    assert counts["curve_fragment"] > 100000 and diff == 0
+
+
+def test_benchmark_scene_full_frame_invariants():
+    """The full 2048x2048 benchmark frame: sort order, permutation, draw list."""
+    import bench
+
+    scene = bench.make_scene()
+    with spr.VGRasterizer(2048, 2048, samples=32) as r:
+        r.add_vg(scene)
+        r.rasterize()
+        n = r.element_number()
+        perm = r.dump("SORT_PERM")
+        assert np.array_equal(np.sort(perm), np.arange(n["curve_fragment"], dtype=np.int32))
+        keys = r.dump("SORT_KEY")
+        pid = r.dump("FRAG_PID") & 0x3FFFFFFF
+        assert np.all(np.diff(pid.astype(np.int64)) >= 0)
+        same = pid[1:] == pid[:-1]
+        assert np.all(keys[1:][same] >= keys[:-1][same])  # signed order within a path
+        assert len(r.dump("DRAW_LIST")) == 4 * (n["merged_fragment"] + n["span"])
+        a = r.read_image().copy()
+        r.rasterize()
+        assert np.array_equal(a, r.read_image())

@@ -1,0 +1,96 @@
+"""The CPU oracle against the reference's own code.
+
+Fixtures in tests/golden/ were produced by tests/golden/make_goldens.py from
+the reference's intersection kernels (ras_cut.h k_make_intersection_0/1), its
+mask helpers (ras_qm_mask.h makeTable, fetchPixelTable, fetchVerticalTable,
+fetchVerticalTable2) and its sample pattern (ras_qm_mask.cu
+vg_sample_position), all compiled from the reference sources.  Where the
+reference tree is mounted, the same code is also run live on fresh scenes.
+"""
+import hashlib
+import json
+import pathlib
+
+import numpy as np
+import pytest
+
+import oracle
+import spr
+
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+
+
+def load_scene(path):
+    d = np.load(path)
+    fields = {f: d[f] for f in spr.Scene.FIELDS if f in d.files}
+    scene = spr.Scene(**fields)
+    tf = d["transform"] if bool(d["has_transform"]) else None
+    return scene, int(d["width"]), int(d["height"]), tf, d["ref_counts"], d["ref_entries"]
+
+
+@pytest.mark.parametrize("samples", [8, 32])
+def test_sample_positions_match_reference(samples):
+    ref = json.loads((GOLDEN / "sample_positions.json").read_text())[str(samples)]
+    cell = oracle.sample_positions(samples)
+    pixel0 = (cell[:samples] * 2).astype(np.float32)  # cell coords of pixel 0 -> pixel coords
+    assert pixel0.view(np.uint32).reshape(-1).tolist() == ref
+
+
+@pytest.mark.parametrize("samples", [8, 32])
+def test_mask_table_matches_reference(samples):
+    digest = json.loads((GOLDEN / "mask_tables.json").read_text())[str(samples)]
+    t = oracle.mask_table(samples)
+    assert hashlib.sha256(t.reshape(-1).tobytes() if samples == 32 else t[:, 0].tobytes()).hexdigest() == digest
+
+
+@pytest.mark.parametrize("samples", [8, 32])
+def test_mask_helpers_match_reference(samples):
+    v = np.load(GOLDEN / "mask_vectors.npz")
+    w = samples // 8
+    for p, exp in zip(v[f"fetch{samples}_in"], v[f"fetch{samples}_out"]):
+        assert np.array_equal(oracle.fetch_pixel_table(samples, p[:2], p[2:]), exp[:w])
+    for (y0, y1), e1, e2 in zip(v[f"vert{samples}_in"], v[f"vert{samples}_out"], v[f"vert2_{samples}_out"]):
+        assert np.array_equal(oracle.vertical_mask(samples, y0), e1[:w])
+        assert np.array_equal(oracle.vertical_mask2(samples, y0, y1), e2[:w])
+
+
+@pytest.mark.parametrize("samples", [8, 32])
+def test_table_lattice_quality(samples):
+    """The reference's (disabled) testFetchTable check: table fetch against the
+    exact half-plane test for every lattice segment; it reports segments with
+    4 or more wrong bits.  The shared table keeps those rare."""
+    h = oracle.fetch_table_selftest(samples, 33)
+    assert h.sum() == 33 ** 4 - 33 ** 3  # every pair with y0 != y1
+    assert h[5:].sum() == 0
+    assert h[4:].sum() / h.sum() < 0.005
+
+
+@pytest.mark.parametrize("name", ["random", "cubics", "mixed", "oddsize", "handmade"])
+def test_intersections_match_reference(name):
+    scene, W, H, tf, counts, entries = load_scene(GOLDEN / f"scene_{name}.npz")
+    r = oracle.run(scene, W, H, samples=8, transform=tf, stop_after=spr.STAGE["INTERSECTION"])
+    assert np.array_equal(r["CURVE_COUNT"], counts)
+    assert np.array_equal(r["INTERSECTION"].reshape(-1, 2), entries)
+
+
+def test_srgb_tables_consistent():
+    dec, th, bins = oracle.srgb_tables()
+    assert np.all(np.diff(dec) > 0) and np.all(np.diff(th) > 0)
+    assert dec[0] == 0.0 and dec[255] == 1.0
+    # every 8-bit code decodes to a value between its two thresholds
+    assert np.all(dec[1:] >= th) and np.all(dec[:-1] < th)
+
+
+@pytest.mark.skipif(not oracle.have_ref(), reason="reference tree not mounted here")
+@pytest.mark.parametrize("kind,size,seed", [(spr.SCENE_RANDOM, 311, 1), (spr.SCENE_MIXED, 512, 2),
+                                            (spr.SCENE_CUBICS, 400, 3), (spr.SCENE_RANDOM, 64, 4)])
+def test_intersections_live_reference(kind, size, seed):
+    scene = spr.Scene.generate(kind, seed=seed, width=size, height=size,
+                               n_paths={0: 20, 1: 150, 2: 12}[kind], n_large=8,
+                               seg_min=8 if kind != spr.SCENE_CUBICS else 16,
+                               seg_max=24 if kind != spr.SCENE_CUBICS else 40,
+                               with_rational=True, with_affine=kind == spr.SCENE_MIXED)
+    r = oracle.run(scene, size, size, samples=32, stop_after=spr.STAGE["INTERSECTION"])
+    counts, entries = oracle.ref_intersections(scene, r["TVERTEX"].reshape(-1, 2), r["PATH_VISIBLE"], size, size)
+    assert np.array_equal(r["CURVE_COUNT"], counts)
+    assert np.array_equal(r["INTERSECTION"].reshape(-1, 2), entries)
