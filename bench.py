@@ -43,8 +43,8 @@ L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 
 
 def workload_config(extra=None):
-    c = {"workload": "plain forward, large scene: 2048x2048 RGBA8, 32 spp ms sRGB, "
-                     "15000 glyph-like + 5000 large paths",
+    c = {"workload": f"plain forward, large scene: {WORKLOAD['width']}x{WORKLOAD['height']} RGBA8, 32 spp ms "
+                     f"sRGB, {WORKLOAD['n_paths']} glyph-like + {WORKLOAD['n_large']} large paths",
          "width": WORKLOAD["width"], "height": WORKLOAD["height"], "samples": SAMPLES,
          "ms_output": MS_OUTPUT, "srgb": SRGB, "glyph_paths": WORKLOAD["n_paths"],
          "large_paths": WORKLOAD["n_large"], "seed": WORKLOAD["seed"],
@@ -52,6 +52,14 @@ def workload_config(extra=None):
     if extra:
         c.update(extra)
     return c
+
+
+def scale_workload(scale):
+    """Scales the workload's size by `scale` (path counts by scale^2); used to
+    profile the same scene family on a case small enough for full captures."""
+    if scale != 1.0:
+        WORKLOAD.update(width=int(round(2048 * scale)), height=int(round(2048 * scale)),
+                        n_paths=int(round(15000 * scale * scale)), n_large=int(round(5000 * scale * scale)))
 
 
 def make_scene():
@@ -270,6 +278,11 @@ def run_ours(args, rank, world, local_rank):
     ms_max = allreduce_max(ms, world)
     value = world * W * H / (ms_max / 1e3) / 1e6
 
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile": True, "ms_per_step": ms_max, "step_ms": {
+                k: sum(v) / len(v) for k, v in steps.items()}, "counts": counts}), flush=True)
+        return
     # ---- end to end through the C ABI with host buffers: scene H2D (pinned),
     #      render, image D2H (pinned), every step
     pinned = [torch.from_numpy(getattr(scene, f)).pin_memory() if getattr(scene, f) is not None else None
@@ -364,7 +377,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="linear size scale of the workload (profiling of smaller cases)")
+    ap.add_argument("--profile", action="store_true",
+                    help="timed GPU frames only (no end-to-end or CPU legs), for profiler runs")
     args = ap.parse_args()
+    scale_workload(args.scale)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
