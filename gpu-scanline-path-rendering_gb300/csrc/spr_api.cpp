@@ -95,7 +95,8 @@ struct spr_handle {
     bool has_affine = false;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
-        wn_scan, draw, heads, flags_tmp, merged, tiles, pair_off, pkey[2], pval[2], bins, image, counters, dump_tmp;
+        wn_scan, draw, heads, flags_tmp, merged, tiles, pair_off, pkey[2], pval[2], bins, image, counters, dump_tmp,
+        overflow;
     uint64_t *skey_sorted = nullptr;
     uint32_t *perm_sorted = nullptr;
     // host staging
@@ -231,7 +232,7 @@ int spr_destroy(spr_handle *h) {
                       &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
                       &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
                       &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
-                      &h->image,      &h->counters, &h->dump_tmp};
+                      &h->image,      &h->counters, &h->dump_tmp, &h->overflow};
     for (DevBuf *b : bufs) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
@@ -376,11 +377,13 @@ int spr_render(spr_handle *h, void *stream) {
     const int ntx = (W + 31) / 32, nrows = (H + 1) / 2;
     const int64_t nbins = (int64_t)ntx * nrows;
     if ((st = ensure(h->bins, 8 * (size_t)nbins))) return st;
+    if ((st = ensure(h->overflow, 4 * (size_t)std::max<int64_t>(resolve_overflow_words(a), 1)))) return st;
     uint32_t *bin_start = h->bins.as<uint32_t>(), *bin_end = bin_start + nbins;
     if (nf == 0) {
         cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
         for (int i = 2; i <= 6; ++i) rec(h, i, s);
-        L += launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(), s);
+        L += launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(),
+                            h->overflow.as<uint32_t>(), s);
         rec(h, 7, s);
         rec(h, 8, s);
         h->launches = L;
@@ -462,7 +465,8 @@ int spr_render(spr_handle *h, void *stream) {
     cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
     L += launch_bin_bounds(pk, npairs, bin_start, bin_end, s);
     rec(h, 7, s);
-    L += launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end, h->image.as<uint32_t>(), s);
+    L += launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end,
+                        h->image.as<uint32_t>(), h->overflow.as<uint32_t>(), s);
     rec(h, 8, s);
     if ((st = cuda_status())) return st;
     if (h->timing) {
@@ -545,7 +549,7 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
                             &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
                             &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
-                            &h->image,      &h->counters, &h->dump_tmp};
+                            &h->image,      &h->counters, &h->dump_tmp, &h->overflow};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;

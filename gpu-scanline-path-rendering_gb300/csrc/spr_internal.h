@@ -95,8 +95,12 @@ int launch_emit_pairs(const FrameArgs &a, const int4 *draw, int64_t n_items, con
                        uint32_t *pair_key, uint32_t *pair_val, cudaStream_t s);
 int launch_bin_bounds(const uint32_t *pair_key, int64_t n_pairs, uint32_t *bin_start, uint32_t *bin_end,
                        cudaStream_t s);
+// overflow: 64 * 32 words per bin for pixels that need explicit samples
+// (32-sample multisample mode only; unused otherwise).
+int64_t resolve_overflow_words(const FrameArgs &a);
 int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_mask, const uint32_t *pair_val,
-                    const uint32_t *bin_start, const uint32_t *bin_end, uint32_t *image, cudaStream_t s);
+                   const uint32_t *bin_start, const uint32_t *bin_end, uint32_t *image, uint32_t *overflow,
+                   cudaStream_t s);
 int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s);
 int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cudaStream_t s);
 int launch_decode_keys(const uint64_t *skey, int64_t nf, int nrows, int32_t *out, cudaStream_t s);

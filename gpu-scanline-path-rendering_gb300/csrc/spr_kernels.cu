@@ -637,10 +637,10 @@ __global__ void k_bin_bounds(const uint32_t *__restrict__ key, int64_t n, uint32
 }
 
 // Shared-memory tables of the resolve.  The sRGB decode table is replicated
-// once per lane (entry k of lane l at k * 32 + l) so that the data-dependent
-// lookups of a warp never collide in a bank.
+// 8 times (entry k of lane l at k * 8 + l % 8) so that data-dependent lookups
+// of a warp rarely collide in a bank.
 struct SmemTables {
-    float dec32[256 * 32];
+    float dec8r[256 * 8];
     float th[256];
 };
 
@@ -672,7 +672,7 @@ __device__ __forceinline__ uint32_t enc_srgb(const float *__restrict__ th, float
 
 template <bool SRGB>
 __device__ __forceinline__ float dec8(const SmemTables &t, uint32_t k, int lane) {
-    if constexpr (SRGB) return t.dec32[k * 32 + lane];
+    if constexpr (SRGB) return t.dec8r[k * 8 + (lane & 7)];
     else return lin8(k);
 }
 
@@ -701,11 +701,13 @@ __device__ __forceinline__ uint32_t blend_sample(const SmemTables &t, int lane, 
 // entries whose masks partition the pixel's samples: equal colours are merged
 // after every blend, so a pixel typically holds 1-3 entries and a blend costs
 // one evaluation per entry instead of one per sample.  A 32-sample pixel that
-// would need more than 16 entries switches to an explicit 32-sample array in
-// the same storage (count = kFull) and switches back once it has 16 or fewer
+// would need more than 8 entries (about 1 pixel event in 2000 on dense
+// scenes) switches to an explicit 32-sample array in a global overflow area
+// owned by its bin (count = kFull) and switches back once it has 8 or fewer
 // distinct colours.  Every sample still gets exactly the value the
 // per-sample rule gives.
 constexpr uint8_t kFull = 0xFF;
+constexpr int kChunk = 64;  // blend tasks per chunk
 
 template <int CAP>
 struct BinState {
@@ -715,8 +717,8 @@ struct BinState {
     uint32_t cm[32];  // column mask of each staged item
     int4 it[32];
     uint4 mm[32];
-    uint32_t task[64];  // packed (pixel, entry, item) blend tasks of one chunk
-    uint32_t tres[64];  // their results
+    uint32_t task[kChunk];  // packed (pixel, entry, item) blend tasks of one chunk
+    uint32_t tres[kChunk];  // their results
 };
 
 // Columns [c0, c1) of a bin as a bit mask.
@@ -726,42 +728,37 @@ __device__ __forceinline__ uint32_t col_bits(int c0, int c1) {
     return hi & ~((1u << c0) - 1u);
 }
 
-template <int CAP>
-__device__ __forceinline__ uint32_t &full_sample(BinState<CAP> &w, int p, int s) {
-    return s < 16 ? w.ecol[s][p] : w.emask[s - 16][p];
-}
+// Explicit samples of pixel p of a bin: ovf[p * 32 + s] (global memory).
+__device__ __forceinline__ uint32_t &full_sample(uint32_t *ovf, int p, int s) { return ovf[p * 32 + s]; }
 
 // Entries -> explicit 32 samples (32-sample pixels only).
-template <int CAP>
-__device__ void to_full(BinState<CAP> &w, int p) {
-    if constexpr (CAP == 16) {
+template <int CAP, bool EXPLICIT>
+__device__ void to_full(BinState<CAP> &w, uint32_t *ovf, int p) {
+    if constexpr (EXPLICIT) {
         const int n = w.cnt[p];
-        uint32_t em[16], ec[16];
-        for (int j = 0; j < n; ++j) em[j] = w.emask[j][p], ec[j] = w.ecol[j][p];
         for (int smp = 0; smp < 32; ++smp) {
             uint32_t v = 0;
             for (int j = 0; j < n; ++j)
-                if ((em[j] >> smp) & 1u) v = ec[j];
-            full_sample(w, p, smp) = v;
+                if ((w.emask[j][p] >> smp) & 1u) v = w.ecol[j][p];
+            full_sample(ovf, p, smp) = v;
         }
         w.cnt[p] = kFull;
     }
 }
 
 // Explicit samples -> entries when at most CAP distinct colours remain.
-template <int CAP>
-__device__ void try_compress(BinState<CAP> &w, int p) {
-    if constexpr (CAP == 16) {
-        uint32_t v[32];
-        for (int smp = 0; smp < 32; ++smp) v[smp] = full_sample(w, p, smp);
-        uint32_t col[16], msk[16];
+template <int CAP, bool EXPLICIT>
+__device__ void try_compress(BinState<CAP> &w, uint32_t *ovf, int p) {
+    if constexpr (EXPLICIT) {
+        uint32_t col[CAP], msk[CAP];
         int n = 0;
         for (int smp = 0; smp < 32; ++smp) {
+            const uint32_t v = full_sample(ovf, p, smp);
             int j = 0;
-            while (j < n && col[j] != v[smp]) ++j;
+            while (j < n && col[j] != v) ++j;
             if (j == n) {
-                if (n == 16) return;  // stays explicit
-                col[n] = v[smp];
+                if (n == CAP) return;  // stays explicit
+                col[n] = v;
                 msk[n] = 0u;
                 ++n;
             }
@@ -804,8 +801,10 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                                                                  const uint32_t *__restrict__ pval,
                                                                  const uint32_t *__restrict__ bstart,
                                                                  const uint32_t *__restrict__ bend,
-                                                                 uint32_t *__restrict__ image) {
-    constexpr int CAP = MS ? (S == 32 ? 16 : 8) : 1;
+                                                                 uint32_t *__restrict__ image,
+                                                                 uint32_t *__restrict__ overflow) {
+    constexpr int CAP = MS ? 8 : 1;
+    constexpr bool EXPLICIT = MS && S == 32;  // entries can exceed CAP
     constexpr uint32_t ALL = MS ? (S == 32 ? 0xFFFFFFFFu : 0xFFu) : 1u;
     constexpr int MW = S / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -813,7 +812,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
     {
         const ResolveTables *rt = a.rtables;
         if constexpr (SRGB)
-            for (int i = threadIdx.x; i < 256 * 32; i += blockDim.x) T.dec32[i] = rt->srgb_dec[i >> 5];
+            for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) T.dec8r[i] = rt->srgb_dec[i >> 3];
         for (int i = threadIdx.x; i < 256; i += blockDim.x) T.th[i] = rt->threshold[i];
     }
     __syncthreads();
@@ -828,6 +827,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
     const int y0 = row * 2;
     const int cols = min(kTileW, a.W - tx0);  // valid columns of this bin
     const int rows = min(2, a.H - y0);        // valid pixel rows
+    uint32_t *ovf = EXPLICIT ? overflow + b * 64 * 32 : nullptr;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int p = lane + 32 * h;
@@ -896,7 +896,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                             splits += ((em & m) != 0u && (em & ~m) != 0u) ? 1 : 0;
                         }
                         if (n + splits > CAP) {
-                            to_full(w, p);
+                            to_full<CAP, EXPLICIT>(w, ovf, p);
                             n = kFull;
                         }
                     }
@@ -921,8 +921,8 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
             }
             const int total = __shfl_sync(0xffffffffu, off, 31);
             off -= ntask;
-            for (int cb = 0; cb < total; cb += 64) {
-                const int ce = min(cb + 64, total);
+            for (int cb = 0; cb < total; cb += kChunk) {
+                const int ce = min(cb + kChunk, total);
                 // write this lane's tasks that fall in [cb, ce)
                 if (off < ce && off + ntask > cb) {
                     int t = off;
@@ -994,16 +994,16 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                     if (msk[py] == 0u) continue;
                     const int p = py * 32 + lane;
                     if (n0[py] == kFull) {
-                        if constexpr (CAP == 16) {
+                        if constexpr (EXPLICIT) {
                             const uint32_t c = (uint32_t)w.it[q].z;
                             const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
                                         sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
                             const float sa = lin8(c >> 24), om = 1.f - sa;
                             for (uint32_t mk = msk[py]; mk; mk &= mk - 1u) {
-                                uint32_t &v = full_sample(w, p, __ffs(mk) - 1);
+                                uint32_t &v = full_sample(ovf, p, __ffs(mk) - 1);
                                 v = blend_sample<SRGB>(T, lane, v, sr, sg, sb, sa, om);
                             }
-                            try_compress(w, p);
+                            try_compress<CAP, EXPLICIT>(w, ovf, p);
                         }
                     } else if (w.cnt[p] > 1) {
                         dedup(w, p);
@@ -1030,8 +1030,8 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
             ia += (long long)weight * (long long)(lin8(v >> 24) * 68719476736.0f);
         };
         if (n == kFull) {
-            if constexpr (CAP == 16)
-                for (int smp = 0; smp < 32; ++smp) add(full_sample(w, p, smp), 1);
+            if constexpr (EXPLICIT)
+                for (int smp = 0; smp < 32; ++smp) add(full_sample(ovf, p, smp), 1);
         } else {
             for (int j = 0; j < n; ++j) add(w.ecol[j][p], __popc(w.emask[j][p]));
         }
@@ -1075,13 +1075,14 @@ __global__ void k_decode_keys(const uint64_t *__restrict__ skey, int64_t n, int 
 
 template <int S, bool MS, bool SRGB>
 void resolve_variant(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
-                     const uint32_t *bstart, const uint32_t *bend, uint32_t *image, cudaStream_t s) {
-    constexpr int CAP = MS ? (S == 32 ? 16 : 8) : 1;
+                     const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
+                     cudaStream_t s) {
+    constexpr int CAP = MS ? 8 : 1;
     const size_t smem = sizeof(SmemTables) + (size_t)kResolveWarps * sizeof(BinState<CAP>);
     cudaFuncSetAttribute(k_resolve<S, MS, SRGB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int64_t nbins = (int64_t)((a.W + kTileW - 1) / kTileW) * ((a.H + 1) / 2);
-    k_resolve<S, MS, SRGB><<<grid_for(nbins, kResolveWarps), kResolveWarps * 32, smem, s>>>(a, draw, merged, pval,
-                                                                                           bstart, bend, image);
+    k_resolve<S, MS, SRGB><<<grid_for(nbins, kResolveWarps), kResolveWarps * 32, smem, s>>>(
+        a, draw, merged, pval, bstart, bend, image, overflow);
 }
 
 }  // namespace
@@ -1166,18 +1167,19 @@ int launch_bin_bounds(const uint32_t *key, int64_t n, uint32_t *start, uint32_t 
 }
 
 int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
-                    const uint32_t *bstart, const uint32_t *bend, uint32_t *image, cudaStream_t s) {
+                    const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
+                    cudaStream_t s) {
     const bool ms = a.ms_output != 0, srgb = a.srgb != 0;
     if (a.S == 8) {
-        if (ms && srgb) resolve_variant<8, true, true>(a, draw, merged, pval, bstart, bend, image, s);
-        else if (ms) resolve_variant<8, true, false>(a, draw, merged, pval, bstart, bend, image, s);
-        else if (srgb) resolve_variant<8, false, true>(a, draw, merged, pval, bstart, bend, image, s);
-        else resolve_variant<8, false, false>(a, draw, merged, pval, bstart, bend, image, s);
+        if (ms && srgb) resolve_variant<8, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else if (ms) resolve_variant<8, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else if (srgb) resolve_variant<8, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else resolve_variant<8, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
     } else {
-        if (ms && srgb) resolve_variant<32, true, true>(a, draw, merged, pval, bstart, bend, image, s);
-        else if (ms) resolve_variant<32, true, false>(a, draw, merged, pval, bstart, bend, image, s);
-        else if (srgb) resolve_variant<32, false, true>(a, draw, merged, pval, bstart, bend, image, s);
-        else resolve_variant<32, false, false>(a, draw, merged, pval, bstart, bend, image, s);
+        if (ms && srgb) resolve_variant<32, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else if (ms) resolve_variant<32, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else if (srgb) resolve_variant<32, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else resolve_variant<32, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
     }
     return 1;
 }
@@ -1187,6 +1189,11 @@ int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cud
     k_selftest_encode<<<4 * 152, 256, 0, s>>>(rt, 0u, 0x3F800100u, bad);
     k_selftest_encode<<<1, 256, 0, s>>>(rt, 0x80000000u, 0x80000100u, bad);
     return 2;
+}
+
+int64_t resolve_overflow_words(const FrameArgs &a) {
+    if (!(a.ms_output && a.S == 32)) return 0;
+    return (int64_t)((a.W + kTileW - 1) / kTileW) * ((a.H + 1) / 2) * 64 * 32;
 }
 
 int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s) {
