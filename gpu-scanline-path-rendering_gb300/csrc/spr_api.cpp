@@ -118,7 +118,7 @@ namespace {
 
 int validate_config(const spr_config *c) {
     if (c->width < 1 || c->height < 1 || c->width > 4096 || c->height > 4096) return SPR_ERR_INVALID_ARG;
-    if (c->samples != 8 && c->samples != 32) return SPR_ERR_INVALID_ARG;
+    if (c->samples != 8 && c->samples != 16 && c->samples != 32) return SPR_ERR_INVALID_ARG;
     return SPR_OK;
 }
 
@@ -256,7 +256,7 @@ int spr_resize(spr_handle *h, int32_t width, int32_t height) {
 
 int spr_set_samples(spr_handle *h, int32_t samples) {
     if (!h) return SPR_ERR_INVALID_ARG;
-    if (samples != 8 && samples != 32) return SPR_ERR_INVALID_ARG;
+    if (samples != 8 && samples != 16 && samples != 32) return SPR_ERR_INVALID_ARG;
     cudaSetDevice(h->cfg.device);
     h->cfg.samples = samples;
     h->frame_valid = false;

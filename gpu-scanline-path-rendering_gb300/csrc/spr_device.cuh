@@ -259,10 +259,16 @@ __device__ __forceinline__ float solve_crossing(const CurveGeom &g, const float 
 
 // Vertical sample-row masks.  Mask bit b of the 2N stacked sample rows of a
 // cell column (N = 8: 16 rows, one 32-bit word duplicated for both pixel
-// columns; N = 32: 64 rows, words (low, high, low, high)).
+// columns; N = 16: 32 rows, words (column 0, column 1); N = 32: 64 rows,
+// words (low, high, low, high)).
 template <int N>
 __device__ __forceinline__ void vertical_mask(float y, uint32_t *out) {
-    if (N == 8) {
+    if (N == 16) {
+        int32_t r = cvt_rzi(roundf(y * 32));
+        uint32_t m = shr32(0xFFFFFFFFu, wsub(32, r));
+        out[0] = m;
+        out[1] = m;
+    } else if (N == 8) {
         int32_t r = cvt_rzi(roundf(y * 16));
         uint32_t m = shr32(0xffffu, wsub(16, r));
         out[0] = m | (m << 16);
@@ -278,7 +284,13 @@ __device__ __forceinline__ void vertical_mask(float y, uint32_t *out) {
 }
 template <int N>
 __device__ __forceinline__ void vertical_mask2(float y0, float y1, uint32_t *out) {
-    if (N == 8) {
+    if (N == 16) {
+        int32_t s0 = max(wsub(32, cvt_rzi_d((double)(y0 * 32) + 0.5)), 0);
+        int32_t s1 = max(wsub(32, cvt_rzi_d((double)(y1 * 32) + 0.5)), 0);
+        uint32_t m = shr32(0xFFFFFFFFu, s0) ^ shr32(0xFFFFFFFFu, s1);
+        out[0] = m;
+        out[1] = m;
+    } else if (N == 8) {
         int32_t s0 = max(wsub(16, cvt_rzi_d((double)(y0 * 16) + 0.5)), 0);
         int32_t s1 = max(wsub(16, cvt_rzi_d((double)(y1 * 16) + 0.5)), 0);
         uint32_t m = shr32(0xffffu, s0) ^ shr32(0xffffu, s1);

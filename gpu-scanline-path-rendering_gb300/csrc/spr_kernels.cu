@@ -325,6 +325,10 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
         if (S == 8) {
             const uint32_t tm = __ldg(a.mask_table + texel);
             mask[0] = (tm & vm[0]) ^ lm[0];
+        } else if (S == 16) {
+            const uint2 tm = __ldg(reinterpret_cast<const uint2 *>(a.mask_table) + texel);
+            mask[0] = (tm.x & vm[0]) ^ lm[0];
+            mask[1] = (tm.y & vm[1]) ^ lm[1];
         } else {
             const uint4 tm = __ldg(reinterpret_cast<const uint4 *>(a.mask_table) + texel);
             mask[0] = (tm.x & vm[0]) ^ lm[0];
@@ -338,6 +342,8 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
     wn_out[i] = (int8_t)swn;
     if (WORDS == 1) {
         mask_out[i] = mask[0];
+    } else if (WORDS == 2) {
+        reinterpret_cast<uint2 *>(mask_out)[i] = make_uint2(mask[0], mask[1]);
     } else {
         reinterpret_cast<uint4 *>(mask_out)[i] = make_uint4(mask[0], mask[1], mask[2], mask[3]);
     }
@@ -558,6 +564,10 @@ __global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, int64_t nf, i
         uint32_t m[WORDS];
         if constexpr (WORDS == 1) {
             m[0] = mask[raw];
+        } else if constexpr (WORDS == 2) {
+            const uint2 v = reinterpret_cast<const uint2 *>(mask)[raw];
+            m[0] = v.x;
+            m[1] = v.y;
         } else {
             const uint4 v = reinterpret_cast<const uint4 *>(mask)[raw];
             m[0] = v.x;
@@ -728,15 +738,23 @@ __device__ __forceinline__ uint32_t col_bits(int c0, int c1) {
     return hi & ~((1u << c0) - 1u);
 }
 
+// Sample mask of pixel k (= px.x * 2 + px.y) of a merged fragment's cell.
+template <int S>
+__device__ __forceinline__ uint32_t cell_pixel_mask(const uint4 &mm, int k) {
+    if constexpr (S == 32) return k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w));
+    else if constexpr (S == 16) return ((k < 2 ? mm.x : mm.y) >> (16 * (k & 1))) & 0xFFFFu;
+    else return (mm.x >> (8 * k)) & 0xFFu;
+}
+
 // Explicit samples of pixel p of a bin: ovf[p * 32 + s] (global memory).
 __device__ __forceinline__ uint32_t &full_sample(uint32_t *ovf, int p, int s) { return ovf[p * 32 + s]; }
 
-// Entries -> explicit 32 samples (32-sample pixels only).
-template <int CAP, bool EXPLICIT>
+// Entries -> explicit S samples (pixels with more than CAP colours).
+template <int S, int CAP, bool EXPLICIT>
 __device__ void to_full(BinState<CAP> &w, uint32_t *ovf, int p) {
     if constexpr (EXPLICIT) {
         const int n = w.cnt[p];
-        for (int smp = 0; smp < 32; ++smp) {
+        for (int smp = 0; smp < S; ++smp) {
             uint32_t v = 0;
             for (int j = 0; j < n; ++j)
                 if ((w.emask[j][p] >> smp) & 1u) v = w.ecol[j][p];
@@ -747,12 +765,12 @@ __device__ void to_full(BinState<CAP> &w, uint32_t *ovf, int p) {
 }
 
 // Explicit samples -> entries when at most CAP distinct colours remain.
-template <int CAP, bool EXPLICIT>
+template <int S, int CAP, bool EXPLICIT>
 __device__ void try_compress(BinState<CAP> &w, uint32_t *ovf, int p) {
     if constexpr (EXPLICIT) {
         uint32_t col[CAP], msk[CAP];
         int n = 0;
-        for (int smp = 0; smp < 32; ++smp) {
+        for (int smp = 0; smp < S; ++smp) {
             const uint32_t v = full_sample(ovf, p, smp);
             int j = 0;
             while (j < n && col[j] != v) ++j;
@@ -804,8 +822,8 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                                                                  uint32_t *__restrict__ image,
                                                                  uint32_t *__restrict__ overflow) {
     constexpr int CAP = MS ? 8 : 1;
-    constexpr bool EXPLICIT = MS && S == 32;  // entries can exceed CAP
-    constexpr uint32_t ALL = MS ? (S == 32 ? 0xFFFFFFFFu : 0xFFu) : 1u;
+    constexpr bool EXPLICIT = MS && S > CAP;  // entries can exceed CAP
+    constexpr uint32_t ALL = MS ? (S == 32 ? 0xFFFFFFFFu : ((1u << S) - 1u)) : 1u;
     constexpr int MW = S / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemTables &T = *reinterpret_cast<SmemTables *>(smem_raw);
@@ -845,10 +863,14 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
             const int x = (int)((uint32_t)it.x & 0xFFFFu) - tx0;
             uint32_t cm;
             if (it.w != 0) {
-                if constexpr (MW == 4)
+                if constexpr (MW == 4) {
                     w.mm[lane] = __ldg(reinterpret_cast<const uint4 *>(merged) + (it.w - 1));
-                else
+                } else if constexpr (MW == 2) {
+                    const uint2 v = __ldg(reinterpret_cast<const uint2 *>(merged) + (it.w - 1));
+                    w.mm[lane] = make_uint4(v.x, v.y, 0u, 0u);
+                } else {
                     w.mm[lane] = make_uint4(__ldg(merged + (it.w - 1)), 0u, 0u, 0u);
+                }
                 cm = col_bits(max(x, 0), min(x + 2, cols));
             } else {
                 cm = col_bits(max(x, 0), min(x + it.y, cols));
@@ -881,10 +903,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                     uint32_t m = ALL;
                     if (frag) {
                         const int k = dx * 2 + py;
-                        if constexpr (MW == 4)
-                            m = k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w));
-                        else
-                            m = (mm.x >> (8 * k)) & 0xFFu;
+                        m = cell_pixel_mask<S>(mm, k);
                         if constexpr (!MS) m = m ? ALL : 0u;
                     }
                     msk[py] = m;
@@ -896,7 +915,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                             splits += ((em & m) != 0u && (em & ~m) != 0u) ? 1 : 0;
                         }
                         if (n + splits > CAP) {
-                            to_full<CAP, EXPLICIT>(w, ovf, p);
+                            to_full<S, CAP, EXPLICIT>(w, ovf, p);
                             n = kFull;
                         }
                     }
@@ -950,8 +969,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                         if (it.w != 0) {
                             const int k = ((p & 31) + tx0 - (int)((uint32_t)it.x & 0xFFFFu)) * 2 + (p >> 5);
                             const uint4 mm = w.mm[tq];
-                            const uint32_t m = MW == 4 ? (k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w)))
-                                                       : ((mm.x >> (8 * k)) & 0xFFu);
+                            const uint32_t m = cell_pixel_mask<S>(mm, k);
                             sa = sa * ((float)__popc(m) / (float)S);
                         }
                     }
@@ -1003,7 +1021,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                                 uint32_t &v = full_sample(ovf, p, __ffs(mk) - 1);
                                 v = blend_sample<SRGB>(T, lane, v, sr, sg, sb, sa, om);
                             }
-                            try_compress<CAP, EXPLICIT>(w, ovf, p);
+                            try_compress<S, CAP, EXPLICIT>(w, ovf, p);
                         }
                     } else if (w.cnt[p] > 1) {
                         dedup(w, p);
@@ -1031,7 +1049,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
         };
         if (n == kFull) {
             if constexpr (EXPLICIT)
-                for (int smp = 0; smp < 32; ++smp) add(full_sample(ovf, p, smp), 1);
+                for (int smp = 0; smp < S; ++smp) add(full_sample(ovf, p, smp), 1);
         } else {
             for (int j = 0; j < n; ++j) add(w.ecol[j][p], __popc(w.emask[j][p]));
         }
@@ -1114,6 +1132,8 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
     if (nf <= 0) return 0;
     if (a.S == 8)
         k_fragment<8><<<grid_for(nf), kThreads, 0, s>>>(a, tvert, entries, nf, key, pidw, wn, mask, sort_key, sort_val);
+    else if (a.S == 16)
+        k_fragment<16><<<grid_for(nf), kThreads, 0, s>>>(a, tvert, entries, nf, key, pidw, wn, mask, sort_key, sort_val);
     else
         k_fragment<32><<<grid_for(nf), kThreads, 0, s>>>(a, tvert, entries, nf, key, pidw, wn, mask, sort_key, sort_val);
     return 1;
@@ -1142,6 +1162,8 @@ int launch_stencil(const FrameArgs &a, int64_t nf, int64_t nm, const uint64_t *s
     if (nm <= 0) return 0;
     if (a.S == 8)
         k_stencil<8><<<grid_for(nm), kThreads, 0, s>>>(a, nf, nm, skey, perm, pidw, mask, wn_scan, heads, merged);
+    else if (a.S == 16)
+        k_stencil<16><<<grid_for(nm), kThreads, 0, s>>>(a, nf, nm, skey, perm, pidw, mask, wn_scan, heads, merged);
     else
         k_stencil<32><<<grid_for(nm), kThreads, 0, s>>>(a, nf, nm, skey, perm, pidw, mask, wn_scan, heads, merged);
     return 1;
@@ -1175,6 +1197,11 @@ int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged,
         else if (ms) resolve_variant<8, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
         else if (srgb) resolve_variant<8, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
         else resolve_variant<8, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+    } else if (a.S == 16) {
+        if (ms && srgb) resolve_variant<16, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else if (ms) resolve_variant<16, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else if (srgb) resolve_variant<16, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        else resolve_variant<16, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
     } else {
         if (ms && srgb) resolve_variant<32, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
         else if (ms) resolve_variant<32, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
@@ -1192,7 +1219,7 @@ int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cud
 }
 
 int64_t resolve_overflow_words(const FrameArgs &a) {
-    if (!(a.ms_output && a.S == 32)) return 0;
+    if (!(a.ms_output && a.S > 8)) return 0;
     return (int64_t)((a.W + kTileW - 1) / kTileW) * ((a.H + 1) / 2) * 64 * 32;
 }
 

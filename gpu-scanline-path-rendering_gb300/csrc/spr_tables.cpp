@@ -30,8 +30,10 @@ void pixel_samples(int n, float *xy) {
         return;
     }
     // 8 samples: row i of 8, column = bit-reversed i (own bit length)
-    // (ras_qm_mask.cu:130-163); rows are already in ascending y.
-    for (int i = 0; i < 8; ++i) {
+    // (ras_qm_mask.cu:130-163); 16 samples apply the same rule to 16 rows.
+    // Rows are already in ascending y.
+    const double gap = 1.0 / n, hgap = gap / 2;
+    for (int i = 0; i < n; ++i) {
         int x = i, r = 0, bc = 0;
         while (x) {
             r = (r << 1) | (x & 1);
@@ -39,9 +41,9 @@ void pixel_samples(int n, float *xy) {
             ++bc;
         }
         double f = r / (float)(1 << bc);
-        int col = (int)(f * 8);
-        xy[2 * i] = (float)(col * 0.125 + 0.0625);
-        xy[2 * i + 1] = (float)(i * 0.125 + 0.0625);
+        int col = (int)(f * n);
+        xy[2 * i] = (float)(col * gap + hgap);
+        xy[2 * i + 1] = (float)(i * gap + hgap);
     }
 }
 

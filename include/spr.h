@@ -98,7 +98,8 @@ typedef struct spr_scene_view {
  * width, height : output buffer size, 1..4096 each (resizeOutputBuffer,
  *                 ras_base.cpp:396-402; the reference caps its buffers at
  *                 4096, ras_define.h:17-20).
- * samples       : samples per pixel, 8 or 32 (setSamples).
+ * samples       : samples per pixel, 8 or 32 (setSamples), or 16 (an
+ *                 extension: the 8-sample bit-reversal pattern on 16 rows).
  * ms_output     : 1 = per-sample coverage resolve (the reference's
  *                 multisample GL output, setMultisampleOutput); 0 = one colour
  *                 per pixel with alpha scaled by coverage.
@@ -136,7 +137,7 @@ int spr_destroy(spr_handle *h);
 
 /* resizeOutputBuffer (ras_base.cpp:396-402). */
 int spr_resize(spr_handle *h, int32_t width, int32_t height);
-/* setSamples (ras_base.h:185); 8 or 32.  Rebuilds the device tables. */
+/* setSamples (ras_base.h:185); 8, 16 or 32.  Rebuilds the device tables. */
 int spr_set_samples(spr_handle *h, int32_t samples);
 /* setMultisampleOutput (ras_base.h:186). */
 int spr_set_multisample_output(spr_handle *h, int32_t enable);

@@ -216,7 +216,10 @@ std::vector<F2> pixel_samples(int n) {
             s[i].y = (float)((2 * i + 1) / 64.0);
         }
     } else {
-        for (int i = 0; i < 8; ++i) {
+        // 8 samples: ras_qm_mask.cu:130-163; 16 samples (an extension, no
+        // counterpart in the reference) apply the same rule to 16 rows.
+        const double gap = 1.0 / n, hgap = gap / 2;
+        for (int i = 0; i < n; ++i) {
             int x = i, y = 0, bc = 0;
             while (x) {
                 y = (y << 1) | (x & 1);
@@ -224,9 +227,9 @@ std::vector<F2> pixel_samples(int n) {
                 ++bc;
             }
             double f = y / (float)(1 << bc);
-            int col = (int)(f * 8);
-            s[i].x = (float)(col * 0.125 + 0.0625);
-            s[i].y = (float)(i * 0.125 + 0.0625);
+            int col = (int)(f * n);
+            s[i].x = (float)(col * gap + hgap);
+            s[i].y = (float)(i * gap + hgap);
         }
         // sort_samples (ras_qm_mask.cu:44-48): by y, then x.  Already ordered.
         std::stable_sort(s.begin(), s.end(), [](const F2 &a, const F2 &b) {
@@ -312,7 +315,12 @@ inline void fetch_pixel_table(const uint32_t *table, int words, F2 P0, F2 P1, ui
 
 // fetchVerticalTable (ras_qm_mask.h:545-560).
 inline void vertical_mask(int n, float y, uint32_t *out) {
-    if (n == 8) {
+    if (n == 16) {  // 32 stacked sample rows; words (column 0, column 1)
+        int32_t r = cvt_rzi(std::round(y * 32));
+        uint32_t m = shr32(0xFFFFFFFFu, wsub(32, r));
+        out[0] = m;
+        out[1] = m;
+    } else if (n == 8) {
         int32_t r = cvt_rzi(std::round(y * 16));
         uint32_t m = shr32(0xffffu, wsub(16, r));
         out[0] = m | (m << 16);
@@ -329,7 +337,13 @@ inline void vertical_mask(int n, float y, uint32_t *out) {
 
 // fetchVerticalTable2 (ras_qm_mask.h:562-598).
 inline void vertical_mask2(int n, float y0, float y1, uint32_t *out) {
-    if (n == 8) {
+    if (n == 16) {
+        int32_t s0 = std::max(wsub(32, cvt_rzi_d((double)(y0 * 32) + 0.5)), 0);
+        int32_t s1 = std::max(wsub(32, cvt_rzi_d((double)(y1 * 32) + 0.5)), 0);
+        uint32_t m = shr32(0xFFFFFFFFu, s0) ^ shr32(0xFFFFFFFFu, s1);
+        out[0] = m;
+        out[1] = m;
+    } else if (n == 8) {
         int32_t s0 = wsub(16, cvt_rzi_d((double)(y0 * 16) + 0.5));
         int32_t s1 = wsub(16, cvt_rzi_d((double)(y1 * 16) + 0.5));
         s0 = std::max(s0, 0);
@@ -920,7 +934,7 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
     if (!scene || !cfgp || !out) return SPR_ERR_INVALID_ARG;
     const orc_config cfg = *cfgp;
     if (cfg.width < 1 || cfg.height < 1 || cfg.width > 4096 || cfg.height > 4096) return SPR_ERR_INVALID_ARG;
-    if (cfg.samples != 8 && cfg.samples != 32) return SPR_ERR_INVALID_ARG;
+    if (cfg.samples != 8 && cfg.samples != 16 && cfg.samples != 32) return SPR_ERR_INVALID_ARG;
     int rc = validate(scene);
     if (rc) return rc;
     int threads = cfg.threads > 0 ? cfg.threads : (int)std::max(1u, std::thread::hardware_concurrency());
@@ -1209,13 +1223,15 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
                             int k = (xx - x) * 2 + py;
                             if (S == 8)
                                 m = (r.merged_mask[(int64_t)(d.w - 1)] >> (8 * k)) & 0xFFu;
+                            else if (S == 16)
+                                m = (r.merged_mask[(int64_t)(d.w - 1) * 2 + (k >> 1)] >> (16 * (k & 1))) & 0xFFFFu;
                             else
                                 m = r.merged_mask[(int64_t)(d.w - 1) * 4 + k];
                         }
                         uint32_t *px = state.data() + ((size_t)py * W + xx) * spp;
                         float a = sa;
                         if (!cfg.ms_output) {
-                            int cnt = __builtin_popcount(S == 8 ? (m & 0xFFu) : m);
+                            int cnt = __builtin_popcount(S == 32 ? m : (m & ((1u << S) - 1u)));
                             a = sa * ((float)cnt / (float)S);
                             m = 1u;
                         }
@@ -1319,14 +1335,14 @@ extern "C" int orc_stage_ms(const orc_result *r, double *ms, int32_t capacity) {
 extern "C" void orc_free(orc_result *r) { delete r; }
 
 extern "C" int orc_sample_positions(int32_t samples, float *out) {
-    if ((samples != 8 && samples != 32) || !out) return SPR_ERR_INVALID_ARG;
+    if ((samples != 8 && samples != 16 && samples != 32) || !out) return SPR_ERR_INVALID_ARG;
     std::vector<F2> c = cell_samples(samples);
     std::memcpy(out, c.data(), c.size() * sizeof(F2));
     return SPR_OK;
 }
 
 extern "C" int orc_mask_table(int32_t samples, uint32_t *out) {
-    if ((samples != 8 && samples != 32) || !out) return SPR_ERR_INVALID_ARG;
+    if ((samples != 8 && samples != 16 && samples != 32) || !out) return SPR_ERR_INVALID_ARG;
     std::vector<uint32_t> t = build_mask_table(samples);
     std::memcpy(out, t.data(), t.size() * 4);
     return SPR_OK;
@@ -1342,9 +1358,9 @@ extern "C" int orc_srgb_tables(float *decode256, float *thresholds255, uint8_t *
 
 extern "C" int orc_fetch_pixel_table(int32_t samples, float p0x, float p0y, float p1x, float p1y,
                                      uint32_t *out_words) {
-    if ((samples != 8 && samples != 32) || !out_words) return SPR_ERR_INVALID_ARG;
-    static std::vector<uint32_t> t8, t32;
-    std::vector<uint32_t> &t = samples == 8 ? t8 : t32;
+    if ((samples != 8 && samples != 16 && samples != 32) || !out_words) return SPR_ERR_INVALID_ARG;
+    static std::vector<uint32_t> t8, t16, t32;
+    std::vector<uint32_t> &t = samples == 8 ? t8 : (samples == 16 ? t16 : t32);
     if (t.empty()) t = build_mask_table(samples);
     fetch_pixel_table(t.data(), samples / 8, F2{p0x, p0y}, F2{p1x, p1y}, out_words);
     return SPR_OK;
@@ -1355,7 +1371,7 @@ extern "C" int orc_fetch_pixel_table(int32_t samples, float p0x, float p0y, floa
 // (P0.y != P1.y), table fetch against the exact "sample right of segment"
 // test; hist[k] counts segments whose worst pixel word differs in k bits.
 extern "C" int orc_fetch_table_selftest(int32_t samples, int32_t res, int64_t *hist33) {
-    if ((samples != 8 && samples != 32) || res < 2 || !hist33) return SPR_ERR_INVALID_ARG;
+    if ((samples != 8 && samples != 16 && samples != 32) || res < 2 || !hist33) return SPR_ERR_INVALID_ARG;
     std::vector<uint32_t> t = build_mask_table(samples);
     std::vector<F2> cs = cell_samples(samples);
     const int words = samples / 8;
@@ -1381,7 +1397,7 @@ extern "C" int orc_fetch_table_selftest(int32_t samples, int32_t res, int64_t *h
                 }
                 worst = __builtin_popcount(got[0] ^ acc);
             } else {
-                for (int j = 0; j < 4; ++j) {
+                for (int j = 0; j < words; ++j) {
                     uint32_t d = 0;
                     for (int k = 0; k < 32; ++k) {
                         F2 P = cs[j * 32 + k];
@@ -1396,7 +1412,7 @@ extern "C" int orc_fetch_table_selftest(int32_t samples, int32_t res, int64_t *h
 }
 
 extern "C" int orc_vertical_mask(int32_t samples, float y, uint32_t *out_words) {
-    if ((samples != 8 && samples != 32) || !out_words) return SPR_ERR_INVALID_ARG;
+    if ((samples != 8 && samples != 16 && samples != 32) || !out_words) return SPR_ERR_INVALID_ARG;
     uint32_t tmp[4];
     vertical_mask(samples, y, tmp);
     std::memcpy(out_words, tmp, 4 * (samples / 8));
@@ -1404,7 +1420,7 @@ extern "C" int orc_vertical_mask(int32_t samples, float y, uint32_t *out_words) 
 }
 
 extern "C" int orc_vertical_mask2(int32_t samples, float y0, float y1, uint32_t *out_words) {
-    if ((samples != 8 && samples != 32) || !out_words) return SPR_ERR_INVALID_ARG;
+    if ((samples != 8 && samples != 16 && samples != 32) || !out_words) return SPR_ERR_INVALID_ARG;
     uint32_t tmp[4];
     vertical_mask2(samples, y0, y1, tmp);
     std::memcpy(out_words, tmp, 4 * (samples / 8));

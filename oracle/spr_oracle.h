@@ -19,7 +19,7 @@ extern "C" {
 typedef struct orc_config {
     int32_t width;
     int32_t height;
-    int32_t samples;   /* 8 or 32 */
+    int32_t samples;   /* 8, 16 or 32 */
     int32_t ms_output; /* 1 = per-sample resolve */
     int32_t srgb;      /* 1 = sRGB blending */
     int32_t threads;   /* host threads; <= 0 = all hardware threads */

@@ -114,6 +114,6 @@ def test_create_without_gpu_fails_cleanly():
 
 
 def test_create_rejects_bad_config_before_touching_the_device():
-    for cfg in (spr.Config(0, 64, 8, 1, 1, 0), spr.Config(64, 5000, 8, 1, 1, 0), spr.Config(64, 64, 16, 1, 1, 0)):
+    for cfg in (spr.Config(0, 64, 8, 1, 1, 0), spr.Config(64, 5000, 8, 1, 1, 0), spr.Config(64, 64, 12, 1, 1, 0)):
         h = C.c_void_p()
         assert spr.lib().spr_create(C.byref(cfg), C.byref(h)) == spr.ERR_INVALID_ARG

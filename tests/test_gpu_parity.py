@@ -56,7 +56,7 @@ def load_golden(name):
 
 
 @pytest.mark.parametrize("name", ["random", "cubics", "mixed", "oddsize", "handmade"])
-@pytest.mark.parametrize("samples", [8, 32])
+@pytest.mark.parametrize("samples", [8, 16, 32])
 def test_golden_scenes(name, samples):
     scene, W, H, tf, counts, entries = load_golden(name)
     check_parity(scene, W, H, samples=samples, transform=tf)
@@ -65,7 +65,7 @@ def test_golden_scenes(name, samples):
         assert np.array_equal(r.dump("INTERSECTION").reshape(-1, 2), entries)
 
 
-@pytest.mark.parametrize("samples", [8, 32])
+@pytest.mark.parametrize("samples", [8, 16, 32])
 @pytest.mark.parametrize("ms", [True, False])
 @pytest.mark.parametrize("srgb", [True, False])
 def test_mode_matrix(samples, ms, srgb):
@@ -76,12 +76,13 @@ def test_mode_matrix(samples, ms, srgb):
 
 @pytest.mark.parametrize("kind,size,n,nl", [(spr.SCENE_RANDOM, 512, 64, 0), (spr.SCENE_MIXED, 768, 900, 60),
                                             (spr.SCENE_CUBICS, 640, 48, 0)])
-def test_scene_families(kind, size, n, nl):
+@pytest.mark.parametrize("samples", [16, 32])
+def test_scene_families(kind, size, n, nl, samples):
     scene = spr.Scene.generate(kind, seed=31, width=size, height=size, n_paths=n, n_large=nl,
                                seg_min=8 if kind != spr.SCENE_CUBICS else 16,
                                seg_max=32 if kind != spr.SCENE_CUBICS else 64, with_rational=True,
                                with_affine=kind == spr.SCENE_MIXED)
-    check_parity(scene, size, size, samples=32)
+    check_parity(scene, size, size, samples=samples)
 
 
 def test_transforms():
