@@ -153,6 +153,23 @@ void gen_random(spr_scene &s, Rng &rng, const spr_scene_spec &sp) {
     }
 }
 
+// Like gen_random, with each path confined to its own random square box.
+void gen_local(spr_scene &s, Rng &rng, const spr_scene_spec &sp) {
+    const double W = sp.width, H = sp.height;
+    const double dim = std::fmin(W, H);
+    for (int p = 0; p < sp.n_paths; ++p) {
+        uint32_t id = s.add_path(rng);
+        const double side = rng.uniform(dim / 32.0, dim / 4.0);
+        const double x0 = rng.uniform(-side * 0.5, W - side * 0.5), y0 = rng.uniform(-side * 0.5, H - side * 0.5);
+        auto rnd_pt = [&]() { return P2{x0 + rng.uniform(0.0, side), y0 + rng.uniform(0.0, side)}; };
+        int n = rng.range(sp.seg_min, sp.seg_max);
+        std::vector<P2> pts(n);
+        for (auto &q : pts) q = rnd_pt();
+        closed_contour(s, rng, id, pts, sp.with_rational != 0, false, false,
+                       [&](P2, P2, double) { return rnd_pt(); });
+    }
+}
+
 // Star-shaped closed loop around the origin: n vertices at radius
 // r * U[rlo, 1], angles jittered; control points offset from the chord.
 std::vector<P2> star(Rng &rng, int n, double r, double rlo) {
@@ -291,9 +308,10 @@ extern "C" int spr_scene_generate(const spr_scene_spec *spec, spr_scene **out) {
     case SPR_SCENE_RANDOM: gen_random(*s, rng, sp); break;
     case SPR_SCENE_MIXED: gen_mixed(*s, rng, sp); break;
     case SPR_SCENE_CUBICS: gen_cubics(*s, rng, sp); break;
+    case SPR_SCENE_LOCAL: gen_local(*s, rng, sp); break;
     default: delete s; return SPR_ERR_INVALID_ARG;
     }
-    if (sp.with_affine && sp.kind == SPR_SCENE_RANDOM) {
+    if (sp.with_affine && (sp.kind == SPR_SCENE_RANDOM || sp.kind == SPR_SCENE_LOCAL)) {
         s->affine.clear();
         for (size_t p = 0; p < s->fill_rule.size(); ++p) s->affine.insert(s->affine.end(), {1.f, 0.f, 0.f, 1.f, 0.f, 0.f});
         s->has_affine = true;

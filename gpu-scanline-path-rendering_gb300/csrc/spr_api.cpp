@@ -93,6 +93,11 @@ struct spr_handle {
     uint32_t P = 0, C = 0, V = 0;
     DevBuf vertex, vpid, curves, rule, fill, affine;
     bool has_affine = false;
+    // batch frames (n_scenes > 0): per-scene viewports/transforms/images and
+    // the scene of every path; single-scene frames use cfg and m
+    int n_scenes = 0;
+    std::vector<SceneInfo> scenes_h;
+    DevBuf scenes_d, path_scene, item_scene;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
         wn_scan, draw, heads, flags_tmp, merged, tiles, pair_off, pkey[2], pval[2], bins, image, counters, dump_tmp,
@@ -153,7 +158,28 @@ FrameArgs make_args(const spr_handle *h) {
     a.fill_rgba = h->fill.as<uint32_t>();
     a.mask_table = h->mask_table.as<uint32_t>();
     a.rtables = h->rtables.as<ResolveTables>();
+    if (h->n_scenes > 0) {
+        a.path_scene = h->path_scene.as<uint32_t>();
+        a.scenes = h->scenes_d.as<SceneInfo>();
+        a.n_scenes = h->n_scenes;
+        const SceneInfo &last = h->scenes_h.back();
+        a.n_bins = (int64_t)last.bin_off + (int64_t)last.ntx * last.nrows;
+    } else {
+        a.path_scene = nullptr;
+        a.scenes = nullptr;
+        a.n_scenes = 0;
+        a.n_bins = (int64_t)((a.W + 31) / 32) * ((a.H + 1) / 2);
+    }
     return a;
+}
+
+// Pixels of the frame's image buffer (all scenes of a batch).
+int64_t frame_pixels(const spr_handle *h) {
+    if (h->n_scenes > 0) {
+        const SceneInfo &last = h->scenes_h.back();
+        return last.image_off + (int64_t)last.W * last.H;
+    }
+    return (int64_t)h->cfg.width * h->cfg.height;
 }
 
 int validate_scene(const spr_scene_view *v) {
@@ -232,7 +258,8 @@ int spr_destroy(spr_handle *h) {
                       &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
                       &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
                       &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
-                      &h->image,      &h->counters, &h->dump_tmp, &h->overflow};
+                      &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
+                      &h->item_scene};
     for (DevBuf *b : bufs) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
@@ -282,6 +309,7 @@ int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     cudaSetDevice(h->cfg.device);
     h->has_scene = false;
     h->frame_valid = false;
+    h->n_scenes = 0;
     const uint32_t P = v->n_paths, C = v->n_curves, V = v->n_vertices;
     // unifyCurveVertexOrder (ras_base.cpp:523-569): reverse a curve unless
     // (y_first, x_first) < (y_last, x_last) comparing float bit patterns.
@@ -343,6 +371,8 @@ int spr_render(spr_handle *h, void *stream) {
     h->host_syncs = 0;
     const FrameArgs a = make_args(h);
     const int W = a.W, H = a.H, WORDS = a.S / 8;
+    const bool batch = h->n_scenes > 0;
+    const int64_t npix = frame_pixels(h);
     if (h->timing) {
         for (auto &e : h->ev)
             if (!e) cudaEventCreate(&e);
@@ -352,7 +382,7 @@ int spr_render(spr_handle *h, void *stream) {
         (st = ensure(h->pvis, h->P)) || (st = ensure(h->counts, 4 * (size_t)h->C + 4)) ||
         (st = ensure(h->offsets, 4 * ((size_t)h->C + 1))) ||
         (st = ensure(h->scan_tmp, 4 * (size_t)scan_tmp_words(std::max<int64_t>(h->C, 1)))) ||
-        (st = ensure(h->image, 4 * (size_t)W * H)))
+        (st = ensure(h->image, 4 * (size_t)npix)))
         return st;
     rec(h, 0, s);
     L += launch_transform(a, h->tvert.as<float2>(), h->pflags.as<uint32_t>(), h->pvis.as<uint8_t>(), s);
@@ -374,8 +404,7 @@ int spr_render(spr_handle *h, void *stream) {
     h->en.merged_fragment = 0;
     h->en.span = 0;
     h->nm = h->ns = h->npairs = 0;
-    const int ntx = (W + 31) / 32, nrows = (H + 1) / 2;
-    const int64_t nbins = (int64_t)ntx * nrows;
+    const int64_t nbins = a.n_bins;
     if ((st = ensure(h->bins, 8 * (size_t)nbins))) return st;
     if ((st = ensure(h->overflow, 4 * (size_t)std::max<int64_t>(resolve_overflow_words(a), 1)))) return st;
     uint32_t *bin_start = h->bins.as<uint32_t>(), *bin_end = bin_start + nbins;
@@ -383,7 +412,7 @@ int spr_render(spr_handle *h, void *stream) {
         cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
         for (int i = 2; i <= 6; ++i) rec(h, i, s);
         L += launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(),
-                            h->overflow.as<uint32_t>(), s);
+                            h->overflow.as<uint32_t>(), h->counters.as<FrameCounters>(), s);
         rec(h, 7, s);
         rec(h, 8, s);
         h->launches = L;
@@ -401,8 +430,10 @@ int spr_render(spr_handle *h, void *stream) {
         (st = ensure(h->sval[1], 4 * (size_t)nf)) || (st = ensure(h->sort_tmp, 4 * (size_t)radix_tmp_words(nf))) ||
         (st = ensure(h->wn_scan, (size_t)nf)) || (st = ensure(h->draw, 16 * 2 * (size_t)nf)) ||
         (st = ensure(h->heads, 4 * (size_t)nf)) || (st = ensure(h->flags_tmp, 4 * (size_t)flags_tmp_words(nf))) ||
-        (st = ensure(h->merged, 4 * (size_t)WORDS * nf)))
+        (st = ensure(h->merged, 4 * (size_t)WORDS * nf)) ||
+        (batch && (st = ensure(h->item_scene, 4 * 2 * (size_t)nf))))
         return st;
+    uint32_t *item_scene = batch ? h->item_scene.as<uint32_t>() : nullptr;
     rec(h, 2, s);
     L += launch_curve_emit(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->offsets.as<uint32_t>(), h->entries.as<int2>(),
                       s);
@@ -422,7 +453,7 @@ int spr_render(spr_handle *h, void *stream) {
     // stages 9-12, 14: winding scan, marks, draw list
     cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);
     L += launch_scan_mark(a, nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
-                     h->draw.as<int4>(), h->heads.as<uint32_t>(), h->counters.as<FrameCounters>(),
+                     h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, h->counters.as<FrameCounters>(),
                      h->flags_tmp.as<uint32_t>(), s);
     cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
     ++h->host_syncs;
@@ -442,7 +473,7 @@ int spr_render(spr_handle *h, void *stream) {
     if ((st = ensure(h->tiles, 4 * ((size_t)items + 1))) || (st = ensure(h->pair_off, 4 * ((size_t)items + 1))))
         return st;
     if ((st = ensure(h->scan_tmp, 4 * (size_t)scan_tmp_words(std::max<int64_t>({items, (int64_t)h->C, 1}))))) return st;
-    L += launch_item_tiles(a, h->draw.as<int4>(), items, h->tiles.as<uint32_t>(), s);
+    L += launch_item_tiles(a, h->draw.as<int4>(), item_scene, items, h->tiles.as<uint32_t>(), s);
     L += scan_exclusive_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), items, h->scan_tmp.as<uint32_t>(), s);
     cudaMemcpyAsync(h->h_u32, h->pair_off.as<uint32_t>() + items, 4, cudaMemcpyDeviceToHost, s);
     ++h->host_syncs;
@@ -453,8 +484,8 @@ int spr_render(spr_handle *h, void *stream) {
         (st = ensure(h->pval[0], 4 * (size_t)npairs)) || (st = ensure(h->pval[1], 4 * (size_t)npairs)) ||
         (st = ensure(h->sort_tmp, 4 * (size_t)std::max(radix_tmp_words(npairs), radix_tmp_words(nf)))))
         return st;
-    L += launch_emit_pairs(a, h->draw.as<int4>(), items, h->pair_off.as<uint32_t>(), h->pkey[0].as<uint32_t>(),
-                      h->pval[0].as<uint32_t>(), s);
+    L += launch_emit_pairs(a, h->draw.as<int4>(), item_scene, items, h->pair_off.as<uint32_t>(),
+                           h->pkey[0].as<uint32_t>(), h->pval[0].as<uint32_t>(), s);
     const bool palt = radix_sort<uint32_t>(h->pkey[0].as<uint32_t>(), h->pval[0].as<uint32_t>(),
                                            h->pkey[1].as<uint32_t>(), h->pval[1].as<uint32_t>(), npairs,
                                            std::max(bits_for((uint64_t)nbins - 1), 1), h->sort_tmp.as<uint32_t>(), s,
@@ -466,7 +497,7 @@ int spr_render(spr_handle *h, void *stream) {
     L += launch_bin_bounds(pk, npairs, bin_start, bin_end, s);
     rec(h, 7, s);
     L += launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end,
-                        h->image.as<uint32_t>(), h->overflow.as<uint32_t>(), s);
+                        h->image.as<uint32_t>(), h->overflow.as<uint32_t>(), h->counters.as<FrameCounters>(), s);
     rec(h, 8, s);
     if ((st = cuda_status())) return st;
     if (h->timing) {
@@ -549,7 +580,8 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
                             &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
                             &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
-                            &h->image,      &h->counters, &h->dump_tmp, &h->overflow};
+                            &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d,
+                            &h->path_scene, &h->item_scene};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;
@@ -627,6 +659,247 @@ const char *spr_status_string(int32_t status) {
     case SPR_ERR_UNSUPPORTED: return "unsupported";
     default: return "unknown status";
     }
+}
+
+}  // extern "C"
+
+// ---- batches --------------------------------------------------------------
+// A batch keeps one handle per sample count present; each handle holds the
+// concatenation of its scenes (path, curve and vertex ids offset) plus the
+// per-scene table, and renders all of them in one launch sequence.
+
+struct spr_batch {
+    int device = 0, ms_output = 1, srgb = 1;
+    bool timing = false;
+    spr_handle *group[3] = {nullptr, nullptr, nullptr};  // samples 8, 16, 32
+    struct Entry {
+        int group;
+        int64_t image_off;
+        int W, H;
+    };
+    std::vector<Entry> entries;
+    bool rendered = false;
+};
+
+namespace {
+
+int group_of(int samples) { return samples == 8 ? 0 : (samples == 16 ? 1 : 2); }
+
+// Concatenates the scenes `idx` of `in` into one scene and uploads it to h,
+// with the per-scene table and the scene of every path.
+int upload_group(spr_handle *h, const spr_batch_scene *in, const std::vector<int> &idx,
+                 std::vector<spr_batch::Entry> &entries, int g) {
+    size_t P = 0, C = 0, V = 0;
+    bool any_affine = false;
+    for (int i : idx) {
+        P += in[i].scene.n_paths;
+        C += in[i].scene.n_curves;
+        V += in[i].scene.n_vertices;
+        any_affine |= in[i].scene.path_affine != nullptr;
+    }
+    if (P > (1u << 30) || C > (1u << 30) || V > (1u << 30)) return SPR_ERR_CAPACITY_EXCEEDED;
+    std::vector<float> vertex(2 * V), arc_w(C, 0.f), affine(any_affine ? 6 * P : 0);
+    std::vector<uint32_t> vpid(V), cvp(C), cpid(C), fill(P), pscene(P);
+    std::vector<uint8_t> ctype(C), rule(P);
+    std::vector<SceneInfo> info(idx.size());
+    size_t p0 = 0, c0 = 0, v0 = 0;
+    int64_t pix = 0;
+    uint32_t bins = 0;
+    for (size_t k = 0; k < idx.size(); ++k) {
+        const spr_batch_scene &b = in[idx[k]];
+        const spr_scene_view &v = b.scene;
+        if (v.n_vertices) std::memcpy(&vertex[2 * v0], v.vertex, 8 * (size_t)v.n_vertices);
+        for (uint32_t i = 0; i < v.n_vertices; ++i) vpid[v0 + i] = v.vertex_path_id[i] + (uint32_t)p0;
+        for (uint32_t i = 0; i < v.n_curves; ++i) {
+            cvp[c0 + i] = v.curve_vertex_pos[i] + (uint32_t)v0;
+            cpid[c0 + i] = v.curve_path_id[i] + (uint32_t)p0;
+            ctype[c0 + i] = v.curve_type[i];
+            if (v.curve_arc_w) arc_w[c0 + i] = v.curve_arc_w[i];
+        }
+        if (v.n_paths) {
+            std::memcpy(&fill[p0], v.path_fill_rgba, 4 * (size_t)v.n_paths);
+            std::memcpy(&rule[p0], v.path_fill_rule, v.n_paths);
+        }
+        for (uint32_t i = 0; i < v.n_paths; ++i) {
+            pscene[p0 + i] = (uint32_t)k;
+            if (any_affine) {
+                static const float id6[6] = {1.f, 0.f, 0.f, 1.f, 0.f, 0.f};
+                std::memcpy(&affine[6 * (p0 + i)], v.path_affine ? v.path_affine + 6 * (size_t)i : id6, 24);
+            }
+        }
+        SceneInfo &si = info[k];
+        si.W = b.width;
+        si.H = b.height;
+        si.ntx = (b.width + 31) / 32;
+        si.nrows = (b.height + 1) / 2;
+        si.image_off = pix;
+        si.bin_off = bins;
+        si.pad = 0;
+        for (int j = 0; j < 16; ++j) si.m[j] = b.has_transform ? b.transform[j] : ((j % 5 == 0) ? 1.f : 0.f);
+        entries[idx[k]] = spr_batch::Entry{g, pix, b.width, b.height};
+        pix += (int64_t)b.width * b.height;
+        if ((int64_t)bins + (int64_t)si.ntx * si.nrows > (int64_t)UINT32_MAX) return SPR_ERR_CAPACITY_EXCEEDED;
+        bins += (uint32_t)(si.ntx * si.nrows);
+        p0 += v.n_paths;
+        c0 += v.n_curves;
+        v0 += v.n_vertices;
+    }
+    spr_scene_view cat{(uint32_t)P,    (uint32_t)C,  (uint32_t)V,  vertex.data(), vpid.data(), cvp.data(),
+                       ctype.data(),   cpid.data(),  arc_w.data(), rule.data(),   fill.data(),
+                       any_affine ? affine.data() : nullptr};
+    int st = spr_set_scene(h, &cat);
+    if (st) return st;
+    if ((st = upload(h->scenes_d, info.data(), info.size())) || (st = upload(h->path_scene, pscene.data(), P)))
+        return st;
+    h->scenes_h = info;
+    h->n_scenes = (int)info.size();
+    return SPR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int spr_batch_create(int32_t device, int32_t ms_output, int32_t srgb, spr_batch **out) {
+    if (!out) return SPR_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return cuda_status();
+    spr_batch *b = new (std::nothrow) spr_batch();
+    if (!b) return SPR_ERR_OUT_OF_MEMORY;
+    b->device = device;
+    b->ms_output = ms_output ? 1 : 0;
+    b->srgb = srgb ? 1 : 0;
+    *out = b;
+    return SPR_OK;
+}
+
+int spr_batch_destroy(spr_batch *b) {
+    if (!b) return SPR_OK;
+    for (spr_handle *&h : b->group) {
+        spr_destroy(h);
+        h = nullptr;
+    }
+    delete b;
+    return SPR_OK;
+}
+
+int spr_batch_set_scenes(spr_batch *b, const spr_batch_scene *scenes, int32_t n) {
+    if (!b || n < 0 || (n > 0 && !scenes)) return SPR_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) {
+        const spr_batch_scene &s = scenes[i];
+        if (s.width < 1 || s.height < 1 || s.width > 4096 || s.height > 4096) return SPR_ERR_INVALID_ARG;
+        if (s.samples != 8 && s.samples != 16 && s.samples != 32) return SPR_ERR_INVALID_ARG;
+        int st = validate_scene(&s.scene);
+        if (st) return st;
+    }
+    cudaSetDevice(b->device);
+    b->rendered = false;
+    b->entries.assign(n, spr_batch::Entry{0, 0, 0, 0});
+    std::vector<int> idx[3];
+    for (int i = 0; i < n; ++i) idx[group_of(scenes[i].samples)].push_back(i);
+    for (int g = 0; g < 3; ++g) {
+        if (idx[g].empty()) {
+            spr_destroy(b->group[g]);
+            b->group[g] = nullptr;
+            continue;
+        }
+        if (!b->group[g]) {
+            const spr_config cfg{scenes[idx[g][0]].width, scenes[idx[g][0]].height, scenes[idx[g][0]].samples,
+                                 b->ms_output, b->srgb, b->device};
+            int st = spr_create(&cfg, &b->group[g]);
+            if (st) return st;
+            b->group[g]->timing = b->timing;
+        }
+        int st = upload_group(b->group[g], scenes, idx[g], b->entries, g);
+        if (st) return st;
+    }
+    return SPR_OK;
+}
+
+int spr_batch_render(spr_batch *b, void *stream) {
+    if (!b) return SPR_ERR_INVALID_ARG;
+    if (b->entries.empty()) return SPR_ERR_NO_SCENE;
+    b->rendered = false;
+    for (spr_handle *h : b->group) {
+        if (!h) continue;
+        int st = spr_render(h, stream);
+        if (st) return st;
+    }
+    b->rendered = true;
+    return SPR_OK;
+}
+
+int spr_batch_image_device_ptr(spr_batch *b, int32_t scene, void **out) {
+    if (!b || !out || scene < 0 || scene >= (int32_t)b->entries.size()) return SPR_ERR_INVALID_ARG;
+    if (!b->rendered) return SPR_ERR_NO_SCENE;
+    const spr_batch::Entry &e = b->entries[scene];
+    *out = b->group[e.group]->image.as<uint32_t>() + e.image_off;
+    return SPR_OK;
+}
+
+int spr_batch_read_image(spr_batch *b, int32_t scene, uint8_t *host_rgba, void *stream) {
+    if (!b || !host_rgba || scene < 0 || scene >= (int32_t)b->entries.size()) return SPR_ERR_INVALID_ARG;
+    if (!b->rendered) return SPR_ERR_NO_SCENE;
+    cudaSetDevice(b->device);
+    const spr_batch::Entry &e = b->entries[scene];
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint32_t *src = b->group[e.group]->image.as<uint32_t>() + e.image_off;
+    if (cudaMemcpyAsync(host_rgba, src, 4 * (size_t)e.W * e.H, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return cuda_status();
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+    return SPR_OK;
+}
+
+int spr_batch_get_counts(spr_batch *b, spr_element_number *total) {
+    if (!b || !total) return SPR_ERR_INVALID_ARG;
+    spr_element_number t{};
+    for (spr_handle *h : b->group) {
+        if (!h) continue;
+        t.path += h->en.path;
+        t.curve += h->en.curve;
+        t.vertex += h->en.vertex;
+        t.curve_fragment += h->en.curve_fragment;
+        t.merged_fragment += h->en.merged_fragment;
+        t.span += h->en.span;
+    }
+    *total = t;
+    return SPR_OK;
+}
+
+int spr_batch_enable_step_timing(spr_batch *b, int32_t enable) {
+    if (!b) return SPR_ERR_INVALID_ARG;
+    b->timing = enable != 0;
+    for (spr_handle *h : b->group)
+        if (h) h->timing = b->timing;
+    return SPR_OK;
+}
+
+int spr_batch_step_timing(spr_batch *b, double *ms, int32_t capacity, int32_t *n_out) {
+    if (!b || !n_out) return SPR_ERR_INVALID_ARG;
+    *n_out = kSteps;
+    if (ms)
+        for (int i = 0; i < kSteps && i < capacity; ++i) {
+            ms[i] = 0.0;
+            for (spr_handle *h : b->group)
+                if (h) ms[i] += h->step_ms[i];
+        }
+    return SPR_OK;
+}
+
+int spr_batch_get_frame_stats(spr_batch *b, spr_frame_stats *out) {
+    if (!b || !out) return SPR_ERR_INVALID_ARG;
+    spr_frame_stats t{};
+    for (spr_handle *h : b->group) {
+        if (!h) continue;
+        spr_frame_stats f{};
+        spr_get_frame_stats(h, &f);
+        t.kernel_launches += f.kernel_launches;
+        t.host_syncs += f.host_syncs;
+        t.resolve_pairs += f.resolve_pairs;
+        t.device_bytes += f.device_bytes;
+    }
+    *out = t;
+    return SPR_OK;
 }
 
 }  // extern "C"

@@ -31,7 +31,22 @@ struct FrameCounters {
     uint32_t n_merged;
     uint32_t n_span;
     uint32_t n_pairs;
-    uint32_t status;  // nonzero: capacity overflow detected on the device
+    uint32_t status;     // nonzero: capacity overflow detected on the device
+    uint32_t bin_queue;  // next resolve bin to hand out (persistent resolve)
+    uint32_t pad[3];
+};
+
+// One scene of a batch frame: its viewport, its resolve bins (ntx columns of
+// 32 pixels x nrows cell rows, numbered from bin_off) and its image (W x H
+// pixels from image_off in the frame's image buffer), and its 4x4 input
+// transform (row-major).
+struct SceneInfo {
+    int32_t W, H;
+    int32_t ntx, nrows;
+    int64_t image_off;
+    uint32_t bin_off;
+    uint32_t pad;
+    float m[16];
 };
 
 // ---- host-built tables (spr_tables.cpp) --------------------------------------
@@ -70,6 +85,13 @@ struct FrameArgs {
     const uint32_t *fill_rgba;
     const uint32_t *mask_table;
     const ResolveTables *rtables;
+    // Batch frames: path p belongs to scenes[path_scene[p]], whose viewport,
+    // transform and image replace W, H and m above.  Both are null for a
+    // single-scene frame.
+    const uint32_t *path_scene;
+    const SceneInfo *scenes;
+    int n_scenes;
+    int64_t n_bins;  // resolve bins of the frame
 };
 
 int launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible,
@@ -83,24 +105,28 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
                      cudaStream_t s);
 int64_t flags_tmp_words(int64_t nf);
 // Winding scan, merged-fragment / span marks, draw list and merged heads.
+// item_scene (batch frames only, else null) receives the scene of each draw item.
 int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                      int8_t *wn_scan, int4 *draw, uint32_t *heads, FrameCounters *counters, uint32_t *tmp,
-                      cudaStream_t s);
+                      int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
+                      uint32_t *tmp, cudaStream_t s);
 int launch_stencil(const FrameArgs &a, int64_t nf, int64_t n_merged, const uint64_t *skey, const uint32_t *perm,
                     const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan, const uint32_t *heads,
                     uint32_t *merged_mask, cudaStream_t s);
-int launch_item_tiles(const FrameArgs &a, const int4 *draw, int64_t n_items, uint32_t *tile_counts,
-                       cudaStream_t s);
-int launch_emit_pairs(const FrameArgs &a, const int4 *draw, int64_t n_items, const uint32_t *pair_offsets,
-                       uint32_t *pair_key, uint32_t *pair_val, cudaStream_t s);
+int launch_item_tiles(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t n_items,
+                       uint32_t *tile_counts, cudaStream_t s);
+int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t n_items,
+                       const uint32_t *pair_offsets, uint32_t *pair_key, uint32_t *pair_val, cudaStream_t s);
 int launch_bin_bounds(const uint32_t *pair_key, int64_t n_pairs, uint32_t *bin_start, uint32_t *bin_end,
                        cudaStream_t s);
-// overflow: 64 * 32 words per bin for pixels that need explicit samples
-// (32-sample multisample mode only; unused otherwise).
+// The resolve is persistent: resolve_warps(a) warps take bins from
+// counters->bin_queue (zeroed by launch_resolve).  overflow: 64 * 32 words
+// per warp for pixels that need explicit samples (multisample modes with
+// more than 8 samples; unused otherwise).
+int64_t resolve_warps(const FrameArgs &a);
 int64_t resolve_overflow_words(const FrameArgs &a);
 int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_mask, const uint32_t *pair_val,
                    const uint32_t *bin_start, const uint32_t *bin_end, uint32_t *image, uint32_t *overflow,
-                   cudaStream_t s);
+                   FrameCounters *counters, cudaStream_t s);
 int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s);
 int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cudaStream_t s);
 int launch_decode_keys(const uint64_t *skey, int64_t nf, int nrows, int32_t *out, cudaStream_t s);

@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "spr_device.cuh"
@@ -28,6 +29,16 @@ namespace {
 constexpr int kThreads = 256;
 
 inline unsigned grid_for(int64_t n, int t = kThreads) { return (unsigned)((n + t - 1) / t); }
+
+// Viewport of the scene that path pid belongs to.
+struct Dim {
+    int W, H;
+};
+__device__ __forceinline__ Dim dim_of(const FrameArgs &a, uint32_t pid) {
+    if (a.path_scene == nullptr) return Dim{a.W, a.H};
+    const SceneInfo *sc = a.scenes + __ldg(a.path_scene + pid);
+    return Dim{sc->W, sc->H};
+}
 
 __device__ __forceinline__ void load_geom(const CurveDesc &d, const float2 *__restrict__ tv, CurveGeom &g) {
     g.type = (int)(d.type & 0xFFu);
@@ -61,15 +72,27 @@ __global__ void k_transform(FrameArgs a, float2 *__restrict__ tvert, uint32_t *_
             p = make_float2(x, y);
         }
         const float iv0 = p.x, iv1 = p.y, iv2 = 0.f, iv3 = 1.f;
+        float m[16];
+        int W = a.W, H = a.H;
+        if (a.path_scene != nullptr) {
+            const SceneInfo *sc = a.scenes + a.path_scene[pid];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) m[k] = sc->m[k];
+            W = sc->W;
+            H = sc->H;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) m[k] = a.m[k];
+        }
         float ov[4];
 #pragma unroll
         for (int r = 0; r < 4; ++r)
-            ov[r] = a.m[4 * r] * iv0 + a.m[4 * r + 1] * iv1 + a.m[4 * r + 2] * iv2 + a.m[4 * r + 3] * iv3;
+            ov[r] = m[4 * r] * iv0 + m[4 * r + 1] * iv1 + m[4 * r + 2] * iv2 + m[4 * r + 3] * iv3;
         ov[0] /= ov[3];
         ov[1] /= ov[3];
         ov[2] /= ov[3];
-        const float w = (float)a.W, h = (float)a.H;
-        const float z = (float)min(a.W, a.H);
+        const float w = (float)W, h = (float)H;
+        const float z = (float)min(W, H);
         const float cutoff = -z * 0.5f;
         if (ov[2] < cutoff) ov[2] = cutoff;
         const float w2 = w * .5f, h2 = h * .5f;
@@ -116,12 +139,13 @@ __global__ void k_curve_count(FrameArgs a, const float2 *__restrict__ tv, const 
     load_geom(d, tv, g);
     float q[5];
     const int np = monotonize(g, vis[d.pid] != 0, q);
+    const Dim dm = dim_of(a, d.pid);
     float v0x = g.px[0], v0y = g.py[0];
     uint32_t p = 0;
     for (int i = 0; i < np; ++i) {
         const float t1 = q[i];
         const float v1x = curve_coord(g.type, g.w, g.px, t1), v1y = curve_coord(g.type, g.w, g.py, t1);
-        const CutRange cr = cut_range(v0x, v0y, v1x, v1y, a.W, a.H);
+        const CutRange cr = cut_range(v0x, v0y, v1x, v1y, dm.W, dm.H);
         p += 1 + cr.nx + cr.ny;
         v0x = v1x;
         v0y = v1y;
@@ -141,6 +165,7 @@ __global__ void k_curve_emit(FrameArgs a, const float2 *__restrict__ tv, const u
     load_geom(d, tv, g);
     float q[5];
     const int np = monotonize(g, vis[d.pid] != 0, q);
+    const Dim dm = dim_of(a, d.pid);
     int2 *out = entries + offsets[cid];
     float t0_ms = 0.f;
     float v0x = g.px[0], v0y = g.py[0];
@@ -150,7 +175,7 @@ __global__ void k_curve_emit(FrameArgs a, const float2 *__restrict__ tv, const u
         const float v1x = curve_coord(g.type, g.w, g.px, traw), v1y = curve_coord(g.type, g.w, g.py, traw);
         const uint32_t tb = fbits(traw) & 0xFFFFFFFCu;
         const float t1_ms = (floorf(v1x) == v1x) ? ffrom(tb | 2u) : ffrom(tb | 3u);
-        const CutRange cr = cut_range(v0x, v0y, v1x, v1y, a.W, a.H);
+        const CutRange cr = cut_range(v0x, v0y, v1x, v1y, dm.W, dm.H);
         int nx = cr.nx, ny = cr.ny;
         const int n_loop = nx + ny + 1;
         float x = (float)(cr.dx < 0.f ? cr.xe : cr.xb);
@@ -240,6 +265,7 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
     const int cid = e0.x;
     const CurveDesc d = a.curves[cid];
     const uint32_t pathid = d.pid;
+    const Dim dm = dim_of(a, pathid);
     int32_t yx = kInvalidKey;
     if (e0.x != e1.x) t1 = 1.f;
     int wnchg = 0, swn = 0;
@@ -259,11 +285,11 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
         const int sl = rev ? f0 : f1;
         const int rx = floor2((vfx + vlx) * 0.5f);
         const int ry = floor2((vfy + vly) * 0.5f);
-        const int px = min(max(rx, -2), (int)(((uint32_t)a.W & 0xFFFFFFFEu) + 2));
-        const int py = min(max(ry, -2), (int)(((uint32_t)a.H & 0xFFFFFFFEu) + 2));
+        const int px = min(max(rx, -2), (int)(((uint32_t)dm.W & 0xFFFFFFFEu) + 2));
+        const int py = min(max(ry, -2), (int)(((uint32_t)dm.H & 0xFFFFFFFEu) + 2));
         const uint32_t ys = (uint32_t)(py + 0x7FFF) << 16;
         const uint32_t xs = (uint32_t)(px + 0x7FFF) & 0xFFFFu;
-        if ((uint32_t)ry < (uint32_t)a.H) yx = (int32_t)(ys | xs);
+        if ((uint32_t)ry < (uint32_t)dm.H) yx = (int32_t)(ys | xs);
         const int wy = py + 1;
         if (vfy == vly) {
             swn = 0;
@@ -347,7 +373,7 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
     } else {
         reinterpret_cast<uint4 *>(mask_out)[i] = make_uint4(mask[0], mask[1], mask[2], mask[3]);
     }
-    const int nrows = (a.H + 1) / 2;
+    const int nrows = (dm.H + 1) / 2;
     sort_key[i] = ((uint64_t)pathid << 24) | (uint64_t)local_sort_key(yx, nrows);
     sort_val[i] = (uint32_t)i;
 }
@@ -430,8 +456,11 @@ struct Mark {
 
 // k_mark_merged_fragment_and_span (cu:462-535) on sorted position i.
 __device__ __forceinline__ Mark mark_at(int64_t i, const uint64_t *__restrict__ skey, const int8_t *__restrict__ wn_scan,
-                                        const uint8_t *__restrict__ rule, int W, int H, int nrows) {
+                                        const FrameArgs &a) {
     const uint64_t k1 = skey[i];
+    const Dim dm = dim_of(a, (uint32_t)(k1 >> 24));
+    const int W = dm.W, H = dm.H, nrows = (H + 1) / 2;
+    const uint8_t *__restrict__ rule = a.fill_rule;
     const uint32_t key1 = (uint32_t)key_from_local((uint32_t)(k1 & 0xFFFFFFu), nrows);
     const int x1 = key_x(key1), y1 = key_y(key1);
     const bool oob = x1 < 0 || y1 < 0 || x1 >= W || y1 >= H;
@@ -456,14 +485,13 @@ __global__ void __launch_bounds__(kFlagThreads) k_flags_reduce(FrameArgs a, int6
                                                                const int8_t *__restrict__ wn_scan,
                                                                uint32_t *__restrict__ fsum, uint32_t *__restrict__ ssum) {
     __shared__ uint32_t sw[kFlagThreads / 32 + 1];
-    const int nrows = (a.H + 1) / 2;
     const int64_t base = (int64_t)blockIdx.x * kFlagTile + (int64_t)threadIdx.x * kFlagItems;
     uint32_t s = 0;
 #pragma unroll
     for (int k = 0; k < kFlagItems; ++k) {
         const int64_t i = base + k;
         if (i < nf) {
-            const Mark m = mark_at(i, skey, wn_scan, a.fill_rule, a.W, a.H, nrows);
+            const Mark m = mark_at(i, skey, wn_scan, a);
             s += m.ff | (m.sf << 16);
         }
     }
@@ -481,16 +509,16 @@ __global__ void __launch_bounds__(kFlagThreads) k_flags_down(FrameArgs a, int64_
                                                              const uint32_t *__restrict__ fsum,
                                                              const uint32_t *__restrict__ ssum, int4 *__restrict__ draw,
                                                              uint32_t *__restrict__ heads,
+                                                             uint32_t *__restrict__ item_scene,
                                                              FrameCounters *__restrict__ counters) {
     __shared__ uint32_t sw[kFlagThreads / 32 + 1];
-    const int nrows = (a.H + 1) / 2;
     const int64_t base = (int64_t)blockIdx.x * kFlagTile + (int64_t)threadIdx.x * kFlagItems;
     Mark mk[kFlagItems];
     uint32_t s = 0;
 #pragma unroll
     for (int k = 0; k < kFlagItems; ++k) {
         const int64_t i = base + k;
-        mk[k] = i < nf ? mark_at(i, skey, wn_scan, a.fill_rule, a.W, a.H, nrows) : Mark{0u, 0u};
+        mk[k] = i < nf ? mark_at(i, skey, wn_scan, a) : Mark{0u, 0u};
         s += mk[k].ff | (mk[k].sf << 16);
     }
     uint32_t total;
@@ -506,7 +534,13 @@ __global__ void __launch_bounds__(kFlagThreads) k_flags_down(FrameArgs a, int64_
             const uint64_t k1 = skey[i];
             const uint32_t p = (uint32_t)(k1 >> 24);
             const int32_t fill = (int32_t)a.fill_rgba[p];
+            const int nrows = (dim_of(a, p).H + 1) / 2;
             const uint32_t key1 = (uint32_t)key_from_local((uint32_t)(k1 & 0xFFFFFFu), nrows);
+            if (item_scene != nullptr) {
+                const uint32_t sc = a.path_scene[p];
+                if (ff) item_scene[nfb + nsb] = sc;
+                if (sf) item_scene[nfb + nsb + ff] = sc;
+            }
             if (ff) {
                 const int32_t pos = (int32_t)(((uint32_t)key_y(key1) << 16) | (uint32_t)key_x(key1));
                 draw[nfb + nsb] = make_int4(pos, 2, fill, (int)(nfb + 1));
@@ -611,27 +645,37 @@ __device__ __forceinline__ void item_cols(const int4 &it, int W, int &x0, int &x
     x1 = min(x + it.y, W);
 }
 
-__global__ void k_item_tiles(FrameArgs a, const int4 *__restrict__ draw, int64_t n, uint32_t *__restrict__ cnt) {
+__global__ void k_item_tiles(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
+                             int64_t n, uint32_t *__restrict__ cnt) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const int W = item_scene != nullptr ? a.scenes[item_scene[i]].W : a.W;
     int x0, x1;
-    item_cols(draw[i], a.W, x0, x1);
+    item_cols(draw[i], W, x0, x1);
     cnt[i] = x1 > x0 ? (uint32_t)((x1 - 1) / kTileW - x0 / kTileW + 1) : 0u;
 }
 
-__global__ void k_emit_pairs(FrameArgs a, const int4 *__restrict__ draw, int64_t n, const uint32_t *__restrict__ offs,
-                             uint32_t *__restrict__ pkey, uint32_t *__restrict__ pval) {
+__global__ void k_emit_pairs(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
+                             int64_t n, const uint32_t *__restrict__ offs, uint32_t *__restrict__ pkey,
+                             uint32_t *__restrict__ pval) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int4 it = draw[i];
+    int W = a.W;
+    uint32_t bin0 = 0;
+    if (item_scene != nullptr) {
+        const SceneInfo *sc = a.scenes + item_scene[i];
+        W = sc->W;
+        bin0 = sc->bin_off;
+    }
     int x0, x1;
-    item_cols(it, a.W, x0, x1);
+    item_cols(it, W, x0, x1);
     if (x1 <= x0) return;
-    const int ntx = (a.W + kTileW - 1) / kTileW;
+    const int ntx = (W + kTileW - 1) / kTileW;
     const int row = (it.x >> 16) / 2;
     uint32_t o = offs[i];
     for (int t = x0 / kTileW; t <= (x1 - 1) / kTileW; ++t) {
-        pkey[o] = (uint32_t)(row * ntx + t);
+        pkey[o] = bin0 + (uint32_t)(row * ntx + t);
         pval[o] = (uint32_t)i;
         ++o;
     }
@@ -813,39 +857,37 @@ __device__ __forceinline__ void dedup(BinState<CAP> &w, int p) {
 // sets are pairwise disjoint and each batch is applied in one step, each
 // lane updating its own two pixels; then every pixel is averaged over its
 // samples with an exact fixed-point sum.
-template <int S, bool MS, bool SRGB>
-__global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
-                                                                 const uint32_t *__restrict__ merged,
-                                                                 const uint32_t *__restrict__ pval,
-                                                                 const uint32_t *__restrict__ bstart,
-                                                                 const uint32_t *__restrict__ bend,
-                                                                 uint32_t *__restrict__ image,
-                                                                 uint32_t *__restrict__ overflow) {
-    constexpr int CAP = MS ? 8 : 1;
+template <int S, bool MS, bool SRGB, int CAP>
+__device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__restrict__ draw,
+                                            const uint32_t *__restrict__ merged, const uint32_t *__restrict__ pval,
+                                            const uint32_t *__restrict__ bstart, const uint32_t *__restrict__ bend,
+                                            uint32_t *__restrict__ image, uint32_t *__restrict__ ovf,
+                                            const SmemTables &T, BinState<CAP> &w, const int lane, const uint32_t b) {
     constexpr bool EXPLICIT = MS && S > CAP;  // entries can exceed CAP
     constexpr uint32_t ALL = MS ? (S == 32 ? 0xFFFFFFFFu : ((1u << S) - 1u)) : 1u;
     constexpr int MW = S / 8;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    SmemTables &T = *reinterpret_cast<SmemTables *>(smem_raw);
-    {
-        const ResolveTables *rt = a.rtables;
-        if constexpr (SRGB)
-            for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) T.dec8r[i] = rt->srgb_dec[i >> 3];
-        for (int i = threadIdx.x; i < 256; i += blockDim.x) T.th[i] = rt->threshold[i];
+    // the bin's scene: viewport, first bin, image
+    int W = a.W, H = a.H;
+    uint32_t lb = b;
+    if (a.scenes != nullptr) {
+        int lo = 0, hi = a.n_scenes - 1;  // last scene whose bin_off <= b
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.scenes[mid].bin_off <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        const SceneInfo *sc = a.scenes + lo;
+        W = sc->W;
+        H = sc->H;
+        lb = b - sc->bin_off;
+        image += sc->image_off;
     }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    BinState<CAP> &w = reinterpret_cast<BinState<CAP> *>(smem_raw + sizeof(SmemTables))[warp];
-    const int ntx = (a.W + kTileW - 1) / kTileW;
-    const int nrows = (a.H + 1) / 2;
-    const int64_t b = (int64_t)blockIdx.x * kResolveWarps + warp;
-    if (b >= (int64_t)ntx * nrows) return;
-    const int row = (int)(b / ntx), tile = (int)(b % ntx);
+    const int ntx = (W + kTileW - 1) / kTileW;
+    const int row = (int)(lb / ntx), tile = (int)(lb % ntx);
     const int tx0 = tile * kTileW;
     const int y0 = row * 2;
-    const int cols = min(kTileW, a.W - tx0);  // valid columns of this bin
-    const int rows = min(2, a.H - y0);        // valid pixel rows
-    uint32_t *ovf = EXPLICIT ? overflow + b * 64 * 32 : nullptr;
+    const int cols = min(kTileW, W - tx0);  // valid columns of this bin
+    const int rows = min(2, H - y0);        // valid pixel rows
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int p = lane + 32 * h;
@@ -1057,7 +1099,43 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
         const float ab = (float)((double)ib * scale), aa = (float)((double)ia * scale);
         const uint32_t out = enc8<SRGB>(T, ar) | (enc8<SRGB>(T, ag) << 8) | (enc8<SRGB>(T, ab) << 16) |
                              (enc_lin(aa) << 24);
-        image[(int64_t)(y0 + py) * a.W + tx0 + lane] = out;
+        image[(int64_t)(y0 + py) * W + tx0 + lane] = out;
+    }
+}
+
+// Persistent resolve: each warp takes bins from the frame's bin queue until
+// it is empty; a warp's overflow slot is reused from bin to bin.
+template <int S, bool MS, bool SRGB>
+__global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
+                                                                 const uint32_t *__restrict__ merged,
+                                                                 const uint32_t *__restrict__ pval,
+                                                                 const uint32_t *__restrict__ bstart,
+                                                                 const uint32_t *__restrict__ bend,
+                                                                 uint32_t *__restrict__ image,
+                                                                 uint32_t *__restrict__ overflow,
+                                                                 uint32_t *__restrict__ bin_queue) {
+    constexpr int CAP = MS ? 8 : 1;
+    constexpr bool EXPLICIT = MS && S > CAP;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SmemTables &T = *reinterpret_cast<SmemTables *>(smem_raw);
+    {
+        const ResolveTables *rt = a.rtables;
+        if constexpr (SRGB)
+            for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) T.dec8r[i] = rt->srgb_dec[i >> 3];
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) T.th[i] = rt->threshold[i];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    BinState<CAP> &w = reinterpret_cast<BinState<CAP> *>(smem_raw + sizeof(SmemTables))[warp];
+    const int64_t slot = (int64_t)blockIdx.x * kResolveWarps + warp;
+    uint32_t *ovf = EXPLICIT ? overflow + slot * 64 * 32 : nullptr;
+    for (;;) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(bin_queue, 1u);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if ((int64_t)b >= a.n_bins) break;
+        resolve_bin<S, MS, SRGB, CAP>(a, draw, merged, pval, bstart, bend, image, ovf, T, w, lane, b);
+        __syncwarp();
     }
 }
 
@@ -1091,16 +1169,32 @@ __global__ void k_decode_keys(const uint64_t *__restrict__ skey, int64_t n, int 
     if (i < n) out[i] = key_from_local((uint32_t)(skey[i] & 0xFFFFFFu), nrows);
 }
 
+constexpr int kResolveBlocksPerSM = 4;  // shared-memory bound: ~53 KB per block
+
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+    }
+    return n;
+}
+
+int64_t resolve_blocks(const FrameArgs &a) {
+    const int64_t need = (a.n_bins + kResolveWarps - 1) / kResolveWarps;
+    return std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sm_count() * kResolveBlocksPerSM));
+}
+
 template <int S, bool MS, bool SRGB>
 void resolve_variant(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
                      const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
-                     cudaStream_t s) {
+                     uint32_t *queue, cudaStream_t s) {
     constexpr int CAP = MS ? 8 : 1;
     const size_t smem = sizeof(SmemTables) + (size_t)kResolveWarps * sizeof(BinState<CAP>);
     cudaFuncSetAttribute(k_resolve<S, MS, SRGB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const int64_t nbins = (int64_t)((a.W + kTileW - 1) / kTileW) * ((a.H + 1) / 2);
-    k_resolve<S, MS, SRGB><<<grid_for(nbins, kResolveWarps), kResolveWarps * 32, smem, s>>>(
-        a, draw, merged, pval, bstart, bend, image, overflow);
+    k_resolve<S, MS, SRGB><<<(unsigned)resolve_blocks(a), kResolveWarps * 32, smem, s>>>(
+        a, draw, merged, pval, bstart, bend, image, overflow, queue);
 }
 
 }  // namespace
@@ -1142,8 +1236,8 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
 int64_t flags_tmp_words(int64_t nf) { return 2 * ((nf + kFlagTile - 1) / kFlagTile + 2); }
 
 int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                      int8_t *wn_scan, int4 *draw, uint32_t *heads, FrameCounters *counters, uint32_t *tmp,
-                      cudaStream_t s) {
+                      int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
+                      uint32_t *tmp, cudaStream_t s) {
     const int64_t ntiles = (nf + kFlagTile - 1) / kFlagTile;
     uint32_t *s0 = tmp, *s1 = tmp + (ntiles + 2);
     k_wn_reduce<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(nf, perm, wn, s0);
@@ -1152,7 +1246,8 @@ int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const
     k_flags_reduce<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(a, nf, skey, wn_scan, s0, s1);
     scan_tiles_inplace(s0, ntiles, s);
     scan_tiles_inplace(s1, ntiles, s);
-    k_flags_down<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(a, nf, ntiles, skey, wn_scan, s0, s1, draw, heads, counters);
+    k_flags_down<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(a, nf, ntiles, skey, wn_scan, s0, s1, draw, heads,
+                                                            item_scene, counters);
     return 8;
 }
 
@@ -1169,16 +1264,17 @@ int launch_stencil(const FrameArgs &a, int64_t nf, int64_t nm, const uint64_t *s
     return 1;
 }
 
-int launch_item_tiles(const FrameArgs &a, const int4 *draw, int64_t n, uint32_t *cnt, cudaStream_t s) {
+int launch_item_tiles(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t n, uint32_t *cnt,
+                      cudaStream_t s) {
     if (n <= 0) return 0;
-    k_item_tiles<<<grid_for(n), kThreads, 0, s>>>(a, draw, n, cnt);
+    k_item_tiles<<<grid_for(n), kThreads, 0, s>>>(a, draw, item_scene, n, cnt);
     return 1;
 }
 
-int launch_emit_pairs(const FrameArgs &a, const int4 *draw, int64_t n, const uint32_t *offs, uint32_t *pkey,
-                       uint32_t *pval, cudaStream_t s) {
+int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t n,
+                      const uint32_t *offs, uint32_t *pkey, uint32_t *pval, cudaStream_t s) {
     if (n <= 0) return 0;
-    k_emit_pairs<<<grid_for(n), kThreads, 0, s>>>(a, draw, n, offs, pkey, pval);
+    k_emit_pairs<<<grid_for(n), kThreads, 0, s>>>(a, draw, item_scene, n, offs, pkey, pval);
     return 1;
 }
 
@@ -1190,23 +1286,26 @@ int launch_bin_bounds(const uint32_t *key, int64_t n, uint32_t *start, uint32_t 
 
 int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
                     const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
-                    cudaStream_t s) {
+                    FrameCounters *counters, cudaStream_t s) {
+    if (a.n_bins <= 0) return 0;
+    uint32_t *queue = &counters->bin_queue;
+    cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
     const bool ms = a.ms_output != 0, srgb = a.srgb != 0;
     if (a.S == 8) {
-        if (ms && srgb) resolve_variant<8, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else if (ms) resolve_variant<8, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else if (srgb) resolve_variant<8, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else resolve_variant<8, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        if (ms && srgb) resolve_variant<8, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else if (ms) resolve_variant<8, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else if (srgb) resolve_variant<8, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else resolve_variant<8, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
     } else if (a.S == 16) {
-        if (ms && srgb) resolve_variant<16, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else if (ms) resolve_variant<16, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else if (srgb) resolve_variant<16, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else resolve_variant<16, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        if (ms && srgb) resolve_variant<16, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else if (ms) resolve_variant<16, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else if (srgb) resolve_variant<16, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else resolve_variant<16, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
     } else {
-        if (ms && srgb) resolve_variant<32, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else if (ms) resolve_variant<32, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else if (srgb) resolve_variant<32, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, s);
-        else resolve_variant<32, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, s);
+        if (ms && srgb) resolve_variant<32, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else if (ms) resolve_variant<32, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else if (srgb) resolve_variant<32, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        else resolve_variant<32, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
     }
     return 1;
 }
@@ -1218,9 +1317,11 @@ int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cud
     return 2;
 }
 
+int64_t resolve_warps(const FrameArgs &a) { return resolve_blocks(a) * kResolveWarps; }
+
 int64_t resolve_overflow_words(const FrameArgs &a) {
     if (!(a.ms_output && a.S > 8)) return 0;
-    return (int64_t)((a.W + kTileW - 1) / kTileW) * ((a.H + 1) / 2) * 64 * 32;
+    return resolve_warps(a) * 64 * 32;
 }
 
 int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s) {

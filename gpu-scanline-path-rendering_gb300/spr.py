@@ -39,7 +39,7 @@ ERR_UNSUPPORTED = 8
 # ---- curve types / fill rules / stages / scene kinds -----------------------
 CURVE_LINEAR, CURVE_QUADRATIC, CURVE_CUBIC, CURVE_RATIONAL = 0x02, 0x03, 0x04, 0x13
 FILL_NONZERO, FILL_EVEN_ODD = 0, 1
-SCENE_RANDOM, SCENE_MIXED, SCENE_CUBICS = 0, 1, 2
+SCENE_RANDOM, SCENE_MIXED, SCENE_CUBICS, SCENE_LOCAL = 0, 1, 2, 3
 
 STAGES = [
     "TVERTEX", "PATH_VISIBLE", "CURVE_COUNT", "INTERSECTION", "FRAG_KEY", "FRAG_PID", "FRAG_WN",
@@ -94,6 +94,11 @@ class SceneSpec(C.Structure):
                 ("with_affine", C.c_int32)]
 
 
+class BatchScene(C.Structure):
+    _fields_ = [("scene", SceneView), ("width", C.c_int32), ("height", C.c_int32), ("samples", C.c_int32),
+                ("has_transform", C.c_int32), ("transform", C.c_float * 16)]
+
+
 _lib = None
 
 
@@ -133,6 +138,16 @@ def lib() -> C.CDLL:
         L.spr_scene_view_of.argtypes = [vp, C.POINTER(SceneView)]
         L.spr_scene_free.argtypes = [vp]
         L.spr_scene_free.restype = None
+        L.spr_batch_create.argtypes = [i32, i32, i32, C.POINTER(vp)]
+        L.spr_batch_destroy.argtypes = [vp]
+        L.spr_batch_set_scenes.argtypes = [vp, C.POINTER(BatchScene), i32]
+        L.spr_batch_render.argtypes = [vp, vp]
+        L.spr_batch_image_device_ptr.argtypes = [vp, i32, C.POINTER(vp)]
+        L.spr_batch_read_image.argtypes = [vp, i32, vp, vp]
+        L.spr_batch_get_counts.argtypes = [vp, C.POINTER(ElementNumber)]
+        L.spr_batch_get_frame_stats.argtypes = [vp, C.POINTER(FrameStats)]
+        L.spr_batch_enable_step_timing.argtypes = [vp, i32]
+        L.spr_batch_step_timing.argtypes = [vp, C.POINTER(C.c_double), i32, C.POINTER(i32)]
         _lib = L
     return _lib
 
@@ -334,3 +349,90 @@ class VGRasterizer:
             check(lib().spr_debug_dump(self._h, sid, out.ctypes.data, need.value, C.byref(need)),
                   f"spr_debug_dump({name})")
         return out
+
+
+class Batch:
+    """Many independent scenes rendered together (spr_batch_*).
+
+    ``set_scenes`` takes a list of ``(scene, width, height, samples)`` or
+    ``(scene, width, height, samples, transform)`` tuples; image ``i`` of
+    ``read_image(i)`` is the one a :class:`VGRasterizer` with the same
+    settings renders for scene ``i``.
+    """
+
+    def __init__(self, ms_output=True, srgb=True, device=0):
+        self._h = C.c_void_p()
+        check(lib().spr_batch_create(device, int(ms_output), int(srgb), C.byref(self._h)), "spr_batch_create")
+        self._sizes = []
+        self._keep = []
+
+    def close(self):
+        if self._h:
+            lib().spr_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_scenes(self, items):
+        arr = (BatchScene * max(len(items), 1))()
+        keep = []
+        for i, it in enumerate(items):
+            scene, w, h, smp = it[:4]
+            tf = it[4] if len(it) > 4 else None
+            arr[i].scene = scene.view()
+            keep.append(scene)
+            arr[i].width, arr[i].height, arr[i].samples = int(w), int(h), int(smp)
+            arr[i].has_transform = 0 if tf is None else 1
+            if tf is not None:
+                m = np.ascontiguousarray(tf, dtype=np.float32).reshape(16)
+                for j in range(16):
+                    arr[i].transform[j] = float(m[j])
+        check(lib().spr_batch_set_scenes(self._h, arr, len(items)), "spr_batch_set_scenes")
+        self._sizes = [(int(it[1]), int(it[2])) for it in items]
+        self._keep = keep
+
+    def render(self, stream=None):
+        check(lib().spr_batch_render(self._h, stream), "spr_batch_render")
+
+    def image_device_ptr(self, i) -> int:
+        p = C.c_void_p()
+        check(lib().spr_batch_image_device_ptr(self._h, i, C.byref(p)), "spr_batch_image_device_ptr")
+        return p.value or 0
+
+    def read_image(self, i, out=None, stream=None) -> np.ndarray:
+        if not 0 <= i < len(self._sizes):
+            raise SprError(ERR_INVALID_ARG, f"spr_batch_read_image: no scene {i}")
+        w, h = self._sizes[i]
+        if out is None:
+            out = np.empty((h, w, 4), dtype=np.uint8)
+        check(lib().spr_batch_read_image(self._h, i, out.ctypes.data, stream), "spr_batch_read_image")
+        return out
+
+    def element_number(self) -> dict:
+        e = ElementNumber()
+        check(lib().spr_batch_get_counts(self._h, C.byref(e)), "spr_batch_get_counts")
+        return e.as_dict()
+
+    def frame_stats(self) -> dict:
+        st = FrameStats()
+        check(lib().spr_batch_get_frame_stats(self._h, C.byref(st)), "spr_batch_get_frame_stats")
+        return {n: int(getattr(st, n)) for n, _ in FrameStats._fields_}
+
+    def enable_step_timing(self, f=True):
+        check(lib().spr_batch_enable_step_timing(self._h, int(f)), "spr_batch_enable_step_timing")
+
+    def step_timing(self) -> dict:
+        buf = (C.c_double * 64)()
+        n = C.c_int32()
+        check(lib().spr_batch_step_timing(self._h, buf, 64, C.byref(n)), "spr_batch_step_timing")
+        return {lib().spr_step_name(i).decode(): buf[i] for i in range(n.value)}

@@ -256,6 +256,42 @@ int spr_scan_offsets_noalloc(const uint32_t *d_counts, uint32_t *d_offsets, int6
 /* Human-readable text for a status code (static string). */
 const char *spr_status_string(int32_t status);
 
+/* ---- batches (an extension: no counterpart in the reference) ------------
+ * Many independent scenes of uneven size rendered together: the scenes are
+ * concatenated on the device, every path carries the index of its scene, and
+ * one launch sequence per sample count present renders all of them, the
+ * resolve taking (scene, cell row, 32-column tile) bins from one device
+ * queue.  Scene i's image is RGBA8, width_i x height_i, the same bytes a
+ * single-scene handle with the same settings renders for it.
+ */
+typedef struct spr_batch spr_batch;
+typedef struct spr_batch_scene {
+    spr_scene_view scene;
+    int32_t width;         /* 1..4096                                        */
+    int32_t height;        /* 1..4096                                        */
+    int32_t samples;       /* 8, 16 or 32                                    */
+    int32_t has_transform; /* 1 = transform (row-major 4x4) is applied       */
+    float transform[16];
+} spr_batch_scene;
+/* ms_output and srgb apply to every scene of the batch. */
+int spr_batch_create(int32_t device, int32_t ms_output, int32_t srgb, spr_batch **out);
+int spr_batch_destroy(spr_batch *b);
+/* Validates and uploads n scenes (the arrays are copied); replaces the
+ * previous set.  SPR_ERR_INVALID_SCENE / SPR_ERR_INVALID_ARG name no scene:
+ * check each with spr_validate_scene to find it. */
+int spr_batch_set_scenes(spr_batch *b, const spr_batch_scene *scenes, int32_t n);
+int spr_batch_render(spr_batch *b, void *stream);
+/* Device pointer to scene i's image (valid until the next set_scenes). */
+int spr_batch_image_device_ptr(spr_batch *b, int32_t scene, void **out);
+int spr_batch_read_image(spr_batch *b, int32_t scene, uint8_t *host_rgba, void *stream);
+/* Totals over the scenes of the last render. */
+int spr_batch_get_counts(spr_batch *b, spr_element_number *total);
+int spr_batch_get_frame_stats(spr_batch *b, spr_frame_stats *out);
+/* Per-step device time of the last render, summed over the sample-count
+ * groups (steps as spr_step_name). */
+int spr_batch_enable_step_timing(spr_batch *b, int32_t enable);
+int spr_batch_step_timing(spr_batch *b, double *ms, int32_t capacity, int32_t *n_out);
+
 /* ---- synthetic scenes ---------------------------------------------------- */
 /*
  * Seeded synthetic scene generator standing in for the reference's MPVG .rvg
@@ -269,8 +305,13 @@ const char *spr_status_string(int32_t status);
  *                       n_paths = glyphs, n_large = large paths.
  *   SPR_SCENE_CUBICS  : n_paths closed paths of seg_min..seg_max cubic
  *                       segments (the differentiable-render scene).
+ *   SPR_SCENE_LOCAL   : as SPR_SCENE_RANDOM, but each path's control points
+ *                       are uniform in its own square box, side U[d/32, d/4]
+ *                       (d = min(width, height)), placed uniformly (the
+ *                       batched scenes: overdraw stays bounded as n_paths
+ *                       grows).
  */
-enum spr_scene_kind { SPR_SCENE_RANDOM = 0, SPR_SCENE_MIXED = 1, SPR_SCENE_CUBICS = 2 };
+enum spr_scene_kind { SPR_SCENE_RANDOM = 0, SPR_SCENE_MIXED = 1, SPR_SCENE_CUBICS = 2, SPR_SCENE_LOCAL = 3 };
 
 typedef struct spr_scene_spec {
     int32_t kind;

@@ -39,7 +39,7 @@ def test_status_strings():
     assert b"unknown" in spr.lib().spr_status_string(99)
 
 
-@pytest.mark.parametrize("kind", [spr.SCENE_RANDOM, spr.SCENE_MIXED, spr.SCENE_CUBICS])
+@pytest.mark.parametrize("kind", [spr.SCENE_RANDOM, spr.SCENE_MIXED, spr.SCENE_CUBICS, spr.SCENE_LOCAL])
 def test_generator_deterministic_and_valid(kind):
     a = spr.Scene.generate(kind, seed=5, width=300, height=200, n_paths=30, n_large=4, seg_min=8,
                            seg_max=20, with_rational=True, with_affine=True)
@@ -117,3 +117,23 @@ def test_create_rejects_bad_config_before_touching_the_device():
     for cfg in (spr.Config(0, 64, 8, 1, 1, 0), spr.Config(64, 5000, 8, 1, 1, 0), spr.Config(64, 64, 12, 1, 1, 0)):
         h = C.c_void_p()
         assert spr.lib().spr_create(C.byref(cfg), C.byref(h)) == spr.ERR_INVALID_ARG
+
+
+def test_local_scene_paths_stay_in_their_boxes():
+    s = spr.Scene.generate(spr.SCENE_LOCAL, seed=12, width=1024, height=768, n_paths=200, seg_min=8, seg_max=32)
+    assert s.validate() == spr.OK and s.n_paths == 200
+    for p in range(s.n_paths):
+        v = s.vertex[s.vertex_path_id == p]
+        ext = v.max(axis=0) - v.min(axis=0)
+        assert ext.max() <= 768 / 4 + 1e-3
+
+
+def test_batch_create_without_gpu_fails_cleanly():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert spr.lib().spr_batch_create(0, 1, 1, C.byref(h)) == spr.ERR_CUDA and not h.value
+    assert spr.lib().spr_batch_create(0, 1, 1, None) == spr.ERR_INVALID_ARG
+    assert spr.lib().spr_batch_render(None, None) == spr.ERR_INVALID_ARG
