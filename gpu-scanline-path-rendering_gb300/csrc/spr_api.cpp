@@ -98,6 +98,11 @@ struct spr_handle {
     int n_scenes = 0;
     std::vector<SceneInfo> scenes_h;
     DevBuf scenes_d, path_scene, item_scene;
+    // differentiable frames: per-fragment chords and left masks, per-item
+    // paths, the per-block tapes, the transformed-vertex gradient and the
+    // stored -> input vertex map
+    DevBuf chord, lmask, item_path, tape, tape_item, grad_tvert, vmap;
+    int tape_depth = 128;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
         wn_scan, draw, heads, flags_tmp, merged, tiles, pair_off, pkey[2], pval[2], bins, image, counters, dump_tmp,
@@ -158,6 +163,9 @@ FrameArgs make_args(const spr_handle *h) {
     a.fill_rgba = h->fill.as<uint32_t>();
     a.mask_table = h->mask_table.as<uint32_t>();
     a.rtables = h->rtables.as<ResolveTables>();
+    a.chord = nullptr;
+    a.lmask = nullptr;
+    a.item_path = nullptr;
     if (h->n_scenes > 0) {
         a.path_scene = h->path_scene.as<uint32_t>();
         a.scenes = h->scenes_d.as<SceneInfo>();
@@ -259,7 +267,8 @@ int spr_destroy(spr_handle *h) {
                       &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
                       &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
                       &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
-                      &h->item_scene};
+                      &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_item,
+                      &h->grad_tvert, &h->vmap};
     for (DevBuf *b : bufs) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
@@ -315,6 +324,8 @@ int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     // (y_first, x_first) < (y_last, x_last) comparing float bit patterns.
     std::vector<float> vert(v->vertex, v->vertex + 2 * (size_t)V);
     std::vector<CurveDesc> cd(C);
+    std::vector<uint32_t> vmap(V);
+    for (uint32_t i = 0; i < V; ++i) vmap[i] = i;
     for (uint32_t i = 0; i < C; ++i) {
         const int type = v->curve_type[i];
         const int vn = type & 7;
@@ -327,6 +338,7 @@ int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
         uint32_t rev = 0;
         if (!(byf < byl || (byf == byl && bxf < bxl))) {
             rev = 1;
+            for (int k = 0; k < vn; ++k) vmap[p + k] = p + vn - 1 - k;
             for (int k = 0; k < vn / 2; ++k) {
                 std::swap(vert[2 * (p + k)], vert[2 * (p + vn - k - 1)]);
                 std::swap(vert[2 * (p + k) + 1], vert[2 * (p + vn - k - 1) + 1]);
@@ -338,6 +350,7 @@ int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
         cd[i].type = (uint32_t)type | (rev << 8);
     }
     if ((st = upload(h->vertex, vert.data(), vert.size()))) return st;
+    if ((st = upload(h->vmap, vmap.data(), vmap.size()))) return st;
     if ((st = upload(h->vpid, v->vertex_path_id, V))) return st;
     if ((st = upload(h->curves, cd.data(), C))) return st;
     if ((st = upload(h->rule, v->path_fill_rule, P))) return st;
@@ -359,7 +372,82 @@ int spr_set_transform(spr_handle *h, const float m[16]) {
     return SPR_OK;
 }
 
-int spr_render(spr_handle *h, void *stream) {
+}  // extern "C"
+
+namespace {
+
+// A differentiable frame: the resolve step becomes the float composite
+// (forward) or its adjoint (backward).  Pointers are device pointers.
+struct DiffCall {
+    bool backward;
+    const float *fill;        // 4 per path
+    const float *grad_image;  // 4 per pixel (backward)
+    float *image;             // 4 per pixel (forward)
+    float *grad_fill;         // 4 per path (backward)
+    float *grad_vertex;       // 2 per input vertex (backward)
+    float *grad_affine;       // 6 per path, or null (backward)
+};
+
+int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint32_t *pv, const uint32_t *bstart,
+               const uint32_t *bend, cudaStream_t s, int *L) {
+    DiffArgs d{};
+    d.fill = reinterpret_cast<const float4 *>(dc.fill);
+    d.grad_image = reinterpret_cast<const float4 *>(dc.grad_image);
+    d.image = reinterpret_cast<float4 *>(dc.image);
+    d.grad_fill = reinterpret_cast<float4 *>(dc.grad_fill);
+    d.draw = h->draw.as<int4>();
+    d.merged = h->merged.as<uint32_t>();
+    d.pval = pv;
+    d.bstart = bstart;
+    d.bend = bend;
+    d.chord = h->chord.as<float4>();
+    d.lmask = h->lmask.as<uint32_t>();
+    d.pidw = h->pidw.as<uint32_t>();
+    d.perm = h->perm_sorted;
+    d.heads = h->heads.as<uint32_t>();
+    d.item_path = h->item_path.as<uint32_t>();
+    d.skey = h->skey_sorted;
+    d.wn_scan = h->wn_scan.as<int8_t>();
+    d.entries = h->entries.as<int2>();
+    d.tvert = h->tvert.as<float2>();
+    d.nf = h->nf;
+    FrameCounters *ctr = h->counters.as<FrameCounters>();
+    d.queue = &ctr->bin_queue;
+    d.status = &ctr->status;
+    if (!dc.backward) {
+        *L += launch_diff_forward(a, d, s);
+        return cuda_status();
+    }
+    int st = ensure(h->grad_tvert, 8 * (size_t)std::max<uint32_t>(h->V, 1));
+    if (st) return st;
+    d.grad_tvert = h->grad_tvert.as<float2>();
+    for (int depth = h->tape_depth;; depth *= 2) {
+        const int64_t words = diff_tape_words(a, depth);
+        if ((st = ensure(h->tape, 16 * (size_t)words)) || (st = ensure(h->tape_item, 4 * (size_t)(words / (a.S / 8)))))
+            return st;
+        d.tape = h->tape.as<float4>();
+        d.tape_item = h->tape_item.as<uint32_t>();
+        d.tape_depth = depth;
+        cudaMemsetAsync(dc.grad_fill, 0, 16 * (size_t)h->P, s);
+        cudaMemsetAsync(h->grad_tvert.p, 0, 8 * (size_t)h->V, s);
+        cudaMemsetAsync(&ctr->status, 0, 4, s);
+        *L += launch_diff_backward(a, d, s);
+        cudaMemcpyAsync(h->h_u32, &ctr->status, 4, cudaMemcpyDeviceToHost, s);
+        ++h->host_syncs;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+        if (!(h->h_u32[0] & 1u)) {
+            h->tape_depth = depth;
+            break;
+        }
+        if (depth >= (1 << 16)) return SPR_ERR_CAPACITY_EXCEEDED;
+    }
+    if (dc.grad_affine) cudaMemsetAsync(dc.grad_affine, 0, 24 * (size_t)h->P, s);
+    *L += launch_diff_vertex(a, h->grad_tvert.as<float2>(), h->vmap.as<uint32_t>(),
+                             reinterpret_cast<float2 *>(dc.grad_vertex), dc.grad_affine, s);
+    return cuda_status();
+}
+
+int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     if (!h) return SPR_ERR_INVALID_ARG;
     if (!h->has_scene) return SPR_ERR_NO_SCENE;
     cudaSetDevice(h->cfg.device);
@@ -369,7 +457,7 @@ int spr_render(spr_handle *h, void *stream) {
     h->frame_valid = false;
     int L = 0;  // kernels launched by this frame
     h->host_syncs = 0;
-    const FrameArgs a = make_args(h);
+    FrameArgs a = make_args(h);
     const int W = a.W, H = a.H, WORDS = a.S / 8;
     const bool batch = h->n_scenes > 0;
     const int64_t npix = frame_pixels(h);
@@ -411,8 +499,12 @@ int spr_render(spr_handle *h, void *stream) {
     if (nf == 0) {
         cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
         for (int i = 2; i <= 6; ++i) rec(h, i, s);
-        L += launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(),
-                            h->overflow.as<uint32_t>(), h->counters.as<FrameCounters>(), s);
+        if (dc) {
+            if ((st = diff_stage(h, a, *dc, nullptr, bin_start, bin_end, s, &L))) return st;
+        } else {
+            L += launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(),
+                                h->overflow.as<uint32_t>(), h->counters.as<FrameCounters>(), s);
+        }
         rec(h, 7, s);
         rec(h, 8, s);
         h->launches = L;
@@ -434,6 +526,14 @@ int spr_render(spr_handle *h, void *stream) {
         (batch && (st = ensure(h->item_scene, 4 * 2 * (size_t)nf))))
         return st;
     uint32_t *item_scene = batch ? h->item_scene.as<uint32_t>() : nullptr;
+    if (dc) {
+        if ((st = ensure(h->chord, 16 * (size_t)nf)) || (st = ensure(h->lmask, 4 * (size_t)WORDS * nf)) ||
+            (st = ensure(h->item_path, 4 * 2 * (size_t)nf)))
+            return st;
+        a.chord = h->chord.as<float4>();
+        a.lmask = h->lmask.as<uint32_t>();
+        a.item_path = h->item_path.as<uint32_t>();
+    }
     rec(h, 2, s);
     L += launch_curve_emit(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->offsets.as<uint32_t>(), h->entries.as<int2>(),
                       s);
@@ -496,8 +596,12 @@ int spr_render(spr_handle *h, void *stream) {
     cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
     L += launch_bin_bounds(pk, npairs, bin_start, bin_end, s);
     rec(h, 7, s);
-    L += launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end,
-                        h->image.as<uint32_t>(), h->overflow.as<uint32_t>(), h->counters.as<FrameCounters>(), s);
+    if (dc) {
+        if ((st = diff_stage(h, a, *dc, pv, bin_start, bin_end, s, &L))) return st;
+    } else {
+        L += launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end,
+                            h->image.as<uint32_t>(), h->overflow.as<uint32_t>(), h->counters.as<FrameCounters>(), s);
+    }
     rec(h, 8, s);
     if ((st = cuda_status())) return st;
     if (h->timing) {
@@ -514,6 +618,28 @@ int spr_render(spr_handle *h, void *stream) {
     h->frame_H = H;
     h->frame_S = a.S;
     return SPR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int spr_render(spr_handle *h, void *stream) { return render_frame(h, stream, nullptr); }
+
+int spr_diff_render(spr_handle *h, const float *fill_rgba, float *image, void *stream) {
+    if (!h || !fill_rgba || !image) return SPR_ERR_INVALID_ARG;
+    if (h->n_scenes > 0) return SPR_ERR_UNSUPPORTED;
+    const DiffCall dc{false, fill_rgba, nullptr, image, nullptr, nullptr, nullptr};
+    return render_frame(h, stream, &dc);
+}
+
+int spr_diff_backward(spr_handle *h, const float *fill_rgba, const float *grad_image, float *grad_fill,
+                      float *grad_vertex, float *grad_affine, void *stream) {
+    if (!h || !fill_rgba || !grad_image || !grad_fill || !grad_vertex) return SPR_ERR_INVALID_ARG;
+    if (h->n_scenes > 0) return SPR_ERR_UNSUPPORTED;
+    if (grad_affine && !h->has_affine) return SPR_ERR_INVALID_ARG;
+    const DiffCall dc{true, fill_rgba, grad_image, nullptr, grad_fill, grad_vertex, grad_affine};
+    return render_frame(h, stream, &dc);
 }
 
 int spr_image_device_ptr(spr_handle *h, void **out) {
@@ -581,7 +707,8 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
                             &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
                             &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d,
-                            &h->path_scene, &h->item_scene};
+                            &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
+                            &h->tape_item,  &h->grad_tvert, &h->vmap};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;

@@ -92,6 +92,11 @@ struct FrameArgs {
     const SceneInfo *scenes;
     int n_scenes;
     int64_t n_bins;  // resolve bins of the frame
+    // Differentiable frames (else null): per fragment its chord in cell
+    // units (q0, q1) and its left mask; per draw item its path.
+    float4 *chord;
+    uint32_t *lmask;
+    uint32_t *item_path;
 };
 
 int launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible,
@@ -130,5 +135,38 @@ int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_
 int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s);
 int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cudaStream_t s);
 int launch_decode_keys(const uint64_t *skey, int64_t nf, int nrows, int32_t *out, cudaStream_t s);
+
+// Differentiable frames (spr_diff.cu).  Device pointers; fill is linear
+// RGBA per path.  Gradients are accumulated (the caller zeroes them).
+struct DiffArgs {
+    const float4 *fill;
+    const float4 *grad_image;  // backward input, dL/d(pixel), W x H
+    float4 *image;             // forward output, W x H
+    float4 *grad_fill;         // per path
+    float2 *grad_tvert;        // per stored vertex, in transformed space
+    const int4 *draw;
+    const uint32_t *merged;
+    const uint32_t *pval, *bstart, *bend;
+    const float4 *chord;
+    const uint32_t *lmask, *pidw, *perm, *heads, *item_path;
+    const uint64_t *skey;
+    const int8_t *wn_scan;
+    const int2 *entries;
+    const float2 *tvert;
+    int64_t nf;
+    float4 *tape;        // per block: tape_depth x (samples per thread) x block threads
+    uint32_t *tape_item; // per block: tape_depth x block threads
+    int tape_depth;
+    uint32_t *queue;     // bin queue (zeroed by the launchers)
+    uint32_t *status;    // bit 0: a tape overflowed (rerun with a deeper tape)
+};
+int64_t diff_blocks(const FrameArgs &a);
+int64_t diff_tape_words(const FrameArgs &a, int depth);  // float4 count; tape_item needs depth * threads * blocks
+int launch_diff_forward(const FrameArgs &a, const DiffArgs &d, cudaStream_t s);
+int launch_diff_backward(const FrameArgs &a, const DiffArgs &d, cudaStream_t s);
+// dL/d(stored vertex in transformed space) -> dL/d(input vertex), dL/d(path affine).
+// vmap: stored vertex -> input vertex index (curves reversed on upload).
+int launch_diff_vertex(const FrameArgs &a, const float2 *grad_tvert, const uint32_t *vmap, float2 *grad_vertex,
+                       float *grad_affine, cudaStream_t s);
 
 }  // namespace spr

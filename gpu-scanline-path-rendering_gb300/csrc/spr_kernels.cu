@@ -270,6 +270,8 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
     if (e0.x != e1.x) t1 = 1.f;
     int wnchg = 0, swn = 0;
     uint32_t mask[4] = {0u, 0u, 0u, 0u};
+    float4 chord = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t lmk[4] = {0u, 0u, 0u, 0u};
     if (t0 < t1) {
         CurveGeom g;
         load_geom(d, tv, g);
@@ -345,6 +347,9 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
         const float bx = (float)px, by = (float)py;
         const float q0x = (c0x - bx) * .5f, q0y = (c0y - by) * .5f;
         const float q1x = (c1x - bx) * .5f, q1y = (c1y - by) * .5f;
+        chord = make_float4(q0x, q0y, q1x, q1y);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) lmk[w] = lm[w];
         uint32_t vm[4];
         vertical_mask2<S>(q0y, q1y, vm);
         const int texel = table_texel(q0x, q0y, q1x, q1y);
@@ -362,6 +367,11 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
             mask[2] = (tm.z & vm[2]) ^ lm[2];
             mask[3] = (tm.w & vm[3]) ^ lm[3];
         }
+    }
+    if (a.chord != nullptr) {
+        a.chord[i] = chord;
+#pragma unroll
+        for (int w = 0; w < WORDS; ++w) a.lmask[i * WORDS + w] = lmk[w];
     }
     key_out[i] = yx;
     pid_out[i] = pathid | ((uint32_t)wnchg << 30);
@@ -540,6 +550,10 @@ __global__ void __launch_bounds__(kFlagThreads) k_flags_down(FrameArgs a, int64_
                 const uint32_t sc = a.path_scene[p];
                 if (ff) item_scene[nfb + nsb] = sc;
                 if (sf) item_scene[nfb + nsb + ff] = sc;
+            }
+            if (a.item_path != nullptr) {
+                if (ff) a.item_path[nfb + nsb] = p;
+                if (sf) a.item_path[nfb + nsb + ff] = p;
             }
             if (ff) {
                 const int32_t pos = (int32_t)(((uint32_t)key_y(key1) << 16) | (uint32_t)key_x(key1));
@@ -754,25 +768,22 @@ __device__ __forceinline__ uint32_t blend_sample(const SmemTables &t, int lane, 
 // Each pixel keeps its samples as a short list of (sample mask, RGBA8 colour)
 // entries whose masks partition the pixel's samples: equal colours are merged
 // after every blend, so a pixel typically holds 1-3 entries and a blend costs
-// one evaluation per entry instead of one per sample.  A 32-sample pixel that
-// would need more than 8 entries (about 1 pixel event in 2000 on dense
-// scenes) switches to an explicit 32-sample array in a global overflow area
-// owned by its bin (count = kFull) and switches back once it has 8 or fewer
-// distinct colours.  Every sample still gets exactly the value the
-// per-sample rule gives.
+// one evaluation per entry instead of one per sample.  A pixel that would
+// need more than kCapMS entries (rare) switches to an explicit per-sample
+// array in a global overflow area owned by the warp resolving its bin
+// (count = kFull) and switches back once it has kCapMS or fewer distinct
+// colours.  Every sample still gets exactly the value the per-sample rule
+// gives.
 constexpr uint8_t kFull = 0xFF;
-constexpr int kChunk = 64;  // blend tasks per chunk
+constexpr int kCapMS = 8;  // entries per pixel in the multisample modes
 
 template <int CAP>
 struct BinState {
     uint32_t emask[CAP][64];
     uint32_t ecol[CAP][64];
     uint8_t cnt[64];
-    uint32_t cm[32];  // column mask of each staged item
-    int4 it[32];
-    uint4 mm[32];
-    uint32_t task[kChunk];  // packed (pixel, entry, item) blend tasks of one chunk
-    uint32_t tres[kChunk];  // their results
+    int4 it[32];  // staged draw items
+    uint4 mm[32];  // their merged sample masks
 };
 
 // Columns [c0, c1) of a bin as a bit mask.
@@ -899,11 +910,11 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
     for (uint32_t base = beg; base < fin; base += 32) {
         __syncwarp();
         const int cnt = (int)min(32u, fin - base);
+        uint32_t cm = 0u;  // columns of this lane's staged item
         if (lane < cnt) {
             const int4 it = draw[pval[base + lane]];
             w.it[lane] = it;
             const int x = (int)((uint32_t)it.x & 0xFFFFu) - tx0;
-            uint32_t cm;
             if (it.w != 0) {
                 if constexpr (MW == 4) {
                     w.mm[lane] = __ldg(reinterpret_cast<const uint4 *>(merged) + (it.w - 1));
@@ -917,161 +928,98 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
             } else {
                 cm = col_bits(max(x, 0), min(x + it.y, cols));
             }
-            w.cm[lane] = cm;
         }
         __syncwarp();
-        int q0 = 0;
-        while (q0 < cnt) {
-            // batch [q0, q1): items with pairwise disjoint column sets; lane =
-            // column, owning pixels p0 = lane and p1 = 32 + lane
-            uint32_t acc = 0u;
-            int q1 = q0;
-            while (q1 < cnt && (acc & w.cm[q1]) == 0u) acc |= w.cm[q1++];
-            int q = -1;
-            uint32_t msk[2] = {0u, 0u};  // sample mask per row (ALL for spans)
-            int n0[2] = {0, 0};          // entry counts before this batch
-            bool frag = false;
-            if ((acc >> lane) & 1u) {
-                q = q0;
-                while (!((w.cm[q] >> lane) & 1u)) ++q;
-                const int4 it = w.it[q];
-                frag = it.w != 0;
-                const int dx = lane + tx0 - (int)((uint32_t)it.x & 0xFFFFu);
-                const uint4 mm = w.mm[q];
+        // mine: bit q = staged item q covers this lane's column (a transpose
+        // of the 32 x 32 bit matrix of column sets)
+        uint32_t mine = 0u;
 #pragma unroll
-                for (int py = 0; py < 2; ++py) {
-                    if (py >= rows) break;
-                    const int p = py * 32 + lane;
-                    uint32_t m = ALL;
-                    if (frag) {
-                        const int k = dx * 2 + py;
-                        m = cell_pixel_mask<S>(mm, k);
-                        if constexpr (!MS) m = m ? ALL : 0u;
-                    }
-                    msk[py] = m;
-                    int n = w.cnt[p];
-                    if (m != 0u && n != kFull && frag && MS) {
-                        int splits = 0;
-                        for (int j = 0; j < n; ++j) {
-                            const uint32_t em = w.emask[j][p];
-                            splits += ((em & m) != 0u && (em & ~m) != 0u) ? 1 : 0;
-                        }
-                        if (n + splits > CAP) {
-                            to_full<S, CAP, EXPLICIT>(w, ovf, p);
-                            n = kFull;
-                        }
-                    }
-                    n0[py] = n;
-                }
-            }
-            // phase A: the entries of this lane's pixels that the batch blends
-            // (a snapshot: splits below rewrite entry masks)
-            uint32_t tj[2] = {0u, 0u};
+        for (int L = 0; L < 32; ++L) {
+            const uint32_t bm = __ballot_sync(0xffffffffu, (cm >> L) & 1u);
+            if (lane == L) mine = bm;
+        }
+        // every lane applies its own items in draw order to its two pixels
+        while (mine) {
+            const int q = __ffs(mine) - 1;
+            mine &= mine - 1u;
+            const int4 it = w.it[q];
+            const bool frag = it.w != 0;
+            const uint32_t c = (uint32_t)it.z;
+            const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
+                        sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
+            const float sa0 = lin8(c >> 24);
+            const int dx = lane + tx0 - (int)((uint32_t)it.x & 0xFFFFu);
+            const uint4 mm = frag ? w.mm[q] : make_uint4(0u, 0u, 0u, 0u);
+            // one-entry memo of blend(dst) for this item (same source, same alpha)
+            uint32_t memo_d = 0u, memo_r = 0u;
+            bool memo = false;
 #pragma unroll
             for (int py = 0; py < 2; ++py) {
-                if (msk[py] == 0u || n0[py] == kFull) continue;
+                if (py >= rows) break;
                 const int p = py * 32 + lane;
-                for (int j = 0; j < n0[py]; ++j) tj[py] |= (w.emask[j][p] & msk[py]) != 0u ? (1u << j) : 0u;
-            }
-            const int ntask = __popc(tj[0]) + __popc(tj[1]);
-            int off = ntask;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(0xffffffffu, off, o);
-                if (lane >= o) off += v;
-            }
-            const int total = __shfl_sync(0xffffffffu, off, 31);
-            off -= ntask;
-            for (int cb = 0; cb < total; cb += kChunk) {
-                const int ce = min(cb + kChunk, total);
-                // write this lane's tasks that fall in [cb, ce)
-                if (off < ce && off + ntask > cb) {
-                    int t = off;
-#pragma unroll
-                    for (int py = 0; py < 2; ++py) {
-                        const int p = py * 32 + lane;
-                        for (uint32_t bits = tj[py]; bits; bits &= bits - 1u) {
-                            const int j = __ffs(bits) - 1;
-                            if (t >= cb && t < ce) w.task[t - cb] = (uint32_t)p | ((uint32_t)j << 6) | ((uint32_t)q << 11);
-                            ++t;
-                        }
-                    }
-                }
-                __syncwarp();
-                // phase B: all lanes blend
-                for (int t = lane; t < ce - cb; t += 32) {
-                    const uint32_t tk = w.task[t];
-                    const int p = (int)(tk & 63u), j = (int)((tk >> 6) & 31u), tq = (int)(tk >> 11);
-                    const int4 it = w.it[tq];
-                    const uint32_t c = (uint32_t)it.z;
-                    const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
-                                sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
-                    float sa = lin8(c >> 24);
+                uint32_t m = ALL;
+                float sa = sa0;
+                if (frag) {
+                    m = cell_pixel_mask<S>(mm, dx * 2 + py);
+                    if (m == 0u) continue;
                     if constexpr (!MS) {
-                        if (it.w != 0) {
-                            const int k = ((p & 31) + tx0 - (int)((uint32_t)it.x & 0xFFFFu)) * 2 + (p >> 5);
-                            const uint4 mm = w.mm[tq];
-                            const uint32_t m = cell_pixel_mask<S>(mm, k);
-                            sa = sa * ((float)__popc(m) / (float)S);
-                        }
+                        sa = sa0 * ((float)__popc(m) / (float)S);
+                        m = ALL;
+                        memo = false;
                     }
-                    w.tres[t] = blend_sample<SRGB>(T, lane, w.ecol[j][p], sr, sg, sb, sa, 1.f - sa);
                 }
-                __syncwarp();
-                // phase C: owners apply their results
-                if (off < ce && off + ntask > cb) {
-                    int t = off;
-#pragma unroll
-                    for (int py = 0; py < 2; ++py) {
-                        const int p = py * 32 + lane;
-                        const uint32_t m = msk[py];
-                        for (uint32_t bits = tj[py]; bits; bits &= bits - 1u) {
-                            const int j = __ffs(bits) - 1;
-                            const uint32_t em = w.emask[j][p];
-                            const uint32_t in = em & m;
-                            if (t >= cb && t < ce) {
-                                const uint32_t nc = w.tres[t - cb];
-                                if (in == em) {
-                                    w.ecol[j][p] = nc;
-                                } else {
-                                    const int nn = w.cnt[p];
-                                    w.emask[j][p] = em & ~m;
-                                    w.emask[nn][p] = in;
-                                    w.ecol[nn][p] = nc;
-                                    w.cnt[p] = (uint8_t)(nn + 1);
-                                }
+                const float om = 1.f - sa;
+                int n = w.cnt[p];
+                if (EXPLICIT && n != kFull && frag) {
+                    int splits = 0;
+                    for (int j = 0; j < n; ++j) {
+                        const uint32_t em = w.emask[j][p];
+                        splits += ((em & m) != 0u && (em & ~m) != 0u) ? 1 : 0;
+                    }
+                    if (n + splits > CAP) {
+                        to_full<S, CAP, EXPLICIT>(w, ovf, p);
+                        n = kFull;
+                    }
+                }
+                if (n == kFull) {
+                    if constexpr (EXPLICIT) {
+                        for (uint32_t mk = m; mk; mk &= mk - 1u) {
+                            uint32_t &v = full_sample(ovf, p, __ffs(mk) - 1);
+                            const uint32_t dv = v;
+                            if (!(memo && dv == memo_d)) {
+                                memo_r = blend_sample<SRGB>(T, lane, dv, sr, sg, sb, sa, om);
+                                memo_d = dv;
+                                memo = true;
                             }
-                            ++t;
+                            v = memo_r;
                         }
+                        try_compress<S, CAP, EXPLICIT>(w, ovf, p);
+                    }
+                    continue;
+                }
+                const int n0 = n;
+                for (int j = 0; j < n0; ++j) {
+                    const uint32_t em = w.emask[j][p];
+                    const uint32_t in = em & m;
+                    if (in == 0u) continue;
+                    const uint32_t dv = w.ecol[j][p];
+                    if (!(memo && dv == memo_d)) {
+                        memo_r = blend_sample<SRGB>(T, lane, dv, sr, sg, sb, sa, om);
+                        memo_d = dv;
+                        memo = true;
+                    }
+                    if (in == em) {
+                        w.ecol[j][p] = memo_r;
+                    } else {
+                        w.emask[j][p] = em & ~m;
+                        w.emask[n][p] = in;
+                        w.ecol[n][p] = memo_r;
+                        ++n;
                     }
                 }
-                __syncwarp();
+                w.cnt[p] = (uint8_t)n;
+                if (n > 1) dedup(w, p);
             }
-            // explicit-sample pixels (rare), then merge equal colours
-            if (q >= 0) {
-#pragma unroll
-                for (int py = 0; py < 2; ++py) {
-                    if (msk[py] == 0u) continue;
-                    const int p = py * 32 + lane;
-                    if (n0[py] == kFull) {
-                        if constexpr (EXPLICIT) {
-                            const uint32_t c = (uint32_t)w.it[q].z;
-                            const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
-                                        sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
-                            const float sa = lin8(c >> 24), om = 1.f - sa;
-                            for (uint32_t mk = msk[py]; mk; mk &= mk - 1u) {
-                                uint32_t &v = full_sample(ovf, p, __ffs(mk) - 1);
-                                v = blend_sample<SRGB>(T, lane, v, sr, sg, sb, sa, om);
-                            }
-                            try_compress<S, CAP, EXPLICIT>(w, ovf, p);
-                        }
-                    } else if (w.cnt[p] > 1) {
-                        dedup(w, p);
-                    }
-                }
-            }
-            __syncwarp();
-            q0 = q1;
         }
     }
     __syncwarp();
@@ -1114,7 +1062,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
                                                                  uint32_t *__restrict__ image,
                                                                  uint32_t *__restrict__ overflow,
                                                                  uint32_t *__restrict__ bin_queue) {
-    constexpr int CAP = MS ? 8 : 1;
+    constexpr int CAP = MS ? kCapMS : 1;
     constexpr bool EXPLICIT = MS && S > CAP;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemTables &T = *reinterpret_cast<SmemTables *>(smem_raw);
@@ -1169,7 +1117,7 @@ __global__ void k_decode_keys(const uint64_t *__restrict__ skey, int64_t n, int 
     if (i < n) out[i] = key_from_local((uint32_t)(skey[i] & 0xFFFFFFu), nrows);
 }
 
-constexpr int kResolveBlocksPerSM = 4;  // shared-memory bound: ~53 KB per block
+constexpr int kResolveBlocksPerSM = 4;  // shared-memory bound: ~50 KB per block
 
 int sm_count() {
     static int n = 0;
@@ -1190,7 +1138,7 @@ template <int S, bool MS, bool SRGB>
 void resolve_variant(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
                      const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
                      uint32_t *queue, cudaStream_t s) {
-    constexpr int CAP = MS ? 8 : 1;
+    constexpr int CAP = MS ? kCapMS : 1;
     const size_t smem = sizeof(SmemTables) + (size_t)kResolveWarps * sizeof(BinState<CAP>);
     cudaFuncSetAttribute(k_resolve<S, MS, SRGB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_resolve<S, MS, SRGB><<<(unsigned)resolve_blocks(a), kResolveWarps * 32, smem, s>>>(
@@ -1320,7 +1268,7 @@ int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cud
 int64_t resolve_warps(const FrameArgs &a) { return resolve_blocks(a) * kResolveWarps; }
 
 int64_t resolve_overflow_words(const FrameArgs &a) {
-    if (!(a.ms_output && a.S > 8)) return 0;
+    if (!(a.ms_output && a.S > kCapMS)) return 0;
     return resolve_warps(a) * 64 * 32;
 }
 

@@ -138,6 +138,8 @@ def lib() -> C.CDLL:
         L.spr_scene_view_of.argtypes = [vp, C.POINTER(SceneView)]
         L.spr_scene_free.argtypes = [vp]
         L.spr_scene_free.restype = None
+        L.spr_diff_render.argtypes = [vp, vp, vp, vp]
+        L.spr_diff_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.spr_batch_create.argtypes = [i32, i32, i32, C.POINTER(vp)]
         L.spr_batch_destroy.argtypes = [vp]
         L.spr_batch_set_scenes.argtypes = [vp, C.POINTER(BatchScene), i32]
@@ -337,6 +339,18 @@ class VGRasterizer:
         n = C.c_int64()
         check(lib().spr_selftest(self._h, C.byref(n)), "spr_selftest")
         return {"srgb_encode_mismatches": int(n.value)}
+
+    def diff_render(self, fill_ptr: int, image_ptr: int, stream=None):
+        """Float composite with per-path linear RGBA fills (device pointers:
+        fill float32[P, 4], image float32[H, W, 4])."""
+        check(lib().spr_diff_render(self._h, fill_ptr, image_ptr, stream), "spr_diff_render")
+
+    def diff_backward(self, fill_ptr: int, grad_image_ptr: int, grad_fill_ptr: int, grad_vertex_ptr: int,
+                      grad_affine_ptr=None, stream=None):
+        """Gradients (device pointers: grad_fill float32[P, 4], grad_vertex
+        float32[V, 2], grad_affine float32[P, 6] or None)."""
+        check(lib().spr_diff_backward(self._h, fill_ptr, grad_image_ptr, grad_fill_ptr, grad_vertex_ptr,
+                                      grad_affine_ptr, stream), "spr_diff_backward")
 
     def dump(self, stage) -> np.ndarray:
         sid = STAGE[stage] if isinstance(stage, str) else int(stage)

@@ -256,6 +256,32 @@ int spr_scan_offsets_noalloc(const uint32_t *d_counts, uint32_t *d_offsets, int6
 /* Human-readable text for a status code (static string). */
 const char *spr_status_string(int32_t status);
 
+/* ---- differentiable rendering (an extension: no counterpart in the reference)
+ * The coverage stages are those of spr_render (bit-exact); the resolve is
+ * replaced by a float composite: every sample is composited in linear RGBA
+ * over opaque white in painter's order, c' = f.rgb * a + c.rgb * (1 - a),
+ * c'.a = a * a + c.a * (1 - a), with the path colours f taken from
+ * fill_rgba (4 floats per path) instead of path_fill_rgba, and a pixel is
+ * the mean of its samples.  All pointers are device pointers.  The handle's
+ * RGBA8 image is not written.  Single-scene handles only
+ * (SPR_ERR_UNSUPPORTED on batches).
+ */
+int spr_diff_render(spr_handle *h, const float *fill_rgba, float *image, void *stream);
+/* Gradients of a loss L given grad_image = dL/d(image) (4 floats per pixel):
+ * grad_fill (4 per path) exactly through the composite; grad_vertex (2 per
+ * input vertex, in the scene's own vertex order) and grad_affine (6 per
+ * path; only with a per-path affine, else pass NULL) by edge sampling: a
+ * pixel is taken as the mean over its sample rows of the row integral of
+ * the composite, and every crossing of a path boundary chord with a sample
+ * row contributes (c_left - c_right) dL/dI / samples to dL/dx of the
+ * crossing, which moves with the chord's end points (points of the curve on
+ * cell lines, or at curve ends and monotone split points) and so with the
+ * control points.  Outputs are overwritten.  The frame's stages are
+ * recomputed (nothing is kept from spr_diff_render).  The per-sample tape
+ * grows by itself (one extra readback per doubling). */
+int spr_diff_backward(spr_handle *h, const float *fill_rgba, const float *grad_image, float *grad_fill,
+                      float *grad_vertex, float *grad_affine, void *stream);
+
 /* ---- batches (an extension: no counterpart in the reference) ------------
  * Many independent scenes of uneven size rendered together: the scenes are
  * concatenated on the device, every path carries the index of its scene, and

@@ -53,6 +53,7 @@ def lib() -> C.CDLL:
         L.orc_vertical_mask.argtypes = [C.c_int32, f, vp]
         L.orc_vertical_mask2.argtypes = [C.c_int32, f, f, vp]
         L.orc_fetch_table_selftest.argtypes = [C.c_int32, C.c_int32, vp]
+        L.orc_diff.argtypes = [C.POINTER(spr.SceneView), C.POINTER(OrcConfig), vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -122,6 +123,33 @@ def run(scene: "spr.Scene", width, height, samples=8, ms_output=True, srgb=True,
     finally:
         if h.value:
             lib().orc_free(h)
+
+
+def diff(scene: "spr.Scene", width, height, fill, grad_image=None, samples=16, transform=None, threads=0):
+    """Reference differentiable render: returns (image (H, W, 4) float64, and
+    when grad_image is given grads {fill (P, 4), vertex (V, 2), affine (P, 6)
+    or None})."""
+    cfg = OrcConfig(width, height, samples, 1, 0, threads, 0 if transform is None else 1, (C.c_float * 16)(), -1)
+    if transform is not None:
+        t = np.asarray(transform, dtype=np.float32).reshape(16)
+        for i in range(16):
+            cfg.transform[i] = float(t[i])
+    fill = np.ascontiguousarray(fill, dtype=np.float32).reshape(-1, 4)
+    img = np.zeros((height, width, 4), np.float64)
+    gi = None if grad_image is None else np.ascontiguousarray(grad_image, dtype=np.float32).reshape(height, width, 4)
+    gf = np.zeros((scene.n_paths, 4), np.float64)
+    gv = np.zeros((scene.n_vertices, 2), np.float64)
+    ga = np.zeros((scene.n_paths, 6), np.float64) if scene.path_affine is not None else None
+    v = scene.view()
+    st = lib().orc_diff(C.byref(v), C.byref(cfg), fill.ctypes.data, None if gi is None else gi.ctypes.data,
+                        img.ctypes.data, gf.ctypes.data if gi is not None else None,
+                        gv.ctypes.data if gi is not None else None,
+                        ga.ctypes.data if (gi is not None and ga is not None) else None)
+    if st != 0:
+        raise spr.SprError(st, "orc_diff")
+    if gi is None:
+        return img, None
+    return img, {"fill": gf, "vertex": gv, "affine": ga}
 
 
 def time_run(scene: "spr.Scene", width, height, samples=8, ms_output=True, srgb=True, threads=0,

@@ -24,6 +24,7 @@
 #include <cstdint>
 #include <cstring>
 #include <functional>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -418,6 +419,17 @@ struct orc_result {
     std::vector<uint32_t> merged_mask;
     std::vector<Int4> draw;
     std::vector<uint8_t> image;
+    // for the differentiable reference: per fragment its chord in cell
+    // units (q0x, q0y, q1x, q1y) and left mask; per draw item its path; per
+    // merged fragment its first sorted position
+    std::vector<float> chord;
+    std::vector<uint32_t> lmask;
+    std::vector<uint32_t> item_path;
+    std::vector<int64_t> heads;
+    std::vector<uint8_t> reversed;
+    std::vector<uint32_t> curve_vpos;
+    std::vector<uint32_t> curve_type;
+    std::vector<float> curve_w;
     double stage_ms[SPR_STAGE_COUNT_] = {};
 };
 
@@ -809,7 +821,7 @@ struct FragCtx {
 
 // k_gen_fragment_and_stencil_mask (cu:112-441) for entry i.
 void make_fragment(const FragCtx &fc, int64_t i, int64_t nf, int32_t *key, uint32_t *pidw, int8_t *wn,
-                   uint32_t *mask) {
+                   uint32_t *mask, float *chord, uint32_t *lmask) {
     const orc_result &r = *fc.r;
     const spr_scene_view *v = fc.s->view;
     Int2 e0 = r.entries[i];
@@ -827,6 +839,8 @@ void make_fragment(const FragCtx &fc, int64_t i, int64_t nf, int32_t *key, uint3
     if (e0.x != e1.x) t1 = 1.f;
     int wnchg = 0, swn = 0;
     for (int w = 0; w < fc.words; ++w) mask[w] = 0;
+    for (int w = 0; w < fc.words; ++w) lmask[w] = 0;
+    for (int k = 0; k < 4; ++k) chord[k] = 0.f;
     if (t0 < t1) {
         CurveGeom g;
         load_geom(*fc.s, r, (uint32_t)cid, g);
@@ -902,6 +916,11 @@ void make_fragment(const FragCtx &fc, int64_t i, int64_t nf, int32_t *key, uint3
         vertical_mask2(fc.S, c0.y, c1.y, vm);
         fetch_pixel_table(fc.table, fc.words, c0, c1, tm);
         for (int w = 0; w < fc.words; ++w) mask[w] = (tm[w] & vm[w]) ^ lm[w];
+        for (int w = 0; w < fc.words; ++w) lmask[w] = lm[w];
+        chord[0] = c0.x;
+        chord[1] = c0.y;
+        chord[2] = c1.x;
+        chord[3] = c1.y;
     }
     key[i] = yx;
     pidw[i] = pathid | ((uint32_t)wnchg << 30);
@@ -958,6 +977,7 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
     r.counts.curve = (int32_t)s.C;
     r.counts.vertex = (int32_t)s.V;
     unify(s);
+    r.reversed = s.reversed;
 
     using clk = std::chrono::steady_clock;
     auto t_prev = clk::now();
@@ -1011,10 +1031,13 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
     r.pid.resize(nf);
     r.wn.resize(nf);
     r.mask.resize(nf * WORDS);
+    r.chord.resize(4 * nf);
+    r.lmask.resize(nf * WORDS);
     FragCtx fc{&s, &r, table.data(), W, H, S, WORDS};
     parallel_for(threads, nf, [&](int64_t b, int64_t e) {
         for (int64_t i = b; i < e; ++i)
-            make_fragment(fc, i, nf, r.key.data(), r.pid.data(), r.wn.data(), r.mask.data() + i * WORDS);
+            make_fragment(fc, i, nf, r.key.data(), r.pid.data(), r.wn.data(), r.mask.data() + i * WORDS,
+                          r.chord.data() + 4 * i, r.lmask.data() + i * WORDS);
     });
     lap(SPR_STAGE_FRAG_MASK);
     if (stop <= SPR_STAGE_FRAG_MASK) return SPR_OK;
@@ -1157,6 +1180,8 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
 
     // -- stage 14: draw list (k_gen_gl_merged_fragment_and_span, cu:789-868) --
     r.draw.resize(nm + ns);
+    r.item_path.resize(nm + ns);
+    r.heads = heads;
     const uint32_t *fill = scene->path_fill_rgba;
     parallel_for(threads, nf, [&](int64_t b, int64_t e) {
         for (int64_t i = b; i < e; ++i) {
@@ -1169,7 +1194,9 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
                 uint32_t k = (uint32_t)r.skey[i];
                 int32_t pos = (int32_t)(((uint32_t)(int32_t)key_y(k) << 16) | (uint32_t)(int32_t)key_x(k));
                 r.draw[nfb + nsb] = Int4{pos, 2, (int32_t)fi, fidx[i]};
+                r.item_path[nfb + nsb] = p;
             }
+            if (sfv) r.item_path[nfb + nsb + ff] = p;
             if (sfv) {
                 uint32_t k0 = (uint32_t)r.skey[i - 1], k1 = (uint32_t)r.skey[i];
                 int y0 = key_y(k0);
@@ -1424,5 +1451,319 @@ extern "C" int orc_vertical_mask2(int32_t samples, float y0, float y1, uint32_t 
     uint32_t tmp[4];
     vertical_mask2(samples, y0, y1, tmp);
     std::memcpy(out_words, tmp, 4 * (samples / 8));
+    return SPR_OK;
+}
+
+// ====================================================== differentiable ==
+// Reference of the differentiable render (float composite + edge-sampled
+// adjoint) of the library, restated per pixel and sample.  Colours and
+// gradients are accumulated in double; the geometric decisions (which sample
+// row a chord crosses, the crossing's pixel, the winding on either side) use
+// the same float arithmetic as the device so both sides take the same
+// crossings.
+namespace {
+
+struct Basis {
+    double B[4];
+    double dx, dy;
+};
+
+Basis curve_basis_d(int type, float w, const double *px, const double *py, double t) {
+    Basis b{{0, 0, 0, 0}, 0, 0};
+    const double u = 1.0 - t;
+    if (type == kLinear) {
+        b.B[0] = u;
+        b.B[1] = t;
+        b.dx = px[1] - px[0];
+        b.dy = py[1] - py[0];
+    } else if (type == kQuad) {
+        b.B[0] = u * u;
+        b.B[1] = 2 * t * u;
+        b.B[2] = t * t;
+        b.dx = 2 * (u * (px[1] - px[0]) + t * (px[2] - px[1]));
+        b.dy = 2 * (u * (py[1] - py[0]) + t * (py[2] - py[1]));
+    } else if (type == kCubic) {
+        b.B[0] = u * u * u;
+        b.B[1] = 3 * t * u * u;
+        b.B[2] = 3 * t * t * u;
+        b.B[3] = t * t * t;
+        b.dx = 3 * (u * u * (px[1] - px[0]) + 2 * t * u * (px[2] - px[1]) + t * t * (px[3] - px[2]));
+        b.dy = 3 * (u * u * (py[1] - py[0]) + 2 * t * u * (py[2] - py[1]) + t * t * (py[3] - py[2]));
+    } else {
+        const double b0 = u * u, b1 = 2 * t * u * w, b2 = t * t, Wt = b0 + b1 + b2;
+        const double iW = Wt != 0 ? 1.0 / Wt : 0.0;
+        b.B[0] = b0 * iW;
+        b.B[1] = b1 * iW;
+        b.B[2] = b2 * iW;
+        const double nx = b0 * px[0] + b1 * px[1] + b2 * px[2], ny = b0 * py[0] + b1 * py[1] + b2 * py[2];
+        const double dnx = 2 * (u * (w * px[1] - px[0]) + t * (px[2] - w * px[1]));
+        const double dny = 2 * (u * (w * py[1] - py[0]) + t * (py[2] - w * py[1]));
+        const double dW = 2 * (u * (w - 1.0) + t * (1.0 - w));
+        b.dx = (dnx - nx * iW * dW) * iW;
+        b.dy = (dny - ny * iW * dW) * iW;
+    }
+    return b;
+}
+
+// dC/dP_j for a chord end: (dCx/dPx, dCx/dPy, dCy/dPx, dCy/dPy) per j.
+void end_jacobian_d(int type, float w, const double *px, const double *py, double t, uint32_t flags, bool fixed,
+                    double (*dC)[4]) {
+    const Basis b = curve_basis_d(type, w, px, py, t);
+    int kind = 0;
+    if (!fixed && !(flags & 2u)) kind = (flags & 1u) ? 2 : 1;
+    if (kind == 1 && std::fabs(b.dx) < 1e-12) kind = 0;
+    if (kind == 2 && std::fabs(b.dy) < 1e-12) kind = 0;
+    for (int j = 0; j < 4; ++j) {
+        const double B = b.B[j];
+        dC[j][0] = dC[j][1] = dC[j][2] = dC[j][3] = 0.0;
+        if (kind == 0) {
+            dC[j][0] = B;
+            dC[j][3] = B;
+        } else if (kind == 1) {
+            dC[j][2] = -(b.dy / b.dx) * B;
+            dC[j][3] = B;
+        } else {
+            dC[j][0] = B;
+            dC[j][1] = -(b.dx / b.dy) * B;
+        }
+    }
+}
+
+inline uint32_t row_bit(const uint32_t *m, int S, int px, int r) {
+    if (S == 32) return (m[2 * px + (r >> 5)] >> (r & 31)) & 1u;
+    if (S == 16) return (m[px] >> r) & 1u;
+    return (m[0] >> r) & 1u;
+}
+
+inline bool filled_w(int w, int rule) { return rule == 0 ? (w & 0x7f) != 0 : (w & 1) != 0; }
+
+}  // namespace
+
+extern "C" int orc_diff(const spr_scene_view *scene, const orc_config *cfgp, const float *fill,
+                        const float *grad_image, double *image, double *grad_fill, double *grad_vertex,
+                        double *grad_affine) {
+    if (!scene || !cfgp || !fill || !image) return SPR_ERR_INVALID_ARG;
+    if (grad_image && (!grad_fill || !grad_vertex)) return SPR_ERR_INVALID_ARG;
+    if (grad_affine && !scene->path_affine) return SPR_ERR_INVALID_ARG;
+    orc_config cfg = *cfgp;
+    cfg.stop_after = SPR_STAGE_DRAW_LIST;
+    orc_result *rp = nullptr;
+    int rc = orc_run(scene, &cfg, &rp);
+    std::unique_ptr<orc_result> hold(rp);
+    if (rc) return rc;
+    const orc_result &r = *rp;
+    const int W = cfg.width, H = cfg.height, S = cfg.samples, WORDS = S / 8;
+    const uint32_t P = scene->n_paths, V = scene->n_vertices;
+    const int64_t nf = (int64_t)r.entries.size();
+    // items touching each pixel, in draw order
+    std::vector<std::vector<int32_t>> items((size_t)W * H);
+    for (size_t it = 0; it < r.draw.size(); ++it) {
+        const Int4 d = r.draw[it];
+        const int x = (int)((uint32_t)d.x & 0xFFFFu), y = (int)(int16_t)(uint16_t)((uint32_t)d.x >> 16);
+        const int len = d.w != 0 ? 2 : d.y;
+        for (int Y = y; Y < y + 2; ++Y)
+            for (int X = x; X < x + len; ++X)
+                if (X >= 0 && X < W && Y >= 0 && Y < H) items[(size_t)Y * W + X].push_back((int32_t)it);
+    }
+    std::fill(image, image + 4 * (size_t)W * H, 0.0);
+    std::vector<double> gt;
+    if (grad_image) {
+        std::fill(grad_fill, grad_fill + 4 * (size_t)P, 0.0);
+        gt.assign(2 * (size_t)V, 0.0);
+    }
+    struct Tape {
+        int32_t it;
+        double c[4];
+        bool cov;
+    };
+    std::vector<Tape> tape;
+    for (int Y = 0; Y < H; ++Y)
+        for (int X = 0; X < W; ++X) {
+            const std::vector<int32_t> &lst = items[(size_t)Y * W + X];
+            const int pxc = X & 1, pyc = Y & 1, k4 = pxc * 2 + pyc;
+            double G[4] = {0, 0, 0, 0};
+            if (grad_image)
+                for (int c = 0; c < 4; ++c) G[c] = grad_image[4 * ((size_t)Y * W + X) + c] / S;
+            for (int i = 0; i < S; ++i) {
+                double col[4] = {1, 1, 1, 1};
+                tape.clear();
+                for (int32_t it : lst) {
+                    const Int4 d = r.draw[it];
+                    bool cov = true;
+                    if (d.w != 0) {
+                        const uint32_t *mm = r.merged_mask.data() + (size_t)(d.w - 1) * WORDS;
+                        uint32_t bit;
+                        if (S == 8) bit = (mm[0] >> (8 * k4 + i)) & 1u;
+                        else if (S == 16) bit = (mm[k4 >> 1] >> (16 * (k4 & 1) + i)) & 1u;
+                        else bit = (mm[k4] >> i) & 1u;
+                        cov = bit != 0;
+                    }
+                    Tape t{it, {col[0], col[1], col[2], col[3]}, cov};
+                    tape.push_back(t);
+                    if (cov) {
+                        const float *f = fill + 4 * (size_t)r.item_path[it];
+                        const double a = f[3], om = 1.0 - a;
+                        for (int c = 0; c < 3; ++c) col[c] = f[c] * a + col[c] * om;
+                        col[3] = a * a + col[3] * om;
+                    }
+                }
+                for (int c = 0; c < 4; ++c) image[4 * ((size_t)Y * W + X) + c] += col[c] / S;
+                if (!grad_image) continue;
+                double lam[4] = {G[0], G[1], G[2], G[3]};
+                const int rrow = pyc * S + i;
+                const float yr = ((float)rrow + 0.5f) / (float)(2 * S);
+                for (int e = (int)tape.size() - 1; e >= 0; --e) {
+                    const Tape &t = tape[e];
+                    const Int4 d = r.draw[t.it];
+                    const uint32_t path = r.item_path[t.it];
+                    const float *f = fill + 4 * (size_t)path;
+                    const double a = f[3], om = 1.0 - a;
+                    const double *cb = t.c;
+                    const double J = lam[0] * a * (f[0] - cb[0]) + lam[1] * a * (f[1] - cb[1]) +
+                                     lam[2] * a * (f[2] - cb[2]) + lam[3] * a * (a - cb[3]);
+                    if (t.cov) {
+                        double *gf = grad_fill + 4 * (size_t)path;
+                        for (int c = 0; c < 3; ++c) gf[c] += lam[c] * a;
+                        gf[3] += lam[0] * (f[0] - cb[0]) + lam[1] * (f[1] - cb[1]) + lam[2] * (f[2] - cb[2]) +
+                                 lam[3] * (2 * a - cb[3]);
+                        for (int c = 0; c < 4; ++c) lam[c] *= om;
+                    }
+                    if (d.w == 0 || J == 0.0) continue;
+                    // crossings of the path's chords in this cell with sample row rrow
+                    const int64_t h = r.heads[d.w - 1];
+                    const int32_t kh = r.skey[h];
+                    const uint32_t ph = r.pid[h] & 0x3FFFFFFFu;
+                    const int w0 = r.wn_scan[h];
+                    const int rule = scene->path_fill_rule[path];
+                    auto in_group = [&](int64_t j) {
+                        return j < nf && r.skey[j] == kh && (r.pid[j] & 0x3FFFFFFFu) == ph;
+                    };
+                    for (int64_t j = h; in_group(j); ++j) {
+                        const int32_t raw = r.perm[j];
+                        const int chg = (int32_t)r.pid[raw] >> 30;
+                        if (chg == 0) continue;
+                        const float *q = r.chord.data() + 4 * (size_t)raw;
+                        if (q[1] == q[3]) continue;
+                        uint32_t vm[4];
+                        vertical_mask2(S, q[1], q[3], vm);
+                        if (!row_bit(vm, S, pxc, rrow)) continue;
+                        const float slope = (q[2] - q[0]) / (q[3] - q[1]);
+                        const float lamf = (yr - q[1]) / (q[3] - q[1]);
+                        const float xc = q[0] + (yr - q[1]) * slope;
+                        const int pc = std::min(std::max((int)std::floor(xc * 2.f), 0), 1);
+                        if (pc != pxc) continue;
+                        int Wn = w0;
+                        for (int64_t j2 = h; in_group(j2); ++j2) {
+                            const int32_t raw2 = r.perm[j2];
+                            const int chg2 = (int32_t)r.pid[raw2] >> 30;
+                            if (chg2 == 0) continue;
+                            uint32_t bit = 0;
+                            if (j2 != j) {
+                                const float *q2 = r.chord.data() + 4 * (size_t)raw2;
+                                if (q2[1] != q2[3]) {
+                                    uint32_t vm2[4];
+                                    vertical_mask2(S, q2[1], q2[3], vm2);
+                                    if (row_bit(vm2, S, pxc, rrow)) {
+                                        const float x2 = q2[0] + (yr - q2[1]) * ((q2[2] - q2[0]) / (q2[3] - q2[1]));
+                                        bit = xc > x2 ? 1u : 0u;
+                                    }
+                                }
+                            }
+                            bit ^= row_bit(r.lmask.data() + (size_t)raw2 * WORDS, S, pxc, rrow);
+                            Wn += chg2 * (int)bit;
+                        }
+                        const bool cl = filled_w(Wn, rule), cr = filled_w(Wn + chg, rule);
+                        if (cl == cr) continue;
+                        const double dLdx = cl ? J : -J;
+                        const Int2 e0 = r.entries[raw];
+                        const Int2 e1 = raw + 1 < nf ? r.entries[raw + 1] : Int2{-1, 0x3f800000};
+                        float t0 = float_of((uint32_t)e0.y & 0xFFFFFFFCu), t1 = float_of((uint32_t)e1.y & 0xFFFFFFFCu);
+                        if (t0 < 0) t0 = 0.f;
+                        if (t1 < 0) t1 = 0.f;
+                        const bool end1 = e0.x != e1.x;
+                        if (end1) t1 = 1.f;
+                        const int cid = e0.x;
+                        const int type = scene->curve_type[cid];
+                        const float wgt = type == kRational ? scene->curve_arc_w[cid] : 0.f;
+                        const uint32_t vp = scene->curve_vertex_pos[cid];
+                        const int n = type & 7;
+                        double px[4] = {0, 0, 0, 0}, py[4] = {0, 0, 0, 0};
+                        for (int k = 0; k < n; ++k) {
+                            px[k] = r.tvertex[vp + k].x;
+                            py[k] = r.tvertex[vp + k].y;
+                        }
+                        double dC0[4][4], dC1[4][4];
+                        end_jacobian_d(type, wgt, px, py, t0, (uint32_t)e0.y & 3u, t0 == 0.f || t0 == 1.f, dC0);
+                        end_jacobian_d(type, wgt, px, py, t1, end1 ? 0u : ((uint32_t)e1.y & 3u),
+                                       end1 || t1 == 0.f || t1 == 1.f, dC1);
+                        const double l = lamf, sl = slope;
+                        for (int k = 0; k < n; ++k) {
+                            const double gx = (1 - l) * dC0[k][0] + l * dC1[k][0] - sl * ((1 - l) * dC0[k][2] + l * dC1[k][2]);
+                            const double gy = (1 - l) * dC0[k][1] + l * dC1[k][1] - sl * ((1 - l) * dC0[k][3] + l * dC1[k][3]);
+                            gt[2 * (vp + k)] += dLdx * gx;
+                            gt[2 * (vp + k) + 1] += dLdx * gy;
+                        }
+                    }
+                }
+            }
+        }
+    if (!grad_image) return SPR_OK;
+    // transformed vertex -> input vertex and path affine
+    float m[16];
+    for (int k = 0; k < 16; ++k) m[k] = cfg.has_transform ? cfg.transform[k] : ((k % 5 == 0) ? 1.f : 0.f);
+    if (grad_affine) std::fill(grad_affine, grad_affine + 6 * (size_t)P, 0.0);
+    std::vector<uint32_t> vmap(V);
+    for (uint32_t i = 0; i < V; ++i) vmap[i] = i;
+    for (uint32_t c = 0; c < scene->n_curves; ++c)
+        if (r.reversed[c]) {
+            const uint32_t p0 = scene->curve_vertex_pos[c];
+            const int vn = scene->curve_type[c] & 7;
+            for (int k = 0; k < vn; ++k) vmap[p0 + k] = p0 + vn - 1 - k;
+        }
+    for (uint32_t i = 0; i < V; ++i) {
+        // the stored (unified) vertex i holds the input vertex vmap[i]
+        const double vx = scene->vertex[2 * vmap[i]], vy = scene->vertex[2 * vmap[i] + 1];
+        const uint32_t pid = scene->vertex_path_id[vmap[i]];
+        double A[6] = {1, 0, 0, 1, 0, 0};
+        double xa = vx, ya = vy;
+        if (scene->path_affine) {
+            for (int k = 0; k < 6; ++k) A[k] = scene->path_affine[6 * (size_t)pid + k];
+            xa = A[0] * vx + A[2] * vy + A[4];
+            ya = A[1] * vx + A[3] * vy + A[5];
+        }
+        double ov[4], dox[4], doy[4];
+        for (int rr = 0; rr < 4; ++rr) {
+            ov[rr] = m[4 * rr] * xa + m[4 * rr + 1] * ya + m[4 * rr + 3];
+            dox[rr] = m[4 * rr];
+            doy[rr] = m[4 * rr + 1];
+        }
+        double q[3], qx[3], qy[3];
+        for (int rr = 0; rr < 3; ++rr) {
+            q[rr] = ov[rr] / ov[3];
+            qx[rr] = (dox[rr] - q[rr] * dox[3]) / ov[3];
+            qy[rr] = (doy[rr] - q[rr] * doy[3]) / ov[3];
+        }
+        const double w = W, hh = H, z = std::min(W, H), cutoff = -z * 0.5;
+        if (q[2] < cutoff) {
+            q[2] = cutoff;
+            qx[2] = qy[2] = 0;
+        }
+        const double den = q[2] + z, f = z / den, fx = -f / den * qx[2], fy = -f / den * qy[2];
+        const double Jxx = qx[0] * f + (q[0] - w * .5) * fx, Jxy = qy[0] * f + (q[0] - w * .5) * fy;
+        const double Jyx = qx[1] * f + (q[1] - hh * .5) * fx, Jyy = qy[1] * f + (q[1] - hh * .5) * fy;
+        const double gx = gt[2 * i], gy = gt[2 * i + 1];
+        const double gxa = Jxx * gx + Jyx * gy, gya = Jxy * gx + Jyy * gy;
+        grad_vertex[2 * vmap[i]] = A[0] * gxa + A[1] * gya;
+        grad_vertex[2 * vmap[i] + 1] = A[2] * gxa + A[3] * gya;
+        if (grad_affine) {
+            double *Ga = grad_affine + 6 * (size_t)pid;
+            Ga[0] += gxa * vx;
+            Ga[1] += gya * vx;
+            Ga[2] += gxa * vy;
+            Ga[3] += gya * vy;
+            Ga[4] += gxa;
+            Ga[5] += gya;
+        }
+    }
     return SPR_OK;
 }

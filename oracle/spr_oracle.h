@@ -58,6 +58,14 @@ int orc_vertical_mask(int32_t samples, float y, uint32_t *out_words);
 int orc_fetch_table_selftest(int32_t samples, int32_t res, int64_t *hist33);
 int orc_vertical_mask2(int32_t samples, float y0, float y1, uint32_t *out_words);
 
+/* Differentiable render reference: the float composite of the draw list with
+ * fill colours fill[4 * path] (linear RGBA) into image[4 * pixel], and, when
+ * grad_image (dL/d(pixel), 4 per pixel) is given, the gradients of L w.r.t.
+ * the fills, the input vertices (2 per vertex) and the per-path affines (6
+ * per path; NULL to skip), by the same edge-sampling rule as the library. */
+int orc_diff(const spr_scene_view *scene, const orc_config *cfg, const float *fill, const float *grad_image,
+             double *image, double *grad_fill, double *grad_vertex, double *grad_affine);
+
 #ifdef __cplusplus
 }
 #endif
