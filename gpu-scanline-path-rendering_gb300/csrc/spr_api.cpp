@@ -101,7 +101,7 @@ struct spr_handle {
     // differentiable frames: per-fragment chords and left masks, per-item
     // paths, the per-block tapes, the transformed-vertex gradient and the
     // stored -> input vertex map
-    DevBuf chord, lmask, item_path, tape, tape_item, grad_tvert, vmap;
+    DevBuf chord, lmask, vmask, item_path, tape, tape_rec, grad_tvert, vmap, bitems, chain;
     int tape_depth = 128;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
@@ -165,6 +165,7 @@ FrameArgs make_args(const spr_handle *h) {
     a.rtables = h->rtables.as<ResolveTables>();
     a.chord = nullptr;
     a.lmask = nullptr;
+    a.vmask = nullptr;
     a.item_path = nullptr;
     if (h->n_scenes > 0) {
         a.path_scene = h->path_scene.as<uint32_t>();
@@ -267,8 +268,8 @@ int spr_destroy(spr_handle *h) {
                       &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
                       &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
                       &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
-                      &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_item,
-                      &h->grad_tvert, &h->vmap};
+                      &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
+                      &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain};
     for (DevBuf *b : bufs) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
@@ -400,8 +401,17 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
     d.pval = pv;
     d.bstart = bstart;
     d.bend = bend;
+    d.npairs = pv ? h->npairs : 0;
+    if (d.npairs > 0) {
+        int st = ensure(h->bitems, 48 * (size_t)d.npairs);
+        if (st) return st;
+        d.bitem = h->bitems.as<uint4>();
+        d.bfill = reinterpret_cast<float4 *>(d.bitem + d.npairs);
+        d.bmm = d.bitem + 2 * d.npairs;
+    }
     d.chord = h->chord.as<float4>();
     d.lmask = h->lmask.as<uint32_t>();
+    d.vmask = h->vmask.as<uint32_t>();
     d.pidw = h->pidw.as<uint32_t>();
     d.perm = h->perm_sorted;
     d.heads = h->heads.as<uint32_t>();
@@ -420,17 +430,22 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
     }
     int st = ensure(h->grad_tvert, 8 * (size_t)std::max<uint32_t>(h->V, 1));
     if (st) return st;
+    if ((st = ensure(h->chain, 16 * (size_t)std::max<int64_t>(h->nf, 1) + 16))) return st;
     d.grad_tvert = h->grad_tvert.as<float2>();
+    d.chain = h->chain.as<float4>() + 1;
+    d.n_chain = reinterpret_cast<uint32_t *>(h->chain.p);
     for (int depth = h->tape_depth;; depth *= 2) {
         const int64_t words = diff_tape_words(a, depth);
-        if ((st = ensure(h->tape, 16 * (size_t)words)) || (st = ensure(h->tape_item, 4 * (size_t)(words / (a.S / 8)))))
+        if ((st = ensure(h->tape, 16 * (size_t)words)) ||
+            (st = ensure(h->tape_rec, 16 * (size_t)diff_tape_rec_words(a, depth))))
             return st;
         d.tape = h->tape.as<float4>();
-        d.tape_item = h->tape_item.as<uint32_t>();
+        d.tape_rec = h->tape_rec.as<float4>();
         d.tape_depth = depth;
         cudaMemsetAsync(dc.grad_fill, 0, 16 * (size_t)h->P, s);
         cudaMemsetAsync(h->grad_tvert.p, 0, 8 * (size_t)h->V, s);
         cudaMemsetAsync(&ctr->status, 0, 4, s);
+        cudaMemsetAsync(d.n_chain, 0, 4, s);
         *L += launch_diff_backward(a, d, s);
         cudaMemcpyAsync(h->h_u32, &ctr->status, 4, cudaMemcpyDeviceToHost, s);
         ++h->host_syncs;
@@ -528,10 +543,11 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     uint32_t *item_scene = batch ? h->item_scene.as<uint32_t>() : nullptr;
     if (dc) {
         if ((st = ensure(h->chord, 16 * (size_t)nf)) || (st = ensure(h->lmask, 4 * (size_t)WORDS * nf)) ||
-            (st = ensure(h->item_path, 4 * 2 * (size_t)nf)))
+            (st = ensure(h->vmask, 4 * (size_t)WORDS * nf)) || (st = ensure(h->item_path, 4 * 2 * (size_t)nf)))
             return st;
         a.chord = h->chord.as<float4>();
         a.lmask = h->lmask.as<uint32_t>();
+        a.vmask = h->vmask.as<uint32_t>();
         a.item_path = h->item_path.as<uint32_t>();
     }
     rec(h, 2, s);
@@ -708,7 +724,7 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
                             &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d,
                             &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
-                            &h->tape_item,  &h->grad_tvert, &h->vmap};
+                            &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;

@@ -35,9 +35,8 @@ namespace spr {
 
 namespace {
 
-constexpr int kDiffThreads = 512;  // 64 pixels x 8 threads; a thread holds S / 8 samples of one pixel
-constexpr int kDiffChunk = 64;     // draw items staged per step
-constexpr int kDiffItemAcc = 1024; // items of a bin with shared-memory fill-gradient accumulators
+constexpr int kDiffThreads = 256;    // 8 warps, each working on its own cells
+constexpr int kDiffPathAcc = 4096;   // paths with shared-memory fill-gradient accumulators (backward)
 constexpr int kTileW = 32;
 
 __device__ __forceinline__ uint32_t pixel_mask(const uint4 &mm, int S, int k) {
@@ -130,173 +129,367 @@ __device__ __forceinline__ void load_curve(const CurveDesc &d, const float2 *__r
     }
 }
 
-// Edge-sampling adjoint of the crossings of the fragments of one merged
-// group (a path's chords in one cell) with sample row r of the cell, owned
-// by cell pixel column px.  J = lambda . (blend(c) - c) of the path at the
-// sample of that row.
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One fragment of a merged group, held by one lane of the cell's warp.
 template <int S>
-__device__ void crossings_adjoint(const FrameArgs &a, const DiffArgs &d, int64_t h, int px, int r, float J,
-                                  int rule) {
+struct GroupFrag {
+    float4 q;          // chord in cell units
+    uint32_t vm[S / 8];  // rows between the chord's end points
+    uint32_t lm[S / 8];  // left mask
+    int chg;           // winding change (0: no contribution)
+    uint32_t raw;
+};
+
+template <int S>
+__device__ __forceinline__ void load_group_frag(const DiffArgs &d, int64_t j, GroupFrag<S> &f) {
     constexpr int WORDS = S / 8;
+    f.raw = d.perm[j];
+    f.chg = (int32_t)d.pidw[f.raw] >> 30;
+    f.q = d.chord[f.raw];
+#pragma unroll
+    for (int w = 0; w < WORDS; ++w) {
+        f.vm[w] = d.vmask[(size_t)f.raw * WORDS + w];
+        f.lm[w] = d.lmask[(size_t)f.raw * WORDS + w];
+    }
+}
+
+template <int S>
+__device__ __forceinline__ GroupFrag<S> shfl_frag(const GroupFrag<S> &f, int src) {
+    GroupFrag<S> o;
+    o.q.x = __shfl_sync(0xffffffffu, f.q.x, src);
+    o.q.y = __shfl_sync(0xffffffffu, f.q.y, src);
+    o.q.z = __shfl_sync(0xffffffffu, f.q.z, src);
+    o.q.w = __shfl_sync(0xffffffffu, f.q.w, src);
+#pragma unroll
+    for (int w = 0; w < S / 8; ++w) {
+        o.vm[w] = __shfl_sync(0xffffffffu, f.vm[w], src);
+        o.lm[w] = __shfl_sync(0xffffffffu, f.lm[w], src);
+    }
+    o.chg = __shfl_sync(0xffffffffu, f.chg, src);
+    o.raw = __shfl_sync(0xffffffffu, f.raw, src);
+    return o;
+}
+
+// Chain of one fragment's crossings to its curve's control points: the
+// crossings contribute sum dL/dx * ((1 - lam) dC0 + lam dC1) projected on x
+// at fixed y, i.e. A * (dC0x - s dC0y) + B * (dC1x - s dC1y).
+__device__ void fragment_chain(const FrameArgs &a, const DiffArgs &d, uint32_t raw, float slope, float A, float B) {
+    const int2 e0 = d.entries[raw];
+    const int2 e1 = (int64_t)raw + 1 < d.nf ? d.entries[raw + 1] : make_int2(-1, 0x3f800000);
+    float t0 = ffrom((uint32_t)e0.y & 0xFFFFFFFCu), t1 = ffrom((uint32_t)e1.y & 0xFFFFFFFCu);
+    if (t0 < 0.f) t0 = 0.f;
+    if (t1 < 0.f) t1 = 0.f;
+    const bool end1 = e0.x != e1.x;
+    if (end1) t1 = 1.f;
+    const CurveDesc cd = a.curves[e0.x];
+    CurveGeom g;
+    load_curve(cd, d.tvert, g);
+    float4 dC0[4], dC1[4];
+    end_point_jacobian(g, t0, (uint32_t)e0.y & 3u, t0 == 0.f || t0 == 1.f, dC0);
+    end_point_jacobian(g, t1, end1 ? 0u : ((uint32_t)e1.y & 3u), end1 || t1 == 0.f || t1 == 1.f, dC1);
+    const int n = g.type & 7;
+    for (int k = 0; k < n; ++k) {
+        const float gx = A * (dC0[k].x - slope * dC0[k].z) + B * (dC1[k].x - slope * dC1[k].z);
+        const float gy = A * (dC0[k].y - slope * dC0[k].w) + B * (dC1[k].y - slope * dC1[k].w);
+        atomicAdd(&d.grad_tvert[cd.vpos + k].x, gx);
+        atomicAdd(&d.grad_tvert[cd.vpos + k].y, gy);
+    }
+}
+
+// Edge-sampling adjoint of one merged group (a path's chords in one cell)
+// for the cell's warp.  Lane l holds samples sub + 8k of cell pixel k4 =
+// l >> 3 and J[k] = lambda . (blend(c) - c) of the path at those samples.
+// Groups are loaded 32 fragments at a time, one per lane, and broadcast by
+// shuffles; every shuffle is executed by the whole warp.
+template <int S>
+__device__ void group_adjoint(const FrameArgs &a, const DiffArgs &d, int64_t h, int rule, const float *J, int lane) {
+    constexpr int SPT = S / 8;
+    const int k4 = lane >> 3, sub = lane & 7, px = k4 >> 1, py = k4 & 1;
     const uint64_t kh = d.skey[h];
     const int w0 = (int)d.wn_scan[h];
-    const float yr = ((float)r + 0.5f) / (float)(2 * S);
-    for (int64_t j = h; j < d.nf && d.skey[j] == kh; ++j) {
-        const uint32_t raw = d.perm[j];
-        const int chg = (int32_t)d.pidw[raw] >> 30;
-        if (chg == 0) continue;
-        const float4 q = d.chord[raw];
-        if (q.y == q.w) continue;
-        uint32_t vm[4];
-        vertical_mask2<S>(q.y, q.w, vm);
-        if (!row_bit<S>(vm, px, r)) continue;
-        const float slope = (q.z - q.x) / (q.w - q.y);
-        const float lam = (yr - q.y) / (q.w - q.y);
-        const float xc = q.x + (yr - q.y) * slope;
-        const int pc = min(max((int)floorf(xc * 2.f), 0), 1);
-        if (pc != px) continue;
-        // winding just left of the crossing
-        int W = w0;
-        for (int64_t j2 = h; j2 < d.nf && d.skey[j2] == kh; ++j2) {
-            const uint32_t raw2 = d.perm[j2];
-            const int chg2 = (int32_t)d.pidw[raw2] >> 30;
-            if (chg2 == 0) continue;
-            uint32_t bit = 0u;
-            if (j2 != j) {
-                const float4 q2 = d.chord[raw2];
-                if (q2.y != q2.w) {
-                    uint32_t vm2[4];
-                    vertical_mask2<S>(q2.y, q2.w, vm2);
-                    if (row_bit<S>(vm2, px, r)) {
-                        const float x2 = q2.x + (yr - q2.y) * ((q2.z - q2.x) / (q2.w - q2.y));
-                        bit = xc > x2 ? 1u : 0u;
+    int gs = 0;  // group size
+    while (h + gs < d.nf && d.skey[h + gs] == kh) ++gs;
+    for (int base = 0; base < gs; base += 32) {
+        const int nw = min(32, gs - base);
+        GroupFrag<S> mine;
+        if (lane < nw) load_group_frag<S>(d, h + base + lane, mine);
+        else mine = GroupFrag<S>{};
+        for (int j = 0; j < nw; ++j) {
+            const GroupFrag<S> f = shfl_frag<S>(mine, j);
+            if (f.chg == 0 || f.q.y == f.q.w) continue;  // uniform
+            const float slope = (f.q.z - f.q.x) / (f.q.w - f.q.y);
+            bool cand[SPT];
+            float xc[SPT], yr[SPT];
+            int W[SPT];
+            bool any = false;
+#pragma unroll
+            for (int k = 0; k < SPT; ++k) {
+                const int r = py * S + sub + 8 * k;
+                yr[k] = ((float)r + 0.5f) / (float)(2 * S);
+                xc[k] = f.q.x + (yr[k] - f.q.y) * slope;
+                const int pc = min(max((int)floorf(xc[k] * 2.f), 0), 1);
+                cand[k] = J[k] != 0.f && row_bit<S>(f.vm, px, r) && pc == px;
+                W[k] = w0;
+                any |= cand[k];
+            }
+            if (!__any_sync(0xffffffffu, any)) continue;
+            // winding just left of each candidate crossing: this window by shuffles ...
+            for (int j2 = 0; j2 < nw; ++j2) {
+                const GroupFrag<S> f2 = shfl_frag<S>(mine, j2);
+                if (f2.chg == 0) continue;  // uniform
+#pragma unroll
+                for (int k = 0; k < SPT; ++k) {
+                    const int r = py * S + sub + 8 * k;
+                    uint32_t bit = 0u;
+                    if (j2 != j && row_bit<S>(f2.vm, px, r)) {
+                        const float x2 = f2.q.x + (yr[k] - f2.q.y) * ((f2.q.z - f2.q.x) / (f2.q.w - f2.q.y));
+                        bit = xc[k] > x2 ? 1u : 0u;
+                    }
+                    bit ^= row_bit<S>(f2.lm, px, r);
+                    W[k] += f2.chg * (int)bit;
+                }
+            }
+            // ... and the other windows of a group of more than 32 fragments from memory
+            if (gs > 32 && any) {
+                for (int j2 = 0; j2 < gs; ++j2) {
+                    if (j2 >= base && j2 < base + nw) continue;
+                    GroupFrag<S> f2;
+                    load_group_frag<S>(d, h + j2, f2);
+                    if (f2.chg == 0) continue;
+#pragma unroll
+                    for (int k = 0; k < SPT; ++k) {
+                        const int r = py * S + sub + 8 * k;
+                        uint32_t bit = 0u;
+                        if (row_bit<S>(f2.vm, px, r)) {
+                            const float x2 = f2.q.x + (yr[k] - f2.q.y) * ((f2.q.z - f2.q.x) / (f2.q.w - f2.q.y));
+                            bit = xc[k] > x2 ? 1u : 0u;
+                        }
+                        bit ^= row_bit<S>(f2.lm, px, r);
+                        W[k] += f2.chg * (int)bit;
                     }
                 }
             }
-            uint32_t lm[4] = {0u, 0u, 0u, 0u};
+            float sA = 0.f, sB = 0.f;
 #pragma unroll
-            for (int w = 0; w < WORDS; ++w) lm[w] = d.lmask[(size_t)raw2 * WORDS + w];
-            bit ^= row_bit<S>(lm, px, r);
-            W += chg2 * (int)bit;
-        }
-        const bool cl = filled(W, rule), cr = filled(W + chg, rule);
-        if (cl == cr) continue;
-        const float dLdx = cl ? J : -J;
-        // chord end points and their motion with the control points
-        const int2 e0 = d.entries[raw];
-        const int2 e1 = (int64_t)raw + 1 < d.nf ? d.entries[raw + 1] : make_int2(-1, 0x3f800000);
-        float t0 = ffrom((uint32_t)e0.y & 0xFFFFFFFCu), t1 = ffrom((uint32_t)e1.y & 0xFFFFFFFCu);
-        if (t0 < 0.f) t0 = 0.f;
-        if (t1 < 0.f) t1 = 0.f;
-        const bool end1 = e0.x != e1.x;
-        if (end1) t1 = 1.f;
-        const CurveDesc cd = a.curves[e0.x];
-        CurveGeom g;
-        load_curve(cd, d.tvert, g);
-        float4 dC0[4], dC1[4];
-        end_point_jacobian(g, t0, (uint32_t)e0.y & 3u, t0 == 0.f || t0 == 1.f, dC0);
-        end_point_jacobian(g, t1, end1 ? 0u : ((uint32_t)e1.y & 3u), end1 || t1 == 0.f || t1 == 1.f, dC1);
-        const int n = g.type & 7;
-        for (int k = 0; k < n; ++k) {
-            const float gx = (1.f - lam) * dC0[k].x + lam * dC1[k].x - slope * ((1.f - lam) * dC0[k].z + lam * dC1[k].z);
-            const float gy = (1.f - lam) * dC0[k].y + lam * dC1[k].y - slope * ((1.f - lam) * dC0[k].w + lam * dC1[k].w);
-            atomicAdd(&d.grad_tvert[cd.vpos + k].x, dLdx * gx);
-            atomicAdd(&d.grad_tvert[cd.vpos + k].y, dLdx * gy);
+            for (int k = 0; k < SPT; ++k) {
+                if (!cand[k]) continue;
+                const bool cl = filled(W[k], rule), cr = filled(W[k] + f.chg, rule);
+                if (cl == cr) continue;
+                const float g = cl ? J[k] : -J[k];
+                const float lam = (yr[k] - f.q.y) / (f.q.w - f.q.y);
+                sA += g * (1.f - lam);
+                sB += g * lam;
+            }
+            sA = warp_sum(sA);
+            sB = warp_sum(sB);
+            if (lane == 0 && (sA != 0.f || sB != 0.f)) {
+                const uint32_t n = atomicAdd(d.n_chain, 1u);
+                if ((int64_t)n < d.nf) d.chain[n] = make_float4(__uint_as_float(f.raw), slope, sA, sB);
+                else atomicOr(d.status, 2u);
+            }
         }
     }
 }
 
-struct DiffSmem {
-    int4 it[kDiffChunk];
-    uint4 mm[kDiffChunk];
-    float4 fill[kDiffChunk];
-    float acc[kDiffItemAcc][4];
-};
+__device__ __forceinline__ uint4 load_merged(const uint32_t *merged, int words, uint32_t g) {
+    if (words == 4) return reinterpret_cast<const uint4 *>(merged)[g];
+    if (words == 2) {
+        const uint2 v = reinterpret_cast<const uint2 *>(merged)[g];
+        return make_uint4(v.x, v.y, 0u, 0u);
+    }
+    return make_uint4(merged[g], 0u, 0u, 0u);
+}
 
+__device__ __forceinline__ void add_fill_grad(const DiffArgs &d, float4 *acc, uint32_t path, float4 g) {
+    if (acc != nullptr) {
+        atomicAdd(&acc[path].x, g.x);
+        atomicAdd(&acc[path].y, g.y);
+        atomicAdd(&acc[path].z, g.z);
+        atomicAdd(&acc[path].w, g.w);
+    } else {
+        atomicAdd(&d.grad_fill[path].x, g.x);
+        atomicAdd(&d.grad_fill[path].y, g.y);
+        atomicAdd(&d.grad_fill[path].z, g.z);
+        atomicAdd(&d.grad_fill[path].w, g.w);
+    }
+}
+
+// The items of the resolve pairs in bin order, one contiguous record each.
+__global__ void k_diff_gather(DiffArgs d, int words) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.npairs) return;
+    const uint32_t idx = d.pval[p];
+    const int4 it = d.draw[idx];
+    const uint32_t path = d.item_path[idx];
+    d.bitem[p] = make_uint4((uint32_t)it.x, (uint32_t)it.y, (uint32_t)it.w, path);
+    d.bfill[p] = d.fill[path];
+    d.bmm[p] = it.w != 0 ? load_merged(d.merged, words, (uint32_t)it.w - 1u) : make_uint4(0u, 0u, 0u, 0u);
+}
+
+// The crossing sums of every fragment chained to its curve's control points.
+__global__ void k_diff_chain(FrameArgs a, DiffArgs d) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)min((uint64_t)*d.n_chain, (uint64_t)d.nf)) return;
+    const float4 r = d.chain[i];
+    fragment_chain(a, d, __float_as_uint(r.x), r.y, r.z, r.w);
+}
+
+// Persistent warps over (bin, cell) units from a queue: warp = one cell of a
+// bin, lane l = pixel k4 = l >> 3 of the cell (k4 = px * 2 + py), samples
+// (l & 7) + 8k.  Every item touching a cell touches all its pixels, so the
+// walk over the bin's items is warp-uniform; the items are read 32 at a time
+// (one per lane), the touching ones found by a ballot and broadcast.  Warps
+// never wait for one another.
 template <int S, bool BWD>
-__global__ void __launch_bounds__(kDiffThreads, 2) k_diff(FrameArgs a, DiffArgs d) {
+__global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs d, int path_acc) {
     constexpr int SPT = S / 8;
     constexpr int WORDS = S / 8;
-    __shared__ DiffSmem sm;
-    __shared__ uint32_t s_bin;
-    const int t = threadIdx.x;
-    const int pix = t >> 3, sub = t & 7;
-    const int row = pix >> 5, col = pix & 31;
-    const int px_in = col & 1, k4 = px_in * 2 + row;
+    extern __shared__ float4 s_acc[];  // fill gradients per path (backward, when path_acc)
+    const int lane = threadIdx.x & 31;
+    const int k4 = lane >> 3, sub = lane & 7;
+    const int px_in = k4 >> 1, py_in = k4 & 1;
     const int ntx = (a.W + kTileW - 1) / kTileW;
-    const size_t slot = blockIdx.x;
+    const size_t wslot = (size_t)blockIdx.x * (kDiffThreads / 32) + (threadIdx.x >> 5);
+    float4 *acc = (BWD && path_acc) ? s_acc : nullptr;
+    if (acc)
+        for (int i = threadIdx.x; i < a.P; i += kDiffThreads) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (BWD) __syncthreads();
+    const int64_t n_units = a.n_bins * (kTileW / 2);
     for (;;) {
-        __syncthreads();
-        if (t == 0) s_bin = atomicAdd(d.queue, 1u);
-        __syncthreads();
-        const uint32_t b = s_bin;
-        if ((int64_t)b >= a.n_bins) break;
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(d.queue, 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if ((int64_t)u >= n_units) break;
+        const uint32_t b = u / (kTileW / 2);
+        const int cw = (int)(u % (kTileW / 2));
         const int tile = (int)(b % ntx), crow = (int)(b / ntx);
-        const int X = tile * kTileW + col, Y = crow * 2 + row;
+        const int cellx = tile * kTileW + 2 * cw;
+        if (cellx >= a.W) continue;
+        const int X = cellx + px_in, Y = crow * 2 + py_in;
         const bool valid = X < a.W && Y < a.H;
         const uint32_t beg = d.bstart[b], fin = d.bend[b];
         float4 c[SPT];
 #pragma unroll
         for (int k = 0; k < SPT; ++k) c[k] = make_float4(1.f, 1.f, 1.f, 1.f);
-        int ne = 0;
-        if (BWD) {
-            const int n_acc = min((int)(fin - beg), kDiffItemAcc);
-            for (int i = t; i < n_acc * 4; i += kDiffThreads) (&sm.acc[0][0])[i] = 0.f;
+        // backward tape: ne item records; nsl sample-state slots (the state
+        // before every fragment and at the start of every run of spans)
+        int ne = 0, nsl = 0, run_slot = -1;
+        float ralpha = 1.f;
+        float4 rbeta = make_float4(0.f, 0.f, 0.f, 0.f);
+        const size_t rbase = wslot * (size_t)d.tape_depth;
+        // the bin's items, 32 at a time (lane l holds item base + l), the next
+        // chunk loaded while the current one is applied
+        uint4 it = make_uint4(0u, 0u, 0u, 0u), my_mm = it;
+        float4 my_fill = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (beg + lane < fin) {
+            it = d.bitem[beg + lane];
+            my_fill = d.bfill[beg + lane];
+            my_mm = d.bmm[beg + lane];
         }
-        for (uint32_t base = beg; base < fin; base += kDiffChunk) {
-            __syncthreads();
-            const int cnt = (int)min((uint32_t)kDiffChunk, fin - base);
-            if (t < cnt) {
-                const uint32_t idx = d.pval[base + t];
-                const int4 it = d.draw[idx];
-                sm.it[t] = it;
-                if (it.w != 0) {
-                    if constexpr (WORDS == 4) {
-                        sm.mm[t] = reinterpret_cast<const uint4 *>(d.merged)[it.w - 1];
-                    } else if constexpr (WORDS == 2) {
-                        const uint2 v = reinterpret_cast<const uint2 *>(d.merged)[it.w - 1];
-                        sm.mm[t] = make_uint4(v.x, v.y, 0u, 0u);
-                    } else {
-                        sm.mm[t] = make_uint4(d.merged[it.w - 1], 0u, 0u, 0u);
+        for (uint32_t base = beg; base < fin; base += 32) {
+            uint4 nit = make_uint4(0u, 0u, 0u, 0u), nmm = nit;
+            float4 nfill = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (base + 32 + lane < fin) {
+                nit = d.bitem[base + 32 + lane];
+                nfill = d.bfill[base + 32 + lane];
+                nmm = d.bmm[base + 32 + lane];
+            }
+            bool touch = false;
+            if (base + lane < fin) {
+                const int x = (int)(it.x & 0xFFFFu);
+                touch = it.z != 0u ? x == cellx : (cellx >= x && cellx < x + (int)it.y);
+            }
+            uint32_t tm = __ballot_sync(0xffffffffu, touch);
+            while (tm) {
+                const int q = __ffs(tm) - 1;
+                tm &= tm - 1u;
+                const uint32_t w = __shfl_sync(0xffffffffu, it.z, q);
+                const uint32_t path = __shfl_sync(0xffffffffu, it.w, q);
+                float4 f;
+                f.x = __shfl_sync(0xffffffffu, my_fill.x, q);
+                f.y = __shfl_sync(0xffffffffu, my_fill.y, q);
+                f.z = __shfl_sync(0xffffffffu, my_fill.z, q);
+                f.w = __shfl_sync(0xffffffffu, my_fill.w, q);
+                const bool frag = w != 0;
+                uint32_t m = 0xFFFFFFFFu;
+                if (frag) {
+                    uint4 mm;
+                    mm.x = __shfl_sync(0xffffffffu, my_mm.x, q);
+                    mm.y = WORDS > 1 ? __shfl_sync(0xffffffffu, my_mm.y, q) : 0u;
+                    mm.z = WORDS > 2 ? __shfl_sync(0xffffffffu, my_mm.z, q) : 0u;
+                    mm.w = WORDS > 2 ? __shfl_sync(0xffffffffu, my_mm.w, q) : 0u;
+                    m = pixel_mask(mm, S, k4);
+                }
+                const float om = 1.f - f.w;
+                // A run of spans (which cover every sample of the cell) is
+                // carried as c = ralpha * c_run + rbeta, c_run the samples'
+                // state where the run starts; states are materialized at
+                // fragments and at the end.
+                if (frag && run_slot >= 0) {
+#pragma unroll
+                    for (int k = 0; k < SPT; ++k)
+                        c[k] = make_float4(ralpha * c[k].x + rbeta.x, ralpha * c[k].y + rbeta.y,
+                                           ralpha * c[k].z + rbeta.z, ralpha * c[k].w + rbeta.w);
+                    run_slot = -1;
+                }
+                int sidx = run_slot;
+                if (frag || run_slot < 0) {
+                    sidx = nsl++;
+                    if (BWD && sidx < d.tape_depth) {
+                        const size_t e = rbase + sidx;
+#pragma unroll
+                        for (int k = 0; k < SPT; ++k) d.tape[(e * SPT + k) * 32 + lane] = c[k];
+                    }
+                    if (!frag) {
+                        run_slot = sidx;
+                        ralpha = 1.f;
+                        rbeta = make_float4(0.f, 0.f, 0.f, 0.f);
                     }
                 }
-                sm.fill[t] = d.fill[d.item_path[idx]];
-            }
-            __syncthreads();
-            if (!valid) continue;
-            for (int q = 0; q < cnt; ++q) {
-                const int4 it = sm.it[q];
-                const int x = (int)((uint32_t)it.x & 0xFFFFu);
-                const bool frag = it.w != 0;
-                const int len = frag ? 2 : it.y;
-                if (X < x || X >= x + len) continue;
-                const uint32_t m = frag ? pixel_mask(sm.mm[q], S, k4) : 0xFFFFFFFFu;
-                const float4 f = sm.fill[q];
-                const float om = 1.f - f.w;
-                uint32_t cov = 0u;
-#pragma unroll
-                for (int k = 0; k < SPT; ++k) cov |= ((m >> (sub + 8 * k)) & 1u) << k;
                 if (BWD) {
                     if (ne < d.tape_depth) {
-                        const size_t e = slot * (size_t)d.tape_depth + ne;
-                        d.tape_item[e * kDiffThreads + t] = (base - beg + (uint32_t)q) | (cov << 24);
-#pragma unroll
-                        for (int k = 0; k < SPT; ++k) d.tape[(e * SPT + k) * kDiffThreads + t] = c[k];
-                    } else {
+                        if (lane == 0) {
+                            float4 *rec = d.tape_rec + (rbase + ne) * 3;
+                            rec[0] = f;
+                            rec[1] = rbeta;
+                            rec[2] = make_float4(ralpha, __uint_as_float(path), __uint_as_float(w),
+                                                 __uint_as_float((uint32_t)sidx));
+                        }
+                    } else if (lane == 0) {
                         atomicOr(d.status, 1u);
                     }
                     ++ne;
                 }
+                if (!frag) {  // the run's composition up to and including this span
+                    rbeta = make_float4(f.x * f.w + rbeta.x * om, f.y * f.w + rbeta.y * om, f.z * f.w + rbeta.z * om,
+                                        f.w * f.w + rbeta.w * om);
+                    ralpha *= om;
+                } else {
 #pragma unroll
-                for (int k = 0; k < SPT; ++k) {
-                    if ((cov >> k) & 1u) {
-                        c[k].x = f.x * f.w + c[k].x * om;
-                        c[k].y = f.y * f.w + c[k].y * om;
-                        c[k].z = f.z * f.w + c[k].z * om;
-                        c[k].w = f.w * f.w + c[k].w * om;
+                    for (int k = 0; k < SPT; ++k) {
+                        if ((m >> (sub + 8 * k)) & 1u) {
+                            c[k].x = f.x * f.w + c[k].x * om;
+                            c[k].y = f.y * f.w + c[k].y * om;
+                            c[k].z = f.z * f.w + c[k].z * om;
+                            c[k].w = f.w * f.w + c[k].w * om;
+                        }
                     }
                 }
             }
+            it = nit;
+            my_fill = nfill;
+            my_mm = nmm;
+        }
+        if (run_slot >= 0) {
+#pragma unroll
+            for (int k = 0; k < SPT; ++k)
+                c[k] = make_float4(ralpha * c[k].x + rbeta.x, ralpha * c[k].y + rbeta.y, ralpha * c[k].z + rbeta.z,
+                                   ralpha * c[k].w + rbeta.w);
         }
         if (!BWD) {
             float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -320,65 +513,128 @@ __global__ void __launch_bounds__(kDiffThreads, 2) k_diff(FrameArgs a, DiffArgs 
             }
             continue;
         }
-        // ---- reverse sweep
-        if (valid && ne <= d.tape_depth) {
-            const float inv = 1.f / (float)S;
-            const float4 G = d.grad_image[(int64_t)Y * a.W + X];
-            float4 lam[SPT];
+        // ---- reverse sweep (warp-uniform)
+        if (ne > d.tape_depth || nsl > d.tape_depth) continue;
+        const float inv = 1.f / (float)S;
+        const float4 G = valid ? d.grad_image[(int64_t)Y * a.W + X] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 lam[SPT];
 #pragma unroll
-            for (int k = 0; k < SPT; ++k) lam[k] = make_float4(G.x * inv, G.y * inv, G.z * inv, G.w * inv);
-            for (int e0 = ne - 1; e0 >= 0; --e0) {
-                const size_t e = slot * (size_t)d.tape_depth + e0;
-                const uint32_t rec = d.tape_item[e * kDiffThreads + t];
-                const uint32_t q = rec & 0xFFFFFFu, cov = rec >> 24;
-                const uint32_t idx = d.pval[beg + q];
-                const int4 it = d.draw[idx];
-                const uint32_t path = d.item_path[idx];
-                const float4 f = d.fill[path];
-                const float av = f.w, om = 1.f - av;
-                float4 gf = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-                for (int k = 0; k < SPT; ++k) {
-                    const float4 cb = d.tape[(e * SPT + k) * kDiffThreads + t];
-                    const float4 l = lam[k];
-                    const float J = l.x * av * (f.x - cb.x) + l.y * av * (f.y - cb.y) + l.z * av * (f.z - cb.z) +
-                                    l.w * av * (av - cb.w);
-                    if ((cov >> k) & 1u) {
-                        gf.x += l.x * av;
-                        gf.y += l.y * av;
-                        gf.z += l.z * av;
-                        gf.w += l.x * (f.x - cb.x) + l.y * (f.y - cb.y) + l.z * (f.z - cb.z) + l.w * (2.f * av - cb.w);
-                        lam[k] = make_float4(l.x * om, l.y * om, l.z * om, l.w * om);
-                    }
-                    if (it.w != 0 && J != 0.f)
-                        crossings_adjoint<S>(a, d, d.heads[it.w - 1], px_in, row * S + sub + 8 * k, J,
-                                             a.fill_rule[path]);
-                }
-                if (gf.x != 0.f || gf.y != 0.f || gf.z != 0.f || gf.w != 0.f) {
-                    if (q < (uint32_t)kDiffItemAcc) {
-                        atomicAdd(&sm.acc[q][0], gf.x);
-                        atomicAdd(&sm.acc[q][1], gf.y);
-                        atomicAdd(&sm.acc[q][2], gf.z);
-                        atomicAdd(&sm.acc[q][3], gf.w);
-                    } else {
-                        atomicAdd(&d.grad_fill[path].x, gf.x);
-                        atomicAdd(&d.grad_fill[path].y, gf.y);
-                        atomicAdd(&d.grad_fill[path].z, gf.z);
-                        atomicAdd(&d.grad_fill[path].w, gf.w);
-                    }
+        for (int k = 0; k < SPT; ++k) lam[k] = make_float4(G.x * inv, G.y * inv, G.z * inv, G.w * inv);
+        int cur_slot = -1;  // run being swept (its start slot), -1 outside runs
+        float pi = 1.f;
+        float4 Lsum = make_float4(0.f, 0.f, 0.f, 0.f), Ksum = Lsum;
+        float4 rf = make_float4(0.f, 0.f, 0.f, 0.f), rbb = rf, rr2 = rf;  // lane l: record e_hi - l
+        for (int e0 = ne - 1; e0 >= 0; --e0) {
+            const int jl = (ne - 1 - e0) & 31;
+            if (jl == 0) {  // the next 32 records, one per lane
+                if (e0 - lane >= 0) {
+                    const float4 *rec = d.tape_rec + (rbase + e0 - lane) * 3;
+                    rf = rec[0];
+                    rbb = rec[1];
+                    rr2 = rec[2];
                 }
             }
+            float4 f, rb, r2;
+            f.x = __shfl_sync(0xffffffffu, rf.x, jl);
+            f.y = __shfl_sync(0xffffffffu, rf.y, jl);
+            f.z = __shfl_sync(0xffffffffu, rf.z, jl);
+            f.w = __shfl_sync(0xffffffffu, rf.w, jl);
+            rb.x = __shfl_sync(0xffffffffu, rbb.x, jl);
+            rb.y = __shfl_sync(0xffffffffu, rbb.y, jl);
+            rb.z = __shfl_sync(0xffffffffu, rbb.z, jl);
+            rb.w = __shfl_sync(0xffffffffu, rbb.w, jl);
+            r2.x = __shfl_sync(0xffffffffu, rr2.x, jl);
+            r2.y = __shfl_sync(0xffffffffu, rr2.y, jl);
+            r2.z = __shfl_sync(0xffffffffu, rr2.z, jl);
+            r2.w = __shfl_sync(0xffffffffu, rr2.w, jl);
+            const float ra = r2.x;
+            const uint32_t path = __float_as_uint(r2.y), w = __float_as_uint(r2.z);
+            const int sidx = (int)__float_as_uint(r2.w);
+            const float av = f.w, om = 1.f - av;
+            if (w == 0u) {
+                // span: every sample covered; inside a run the samples' adjoints
+                // are the run end's times the scalar pi, so the fill gradient
+                // needs only the run's sums Lsum = sum lambda and Ksum = sum
+                // lambda * c_run (c before the span = ra * c_run + rb).
+                if (sidx != cur_slot) {
+                    if (cur_slot >= 0) {
+#pragma unroll
+                        for (int k = 0; k < SPT; ++k)
+                            lam[k] = make_float4(lam[k].x * pi, lam[k].y * pi, lam[k].z * pi, lam[k].w * pi);
+                    }
+                    const size_t es = rbase + sidx;
+                    float4 ls = make_float4(0.f, 0.f, 0.f, 0.f), ks = ls;
+#pragma unroll
+                    for (int k = 0; k < SPT; ++k) {
+                        const float4 cr = d.tape[(es * SPT + k) * 32 + lane];
+                        ls.x += lam[k].x;
+                        ls.y += lam[k].y;
+                        ls.z += lam[k].z;
+                        ls.w += lam[k].w;
+                        ks.x += lam[k].x * cr.x;
+                        ks.y += lam[k].y * cr.y;
+                        ks.z += lam[k].z * cr.z;
+                        ks.w += lam[k].w * cr.w;
+                    }
+                    Lsum = make_float4(warp_sum(ls.x), warp_sum(ls.y), warp_sum(ls.z), warp_sum(ls.w));
+                    Ksum = make_float4(warp_sum(ks.x), warp_sum(ks.y), warp_sum(ks.z), warp_sum(ks.w));
+                    cur_slot = sidx;
+                    pi = 1.f;
+                }
+                const float cx = ra * Ksum.x + rb.x * Lsum.x, cy = ra * Ksum.y + rb.y * Lsum.y;
+                const float cz = ra * Ksum.z + rb.z * Lsum.z, cw = ra * Ksum.w + rb.w * Lsum.w;
+                const float4 gf = make_float4(
+                    pi * av * Lsum.x, pi * av * Lsum.y, pi * av * Lsum.z,
+                    pi * (Lsum.x * f.x - cx + Lsum.y * f.y - cy + Lsum.z * f.z - cz + 2.f * av * Lsum.w - cw));
+                if (lane == 0 && (gf.x != 0.f || gf.y != 0.f || gf.z != 0.f || gf.w != 0.f))
+                    add_fill_grad(d, acc, path, gf);
+                pi *= om;
+                continue;
+            }
+            // fragment: per-sample coverage; first close a pending run
+            if (cur_slot >= 0) {
+#pragma unroll
+                for (int k = 0; k < SPT; ++k)
+                    lam[k] = make_float4(lam[k].x * pi, lam[k].y * pi, lam[k].z * pi, lam[k].w * pi);
+                cur_slot = -1;
+            }
+            const uint32_t m = pixel_mask(load_merged(d.merged, WORDS, w - 1u), S, k4);
+            const size_t es = rbase + sidx;
+            float4 gf = make_float4(0.f, 0.f, 0.f, 0.f);
+            float J[SPT];
+#pragma unroll
+            for (int k = 0; k < SPT; ++k) {
+                const float4 cb = d.tape[(es * SPT + k) * 32 + lane];
+                const float4 l = lam[k];
+                J[k] = l.x * av * (f.x - cb.x) + l.y * av * (f.y - cb.y) + l.z * av * (f.z - cb.z) +
+                       l.w * av * (av - cb.w);
+                if ((m >> (sub + 8 * k)) & 1u) {
+                    gf.x += l.x * av;
+                    gf.y += l.y * av;
+                    gf.z += l.z * av;
+                    gf.w += l.x * (f.x - cb.x) + l.y * (f.y - cb.y) + l.z * (f.z - cb.z) + l.w * (2.f * av - cb.w);
+                    lam[k] = make_float4(l.x * om, l.y * om, l.z * om, l.w * om);
+                }
+            }
+            group_adjoint<S>(a, d, d.heads[w - 1], a.fill_rule[path], J, lane);
+            gf.x = warp_sum(gf.x);
+            gf.y = warp_sum(gf.y);
+            gf.z = warp_sum(gf.z);
+            gf.w = warp_sum(gf.w);
+            if (lane == 0 && (gf.x != 0.f || gf.y != 0.f || gf.z != 0.f || gf.w != 0.f))
+                add_fill_grad(d, acc, path, gf);
         }
+    }
+    if (acc) {
         __syncthreads();
-        const int n_acc = min((int)(fin - beg), kDiffItemAcc);
-        for (int q = t; q < n_acc; q += kDiffThreads) {
-            const float *v = sm.acc[q];
-            if (v[0] == 0.f && v[1] == 0.f && v[2] == 0.f && v[3] == 0.f) continue;
-            const uint32_t path = d.item_path[d.pval[beg + q]];
-            atomicAdd(&d.grad_fill[path].x, v[0]);
-            atomicAdd(&d.grad_fill[path].y, v[1]);
-            atomicAdd(&d.grad_fill[path].z, v[2]);
-            atomicAdd(&d.grad_fill[path].w, v[3]);
+        for (int i = threadIdx.x; i < a.P; i += kDiffThreads) {
+            const float4 v = acc[i];
+            if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+                atomicAdd(&d.grad_fill[i].x, v.x);
+                atomicAdd(&d.grad_fill[i].y, v.y);
+                atomicAdd(&d.grad_fill[i].z, v.z);
+                atomicAdd(&d.grad_fill[i].w, v.w);
+            }
         }
     }
 }
@@ -455,20 +711,44 @@ int launch_diff(const FrameArgs &a, const DiffArgs &d, cudaStream_t s) {
     if (a.n_bins <= 0) return 0;
     cudaMemsetAsync(d.queue, 0, sizeof(uint32_t), s);
     const unsigned grid = (unsigned)diff_blocks(a);
-    if (a.S == 8) k_diff<8, BWD><<<grid, kDiffThreads, 0, s>>>(a, d);
-    else if (a.S == 16) k_diff<16, BWD><<<grid, kDiffThreads, 0, s>>>(a, d);
-    else k_diff<32, BWD><<<grid, kDiffThreads, 0, s>>>(a, d);
-    return 1;
+    int n = 1;
+    if (d.npairs > 0) {
+        k_diff_gather<<<(unsigned)((d.npairs + 255) / 256), 256, 0, s>>>(d, a.S / 8);
+        ++n;
+    }
+    const int path_acc = (BWD && a.P <= kDiffPathAcc) ? 1 : 0;
+    const size_t smem = path_acc ? sizeof(float4) * (size_t)std::max(a.P, 1) : 0;
+    if (a.S == 8) {
+        cudaFuncSetAttribute(k_diff<8, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_diff<8, BWD><<<grid, kDiffThreads, smem, s>>>(a, d, path_acc);
+    } else if (a.S == 16) {
+        cudaFuncSetAttribute(k_diff<16, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_diff<16, BWD><<<grid, kDiffThreads, smem, s>>>(a, d, path_acc);
+    } else {
+        cudaFuncSetAttribute(k_diff<32, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_diff<32, BWD><<<grid, kDiffThreads, smem, s>>>(a, d, path_acc);
+    }
+    if (BWD && d.nf > 0) {
+        k_diff_chain<<<(unsigned)((d.nf + 255) / 256), 256, 0, s>>>(a, d);
+        ++n;
+    }
+    return n;
 }
 
 }  // namespace
 
 int64_t diff_blocks(const FrameArgs &a) {
-    return std::max<int64_t>(1, std::min<int64_t>(a.n_bins, (int64_t)diff_sm_count() * 2));
+    const int64_t units = a.n_bins * (kTileW / 2);
+    const int64_t per_block = kDiffThreads / 32;
+    return std::max<int64_t>(1, std::min<int64_t>((units + per_block - 1) / per_block, (int64_t)diff_sm_count() * 4));
 }
 
 int64_t diff_tape_words(const FrameArgs &a, int depth) {
     return diff_blocks(a) * (int64_t)depth * (a.S / 8) * kDiffThreads;
+}
+
+int64_t diff_tape_rec_words(const FrameArgs &a, int depth) {
+    return diff_blocks(a) * (int64_t)(kDiffThreads / 32) * depth * 3;
 }
 
 int launch_diff_forward(const FrameArgs &a, const DiffArgs &d, cudaStream_t s) { return launch_diff<false>(a, d, s); }

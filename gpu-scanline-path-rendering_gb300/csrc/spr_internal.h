@@ -96,6 +96,7 @@ struct FrameArgs {
     // units (q0, q1) and its left mask; per draw item its path.
     float4 *chord;
     uint32_t *lmask;
+    uint32_t *vmask;  // rows between the chord's end points (vertical_mask2)
     uint32_t *item_path;
 };
 
@@ -147,21 +148,32 @@ struct DiffArgs {
     const int4 *draw;
     const uint32_t *merged;
     const uint32_t *pval, *bstart, *bend;
+    int64_t npairs;
+    // the resolve pairs' items gathered in bin order: (pos, length, merged
+    // index + 1, path), the path's fill, the merged sample mask
+    uint4 *bitem;
+    float4 *bfill;
+    uint4 *bmm;
     const float4 *chord;
-    const uint32_t *lmask, *pidw, *perm, *heads, *item_path;
+    const uint32_t *lmask, *vmask, *pidw, *perm, *heads, *item_path;
+    // per fragment crossing sums (raw fragment, slope, sum dL/dx (1 - lam),
+    // sum dL/dx lam), chained to the control points by a second kernel
+    float4 *chain;
+    uint32_t *n_chain;
     const uint64_t *skey;
     const int8_t *wn_scan;
     const int2 *entries;
     const float2 *tvert;
     int64_t nf;
-    float4 *tape;        // per block: tape_depth x (samples per thread) x block threads
-    uint32_t *tape_item; // per block: tape_depth x block threads
+    float4 *tape;      // per block: tape_depth x (samples per thread) x block threads (sample states)
+    float4 *tape_rec;  // per block: warps x tape_depth x 4 (per-cell item records)
     int tape_depth;
     uint32_t *queue;     // bin queue (zeroed by the launchers)
-    uint32_t *status;    // bit 0: a tape overflowed (rerun with a deeper tape)
+    uint32_t *status;    // bit 0: a tape overflowed (rerun with a deeper tape); bit 1: chain list full
 };
 int64_t diff_blocks(const FrameArgs &a);
-int64_t diff_tape_words(const FrameArgs &a, int depth);  // float4 count; tape_item needs depth * threads * blocks
+int64_t diff_tape_words(const FrameArgs &a, int depth);      // float4 count of the sample-state tape
+int64_t diff_tape_rec_words(const FrameArgs &a, int depth);  // float4 count of the item records
 int launch_diff_forward(const FrameArgs &a, const DiffArgs &d, cudaStream_t s);
 int launch_diff_backward(const FrameArgs &a, const DiffArgs &d, cudaStream_t s);
 // dL/d(stored vertex in transformed space) -> dL/d(input vertex), dL/d(path affine).

@@ -370,8 +370,13 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
     }
     if (a.chord != nullptr) {
         a.chord[i] = chord;
+        uint32_t vmk[4] = {0u, 0u, 0u, 0u};
+        if (chord.y != chord.w) vertical_mask2<S>(chord.y, chord.w, vmk);
 #pragma unroll
-        for (int w = 0; w < WORDS; ++w) a.lmask[i * WORDS + w] = lmk[w];
+        for (int w = 0; w < WORDS; ++w) {
+            a.lmask[i * WORDS + w] = lmk[w];
+            a.vmask[i * WORDS + w] = vmk[w];
+        }
     }
     key_out[i] = yx;
     pid_out[i] = pathid | ((uint32_t)wnchg << 30);
