@@ -11,6 +11,11 @@ MPVG documents are not available).  One step = one frame through the C ABI
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+The line also carries "batched" (256 uneven scenes: one batched render
+against one launch sequence per scene, scenes/s) and "differentiable"
+(1024x1024, 256 cubic paths, 16 spp: forward, forward + L2 gradient +
+backward, and the plain RGBA8 frame, ms) unless --no-extras.
+
 --impl reference times the CPU oracle -- the C++ restatement of the
 reference pipeline (its own GPU code needs OpenGL, unavailable on this machine)
 -- on all host threads, each step a 2048x512 band of the same scene.
@@ -224,6 +229,150 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------- added rows --
+BATCH = dict(n_scenes=256, seed=20261203, sizes=(256, 512, 1024, 2048), samples=(8, 32), paths=(10, 5000),
+             seg_min=8, seg_max=32)
+DIFF = dict(width=1024, height=1024, n_paths=256, seg_min=16, seg_max=64, samples=16, seed=20261203,
+            jitter_px=2.0, color_sigma=0.05)
+
+
+def batch_items():
+    """The batched workload: 256 scenes, path count log-uniform in 10-5000,
+    square resolution from {256, 512, 1024, 2048}, 8 or 32 spp, paths of
+    8-32 mixed segments with control points uniform in a per-path box (side
+    U[d/32, d/4])."""
+    import numpy as np
+
+    import spr
+
+    rng = np.random.default_rng(BATCH["seed"])
+    items = []
+    for i in range(BATCH["n_scenes"]):
+        d = int(rng.choice(BATCH["sizes"]))
+        smp = int(rng.choice(BATCH["samples"]))
+        n = int(np.exp(rng.uniform(np.log(BATCH["paths"][0]), np.log(BATCH["paths"][1]))))
+        sc = spr.Scene.generate(spr.SCENE_LOCAL, seed=BATCH["seed"] + 1 + i, width=d, height=d, n_paths=n,
+                                seg_min=BATCH["seg_min"], seg_max=BATCH["seg_max"])
+        items.append((sc, d, d, smp))
+    return items
+
+
+def _timed(dev, stream, fn, n):
+    import torch
+
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    fn()
+    torch.cuda.synchronize(dev)
+    ts = []
+    for _ in range(n):
+        ev[0].record(stream)
+        fn()
+        ev[1].record(stream)
+        ev[1].synchronize()
+        ts.append(ev[0].elapsed_time(ev[1]))
+    return sum(ts) / len(ts)
+
+
+def run_batched(dev, stream, steps=3):
+    """Scenes/s of one batched render of the whole set against one launch
+    sequence (spr_render) per scene, both from device-resident scenes."""
+    import spr
+
+    items = batch_items()
+    sp = stream.cuda_stream
+    with spr.Batch(device=dev.index) as b:
+        b.set_scenes(items)
+        batch_ms = _timed(dev, stream, lambda: b.render(sp), steps)
+        counts = b.element_number()
+        st = b.frame_stats()
+    hs = []
+    for sc, W, H, smp in items:
+        r = spr.VGRasterizer(W, H, samples=smp, device=dev.index)
+        r.add_vg(sc)
+        hs.append(r)
+
+    def each():
+        for r in hs:
+            r.rasterize(sp)
+
+    single_ms = _timed(dev, stream, each, max(1, steps - 1))
+    launches = sum(r.frame_stats()["kernel_launches"] for r in hs)
+    for r in hs:
+        r.close()
+    n = len(items)
+    return {"workload": "256 scenes, paths log-uniform 10-5000, 256^2-2048^2, 8/32 spp ms sRGB, "
+                        "8-32 mixed segments per path in a per-path box",
+            "scenes": n, "pixels": int(sum(W * H for _, W, H, _ in items)), "counts": counts,
+            "scenes_per_s": n / (batch_ms / 1e3), "ms_per_batch": batch_ms,
+            "per_scene_scenes_per_s": n / (single_ms / 1e3), "per_scene_ms": single_ms,
+            "speedup": single_ms / batch_ms, "launches_batched": st["kernel_launches"],
+            "launches_per_scene_total": launches, "host_syncs_batched": st["host_syncs"],
+            "device_bytes_batched": st["device_bytes"]}
+
+
+def run_diff(dev, stream, steps=5):
+    """Differentiable render: forward (float composite), L2-loss gradient and
+    backward (edge-sampled adjoint) against a target rendered with control
+    points perturbed by N(0, 2 px) and colours by N(0, 0.05); the plain
+    RGBA8 frame of the same scene beside it."""
+    import numpy as np
+    import torch
+
+    import spr
+
+    W, H = DIFF["width"], DIFF["height"]
+    sc = spr.Scene.generate(spr.SCENE_CUBICS, seed=DIFF["seed"], width=W, height=H, n_paths=DIFF["n_paths"],
+                            seg_min=DIFF["seg_min"], seg_max=DIFF["seg_max"])
+    rng = np.random.default_rng(DIFF["seed"])
+    P = sc.n_paths
+    fill0 = np.c_[rng.uniform(0, 1, (P, 3)), rng.uniform(0.5, 1, (P, 1))].astype(np.float32)
+    tgt = sc.copy()
+    tgt.vertex = tgt.vertex + rng.normal(0, DIFF["jitter_px"], tgt.vertex.shape).astype(np.float32)
+    fill_t = np.clip(fill0 + rng.normal(0, DIFF["color_sigma"], fill0.shape), 0, 1).astype(np.float32)
+    sp = stream.cuda_stream
+    fill = torch.tensor(fill0, device=dev)
+    img = torch.empty((H, W, 4), device=dev)
+    target = torch.empty((H, W, 4), device=dev)
+    gf = torch.empty_like(fill)
+    gv = torch.empty((sc.n_vertices, 2), device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    with spr.VGRasterizer(W, H, samples=DIFF["samples"], device=dev.index) as r:
+        r.add_vg(tgt)
+        ft = torch.tensor(fill_t, device=dev)
+        r.diff_render(ft.data_ptr(), target.data_ptr(), sp)
+        r.add_vg(sc)
+        loss = torch.zeros((), device=dev)
+
+        def step():
+            r.diff_render(fill.data_ptr(), img.data_ptr(), sp)
+            ev[1].record(stream)
+            diff = img - target
+            loss.copy_((diff * diff).sum())
+            g = (2.0 * diff).contiguous()
+            r.diff_backward(fill.data_ptr(), g.data_ptr(), gf.data_ptr(), gv.data_ptr(), None, sp)
+
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize(dev)
+        fwd, tot = [], []
+        for _ in range(steps):
+            ev[0].record(stream)
+            step()
+            ev[2].record(stream)
+            ev[2].synchronize()
+            fwd.append(ev[0].elapsed_time(ev[1]))
+            tot.append(ev[0].elapsed_time(ev[2]))
+        dev_bytes = r.frame_stats()["device_bytes"]
+        plain = _timed(dev, stream, lambda: r.rasterize(sp), steps)
+        counts = r.element_number()
+    f, t = sum(fwd) / len(fwd), sum(tot) / len(tot)
+    return {"workload": f"{W}x{H}, {P} closed paths of 16-64 cubic segments, 16 spp, L2 loss vs a target with "
+                        "control points + N(0, 2 px) and colours + N(0, 0.05)",
+            "counts": counts, "fwd_ms": f, "fwd_bwd_ms": t, "fwd_bwd_over_fwd": t / f,
+            "plain_rgba8_ms": plain, "fwd_bwd_over_plain": t / plain, "loss": float(loss),
+            "device_bytes": dev_bytes}
+
+
 # ------------------------------------------------------------- GPU arm --
 def run_ours(args, rank, world, local_rank):
     import numpy as np
@@ -348,6 +497,10 @@ def run_ours(args, rank, world, local_rank):
                                    f"one frame, all stages, {cores} threads",
                          "ms": cpu_ms},
     }
+    if not args.no_extras:  # the batched and differentiable rows, on this GPU after the plain frames
+        del flush
+        line["batched"] = run_batched(dev, stream)
+        line["differentiable"] = run_diff(dev, stream)
     print(json.dumps(line), flush=True)
 
 
@@ -379,6 +532,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="linear size scale of the workload (profiling of smaller cases)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched-scenes and differentiable-render measurements")
     ap.add_argument("--profile", action="store_true",
                     help="timed GPU frames only (no end-to-end or CPU legs), for profiler runs")
     args = ap.parse_args()
