@@ -101,7 +101,7 @@ struct spr_handle {
     // differentiable frames: per-fragment chords and left masks, per-item
     // paths, the per-block tapes, the transformed-vertex gradient and the
     // stored -> input vertex map
-    DevBuf chord, lmask, vmask, item_path, tape, tape_rec, grad_tvert, vmap, bitems, chain;
+    DevBuf chord, lmask, vmask, item_path, tape, tape_rec, grad_tvert, vmap, bitems, chain, ekey[2], eval[2];
     int tape_depth = 128;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
@@ -269,7 +269,8 @@ int spr_destroy(spr_handle *h) {
                       &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
                       &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
                       &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
-                      &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain};
+                      &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
+                      &h->eval[1]};
     for (DevBuf *b : bufs) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
@@ -551,8 +552,23 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         a.item_path = h->item_path.as<uint32_t>();
     }
     rec(h, 2, s);
-    L += launch_curve_emit(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->offsets.as<uint32_t>(), h->entries.as<int2>(),
-                      s);
+    // emission order: curves sorted by estimated cost (16-bit keys, two passes)
+    const uint32_t *order = nullptr;
+    if (h->C >= 4096) {
+        if ((st = ensure(h->ekey[0], 4 * (size_t)h->C)) || (st = ensure(h->ekey[1], 4 * (size_t)h->C)) ||
+            (st = ensure(h->eval[0], 4 * (size_t)h->C)) || (st = ensure(h->eval[1], 4 * (size_t)h->C)) ||
+            (st = ensure(h->sort_tmp, 4 * (size_t)std::max(radix_tmp_words(nf), radix_tmp_words(h->C)))))
+            return st;
+        L += launch_emit_keys(a, h->counts.as<uint32_t>(), h->ekey[0].as<uint32_t>(), h->eval[0].as<uint32_t>(), s);
+        int el = 0;
+        const bool ealt = radix_sort<uint32_t>(h->ekey[0].as<uint32_t>(), h->eval[0].as<uint32_t>(),
+                                               h->ekey[1].as<uint32_t>(), h->eval[1].as<uint32_t>(), h->C, 16,
+                                               h->sort_tmp.as<uint32_t>(), s, &el);
+        L += el;
+        order = ealt ? h->eval[1].as<uint32_t>() : h->eval[0].as<uint32_t>();
+    }
+    L += launch_curve_emit(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->offsets.as<uint32_t>(), order,
+                           h->entries.as<int2>(), s);
     L += launch_fragment(a, h->tvert.as<float2>(), h->entries.as<int2>(), nf, h->key.as<int32_t>(), h->pidw.as<uint32_t>(),
                     h->wn.as<int8_t>(), h->mask.as<uint32_t>(), h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), s);
     rec(h, 3, s);
@@ -724,7 +740,8 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
                             &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d,
                             &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
-                            &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain};
+                            &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
+                      &h->eval[1]};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;

@@ -104,8 +104,11 @@ int launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, ui
                       cudaStream_t s);
 int launch_curve_count(const FrameArgs &a, const float2 *tvert, const uint8_t *path_visible, uint32_t *counts,
                         cudaStream_t s);
+// Sort keys of the emission order (curves by decreasing estimated cost).
+int launch_emit_keys(const FrameArgs &a, const uint32_t *counts, uint32_t *key, uint32_t *val, cudaStream_t s);
+// order: curve processed by thread i (null = identity); outputs do not depend on it.
 int launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *path_visible,
-                       const uint32_t *offsets, int2 *entries, cudaStream_t s);
+                       const uint32_t *offsets, const uint32_t *order, int2 *entries, cudaStream_t s);
 int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t nf, int32_t *key,
                      uint32_t *pidw, int8_t *wn, uint32_t *mask, uint64_t *sort_key, uint32_t *sort_val,
                      cudaStream_t s);

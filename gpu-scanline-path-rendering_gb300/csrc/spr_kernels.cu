@@ -156,10 +156,25 @@ __global__ void k_curve_count(FrameArgs a, const float2 *__restrict__ tv, const 
 // Entries of one curve in t order: each monotone piece emits its start and
 // every crossing with a vertical (x = even) or horizontal (y = even) cell
 // line, the two crossing chains merged by t; equal t values OR their flags.
+// Emission order: curves by decreasing estimated cost (entries, a cubic's
+// bisection weighted 8x), so that a warp's curves take similar time and the
+// longest start first.  key = 0xFFFF - cost (ascending sort).
+__global__ void k_emit_keys(FrameArgs a, const uint32_t *__restrict__ counts, uint32_t *__restrict__ key,
+                            uint32_t *__restrict__ val) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.C) return;
+    const uint32_t type = a.curves[c].type & 0xFFu;
+    const uint32_t cost = counts[c] * (type == (uint32_t)kCubic ? 8u : 1u);
+    key[c] = 0xFFFFu - min(cost, 0xFFFFu);
+    val[c] = (uint32_t)c;
+}
+
 __global__ void k_curve_emit(FrameArgs a, const float2 *__restrict__ tv, const uint8_t *__restrict__ vis,
-                             const uint32_t *__restrict__ offsets, int2 *__restrict__ entries) {
-    const int cid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cid >= a.C) return;
+                             const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ order,
+                             int2 *__restrict__ entries) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.C) return;
+    const int cid = order != nullptr ? (int)order[i] : i;
     const CurveDesc d = a.curves[cid];
     CurveGeom g;
     load_geom(d, tv, g);
@@ -1166,10 +1181,16 @@ int launch_curve_count(const FrameArgs &a, const float2 *tvert, const uint8_t *v
     return 1;
 }
 
-int launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *vis, const uint32_t *offsets,
-                       int2 *entries, cudaStream_t s) {
+int launch_emit_keys(const FrameArgs &a, const uint32_t *counts, uint32_t *key, uint32_t *val, cudaStream_t s) {
     if (a.C <= 0) return 0;
-    k_curve_emit<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, offsets, entries);
+    k_emit_keys<<<grid_for(a.C), kThreads, 0, s>>>(a, counts, key, val);
+    return 1;
+}
+
+int launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *vis, const uint32_t *offsets,
+                       const uint32_t *order, int2 *entries, cudaStream_t s) {
+    if (a.C <= 0) return 0;
+    k_curve_emit<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, offsets, order, entries);
     return 1;
 }
 
