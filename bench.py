@@ -285,6 +285,10 @@ def run_batched(dev, stream, steps=3):
         batch_ms = _timed(dev, stream, lambda: b.render(sp), steps)
         counts = b.element_number()
         st = b.frame_stats()
+        b.enable_step_timing(True)
+        b.render(sp)
+        step_ms = b.step_timing()
+        b.enable_step_timing(False)
     hs = []
     for sc, W, H, smp in items:
         r = spr.VGRasterizer(W, H, samples=smp, device=dev.index)
@@ -307,7 +311,7 @@ def run_batched(dev, stream, steps=3):
             "per_scene_scenes_per_s": n / (single_ms / 1e3), "per_scene_ms": single_ms,
             "speedup": single_ms / batch_ms, "launches_batched": st["kernel_launches"],
             "launches_per_scene_total": launches, "host_syncs_batched": st["host_syncs"],
-            "device_bytes_batched": st["device_bytes"]}
+            "device_bytes_batched": st["device_bytes"], "step_ms_batched": step_ms}
 
 
 def run_diff(dev, stream, steps=5):
@@ -536,6 +540,9 @@ def main():
                     help="skip the batched-scenes and differentiable-render measurements")
     ap.add_argument("--profile", action="store_true",
                     help="timed GPU frames only (no end-to-end or CPU legs), for profiler runs")
+    ap.add_argument("--part", choices=["all", "batched", "diff"], default="all",
+                    help="run only the batched or the differentiable measurement (one JSON object), "
+                         "for profiler runs")
     args = ap.parse_args()
     scale_workload(args.scale)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -543,6 +550,15 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.part != "all":
+        import torch
+
+        dev = torch.device("cuda", local_rank)
+        torch.cuda.set_device(dev)
+        stream = torch.cuda.current_stream(dev)
+        fn = run_batched if args.part == "batched" else run_diff
+        print(json.dumps({args.part: fn(dev, stream, steps=max(1, args.steps))}), flush=True)
         return
     if world > 1:
         import torch
