@@ -730,6 +730,7 @@ __global__ void k_bin_bounds(const uint32_t *__restrict__ key, int64_t n, uint32
 struct SmemTables {
     float dec8r[256 * 8];
     float th[256];
+    uint8_t bin[4096];  // number of thresholds <= b / 4096
 };
 
 __device__ __forceinline__ float lin8(uint32_t k) { return (float)k * (1.f / 255.f); }
@@ -744,18 +745,15 @@ __device__ __forceinline__ uint32_t enc_lin(float v) {
 }
 
 // sRGB encode: the number of thresholds t[k] (the linear value at which the
-// 8-bit code steps from k to k+1) that are <= v.  A closed-form estimate
-// (within one code of the answer) is corrected by exact comparisons against
-// the thresholds, so the result is exactly the table definition.
-__device__ __forceinline__ uint32_t enc_srgb(const float *__restrict__ th, float v) {
+// 8-bit code steps from k to k+1) that are <= v.  The thresholds are at
+// least 3.0e-4 apart, wider than the 1/4096 bins of `bin`, so a bin holds at
+// most one of them: the count is the bin's base plus one comparison.
+__device__ __forceinline__ uint32_t enc_srgb(const SmemTables &t, float v) {
     const float c = clamp01(v);
-    const float e = c <= 0.0031308f ? c * 12.92f : 1.055f * __powf(c, 1.f / 2.4f) - 0.055f;
-    int k = min(max(__float2int_rn(e * 255.f), 0), 255);
-    // th[-1] = -inf and th[255] = +inf are implied by the clamps below
-    const float lo = th[max(k - 1, 0)], hi = th[k];
-    if (k > 0 && c < lo) return (uint32_t)(k - 1);
-    if (k < 255 && c >= hi) return (uint32_t)(k + 1);
-    return (uint32_t)k;
+    const int b = min(cvt_rzi(c * 4096.f), 4095);
+    uint32_t k = t.bin[b];
+    if (k < 255u && c >= t.th[k]) ++k;
+    return k;
 }
 
 template <bool SRGB>
@@ -766,7 +764,7 @@ __device__ __forceinline__ float dec8(const SmemTables &t, uint32_t k, int lane)
 
 template <bool SRGB>
 __device__ __forceinline__ uint32_t enc8(const SmemTables &t, float v) {
-    if constexpr (SRGB) return enc_srgb(t.th, v);
+    if constexpr (SRGB) return enc_srgb(t, v);
     else return enc_lin(v);
 }
 
@@ -1091,6 +1089,9 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
         if constexpr (SRGB)
             for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) T.dec8r[i] = rt->srgb_dec[i >> 3];
         for (int i = threadIdx.x; i < 256; i += blockDim.x) T.th[i] = rt->threshold[i];
+        if constexpr (SRGB)
+            for (int i = threadIdx.x; i < 1024; i += blockDim.x)
+                reinterpret_cast<uint32_t *>(T.bin)[i] = reinterpret_cast<const uint32_t *>(rt->bin)[i];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1107,22 +1108,27 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
     }
 }
 
-// Exhaustive check of enc_srgb against the table definition (bins + one
-// threshold step) over every float bit pattern in [lo, hi).
+// Exhaustive check of enc_srgb against the definition (the number of
+// thresholds <= the clamped value, by binary search) over every float bit
+// pattern in [lo, hi).
 __global__ void k_selftest_encode(const ResolveTables *__restrict__ rt, uint32_t lo, uint32_t hi,
                                   unsigned long long *__restrict__ bad) {
-    __shared__ float th[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) th[i] = rt->threshold[i];
+    __shared__ SmemTables T;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) T.th[i] = rt->threshold[i];
+    for (int i = threadIdx.x; i < 4096; i += blockDim.x) T.bin[i] = rt->bin[i];
     __syncthreads();
     unsigned long long local = 0;
     for (uint64_t u = lo + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < hi;
          u += (uint64_t)gridDim.x * blockDim.x) {
         const float v = __uint_as_float((uint32_t)u);
         const float c = fmin_r(fmax_r(v, 0.f), 1.f);
-        const int bb = min(cvt_rzi(c * 4096.f), 4095);
-        uint32_t k = rt->bin[bb];
-        if (k < 255 && c >= th[k]) ++k;
-        if (enc_srgb(th, v) != k) ++local;
+        int a = 0, b = 255;  // thresholds th[0..254] ascending: count those <= c
+        while (a < b) {
+            const int m = (a + b) >> 1;
+            if (T.th[m] <= c) a = m + 1;
+            else b = m;
+        }
+        if (enc_srgb(T, v) != (uint32_t)a) ++local;
     }
     if (local) atomicAdd(bad, local);
 }
