@@ -129,17 +129,32 @@ __global__ void k_radix_hist(const K *__restrict__ keys, int64_t n, int shift, u
     counts[(int64_t)threadIdx.x * ntiles + blockIdx.x] = hist[threadIdx.x];
 }
 
+// Shared memory of the scatter: the tile reordered by digit, then written
+// out in digit runs (consecutive elements of a digit go to consecutive
+// global positions, so the writes coalesce).
+template <class K>
+struct ScatterSmem {
+    K key[kRadixTile];
+    uint32_t val[kRadixTile];
+    uint32_t whist[kRadixWarps][256];
+    uint32_t lstart[256];  // first local position of each digit
+    uint32_t gstart[256];  // the tile's first global position of each digit
+};
+
 template <class K>
 __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const K *__restrict__ keys,
                                                                   const uint32_t *__restrict__ vals, int64_t n,
                                                                   int shift, const uint32_t *__restrict__ offsets,
                                                                   int64_t ntiles, K *__restrict__ keys_out,
                                                                   uint32_t *__restrict__ vals_out) {
-    __shared__ uint32_t whist[kRadixWarps][256];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ScatterSmem<K> &sm = *reinterpret_cast<ScatterSmem<K> *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&whist[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&sm.whist[0][0])[i] = 0;
     __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * kRadixTile + (int64_t)warp * kRadixWarpSpan;
+    const int64_t tile0 = (int64_t)blockIdx.x * kRadixTile;
+    const int64_t base = tile0 + (int64_t)warp * kRadixWarpSpan;
+    const int cnt = (int)min((int64_t)kRadixTile, n - tile0);
     K kk[kRadixItems];
     uint32_t vv[kRadixItems];
     uint32_t rank[kRadixItems];
@@ -152,33 +167,66 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const K *__rest
         uint32_t d = valid ? ((uint32_t)(kk[r] >> shift) & 0xFFu) : (256u + lane);
         uint32_t peers = __match_any_sync(0xffffffffu, d);
         uint32_t before = __popc(peers & ((1u << lane) - 1u));
-        uint32_t cur = valid ? whist[warp][d] : 0u;
+        uint32_t cur = valid ? sm.whist[warp][d] : 0u;
         __syncwarp();
-        if (valid && before == 0) whist[warp][d] = cur + __popc(peers);
+        if (valid && before == 0) sm.whist[warp][d] = cur + __popc(peers);
         __syncwarp();
         rank[r] = cur + before;
     }
     __syncthreads();
     {
-        const int d = threadIdx.x;  // one digit per thread
-        uint32_t acc = offsets[(int64_t)d * ntiles + blockIdx.x];
+        const int d = threadIdx.x;  // one digit per thread: the tile's count of d, per-warp local offsets
+        uint32_t tot = 0;
 #pragma unroll
         for (int w = 0; w < kRadixWarps; ++w) {
-            uint32_t c = whist[w][d];
-            whist[w][d] = acc;
-            acc += c;
+            const uint32_t c = sm.whist[w][d];
+            sm.whist[w][d] = tot;
+            tot += c;
         }
+        // exclusive scan of the digit totals over the block
+        __shared__ uint32_t wsum[kRadixWarps + 1];
+        uint32_t inc = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t t = lane < kRadixWarps ? wsum[lane] : 0u, ti = t;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, ti, o);
+                if (lane >= o) ti += v;
+            }
+            if (lane < kRadixWarps) wsum[lane] = ti - t;
+        }
+        __syncthreads();
+        const uint32_t ls = wsum[warp] + inc - tot;
+        sm.lstart[d] = ls;
+        sm.gstart[d] = offsets[(int64_t)d * ntiles + blockIdx.x];
+#pragma unroll
+        for (int w = 0; w < kRadixWarps; ++w) sm.whist[w][d] += ls;
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kRadixItems; ++r) {
         int64_t i = base + r * 32 + lane;
         if (i < n) {
-            uint32_t d = (uint32_t)(kk[r] >> shift) & 0xFFu;
-            uint32_t pos = whist[warp][d] + rank[r];
-            keys_out[pos] = kk[r];
-            vals_out[pos] = vv[r];
+            const uint32_t d = (uint32_t)(kk[r] >> shift) & 0xFFu;
+            const uint32_t lp = sm.whist[warp][d] + rank[r];
+            sm.key[lp] = kk[r];
+            sm.val[lp] = vv[r];
         }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += kRadixThreads) {
+        const K k = sm.key[i];
+        const uint32_t d = (uint32_t)(k >> shift) & 0xFFu;
+        const uint32_t pos = sm.gstart[d] + (uint32_t)i - sm.lstart[d];
+        keys_out[pos] = k;
+        vals_out[pos] = sm.val[i];
     }
 }
 
@@ -221,6 +269,7 @@ bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_
     uint32_t *offsets = tmp + (c + 1);
     uint32_t *scan_tmp = tmp + 2 * (c + 1);
     bool alt = false;
+    cudaFuncSetAttribute(k_radix_scatter<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ScatterSmem<K>));
     for (int shift = 0; shift < key_bits; shift += 8) {
         const K *ki = alt ? keys_alt : keys;
         const uint32_t *vi = alt ? vals_alt : vals;
@@ -228,7 +277,8 @@ bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_
         uint32_t *vo = alt ? vals : vals_alt;
         k_radix_hist<K><<<(unsigned)ntiles, kRadixThreads, 0, s>>>(ki, n, shift, counts, ntiles);
         *launches += 2 + scan_exclusive_u32(counts, offsets, c, scan_tmp, s);
-        k_radix_scatter<K><<<(unsigned)ntiles, kRadixThreads, 0, s>>>(ki, vi, n, shift, offsets, ntiles, ko, vo);
+        k_radix_scatter<K><<<(unsigned)ntiles, kRadixThreads, sizeof(ScatterSmem<K>), s>>>(ki, vi, n, shift, offsets,
+                                                                                       ntiles, ko, vo);
         alt = !alt;
     }
     return alt;
