@@ -289,6 +289,11 @@ def run_batched(dev, stream, steps=3):
         b.render(sp)
         step_ms = b.step_timing()
         b.enable_step_timing(False)
+        b.set_graph_replay(True)  # unchanged scenes: the captured launch sequence, no host reads
+        for _ in range(2):
+            b.render(sp)
+        graph_ms = _timed(dev, stream, lambda: b.render(sp), steps)
+        graph_syncs = b.frame_stats()["host_syncs"]
     hs = []
     for sc, W, H, smp in items:
         r = spr.VGRasterizer(W, H, samples=smp, device=dev.index)
@@ -311,7 +316,9 @@ def run_batched(dev, stream, steps=3):
             "per_scene_scenes_per_s": n / (single_ms / 1e3), "per_scene_ms": single_ms,
             "speedup": single_ms / batch_ms, "launches_batched": st["kernel_launches"],
             "launches_per_scene_total": launches, "host_syncs_batched": st["host_syncs"],
-            "device_bytes_batched": st["device_bytes"], "step_ms_batched": step_ms}
+            "device_bytes_batched": st["device_bytes"], "step_ms_batched": step_ms,
+            "graph_replay": {"ms_per_batch": graph_ms, "scenes_per_s": n / (graph_ms / 1e3),
+                             "speedup": single_ms / graph_ms, "host_syncs": graph_syncs}}
 
 
 def run_diff(dev, stream, steps=5):

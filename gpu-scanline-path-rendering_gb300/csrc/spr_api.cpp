@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -44,9 +45,14 @@ struct DevBuf {
     }
 };
 
+// Bumped whenever a buffer is reallocated: a captured frame graph holds the
+// buffer addresses of its capture and is replayed only while this is unchanged.
+std::atomic<uint64_t> g_alloc_gen{0};
+
 int ensure(DevBuf &b, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (b.bytes >= bytes) return SPR_OK;
+    g_alloc_gen.fetch_add(1);
     b.release();
     size_t want = bytes + bytes / 4;
     want = (want + 255) & ~(size_t)255;
@@ -118,6 +124,14 @@ struct spr_handle {
     bool frame_valid = false;
     int launches = 0, host_syncs = 0;
     int frame_W = 0, frame_H = 0, frame_S = 8;
+    // graph replay of unchanged frames: the launch sequence of the last eager
+    // frame, captured with its sizes (no host reads)
+    bool graph_mode = false, capturing = false, graph_failed = false;
+    cudaGraphExec_t gexec = nullptr;
+    uint64_t gexec_gen = 0;
+    cudaStream_t cap_stream = nullptr;
+    int64_t cap_nf = 0, cap_nm = 0, cap_ns = 0, cap_np = 0;
+    int graph_replays = 0;
     // timing
     bool timing = false;
     cudaEvent_t ev[kSteps + 1] = {};
@@ -125,6 +139,12 @@ struct spr_handle {
 };
 
 namespace {
+
+void drop_graph(spr_handle *h) {
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+    h->graph_failed = false;
+}
 
 int validate_config(const spr_config *c) {
     if (c->width < 1 || c->height < 1 || c->width > 4096 || c->height > 4096) return SPR_ERR_INVALID_ARG;
@@ -261,6 +281,8 @@ int spr_create(const spr_config *config, spr_handle **out) {
 int spr_destroy(spr_handle *h) {
     if (!h) return SPR_OK;
     cudaSetDevice(h->cfg.device);
+    drop_graph(h);
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     DevBuf *bufs[] = {&h->mask_table, &h->rtables, &h->vertex,   &h->vpid,      &h->curves,  &h->rule,
                       &h->fill,       &h->affine,  &h->tvert,    &h->pflags,    &h->pvis,    &h->counts,
                       &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
@@ -282,6 +304,7 @@ int spr_destroy(spr_handle *h) {
 
 int spr_resize(spr_handle *h, int32_t width, int32_t height) {
     if (!h) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
     spr_config c = h->cfg;
     c.width = width;
     c.height = height;
@@ -294,6 +317,7 @@ int spr_resize(spr_handle *h, int32_t width, int32_t height) {
 
 int spr_set_samples(spr_handle *h, int32_t samples) {
     if (!h) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
     if (samples != 8 && samples != 16 && samples != 32) return SPR_ERR_INVALID_ARG;
     cudaSetDevice(h->cfg.device);
     h->cfg.samples = samples;
@@ -303,18 +327,21 @@ int spr_set_samples(spr_handle *h, int32_t samples) {
 
 int spr_set_multisample_output(spr_handle *h, int32_t enable) {
     if (!h) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
     h->cfg.ms_output = enable ? 1 : 0;
     return SPR_OK;
 }
 
 int spr_enable_srgb_correction(spr_handle *h, int32_t enable) {
     if (!h) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
     h->cfg.srgb = enable ? 1 : 0;
     return SPR_OK;
 }
 
 int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     if (!h) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
     int st = validate_scene(v);
     if (st) return st;
     cudaSetDevice(h->cfg.device);
@@ -370,6 +397,7 @@ int spr_validate_scene(const spr_scene_view *scene) { return validate_scene(scen
 
 int spr_set_transform(spr_handle *h, const float m[16]) {
     if (!h || !m) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
     std::memcpy(h->m, m, sizeof(h->m));
     return SPR_OK;
 }
@@ -494,11 +522,16 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     // stages 4-5: monotone pieces, entry counts, exclusive scan
     L += launch_curve_count(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->counts.as<uint32_t>(), s);
     L += scan_exclusive_u32(h->counts.as<uint32_t>(), h->offsets.as<uint32_t>(), h->C, h->scan_tmp.as<uint32_t>(), s);
-    cudaMemcpyAsync(h->h_u32, h->offsets.as<uint32_t>() + h->C, 4, cudaMemcpyDeviceToHost, s);
-    ++h->host_syncs;
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
-    if ((st = cuda_status())) return st;
-    const int64_t nf = h->h_u32[0];
+    // under capture the sizes are those of the eager frame just rendered
+    const bool cap = h->capturing;
+    const int64_t cap_nm = h->cap_nm, cap_ns = h->cap_ns, cap_np = h->cap_np;
+    if (!cap) {
+        cudaMemcpyAsync(h->h_u32, h->offsets.as<uint32_t>() + h->C, 4, cudaMemcpyDeviceToHost, s);
+        ++h->host_syncs;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+        if ((st = cuda_status())) return st;
+    }
+    const int64_t nf = cap ? h->cap_nf : h->h_u32[0];
     if (nf > INT32_MAX) return SPR_ERR_CAPACITY_EXCEEDED;
     h->nf = nf;
     h->en.path = (int32_t)h->P;
@@ -587,12 +620,14 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     L += launch_scan_mark(a, nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
                      h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, h->counters.as<FrameCounters>(),
                      h->flags_tmp.as<uint32_t>(), s);
-    cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
-    ++h->host_syncs;
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
-    if ((st = cuda_status())) return st;
-    h->nm = h->h_counters->n_merged;
-    h->ns = h->h_counters->n_span;
+    if (!cap) {
+        cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
+        ++h->host_syncs;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+        if ((st = cuda_status())) return st;
+    }
+    h->nm = cap ? cap_nm : h->h_counters->n_merged;
+    h->ns = cap ? cap_ns : h->h_counters->n_span;
     h->en.merged_fragment = (int32_t)h->nm;
     h->en.span = (int32_t)h->ns;
     rec(h, 5, s);
@@ -607,10 +642,12 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     if ((st = ensure(h->scan_tmp, 4 * (size_t)scan_tmp_words(std::max<int64_t>({items, (int64_t)h->C, 1}))))) return st;
     L += launch_item_tiles(a, h->draw.as<int4>(), item_scene, items, h->tiles.as<uint32_t>(), s);
     L += scan_exclusive_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), items, h->scan_tmp.as<uint32_t>(), s);
-    cudaMemcpyAsync(h->h_u32, h->pair_off.as<uint32_t>() + items, 4, cudaMemcpyDeviceToHost, s);
-    ++h->host_syncs;
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
-    const int64_t npairs = h->h_u32[0];
+    if (!cap) {
+        cudaMemcpyAsync(h->h_u32, h->pair_off.as<uint32_t>() + items, 4, cudaMemcpyDeviceToHost, s);
+        ++h->host_syncs;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+    }
+    const int64_t npairs = cap ? cap_np : h->h_u32[0];
     h->npairs = npairs;
     if ((st = ensure(h->pkey[0], 4 * (size_t)npairs)) || (st = ensure(h->pkey[1], 4 * (size_t)npairs)) ||
         (st = ensure(h->pval[0], 4 * (size_t)npairs)) || (st = ensure(h->pval[1], 4 * (size_t)npairs)) ||
@@ -656,7 +693,65 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
 
 extern "C" {
 
-int spr_render(spr_handle *h, void *stream) { return render_frame(h, stream, nullptr); }
+int spr_render(spr_handle *h, void *stream) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    if (!h->graph_mode || h->timing || !h->has_scene) return render_frame(h, stream, nullptr);
+    cudaSetDevice(h->cfg.device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (h->gexec && h->gexec_gen != g_alloc_gen.load()) drop_graph(h);  // a buffer moved
+    if (h->gexec) {
+        if (cudaGraphLaunch(h->gexec, s) != cudaSuccess) return cuda_status();
+        h->host_syncs = 0;
+        h->frame_valid = true;
+        ++h->graph_replays;
+        return cuda_status();
+    }
+    int st = render_frame(h, stream, nullptr);
+    if (st || h->graph_failed) return st;
+    // capture this frame's launch sequence with its sizes
+    if (!h->cap_stream && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cuda_status();
+    const uint64_t gen = g_alloc_gen.load();
+    h->cap_nf = h->nf;
+    h->cap_nm = h->nm;
+    h->cap_ns = h->ns;
+    h->cap_np = h->npairs;
+    const int host_syncs = h->host_syncs, launches = h->launches;
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+    if (ok) {
+        h->capturing = true;
+        const int cst = render_frame(h, h->cap_stream, nullptr);
+        h->capturing = false;
+        ok = cudaStreamEndCapture(h->cap_stream, &g) == cudaSuccess && cst == SPR_OK && g != nullptr;
+    }
+    ok = ok && g_alloc_gen.load() == gen && cudaGraphInstantiate(&h->gexec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {  // stay eager for this scene
+        cudaGetLastError();
+        if (h->gexec) cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+        h->graph_failed = true;
+    }
+    h->gexec_gen = gen;
+    h->host_syncs = host_syncs;
+    h->launches = launches;
+    h->frame_valid = true;
+    return SPR_OK;
+}
+
+int spr_set_graph_replay(spr_handle *h, int32_t enable) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    h->graph_mode = enable != 0;
+    if (!h->graph_mode) drop_graph(h);
+    return SPR_OK;
+}
+
+int spr_graph_replays(spr_handle *h, int32_t *out) {
+    if (!h || !out) return SPR_ERR_INVALID_ARG;
+    *out = h->graph_replays;
+    return SPR_OK;
+}
 
 int spr_diff_render(spr_handle *h, const float *fill_rgba, float *image, void *stream) {
     if (!h || !fill_rgba || !image) return SPR_ERR_INVALID_ARG;
@@ -830,7 +925,7 @@ const char *spr_status_string(int32_t status) {
 
 struct spr_batch {
     int device = 0, ms_output = 1, srgb = 1;
-    bool timing = false;
+    bool timing = false, graph = false;
     spr_handle *group[3] = {nullptr, nullptr, nullptr};  // samples 8, 16, 32
     struct Entry {
         int group;
@@ -969,6 +1064,7 @@ int spr_batch_set_scenes(spr_batch *b, const spr_batch_scene *scenes, int32_t n)
             int st = spr_create(&cfg, &b->group[g]);
             if (st) return st;
             b->group[g]->timing = b->timing;
+            b->group[g]->graph_mode = b->graph;
         }
         int st = upload_group(b->group[g], scenes, idx[g], b->entries, g);
         if (st) return st;
@@ -1023,6 +1119,14 @@ int spr_batch_get_counts(spr_batch *b, spr_element_number *total) {
         t.span += h->en.span;
     }
     *total = t;
+    return SPR_OK;
+}
+
+int spr_batch_set_graph_replay(spr_batch *b, int32_t enable) {
+    if (!b) return SPR_ERR_INVALID_ARG;
+    b->graph = enable != 0;
+    for (spr_handle *h : b->group)
+        if (h) spr_set_graph_replay(h, enable);
     return SPR_OK;
 }
 

@@ -138,6 +138,9 @@ def lib() -> C.CDLL:
         L.spr_scene_view_of.argtypes = [vp, C.POINTER(SceneView)]
         L.spr_scene_free.argtypes = [vp]
         L.spr_scene_free.restype = None
+        L.spr_set_graph_replay.argtypes = [vp, i32]
+        L.spr_graph_replays.argtypes = [vp, C.POINTER(i32)]
+        L.spr_batch_set_graph_replay.argtypes = [vp, i32]
         L.spr_diff_render.argtypes = [vp, vp, vp, vp]
         L.spr_diff_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.spr_batch_create.argtypes = [i32, i32, i32, C.POINTER(vp)]
@@ -340,6 +343,14 @@ class VGRasterizer:
         check(lib().spr_selftest(self._h, C.byref(n)), "spr_selftest")
         return {"srgb_encode_mismatches": int(n.value)}
 
+    def set_graph_replay(self, f=True):
+        check(lib().spr_set_graph_replay(self._h, int(f)), "spr_set_graph_replay")
+
+    def graph_replays(self) -> int:
+        n = C.c_int32()
+        check(lib().spr_graph_replays(self._h, C.byref(n)), "spr_graph_replays")
+        return int(n.value)
+
     def diff_render(self, fill_ptr: int, image_ptr: int, stream=None):
         """Float composite with per-path linear RGBA fills (device pointers:
         fill float32[P, 4], image float32[H, W, 4])."""
@@ -441,6 +452,9 @@ class Batch:
         st = FrameStats()
         check(lib().spr_batch_get_frame_stats(self._h, C.byref(st)), "spr_batch_get_frame_stats")
         return {n: int(getattr(st, n)) for n, _ in FrameStats._fields_}
+
+    def set_graph_replay(self, f=True):
+        check(lib().spr_batch_set_graph_replay(self._h, int(f)), "spr_batch_set_graph_replay")
 
     def enable_step_timing(self, f=True):
         check(lib().spr_batch_enable_step_timing(self._h, int(f)), "spr_batch_enable_step_timing")

@@ -189,6 +189,19 @@ int spr_get_counts(spr_handle *h, spr_element_number *out);
  * spr_step_timing returns the per-stage milliseconds of the last frame. */
 int spr_enable_step_timing(spr_handle *h, int32_t enable);
 int spr_step_timing(spr_handle *h, double *ms, int32_t capacity, int32_t *n_out);
+/* Graph replay (an extension: no counterpart in the reference).  When it is
+ * enabled, the first spr_render after any change to the handle (scene,
+ * transform, size, samples, output modes) renders normally and then captures
+ * the same launch sequence, with that frame's sizes, in a CUDA graph; later
+ * spr_render calls of the unchanged handle launch the graph, with no host
+ * reads or synchronizations, and give the same bytes.  A reallocation of any
+ * of the library's device buffers (a larger scene on another handle, a stage
+ * dump, a differentiable frame) drops the graph and the next frame captures
+ * again.  Off by default; frames with step timing render normally. */
+int spr_set_graph_replay(spr_handle *h, int32_t enable);
+/* Number of frames of this handle served by graph launches. */
+int spr_graph_replays(spr_handle *h, int32_t *count);
+
 /* Work statistics of the last spr_render. */
 typedef struct spr_frame_stats {
     int32_t kernel_launches; /* CUDA kernels launched by the frame          */
@@ -313,6 +326,8 @@ int spr_batch_read_image(spr_batch *b, int32_t scene, uint8_t *host_rgba, void *
 /* Totals over the scenes of the last render. */
 int spr_batch_get_counts(spr_batch *b, spr_element_number *total);
 int spr_batch_get_frame_stats(spr_batch *b, spr_frame_stats *out);
+/* spr_set_graph_replay for every sample-count group of the batch. */
+int spr_batch_set_graph_replay(spr_batch *b, int32_t enable);
 /* Per-step device time of the last render, summed over the sample-count
  * groups (steps as spr_step_name). */
 int spr_batch_enable_step_timing(spr_batch *b, int32_t enable);
