@@ -108,6 +108,8 @@ struct spr_handle {
     // paths, the per-block tapes, the transformed-vertex gradient and the
     // stored -> input vertex map
     DevBuf chord, lmask, vmask, item_path, tape, tape_rec, grad_tvert, vmap, bitems, chain, ekey[2], eval[2];
+    // raw curve arrays of the device-side scene upload
+    DevBuf sc_vpos, sc_type, sc_pid, sc_w, scene_flags;
     int tape_depth = 128;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
@@ -211,7 +213,9 @@ int64_t frame_pixels(const spr_handle *h) {
     return (int64_t)h->cfg.width * h->cfg.height;
 }
 
-int validate_scene(const spr_scene_view *v) {
+// The view's pointers and sizes (the element checks follow in validate_scene
+// on the host, or in k_scene_vertices / k_scene_curves on the device).
+int validate_view(const spr_scene_view *v) {
     if (!v) return SPR_ERR_INVALID_ARG;
     if ((v->n_vertices && (!v->vertex || !v->vertex_path_id)) ||
         (v->n_curves && (!v->curve_vertex_pos || !v->curve_type || !v->curve_path_id)) ||
@@ -219,6 +223,12 @@ int validate_scene(const spr_scene_view *v) {
         return SPR_ERR_INVALID_ARG;
     if (v->n_vertices > (1u << 30) || v->n_curves > (1u << 30) || v->n_paths > (1u << 30))
         return SPR_ERR_INVALID_SCENE;
+    return SPR_OK;
+}
+
+int validate_scene(const spr_scene_view *v) {
+    int st = validate_view(v);
+    if (st) return st;
     uint32_t last = 0;
     for (uint32_t i = 0; i < v->n_curves; ++i) {
         const int t = v->curve_type[i];
@@ -292,7 +302,7 @@ int spr_destroy(spr_handle *h) {
                       &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
                       &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
                       &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
-                      &h->eval[1]};
+                      &h->eval[1], &h->sc_vpos, &h->sc_type, &h->sc_pid, &h->sc_w, &h->scene_flags};
     for (DevBuf *b : bufs) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
@@ -339,15 +349,15 @@ int spr_enable_srgb_correction(spr_handle *h, int32_t enable) {
     return SPR_OK;
 }
 
-int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
-    if (!h) return SPR_ERR_INVALID_ARG;
-    drop_graph(h);
+}  // extern "C"
+
+namespace {
+
+// Host path of spr_set_scene (validation and orientation on the CPU), for
+// scenes whose curves share or reorder vertex ranges.
+int set_scene_host(spr_handle *h, const spr_scene_view *v) {
     int st = validate_scene(v);
     if (st) return st;
-    cudaSetDevice(h->cfg.device);
-    h->has_scene = false;
-    h->frame_valid = false;
-    h->n_scenes = 0;
     const uint32_t P = v->n_paths, C = v->n_curves, V = v->n_vertices;
     // unifyCurveVertexOrder (ras_base.cpp:523-569): reverse a curve unless
     // (y_first, x_first) < (y_last, x_last) comparing float bit patterns.
@@ -386,6 +396,61 @@ int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     if ((st = upload(h->fill, v->path_fill_rgba, P))) return st;
     h->has_affine = v->path_affine != nullptr;
     if (h->has_affine && (st = upload(h->affine, v->path_affine, 6 * (size_t)P))) return st;
+    h->P = P;
+    h->C = C;
+    h->V = V;
+    h->has_scene = true;
+    return SPR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
+    int st = validate_view(v);
+    if (st) return st;
+    cudaSetDevice(h->cfg.device);
+    h->has_scene = false;
+    h->frame_valid = false;
+    h->n_scenes = 0;
+    const uint32_t P = v->n_paths, C = v->n_curves, V = v->n_vertices;
+    // the caller's arrays straight to the device, then validation and
+    // orientation there (one read-back of the flags)
+    if ((st = ensure(h->vertex, 8 * (size_t)V)) || (st = ensure(h->vpid, 4 * (size_t)V)) ||
+        (st = ensure(h->vmap, 4 * (size_t)V)) || (st = ensure(h->curves, sizeof(CurveDesc) * (size_t)C)) ||
+        (st = ensure(h->sc_vpos, 4 * (size_t)C)) || (st = ensure(h->sc_type, (size_t)C)) ||
+        (st = ensure(h->sc_pid, 4 * (size_t)C)) || (st = ensure(h->sc_w, 4 * (size_t)C)) ||
+        (st = ensure(h->rule, (size_t)P)) || (st = ensure(h->fill, 4 * (size_t)P)) ||
+        (st = ensure(h->scene_flags, 4)) || (v->path_affine && (st = ensure(h->affine, 24 * (size_t)P))))
+        return st;
+    cudaStream_t s = nullptr;
+    auto put = [&](DevBuf &b, const void *src, size_t bytes) {
+        if (bytes) cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s);
+    };
+    put(h->vertex, v->vertex, 8 * (size_t)V);
+    put(h->vpid, v->vertex_path_id, 4 * (size_t)V);
+    put(h->sc_vpos, v->curve_vertex_pos, 4 * (size_t)C);
+    put(h->sc_type, v->curve_type, (size_t)C);
+    put(h->sc_pid, v->curve_path_id, 4 * (size_t)C);
+    if (v->curve_arc_w) put(h->sc_w, v->curve_arc_w, 4 * (size_t)C);
+    put(h->rule, v->path_fill_rule, (size_t)P);
+    put(h->fill, v->path_fill_rgba, 4 * (size_t)P);
+    if (v->path_affine) put(h->affine, v->path_affine, 24 * (size_t)P);
+    cudaMemsetAsync(h->scene_flags.p, 0, 4, s);
+    launch_scene_prepare(h->sc_vpos.as<uint32_t>(), h->sc_type.as<uint8_t>(), h->sc_pid.as<uint32_t>(),
+                         v->curve_arc_w ? h->sc_w.as<float>() : nullptr, C, V, P, h->vertex.as<float2>(),
+                         h->vpid.as<uint32_t>(), h->vmap.as<uint32_t>(), h->curves.as<CurveDesc>(),
+                         h->scene_flags.as<uint32_t>(), s);
+    cudaMemcpyAsync(h->h_u32, h->scene_flags.p, 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+    if ((st = cuda_status())) return st;
+    const uint32_t flags = h->h_u32[0];
+    if (flags & 1u) return SPR_ERR_INVALID_SCENE;
+    if (flags & 2u) return set_scene_host(h, v);
+    h->has_affine = v->path_affine != nullptr;
     h->P = P;
     h->C = C;
     h->V = V;
@@ -836,7 +901,7 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d,
                             &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
                             &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
-                      &h->eval[1]};
+                      &h->eval[1],     &h->sc_vpos,    &h->sc_type,   &h->sc_pid,    &h->sc_w,      &h->scene_flags};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;

@@ -137,6 +137,13 @@ int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_
                    const uint32_t *bin_start, const uint32_t *bin_end, uint32_t *image, uint32_t *overflow,
                    FrameCounters *counters, cudaStream_t s);
 int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s);
+// Scene upload on the device: validation, curve orientation (vertices
+// reversed in place), curve descriptors, the stored -> input vertex map.
+// flags (zeroed by the caller): bit 0 invalid scene, bit 1 overlapping or
+// unordered curve vertex ranges.
+int launch_scene_prepare(const uint32_t *cvp, const uint8_t *ctype, const uint32_t *cpid, const float *arcw,
+                         uint32_t C, uint32_t V, uint32_t P, float2 *vert, const uint32_t *vpid, uint32_t *vmap,
+                         CurveDesc *cd, uint32_t *flags, cudaStream_t s);
 int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cudaStream_t s);
 int launch_decode_keys(const uint64_t *skey, int64_t nf, int nrows, int32_t *out, cudaStream_t s);
 

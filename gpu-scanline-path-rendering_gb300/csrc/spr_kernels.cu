@@ -1133,6 +1133,57 @@ __global__ void k_selftest_encode(const ResolveTables *__restrict__ rt, uint32_t
     if (local) atomicAdd(bad, local);
 }
 
+// ---------------------------------------------------- scene upload --
+// Checks of spr_validate_scene and unifyCurveVertexOrder (ras_base.cpp:523-569)
+// on the device.  flags: bit 0 = invalid scene, bit 1 = vertex ranges of
+// consecutive curves not disjoint and ascending (the in-place reversal would
+// depend on the curve order: the host path handles such scenes).
+__global__ void k_scene_vertices(const uint32_t *__restrict__ vpid, uint32_t V, uint32_t P,
+                                 uint32_t *__restrict__ vmap, uint32_t *__restrict__ flags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    vmap[i] = i;
+    if (vpid[i] >= P) atomicOr(flags, 1u);
+}
+
+__global__ void k_scene_curves(const uint32_t *__restrict__ cvp, const uint8_t *__restrict__ ctype,
+                               const uint32_t *__restrict__ cpid, const float *__restrict__ arcw, uint32_t C,
+                               uint32_t V, uint32_t P, float2 *__restrict__ vert, uint32_t *__restrict__ vmap,
+                               CurveDesc *__restrict__ cd, uint32_t *__restrict__ flags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C) return;
+    const int type = ctype[i];
+    const bool known = type == kLinear || type == kQuad || type == kCubic || type == kRational;
+    const int vn = type & 7;
+    const uint32_t p = cvp[i], pid = cpid[i];
+    bool bad = !known || (type == kRational && arcw == nullptr) || (uint64_t)p + (uint64_t)vn > V || pid >= P ||
+               (i > 0 && pid < cpid[i - 1]);
+    if (bad) {
+        atomicOr(flags, 1u);
+        return;
+    }
+    if (i + 1 < C && (uint64_t)p + (uint64_t)vn > (uint64_t)cvp[i + 1]) atomicOr(flags, 2u);
+    // reverse unless (y_first, x_first) < (y_last, x_last) as float bit patterns
+    const float2 vf = vert[p], vl = vert[p + vn - 1];
+    const uint32_t bxf = __float_as_uint(vf.x), byf = __float_as_uint(vf.y);
+    const uint32_t bxl = __float_as_uint(vl.x), byl = __float_as_uint(vl.y);
+    const uint32_t rev = (byf < byl || (byf == byl && bxf < bxl)) ? 0u : 1u;
+    CurveDesc d;
+    d.vpos = p;
+    d.pid = pid;
+    d.w = type == kRational ? arcw[i] : 0.f;
+    d.type = (uint32_t)type | (rev << 8);
+    cd[i] = d;
+    if (rev) {
+        for (int k = 0; k < vn / 2; ++k) {
+            const float2 t = vert[p + k];
+            vert[p + k] = vert[p + vn - 1 - k];
+            vert[p + vn - 1 - k] = t;
+        }
+        for (int k = 0; k < vn; ++k) vmap[p + k] = p + vn - 1 - k;
+    }
+}
+
 __global__ void k_fill(uint32_t *image, int64_t n, uint32_t v) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) image[i] = v;
@@ -1302,6 +1353,15 @@ int64_t resolve_warps(const FrameArgs &a) { return resolve_blocks(a) * kResolveW
 int64_t resolve_overflow_words(const FrameArgs &a) {
     if (!(a.ms_output && a.S > kCapMS)) return 0;
     return resolve_warps(a) * 64 * 32;
+}
+
+int launch_scene_prepare(const uint32_t *cvp, const uint8_t *ctype, const uint32_t *cpid, const float *arcw,
+                         uint32_t C, uint32_t V, uint32_t P, float2 *vert, const uint32_t *vpid, uint32_t *vmap,
+                         CurveDesc *cd, uint32_t *flags, cudaStream_t s) {
+    int n = 0;
+    if (V > 0) k_scene_vertices<<<grid_for(V), kThreads, 0, s>>>(vpid, V, P, vmap, flags), ++n;
+    if (C > 0) k_scene_curves<<<grid_for(C), kThreads, 0, s>>>(cvp, ctype, cpid, arcw, C, V, P, vert, vmap, cd, flags), ++n;
+    return n;
 }
 
 int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s) {
