@@ -156,16 +156,17 @@ __global__ void k_curve_count(FrameArgs a, const float2 *__restrict__ tv, const 
 // Entries of one curve in t order: each monotone piece emits its start and
 // every crossing with a vertical (x = even) or horizontal (y = even) cell
 // line, the two crossing chains merged by t; equal t values OR their flags.
-// Emission order: curves by decreasing estimated cost (entries, a cubic's
-// bisection weighted 8x), so that a warp's curves take similar time and the
-// longest start first.  key = 0xFFFF - cost (ascending sort).
+// Emission order: curves grouped by type (cubics, whose crossings are
+// bisections, first) and within a type by decreasing entry count, so that
+// the curves of a warp run the same solver the same number of times and
+// the longest start first.  16-bit key, ascending.
 __global__ void k_emit_keys(FrameArgs a, const uint32_t *__restrict__ counts, uint32_t *__restrict__ key,
                             uint32_t *__restrict__ val) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.C) return;
     const uint32_t type = a.curves[c].type & 0xFFu;
-    const uint32_t cost = counts[c] * (type == (uint32_t)kCubic ? 8u : 1u);
-    key[c] = 0xFFFFu - min(cost, 0xFFFFu);
+    const uint32_t rank = type == (uint32_t)kCubic ? 0u : (type == (uint32_t)kRational ? 1u : (type == (uint32_t)kQuad ? 2u : 3u));
+    key[c] = (rank << 13) | (0x1FFFu - min(counts[c], 0x1FFFu));
     val[c] = (uint32_t)c;
 }
 
