@@ -108,8 +108,9 @@ struct spr_handle {
     // paths, the per-block tapes, the transformed-vertex gradient and the
     // stored -> input vertex map
     DevBuf chord, lmask, vmask, item_path, tape, tape_rec, grad_tvert, vmap, bitems, chain, ekey[2], eval[2];
-    // raw curve arrays of the device-side scene upload
+    // raw curve arrays of the device-side scene upload (kept for vertex updates)
     DevBuf sc_vpos, sc_type, sc_pid, sc_w, scene_flags;
+    bool scene_on_device = false, scene_has_arcw = false;
     int tape_depth = 128;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
@@ -449,7 +450,10 @@ int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     if ((st = cuda_status())) return st;
     const uint32_t flags = h->h_u32[0];
     if (flags & 1u) return SPR_ERR_INVALID_SCENE;
+    h->scene_on_device = false;
     if (flags & 2u) return set_scene_host(h, v);
+    h->scene_on_device = true;
+    h->scene_has_arcw = v->curve_arc_w != nullptr;
     h->has_affine = v->path_affine != nullptr;
     h->P = P;
     h->C = C;
@@ -816,6 +820,24 @@ int spr_graph_replays(spr_handle *h, int32_t *out) {
     if (!h || !out) return SPR_ERR_INVALID_ARG;
     *out = h->graph_replays;
     return SPR_OK;
+}
+
+int spr_update_vertices(spr_handle *h, const float *vertex, void *stream) {
+    if (!h || !vertex) return SPR_ERR_INVALID_ARG;
+    if (!h->has_scene) return SPR_ERR_NO_SCENE;
+    if (!h->scene_on_device) return SPR_ERR_UNSUPPORTED;
+    cudaSetDevice(h->cfg.device);
+    drop_graph(h);
+    h->frame_valid = false;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (h->V && cudaMemcpyAsync(h->vertex.p, vertex, 8 * (size_t)h->V, cudaMemcpyDefault, s) != cudaSuccess)
+        return cuda_status();
+    cudaMemsetAsync(h->scene_flags.p, 0, 4, s);
+    launch_scene_prepare(h->sc_vpos.as<uint32_t>(), h->sc_type.as<uint8_t>(), h->sc_pid.as<uint32_t>(),
+                         h->scene_has_arcw ? h->sc_w.as<float>() : nullptr, h->C, h->V, h->P, h->vertex.as<float2>(),
+                         h->vpid.as<uint32_t>(), h->vmap.as<uint32_t>(), h->curves.as<CurveDesc>(),
+                         h->scene_flags.as<uint32_t>(), s);
+    return cuda_status();
 }
 
 int spr_diff_render(spr_handle *h, const float *fill_rgba, float *image, void *stream) {
@@ -1185,6 +1207,51 @@ int spr_batch_get_counts(spr_batch *b, spr_element_number *total) {
     }
     *total = t;
     return SPR_OK;
+}
+
+namespace {
+// The one group handle of a batch whose scenes share a sample count (its
+// concatenation order is the scene order), else null.
+spr_handle *single_group(spr_batch *b) {
+    spr_handle *one = nullptr;
+    for (spr_handle *h : b->group) {
+        if (!h) continue;
+        if (one) return nullptr;
+        one = h;
+    }
+    return one;
+}
+}  // namespace
+
+int spr_batch_diff_render(spr_batch *b, const float *fill_rgba, float *image, void *stream) {
+    if (!b || !fill_rgba || !image) return SPR_ERR_INVALID_ARG;
+    if (b->entries.empty()) return SPR_ERR_NO_SCENE;
+    spr_handle *h = single_group(b);
+    if (!h) return SPR_ERR_UNSUPPORTED;
+    b->rendered = false;
+    const DiffCall dc{false, fill_rgba, nullptr, image, nullptr, nullptr, nullptr};
+    return render_frame(h, stream, &dc);
+}
+
+int spr_batch_diff_backward(spr_batch *b, const float *fill_rgba, const float *grad_image, float *grad_fill,
+                            float *grad_vertex, float *grad_affine, void *stream) {
+    if (!b || !fill_rgba || !grad_image || !grad_fill || !grad_vertex) return SPR_ERR_INVALID_ARG;
+    if (b->entries.empty()) return SPR_ERR_NO_SCENE;
+    spr_handle *h = single_group(b);
+    if (!h) return SPR_ERR_UNSUPPORTED;
+    if (grad_affine && !h->has_affine) return SPR_ERR_INVALID_ARG;
+    b->rendered = false;
+    const DiffCall dc{true, fill_rgba, grad_image, nullptr, grad_fill, grad_vertex, grad_affine};
+    return render_frame(h, stream, &dc);
+}
+
+int spr_batch_update_vertices(spr_batch *b, const float *vertex, void *stream) {
+    if (!b || !vertex) return SPR_ERR_INVALID_ARG;
+    if (b->entries.empty()) return SPR_ERR_NO_SCENE;
+    spr_handle *h = single_group(b);
+    if (!h) return SPR_ERR_UNSUPPORTED;
+    b->rendered = false;
+    return spr_update_vertices(h, vertex, stream);
 }
 
 int spr_batch_set_graph_replay(spr_batch *b, int32_t enable) {

@@ -319,6 +319,31 @@ __device__ __forceinline__ void add_fill_grad(const DiffArgs &d, float4 *acc, ui
     }
 }
 
+// The scene of resolve bin b: viewport, the bin index within the scene and
+// the scene's first pixel (batch frames; a single scene otherwise).
+struct BinScene {
+    int W, H;
+    uint32_t lb;
+    int64_t image_off;
+};
+__device__ __forceinline__ BinScene bin_scene(const FrameArgs &a, uint32_t b) {
+    BinScene r{a.W, a.H, b, 0};
+    if (a.scenes != nullptr) {
+        int lo = 0, hi = a.n_scenes - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.scenes[mid].bin_off <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        const SceneInfo *sc = a.scenes + lo;
+        r.W = sc->W;
+        r.H = sc->H;
+        r.lb = b - sc->bin_off;
+        r.image_off = sc->image_off;
+    }
+    return r;
+}
+
 // The items of the resolve pairs in bin order, one contiguous record each.
 __global__ void k_diff_gather(DiffArgs d, int words) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -353,7 +378,6 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs 
     const int lane = threadIdx.x & 31;
     const int k4 = lane >> 3, sub = lane & 7;
     const int px_in = k4 >> 1, py_in = k4 & 1;
-    const int ntx = (a.W + kTileW - 1) / kTileW;
     const size_t wslot = (size_t)blockIdx.x * (kDiffThreads / 32) + (threadIdx.x >> 5);
     float4 *acc = (BWD && path_acc) ? s_acc : nullptr;
     if (acc)
@@ -367,11 +391,14 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs 
         if ((int64_t)u >= n_units) break;
         const uint32_t b = u / (kTileW / 2);
         const int cw = (int)(u % (kTileW / 2));
-        const int tile = (int)(b % ntx), crow = (int)(b / ntx);
+        const BinScene bs = bin_scene(a, b);
+        const int ntx = (bs.W + kTileW - 1) / kTileW;
+        const int tile = (int)(bs.lb % ntx), crow = (int)(bs.lb / ntx);
         const int cellx = tile * kTileW + 2 * cw;
-        if (cellx >= a.W) continue;
+        if (cellx >= bs.W) continue;
         const int X = cellx + px_in, Y = crow * 2 + py_in;
-        const bool valid = X < a.W && Y < a.H;
+        const bool valid = X < bs.W && Y < bs.H;
+        const int64_t pix = bs.image_off + (int64_t)Y * bs.W + X;
         const uint32_t beg = d.bstart[b], fin = d.bend[b];
         float4 c[SPT];
 #pragma unroll
@@ -509,14 +536,14 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs 
             }
             if (valid && sub == 0) {
                 const float inv = 1.f / (float)S;
-                d.image[(int64_t)Y * a.W + X] = make_float4(sum.x * inv, sum.y * inv, sum.z * inv, sum.w * inv);
+                d.image[pix] = make_float4(sum.x * inv, sum.y * inv, sum.z * inv, sum.w * inv);
             }
             continue;
         }
         // ---- reverse sweep (warp-uniform)
         if (ne > d.tape_depth || nsl > d.tape_depth) continue;
         const float inv = 1.f / (float)S;
-        const float4 G = valid ? d.grad_image[(int64_t)Y * a.W + X] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 G = valid ? d.grad_image[pix] : make_float4(0.f, 0.f, 0.f, 0.f);
         float4 lam[SPT];
 #pragma unroll
         for (int k = 0; k < SPT; ++k) lam[k] = make_float4(G.x * inv, G.y * inv, G.z * inv, G.w * inv);
@@ -657,12 +684,24 @@ __global__ void k_diff_vertex(FrameArgs a, const float2 *__restrict__ gt, const 
         xa = A[0] * p.x + A[2] * p.y + A[4];
         ya = A[1] * p.x + A[3] * p.y + A[5];
     }
+    float m[16];
+    int Wv = a.W, Hv = a.H;
+    if (a.path_scene != nullptr) {
+        const SceneInfo *sc = a.scenes + a.path_scene[pid];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) m[k] = sc->m[k];
+        Wv = sc->W;
+        Hv = sc->H;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) m[k] = a.m[k];
+    }
     float ov[4], dox[4], doy[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        ov[r] = a.m[4 * r] * xa + a.m[4 * r + 1] * ya + a.m[4 * r + 3];
-        dox[r] = a.m[4 * r];
-        doy[r] = a.m[4 * r + 1];
+        ov[r] = m[4 * r] * xa + m[4 * r + 1] * ya + m[4 * r + 3];
+        dox[r] = m[4 * r];
+        doy[r] = m[4 * r + 1];
     }
     float q[3], qx[3], qy[3];
     const float i3 = 1.f / ov[3];
@@ -672,7 +711,7 @@ __global__ void k_diff_vertex(FrameArgs a, const float2 *__restrict__ gt, const 
         qx[r] = (dox[r] - q[r] * dox[3]) * i3;
         qy[r] = (doy[r] - q[r] * doy[3]) * i3;
     }
-    const float w = (float)a.W, h = (float)a.H, z = (float)min(a.W, a.H);
+    const float w = (float)Wv, h = (float)Hv, z = (float)min(Wv, Hv);
     const float cutoff = -z * 0.5f;
     if (q[2] < cutoff) {
         q[2] = cutoff;

@@ -141,6 +141,10 @@ def lib() -> C.CDLL:
         L.spr_set_graph_replay.argtypes = [vp, i32]
         L.spr_graph_replays.argtypes = [vp, C.POINTER(i32)]
         L.spr_batch_set_graph_replay.argtypes = [vp, i32]
+        L.spr_update_vertices.argtypes = [vp, vp, vp]
+        L.spr_batch_diff_render.argtypes = [vp, vp, vp, vp]
+        L.spr_batch_diff_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.spr_batch_update_vertices.argtypes = [vp, vp, vp]
         L.spr_diff_render.argtypes = [vp, vp, vp, vp]
         L.spr_diff_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.spr_batch_create.argtypes = [i32, i32, i32, C.POINTER(vp)]
@@ -351,6 +355,10 @@ class VGRasterizer:
         check(lib().spr_graph_replays(self._h, C.byref(n)), "spr_graph_replays")
         return int(n.value)
 
+    def update_vertices(self, vertex_ptr: int, stream=None):
+        """New vertex positions (pointer to float32[V, 2], host or device)."""
+        check(lib().spr_update_vertices(self._h, vertex_ptr, stream), "spr_update_vertices")
+
     def diff_render(self, fill_ptr: int, image_ptr: int, stream=None):
         """Float composite with per-path linear RGBA fills (device pointers:
         fill float32[P, 4], image float32[H, W, 4])."""
@@ -455,6 +463,23 @@ class Batch:
 
     def set_graph_replay(self, f=True):
         check(lib().spr_batch_set_graph_replay(self._h, int(f)), "spr_batch_set_graph_replay")
+
+    def image_offsets(self):
+        """First pixel of every scene's image in the concatenated image of a
+        single-sample-count batch (scene order)."""
+        import numpy as _np
+        return _np.concatenate([[0], _np.cumsum([w * h for w, h in self._sizes])]).astype(_np.int64)
+
+    def diff_render(self, fill_ptr: int, image_ptr: int, stream=None):
+        check(lib().spr_batch_diff_render(self._h, fill_ptr, image_ptr, stream), "spr_batch_diff_render")
+
+    def diff_backward(self, fill_ptr: int, grad_image_ptr: int, grad_fill_ptr: int, grad_vertex_ptr: int,
+                      grad_affine_ptr=None, stream=None):
+        check(lib().spr_batch_diff_backward(self._h, fill_ptr, grad_image_ptr, grad_fill_ptr, grad_vertex_ptr,
+                                            grad_affine_ptr, stream), "spr_batch_diff_backward")
+
+    def update_vertices(self, vertex_ptr: int, stream=None):
+        check(lib().spr_batch_update_vertices(self._h, vertex_ptr, stream), "spr_batch_update_vertices")
 
     def enable_step_timing(self, f=True):
         check(lib().spr_batch_enable_step_timing(self._h, int(f)), "spr_batch_enable_step_timing")

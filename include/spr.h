@@ -276,8 +276,7 @@ const char *spr_status_string(int32_t status);
  * c'.a = a * a + c.a * (1 - a), with the path colours f taken from
  * fill_rgba (4 floats per path) instead of path_fill_rgba, and a pixel is
  * the mean of its samples.  All pointers are device pointers.  The handle's
- * RGBA8 image is not written.  Single-scene handles only
- * (SPR_ERR_UNSUPPORTED on batches).
+ * RGBA8 image is not written (batches: spr_batch_diff_render).
  */
 int spr_diff_render(spr_handle *h, const float *fill_rgba, float *image, void *stream);
 /* Gradients of a loss L given grad_image = dL/d(image) (4 floats per pixel):
@@ -294,6 +293,12 @@ int spr_diff_render(spr_handle *h, const float *fill_rgba, float *image, void *s
  * grows by itself (one extra readback per doubling). */
 int spr_diff_backward(spr_handle *h, const float *fill_rgba, const float *grad_image, float *grad_fill,
                       float *grad_vertex, float *grad_affine, void *stream);
+/* New positions of the scene's vertices (2 floats per vertex, in the scene's
+ * order; host or device memory), keeping everything else of the last
+ * spr_set_scene: the curves are oriented again on the device, with no host
+ * synchronization (an extension, for fitting loops).  SPR_ERR_UNSUPPORTED
+ * for scenes whose curves share vertices (those are oriented on the host). */
+int spr_update_vertices(spr_handle *h, const float *vertex, void *stream);
 
 /* ---- batches (an extension: no counterpart in the reference) ------------
  * Many independent scenes of uneven size rendered together: the scenes are
@@ -328,6 +333,15 @@ int spr_batch_get_counts(spr_batch *b, spr_element_number *total);
 int spr_batch_get_frame_stats(spr_batch *b, spr_frame_stats *out);
 /* spr_set_graph_replay for every sample-count group of the batch. */
 int spr_batch_set_graph_replay(spr_batch *b, int32_t enable);
+/* Differentiable rendering of a batch whose scenes share one sample count
+ * (else SPR_ERR_UNSUPPORTED): as spr_diff_render / spr_diff_backward /
+ * spr_update_vertices, with fills, gradients and vertices of all scenes
+ * concatenated in scene order and the images concatenated likewise (scene
+ * i's image starts at the sum of the earlier scenes' width x height). */
+int spr_batch_diff_render(spr_batch *b, const float *fill_rgba, float *image, void *stream);
+int spr_batch_diff_backward(spr_batch *b, const float *fill_rgba, const float *grad_image, float *grad_fill,
+                            float *grad_vertex, float *grad_affine, void *stream);
+int spr_batch_update_vertices(spr_batch *b, const float *vertex, void *stream);
 /* Per-step device time of the last render, summed over the sample-count
  * groups (steps as spr_step_name). */
 int spr_batch_enable_step_timing(spr_batch *b, int32_t enable);
