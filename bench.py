@@ -384,6 +384,90 @@ def run_diff(dev, stream, steps=5):
             "device_bytes": dev_bytes}
 
 
+BDIFF = dict(n_scenes=64, seed=20261204, sizes=(512, 640, 768, 896, 1024), paths=(128, 512), seg_min=16,
+             seg_max=64, samples=16, steps=100, lr_fill=0.5, lr_point=4.0)
+
+
+def run_batched_diff(dev, stream, steps=None):
+    """Batched forward + backward: 64 scenes of uneven size fitted by plain
+    gradient descent on contour points and fill colours (L2 loss against
+    targets rendered with points + N(0, 2 px) and colours + N(0, 0.05)); each
+    step moves the vertices on the device (spr_batch_update_vertices),
+    renders, takes the loss gradient and runs the backward, which recomputes
+    every stage."""
+    import numpy as np
+    import torch
+
+    import spr
+
+    steps = steps or BDIFF["steps"]
+    rng = np.random.default_rng(BDIFF["seed"])
+    items, fills, tgt_v, tgt_f, keys = [], [], [], [], []
+    for i in range(BDIFF["n_scenes"]):
+        d = int(rng.choice(BDIFF["sizes"]))
+        n = int(rng.integers(BDIFF["paths"][0], BDIFF["paths"][1] + 1))
+        sc = spr.Scene.generate(spr.SCENE_CUBICS, seed=BDIFF["seed"] + 1 + i, width=d, height=d, n_paths=n,
+                                seg_min=BDIFF["seg_min"], seg_max=BDIFF["seg_max"])
+        items.append((sc, d, d, BDIFF["samples"]))
+        f = np.c_[rng.uniform(0, 1, (n, 3)), rng.uniform(0.5, 1, (n, 1))].astype(np.float32)
+        fills.append(f)
+        tgt_v.append(sc.vertex + rng.normal(0, 2.0, sc.vertex.shape).astype(np.float32))
+        tgt_f.append(np.clip(f + rng.normal(0, 0.05, f.shape), 0, 1).astype(np.float32))
+    # contour points: the coincident end points of consecutive curves are one parameter
+    vert = np.concatenate([it[0].vertex for it in items])
+    pid = np.concatenate([it[0].vertex_path_id + sum(x[0].n_paths for x in items[:k]) for k, it in enumerate(items)])
+    key = np.c_[pid.astype(np.float64), vert.astype(np.float64)]
+    uniq, inv = np.unique(key, axis=0, return_inverse=True)
+    idx = torch.tensor(inv.reshape(-1), device=dev)
+    sp = stream.cuda_stream
+    pts = torch.tensor(uniq[:, 1:].astype(np.float32), device=dev)
+    fill = torch.tensor(np.concatenate(fills), device=dev)
+    V, P = vert.shape[0], fill.shape[0]
+    gf = torch.empty((P, 4), device=dev)
+    gv = torch.empty((V, 2), device=dev)
+    torch.cuda.reset_peak_memory_stats(dev)
+    with spr.Batch(device=dev.index) as b:
+        b.set_scenes(items)
+        npix = int(b.image_offsets()[-1])
+        img = torch.empty((npix, 4), device=dev)
+        target = torch.empty((npix, 4), device=dev)
+        b.update_vertices(torch.tensor(np.concatenate(tgt_v), device=dev).data_ptr(), sp)
+        b.diff_render(torch.tensor(np.concatenate(tgt_f), device=dev).data_ptr(), target.data_ptr(), sp)
+        losses = []
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        fwd_ms, tot_ms = [], []
+        for k in range(steps):
+            ev[0].record(stream)
+            v = pts[idx].contiguous()
+            b.update_vertices(v.data_ptr(), sp)
+            b.diff_render(fill.data_ptr(), img.data_ptr(), sp)
+            ev[1].record(stream)
+            diff = img - target
+            g = (2.0 * diff).contiguous()
+            b.diff_backward(fill.data_ptr(), g.data_ptr(), gf.data_ptr(), gv.data_ptr(), None, sp)
+            with torch.no_grad():
+                gpt = torch.zeros_like(pts).index_add_(0, idx, gv)
+                fill -= BDIFF["lr_fill"] * gf / npix * 1e3
+                fill.clamp_(0.0, 1.0)
+                pts -= BDIFF["lr_point"] * gpt / (gpt.abs().max() + 1e-12)
+            ev[2].record(stream)
+            ev[2].synchronize()
+            fwd_ms.append(ev[0].elapsed_time(ev[1]))
+            tot_ms.append(ev[0].elapsed_time(ev[2]))
+            if k in (0, steps - 1):
+                losses.append(float((diff * diff).sum()))
+        dev_bytes = b.frame_stats()["device_bytes"]
+    peak = torch.cuda.max_memory_allocated(dev) + dev_bytes
+    n = len(items)
+    f_ms, t_ms = sum(fwd_ms[1:]) / (len(fwd_ms) - 1), sum(tot_ms[1:]) / (len(tot_ms) - 1)
+    return {"workload": f"{n} scenes of 128-512 closed cubic paths (16-64 segments), 512^2-1024^2, 16 spp; "
+                        f"{steps} descent steps on contour points and fills (L2 to perturbed targets)",
+            "pixels": npix, "paths": P, "vertices": V, "steps": steps,
+            "fwd_ms_per_scene": f_ms / n, "fwd_bwd_ms_per_scene": t_ms / n, "step_ms": t_ms,
+            "fwd_bwd_over_fwd": t_ms / f_ms, "loss_first": losses[0], "loss_last": losses[-1],
+            "peak_hbm_bytes": int(peak), "graph": "no: sizes change as the geometry moves (read back per step)"}
+
+
 # ------------------------------------------------------------- GPU arm --
 def run_ours(args, rank, world, local_rank):
     import numpy as np
@@ -512,6 +596,7 @@ def run_ours(args, rank, world, local_rank):
         del flush
         line["batched"] = run_batched(dev, stream)
         line["differentiable"] = run_diff(dev, stream)
+        line["batched_differentiable"] = run_batched_diff(dev, stream)
     print(json.dumps(line), flush=True)
 
 
@@ -547,7 +632,7 @@ def main():
                     help="skip the batched-scenes and differentiable-render measurements")
     ap.add_argument("--profile", action="store_true",
                     help="timed GPU frames only (no end-to-end or CPU legs), for profiler runs")
-    ap.add_argument("--part", choices=["all", "batched", "diff"], default="all",
+    ap.add_argument("--part", choices=["all", "batched", "diff", "batched_diff"], default="all",
                     help="run only the batched or the differentiable measurement (one JSON object), "
                          "for profiler runs")
     args = ap.parse_args()
@@ -564,8 +649,8 @@ def main():
         dev = torch.device("cuda", local_rank)
         torch.cuda.set_device(dev)
         stream = torch.cuda.current_stream(dev)
-        fn = run_batched if args.part == "batched" else run_diff
-        print(json.dumps({args.part: fn(dev, stream, steps=max(1, args.steps))}), flush=True)
+        fn = {"batched": run_batched, "diff": run_diff, "batched_diff": run_batched_diff}[args.part]
+        print(json.dumps({args.part: fn(dev, stream, steps=max(2, args.steps))}), flush=True)
         return
     if world > 1:
         import torch

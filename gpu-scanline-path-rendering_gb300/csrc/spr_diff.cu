@@ -37,6 +37,7 @@ namespace {
 
 constexpr int kDiffThreads = 256;    // 8 warps, each working on its own cells
 constexpr int kDiffPathAcc = 4096;   // paths with shared-memory fill-gradient accumulators (backward)
+constexpr int kDiffCacheSlots = 256; // else: slots of each warp's path-gradient cache
 constexpr int kTileW = 32;
 
 __device__ __forceinline__ uint32_t pixel_mask(const uint4 &mm, int S, int k) {
@@ -138,7 +139,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 // One fragment of a merged group, held by one lane of the cell's warp.
 template <int S>
 struct GroupFrag {
-    float4 q;          // chord in cell units
+    float4 q;          // chord in cell units: x0, y0, slope dx/dy (0 when horizontal), y1
     uint32_t vm[S / 8];  // rows between the chord's end points
     uint32_t lm[S / 8];  // left mask
     int chg;           // winding change (0: no contribution)
@@ -150,7 +151,8 @@ __device__ __forceinline__ void load_group_frag(const DiffArgs &d, int64_t j, Gr
     constexpr int WORDS = S / 8;
     f.raw = d.perm[j];
     f.chg = (int32_t)d.pidw[f.raw] >> 30;
-    f.q = d.chord[f.raw];
+    const float4 c = d.chord[f.raw];
+    f.q = make_float4(c.x, c.y, c.w != c.y ? (c.z - c.x) / (c.w - c.y) : 0.f, c.w);
 #pragma unroll
     for (int w = 0; w < WORDS; ++w) {
         f.vm[w] = d.vmask[(size_t)f.raw * WORDS + w];
@@ -210,10 +212,19 @@ template <int S>
 __device__ void group_adjoint(const FrameArgs &a, const DiffArgs &d, int64_t h, int rule, const float *J, int lane) {
     constexpr int SPT = S / 8;
     const int k4 = lane >> 3, sub = lane & 7, px = k4 >> 1, py = k4 & 1;
-    const uint64_t kh = d.skey[h];
     const int w0 = (int)d.wn_scan[h];
-    int gs = 0;  // group size
-    while (h + gs < d.nf && d.skey[h + gs] == kh) ++gs;
+    // group size: the run of equal keys from h, 32 keys per step
+    const uint64_t kh = d.skey[h];
+    int gs = 0;
+    for (;;) {
+        const int64_t j = h + gs + lane;
+        const uint32_t ends = __ballot_sync(0xffffffffu, j >= d.nf || d.skey[j] != kh);
+        if (ends) {
+            gs += __ffs(ends) - 1;
+            break;
+        }
+        gs += 32;
+    }
     for (int base = 0; base < gs; base += 32) {
         const int nw = min(32, gs - base);
         GroupFrag<S> mine;
@@ -222,7 +233,7 @@ __device__ void group_adjoint(const FrameArgs &a, const DiffArgs &d, int64_t h, 
         for (int j = 0; j < nw; ++j) {
             const GroupFrag<S> f = shfl_frag<S>(mine, j);
             if (f.chg == 0 || f.q.y == f.q.w) continue;  // uniform
-            const float slope = (f.q.z - f.q.x) / (f.q.w - f.q.y);
+            const float slope = f.q.z;
             bool cand[SPT];
             float xc[SPT], yr[SPT];
             int W[SPT];
@@ -247,7 +258,7 @@ __device__ void group_adjoint(const FrameArgs &a, const DiffArgs &d, int64_t h, 
                     const int r = py * S + sub + 8 * k;
                     uint32_t bit = 0u;
                     if (j2 != j && row_bit<S>(f2.vm, px, r)) {
-                        const float x2 = f2.q.x + (yr[k] - f2.q.y) * ((f2.q.z - f2.q.x) / (f2.q.w - f2.q.y));
+                        const float x2 = f2.q.x + (yr[k] - f2.q.y) * f2.q.z;
                         bit = xc[k] > x2 ? 1u : 0u;
                     }
                     bit ^= row_bit<S>(f2.lm, px, r);
@@ -266,7 +277,7 @@ __device__ void group_adjoint(const FrameArgs &a, const DiffArgs &d, int64_t h, 
                         const int r = py * S + sub + 8 * k;
                         uint32_t bit = 0u;
                         if (row_bit<S>(f2.vm, px, r)) {
-                            const float x2 = f2.q.x + (yr[k] - f2.q.y) * ((f2.q.z - f2.q.x) / (f2.q.w - f2.q.y));
+                            const float x2 = f2.q.x + (yr[k] - f2.q.y) * f2.q.z;
                             bit = xc[k] > x2 ? 1u : 0u;
                         }
                         bit ^= row_bit<S>(f2.lm, px, r);
@@ -305,17 +316,41 @@ __device__ __forceinline__ uint4 load_merged(const uint32_t *merged, int words, 
     return make_uint4(merged[g], 0u, 0u, 0u);
 }
 
-__device__ __forceinline__ void add_fill_grad(const DiffArgs &d, float4 *acc, uint32_t path, float4 g) {
-    if (acc != nullptr) {
+__device__ __forceinline__ void global_fill_grad(const DiffArgs &d, uint32_t path, float4 g) {
+    atomicAdd(&d.grad_fill[path].x, g.x);
+    atomicAdd(&d.grad_fill[path].y, g.y);
+    atomicAdd(&d.grad_fill[path].z, g.z);
+    atomicAdd(&d.grad_fill[path].w, g.w);
+}
+
+// A fill gradient (lane 0 of the warp): into the block's per-path
+// accumulators (acc) when every path has one; else into the warp's
+// direct-mapped cache (slot = path mod kDiffCacheSlots, tag = path), whose
+// evicted entries go to the global gradient.  Neighbouring cells share most
+// of their paths, so the cache turns most global atomics into register adds.
+__device__ __forceinline__ void add_fill_grad(const DiffArgs &d, float4 *acc, float4 *cache, uint32_t *tag,
+                                              uint32_t path, float4 g) {
+    if (cache != nullptr) {
+        const uint32_t slot = path & (kDiffCacheSlots - 1);
+        const uint32_t t = tag[slot];
+        if (t == path) {
+            float4 &v = cache[slot];
+            v.x += g.x;
+            v.y += g.y;
+            v.z += g.z;
+            v.w += g.w;
+        } else {
+            if (t != 0xFFFFFFFFu) global_fill_grad(d, t, cache[slot]);
+            cache[slot] = g;
+            tag[slot] = path;
+        }
+    } else if (acc != nullptr) {
         atomicAdd(&acc[path].x, g.x);
         atomicAdd(&acc[path].y, g.y);
         atomicAdd(&acc[path].z, g.z);
         atomicAdd(&acc[path].w, g.w);
     } else {
-        atomicAdd(&d.grad_fill[path].x, g.x);
-        atomicAdd(&d.grad_fill[path].y, g.y);
-        atomicAdd(&d.grad_fill[path].z, g.z);
-        atomicAdd(&d.grad_fill[path].w, g.w);
+        global_fill_grad(d, path, g);
     }
 }
 
@@ -370,18 +405,26 @@ __global__ void k_diff_chain(FrameArgs a, DiffArgs d) {
 // walk over the bin's items is warp-uniform; the items are read 32 at a time
 // (one per lane), the touching ones found by a ballot and broadcast.  Warps
 // never wait for one another.
-template <int S, bool BWD>
-__global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs d, int path_acc) {
+template <int S, bool BWD, bool CACHE>
+__global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs d) {
     constexpr int SPT = S / 8;
     constexpr int WORDS = S / 8;
-    extern __shared__ float4 s_acc[];  // fill gradients per path (backward, when path_acc)
+    extern __shared__ float4 s_acc[];  // fill-gradient accumulators (backward)
     const int lane = threadIdx.x & 31;
     const int k4 = lane >> 3, sub = lane & 7;
     const int px_in = k4 >> 1, py_in = k4 & 1;
     const size_t wslot = (size_t)blockIdx.x * (kDiffThreads / 32) + (threadIdx.x >> 5);
-    float4 *acc = (BWD && path_acc) ? s_acc : nullptr;
+    // fill-gradient accumulators: per path for the block (few paths), else
+    // (CACHE) a path cache per warp: values, then tags
+    float4 *acc = (BWD && !CACHE) ? s_acc : nullptr;
+    float4 *cache = (BWD && CACHE) ? s_acc + (threadIdx.x >> 5) * kDiffCacheSlots : nullptr;
+    uint32_t *tag = (BWD && CACHE) ? reinterpret_cast<uint32_t *>(s_acc + (kDiffThreads / 32) * kDiffCacheSlots) +
+                                         (threadIdx.x >> 5) * kDiffCacheSlots
+                                   : nullptr;
     if (acc)
         for (int i = threadIdx.x; i < a.P; i += kDiffThreads) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tag)
+        for (int i = lane; i < kDiffCacheSlots; i += 32) tag[i] = 0xFFFFFFFFu;
     if (BWD) __syncthreads();
     const int64_t n_units = a.n_bins * (kTileW / 2);
     for (;;) {
@@ -614,7 +657,7 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs 
                     pi * av * Lsum.x, pi * av * Lsum.y, pi * av * Lsum.z,
                     pi * (Lsum.x * f.x - cx + Lsum.y * f.y - cy + Lsum.z * f.z - cz + 2.f * av * Lsum.w - cw));
                 if (lane == 0 && (gf.x != 0.f || gf.y != 0.f || gf.z != 0.f || gf.w != 0.f))
-                    add_fill_grad(d, acc, path, gf);
+                    add_fill_grad(d, acc, cache, tag, path, gf);
                 pi *= om;
                 continue;
             }
@@ -649,8 +692,13 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs 
             gf.z = warp_sum(gf.z);
             gf.w = warp_sum(gf.w);
             if (lane == 0 && (gf.x != 0.f || gf.y != 0.f || gf.z != 0.f || gf.w != 0.f))
-                add_fill_grad(d, acc, path, gf);
+                add_fill_grad(d, acc, cache, tag, path, gf);
         }
+    }
+    if (tag) {  // the warp's cached gradients
+        __syncwarp();
+        for (int i = lane; i < kDiffCacheSlots; i += 32)
+            if (tag[i] != 0xFFFFFFFFu) global_fill_grad(d, tag[i], cache[i]);
     }
     if (acc) {
         __syncthreads();
@@ -745,6 +793,14 @@ int diff_sm_count() {
     return n;
 }
 
+template <int S, bool BWD, bool CACHE>
+void run_diff(const FrameArgs &a, const DiffArgs &d, unsigned grid, size_t smem, cudaStream_t s) {
+    if constexpr (BWD || !CACHE) {  // the forward pass accumulates nothing
+        cudaFuncSetAttribute(k_diff<S, BWD, CACHE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_diff<S, BWD, CACHE><<<grid, kDiffThreads, smem, s>>>(a, d);
+    }
+}
+
 template <bool BWD>
 int launch_diff(const FrameArgs &a, const DiffArgs &d, cudaStream_t s) {
     if (a.n_bins <= 0) return 0;
@@ -755,17 +811,18 @@ int launch_diff(const FrameArgs &a, const DiffArgs &d, cudaStream_t s) {
         k_diff_gather<<<(unsigned)((d.npairs + 255) / 256), 256, 0, s>>>(d, a.S / 8);
         ++n;
     }
-    const int path_acc = (BWD && a.P <= kDiffPathAcc) ? 1 : 0;
-    const size_t smem = path_acc ? sizeof(float4) * (size_t)std::max(a.P, 1) : 0;
+    // backward: block-wide per-path accumulators up to kDiffPathAcc paths,
+    // per-warp path caches beyond
+    const bool cache = BWD && a.P > kDiffPathAcc;
+    const size_t smem = !BWD  ? 0
+                        : cache ? (sizeof(float4) + sizeof(uint32_t)) * kDiffCacheSlots * (kDiffThreads / 32)
+                                : sizeof(float4) * (size_t)std::max(a.P, 1);
     if (a.S == 8) {
-        cudaFuncSetAttribute(k_diff<8, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_diff<8, BWD><<<grid, kDiffThreads, smem, s>>>(a, d, path_acc);
+        cache ? run_diff<8, BWD, true>(a, d, grid, smem, s) : run_diff<8, BWD, false>(a, d, grid, smem, s);
     } else if (a.S == 16) {
-        cudaFuncSetAttribute(k_diff<16, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_diff<16, BWD><<<grid, kDiffThreads, smem, s>>>(a, d, path_acc);
+        cache ? run_diff<16, BWD, true>(a, d, grid, smem, s) : run_diff<16, BWD, false>(a, d, grid, smem, s);
     } else {
-        cudaFuncSetAttribute(k_diff<32, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_diff<32, BWD><<<grid, kDiffThreads, smem, s>>>(a, d, path_acc);
+        cache ? run_diff<32, BWD, true>(a, d, grid, smem, s) : run_diff<32, BWD, false>(a, d, grid, smem, s);
     }
     if (BWD && d.nf > 0) {
         k_diff_chain<<<(unsigned)((d.nf + 255) / 256), 256, 0, s>>>(a, d);

@@ -112,6 +112,22 @@ def test_transform_and_deep_overlap():
     assert rel(gf, ref["fill"]) < REL_TOL and rel(gv, ref["vertex"]) < REL_TOL
 
 
+def test_many_paths():
+    """More paths than the block-wide fill-gradient accumulators hold (4096):
+    the backward pass accumulates in per-warp path caches instead, whose
+    evictions (paths equal modulo the cache size) go to the global gradient."""
+    W, H = 128, 128
+    sc = spr.Scene.generate(spr.SCENE_MIXED, seed=81, width=W, height=H, n_paths=4200, n_large=60, seg_min=3,
+                            seg_max=6)
+    assert sc.n_paths > 4096
+    fill = fills(sc.n_paths, 3)
+    G = np.random.default_rng(8).normal(size=(H, W, 4)).astype(np.float32)
+    img, gf, gv, _ = gpu_diff(sc, W, H, fill, G, 8)
+    ref_img, ref = oracle.diff(sc, W, H, fill, grad_image=G, samples=8)
+    assert np.abs(img - ref_img).max() < 1e-5
+    assert rel(gf, ref["fill"]) < REL_TOL and rel(gv, ref["vertex"]) < REL_TOL
+
+
 def test_empty_scene_and_errors():
     empty = spr.Scene(np.zeros((0, 2), np.float32), [], [], [], [], [], [], [])
     with spr.VGRasterizer(48, 40, samples=16) as r:
