@@ -130,10 +130,42 @@ __device__ __forceinline__ void load_curve(const CurveDesc &d, const float2 *__r
     }
 }
 
-__device__ __forceinline__ float warp_sum(float v) {
+// Warp sums of N values (N = 2, 4, 8), returned to every lane: a
+// reduce-scatter in which a lane keeps, at the exchange across lane bit O, the
+// half of its partial sums that its side owns (M values), then plain
+// butterflies over the remaining lane bits and one broadcast per value; value
+// i ends in lane i * 32 / N.  2N + 4 - log2(N) shuffles instead of 5N.
+template <int M, int O, int N>
+__device__ __forceinline__ void reduce_scatter(float (&t)[N], int lane) {
+    if constexpr (M >= 1) {
+        const bool hi = (lane & O) != 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
+        for (int i = 0; i < M; ++i) {
+            const float keep = hi ? t[M + i] : t[i];
+            const float send = hi ? t[i] : t[M + i];
+            t[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+        }
+        reduce_scatter<M / 2, O / 2, N>(t, lane);
+    } else {
+#pragma unroll
+        for (int o = O; o >= 1; o >>= 1) t[0] += __shfl_xor_sync(0xffffffffu, t[0], o);
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void warp_sums(float (&v)[N], int lane) {
+    float t[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) t[i] = v[i];
+    reduce_scatter<N / 2, 16, N>(t, lane);
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = __shfl_sync(0xffffffffu, t[0], i * (32 / N));
+}
+
+__device__ __forceinline__ float4 warp_sum4(float4 x, int lane) {
+    float v[4] = {x.x, x.y, x.z, x.w};
+    warp_sums<4>(v, lane);
+    return make_float4(v[0], v[1], v[2], v[3]);
 }
 
 // One fragment of a merged group, held by one lane of the cell's warp.
@@ -296,8 +328,10 @@ __device__ void group_adjoint(const FrameArgs &a, const DiffArgs &d, int64_t h, 
                 sA += g * (1.f - lam);
                 sB += g * lam;
             }
-            sA = warp_sum(sA);
-            sB = warp_sum(sB);
+            float sAB[2] = {sA, sB};
+            warp_sums<2>(sAB, lane);
+            sA = sAB[0];
+            sB = sAB[1];
             if (lane == 0 && (sA != 0.f || sB != 0.f)) {
                 const uint32_t n = atomicAdd(d.n_chain, 1u);
                 if ((int64_t)n < d.nf) d.chain[n] = make_float4(__uint_as_float(f.raw), slope, sA, sB);
@@ -646,8 +680,10 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs 
                         ks.z += lam[k].z * cr.z;
                         ks.w += lam[k].w * cr.w;
                     }
-                    Lsum = make_float4(warp_sum(ls.x), warp_sum(ls.y), warp_sum(ls.z), warp_sum(ls.w));
-                    Ksum = make_float4(warp_sum(ks.x), warp_sum(ks.y), warp_sum(ks.z), warp_sum(ks.w));
+                    float lk[8] = {ls.x, ls.y, ls.z, ls.w, ks.x, ks.y, ks.z, ks.w};
+                    warp_sums<8>(lk, lane);
+                    Lsum = make_float4(lk[0], lk[1], lk[2], lk[3]);
+                    Ksum = make_float4(lk[4], lk[5], lk[6], lk[7]);
                     cur_slot = sidx;
                     pi = 1.f;
                 }
@@ -687,10 +723,7 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs 
                 }
             }
             group_adjoint<S>(a, d, d.heads[w - 1], a.fill_rule[path], J, lane);
-            gf.x = warp_sum(gf.x);
-            gf.y = warp_sum(gf.y);
-            gf.z = warp_sum(gf.z);
-            gf.w = warp_sum(gf.w);
+            gf = warp_sum4(gf, lane);
             if (lane == 0 && (gf.x != 0.f || gf.y != 0.f || gf.z != 0.f || gf.w != 0.f))
                 add_fill_grad(d, acc, cache, tag, path, gf);
         }

@@ -176,7 +176,7 @@ struct DiffArgs {
     const float2 *tvert;
     int64_t nf;
     float4 *tape;      // per block: tape_depth x (samples per thread) x block threads (sample states)
-    float4 *tape_rec;  // per block: warps x tape_depth x 4 (per-cell item records)
+    float4 *tape_rec;  // per block: warps x tape_depth x 3 (per-cell item records)
     int tape_depth;
     uint32_t *queue;     // bin queue (zeroed by the launchers)
     uint32_t *status;    // bit 0: a tape overflowed (rerun with a deeper tape); bit 1: chain list full
