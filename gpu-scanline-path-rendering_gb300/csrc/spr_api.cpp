@@ -118,6 +118,10 @@ struct spr_handle {
         overflow;
     uint64_t *skey_sorted = nullptr;
     uint32_t *perm_sorted = nullptr;
+    const uint32_t *pv_sorted = nullptr;  // resolve pairs in bin order
+    // the buffers hold a differentiable forward frame of the current inputs:
+    // a backward needs no new geometry pass
+    bool diff_ready = false;
     // host staging
     FrameCounters *h_counters = nullptr;
     uint32_t *h_u32 = nullptr;
@@ -144,6 +148,7 @@ struct spr_handle {
 namespace {
 
 void drop_graph(spr_handle *h) {
+    h->diff_ready = false;  // every caller changes the frame's inputs
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
     h->graph_failed = false;
@@ -568,6 +573,7 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     int st = build_tables(h);
     if (st) return st;
     h->frame_valid = false;
+    h->diff_ready = false;
     int L = 0;  // kernels launched by this frame
     h->host_syncs = 0;
     FrameArgs a = make_args(h);
@@ -626,6 +632,8 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         rec(h, 7, s);
         rec(h, 8, s);
         h->launches = L;
+        h->pv_sorted = nullptr;
+        h->diff_ready = dc && !dc->backward;
         h->frame_valid = true;
         h->frame_W = W;
         h->frame_H = H;
@@ -751,11 +759,41 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         }
     }
     h->launches = L;
+    h->pv_sorted = pv;
+    h->diff_ready = dc && !dc->backward;
     h->frame_valid = true;
     h->frame_W = W;
     h->frame_H = H;
     h->frame_S = a.S;
     return SPR_OK;
+}
+
+// Backward of the differentiable forward frame still held in the buffers
+// (nothing changed since): the adjoint kernels only.
+int backward_of_held_frame(spr_handle *h, void *stream, const DiffCall &dc) {
+    cudaSetDevice(h->cfg.device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    FrameArgs a = make_args(h);
+    if (h->nf > 0) {
+        a.chord = h->chord.as<float4>();
+        a.lmask = h->lmask.as<uint32_t>();
+        a.vmask = h->vmask.as<uint32_t>();
+        a.item_path = h->item_path.as<uint32_t>();
+    }
+    int L = 0;
+    h->host_syncs = 0;
+    uint32_t *bin_start = h->bins.as<uint32_t>();
+    const int st = diff_stage(h, a, dc, h->pv_sorted, bin_start, bin_start + a.n_bins, s, &L);
+    h->launches = L;
+    return st ? st : cuda_status();
+}
+
+// A backward: after a differentiable forward of the same inputs (and with
+// step timing off) the held frame's buffers are reused, else every stage is
+// recomputed.
+int backward_frame(spr_handle *h, void *stream, const DiffCall &dc) {
+    if (h->diff_ready && !h->timing) return backward_of_held_frame(h, stream, dc);
+    return render_frame(h, stream, &dc);
 }
 
 }  // namespace
@@ -853,7 +891,7 @@ int spr_diff_backward(spr_handle *h, const float *fill_rgba, const float *grad_i
     if (h->n_scenes > 0) return SPR_ERR_UNSUPPORTED;
     if (grad_affine && !h->has_affine) return SPR_ERR_INVALID_ARG;
     const DiffCall dc{true, fill_rgba, grad_image, nullptr, grad_fill, grad_vertex, grad_affine};
-    return render_frame(h, stream, &dc);
+    return backward_frame(h, stream, dc);
 }
 
 int spr_image_device_ptr(spr_handle *h, void **out) {
@@ -1242,7 +1280,7 @@ int spr_batch_diff_backward(spr_batch *b, const float *fill_rgba, const float *g
     if (grad_affine && !h->has_affine) return SPR_ERR_INVALID_ARG;
     b->rendered = false;
     const DiffCall dc{true, fill_rgba, grad_image, nullptr, grad_fill, grad_vertex, grad_affine};
-    return render_frame(h, stream, &dc);
+    return backward_frame(h, stream, dc);
 }
 
 int spr_batch_update_vertices(spr_batch *b, const float *vertex, void *stream) {

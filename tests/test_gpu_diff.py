@@ -297,3 +297,47 @@ def test_update_vertices_equals_a_new_upload():
         b.diff_render(fill.data_ptr(), ib.data_ptr())
         torch.cuda.synchronize()
         assert torch.equal(ia, ib)
+
+
+def test_backward_reuses_the_held_forward_frame():
+    """A backward right after a differentiable forward of the same inputs runs
+    the adjoint kernels only (one host read: the tape-depth check); any
+    change in between (a plain frame, moved vertices) makes it recompute
+    every stage.  Gradients agree either way."""
+    W, H = 160, 112
+    sc = spr.Scene.generate(spr.SCENE_CUBICS, seed=41, width=W, height=H, n_paths=30, seg_min=6, seg_max=16)
+    moved = sc.copy()
+    moved.vertex = (sc.vertex + np.random.default_rng(6).normal(0, 2.0, sc.vertex.shape)).astype(np.float32)
+    f = torch.tensor(fills(sc.n_paths, 12), device="cuda")
+    g = torch.tensor(smooth_weights(W, H), device="cuda")
+    img = torch.empty((H, W, 4), device="cuda")
+
+    def backward(r):
+        gf = torch.empty_like(f)
+        gv = torch.empty((sc.n_vertices, 2), device="cuda")
+        r.diff_backward(f.data_ptr(), g.data_ptr(), gf.data_ptr(), gv.data_ptr())
+        torch.cuda.synchronize()
+        return gf.cpu().numpy(), gv.cpu().numpy(), r.frame_stats()
+
+    with spr.VGRasterizer(W, H, samples=16) as r:
+        r.add_vg(sc)
+        r.diff_render(f.data_ptr(), img.data_ptr())
+        gf1, gv1, st1 = backward(r)
+        gf2, gv2, st2 = backward(r)  # still held
+        r.rasterize()
+        gf3, gv3, st3 = backward(r)  # recomputed
+        assert st1["host_syncs"] == 1 and st2["host_syncs"] == 1 and st3["host_syncs"] == 4
+        assert st1["kernel_launches"] < st3["kernel_launches"]
+        for a, b in ((gf1, gf2), (gf1, gf3), (gv1, gv2), (gv1, gv3)):
+            assert rel(a, b) < 1e-5
+        # moved vertices between the forward and the backward
+        r.diff_render(f.data_ptr(), img.data_ptr())
+        vdev = torch.tensor(moved.vertex, device="cuda")
+        r.update_vertices(vdev.data_ptr())
+        gf4, gv4, st4 = backward(r)
+        assert st4["host_syncs"] == 4
+    with spr.VGRasterizer(W, H, samples=16) as r:
+        r.add_vg(moved)
+        r.diff_render(f.data_ptr(), img.data_ptr())
+        gf5, gv5, _ = backward(r)
+    assert rel(gf4, gf5) < 1e-5 and rel(gv4, gv5) < 1e-5
