@@ -434,37 +434,46 @@ def run_batched_diff(dev, stream, steps=None):
         b.update_vertices(torch.tensor(np.concatenate(tgt_v), device=dev).data_ptr(), sp)
         b.diff_render(torch.tensor(np.concatenate(tgt_f), device=dev).data_ptr(), target.data_ptr(), sp)
         losses = []
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        fwd_ms, tot_ms = [], []
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        fwd_ms, bwd_ms, tot_ms = [], [], []
         for k in range(steps):
             ev[0].record(stream)
             v = pts[idx].contiguous()
             b.update_vertices(v.data_ptr(), sp)
-            b.diff_render(fill.data_ptr(), img.data_ptr(), sp)
             ev[1].record(stream)
+            b.diff_render(fill.data_ptr(), img.data_ptr(), sp)
+            ev[2].record(stream)
             diff = img - target
             g = (2.0 * diff).contiguous()
+            ev[3].record(stream)
             b.diff_backward(fill.data_ptr(), g.data_ptr(), gf.data_ptr(), gv.data_ptr(), None, sp)
+            ev[4].record(stream)
             with torch.no_grad():
                 gpt = torch.zeros_like(pts).index_add_(0, idx, gv)
                 fill -= BDIFF["lr_fill"] * gf / npix * 1e3
                 fill.clamp_(0.0, 1.0)
                 pts -= BDIFF["lr_point"] * gpt / (gpt.abs().max() + 1e-12)
-            ev[2].record(stream)
-            ev[2].synchronize()
-            fwd_ms.append(ev[0].elapsed_time(ev[1]))
-            tot_ms.append(ev[0].elapsed_time(ev[2]))
+            ev[5].record(stream)
+            ev[5].synchronize()
+            fwd_ms.append(ev[1].elapsed_time(ev[2]))
+            bwd_ms.append(ev[3].elapsed_time(ev[4]))
+            tot_ms.append(ev[0].elapsed_time(ev[5]))
             if k in (0, steps - 1):
                 losses.append(float((diff * diff).sum()))
         dev_bytes = b.frame_stats()["device_bytes"]
     peak = torch.cuda.max_memory_allocated(dev) + dev_bytes
     n = len(items)
-    f_ms, t_ms = sum(fwd_ms[1:]) / (len(fwd_ms) - 1), sum(tot_ms[1:]) / (len(tot_ms) - 1)
+    def mean(x):
+        return sum(x[1:]) / (len(x) - 1)
+
+    f_ms, b_ms, t_ms = mean(fwd_ms), mean(bwd_ms), mean(tot_ms)
     return {"workload": f"{n} scenes of 128-512 closed cubic paths (16-64 segments), 512^2-1024^2, 16 spp; "
                         f"{steps} descent steps on contour points and fills (L2 to perturbed targets)",
             "pixels": npix, "paths": P, "vertices": V, "steps": steps,
-            "fwd_ms_per_scene": f_ms / n, "fwd_bwd_ms_per_scene": t_ms / n, "step_ms": t_ms,
-            "fwd_bwd_over_fwd": t_ms / f_ms, "loss_first": losses[0], "loss_last": losses[-1],
+            "fwd_ms_per_scene": f_ms / n, "fwd_bwd_ms_per_scene": (f_ms + b_ms) / n,
+            "fwd_bwd_over_fwd": (f_ms + b_ms) / f_ms,
+            "step_ms": t_ms, "step": "vertex update + forward + loss gradient + backward + descent update",
+            "loss_first": losses[0], "loss_last": losses[-1],
             "peak_hbm_bytes": int(peak), "graph": "no: sizes change as the geometry moves (read back per step)"}
 
 

@@ -108,6 +108,10 @@ struct spr_handle {
     // paths, the per-block tapes, the transformed-vertex gradient and the
     // stored -> input vertex map
     DevBuf chord, lmask, vmask, item_path, tape, tape_rec, grad_tvert, vmap, bitems, chain, ekey[2], eval[2];
+    // 256-sample frames: the pass being rendered, the passes' fixed-point
+    // sample sums, and a pass's fill gradient / the summed vertex gradient
+    int pass = 0;
+    DevBuf sums, gfill_pass, gtvert_total;
     // raw curve arrays of the device-side scene upload (kept for vertex updates)
     DevBuf sc_vpos, sc_type, sc_pid, sc_w, scene_flags;
     bool scene_on_device = false, scene_has_arcw = false;
@@ -156,15 +160,23 @@ void drop_graph(spr_handle *h) {
 
 int validate_config(const spr_config *c) {
     if (c->width < 1 || c->height < 1 || c->width > 4096 || c->height > 4096) return SPR_ERR_INVALID_ARG;
-    if (c->samples != 8 && c->samples != 16 && c->samples != 32) return SPR_ERR_INVALID_ARG;
+    if (c->samples != 8 && c->samples != 16 && c->samples != 32 && c->samples != 256) return SPR_ERR_INVALID_ARG;
+    // 256 samples are resolved per sample only: the coverage-as-alpha output
+    // needs every sample of an item at once, which the passes do not have
+    if (c->samples == 256 && !c->ms_output) return SPR_ERR_INVALID_ARG;
     return SPR_OK;
 }
 
 int build_tables(spr_handle *h) {
     if (h->table_samples == h->cfg.samples) return SPR_OK;
-    const int words = h->cfg.samples / 8;
-    std::vector<uint32_t> t((size_t)65536 * words);
-    build_mask_table(h->cfg.samples, t.data());
+    const bool passes = h->cfg.samples == 256;
+    const int words = passes ? 4 : h->cfg.samples / 8;
+    std::vector<uint32_t> t((size_t)65536 * words * (passes ? kPasses256 : 1));
+    if (passes) {
+        for (int g = 0; g < kPasses256; ++g) build_pass_mask_table_256(g, t.data() + (size_t)g * 65536 * 4);
+    } else {
+        build_mask_table(h->cfg.samples, t.data());
+    }
     int st = ensure(h->mask_table, t.size() * 4);
     if (st) return st;
     if (cudaMemcpy(h->mask_table.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) return cuda_status();
@@ -195,6 +207,14 @@ FrameArgs make_args(const spr_handle *h) {
     a.lmask = nullptr;
     a.vmask = nullptr;
     a.item_path = nullptr;
+    a.pass_dy = 0.f;
+    a.sums = nullptr;
+    if (h->cfg.samples == 256) {  // the current pass of 32 samples
+        a.S = 32;
+        a.pass_dy = pass_shift_256(h->pass);
+        a.mask_table += (size_t)h->pass * 65536 * 4;
+        a.sums = h->sums.as<long long>();
+    }
     if (h->n_scenes > 0) {
         a.path_scene = h->path_scene.as<uint32_t>();
         a.scenes = h->scenes_d.as<SceneInfo>();
@@ -334,7 +354,8 @@ int spr_resize(spr_handle *h, int32_t width, int32_t height) {
 int spr_set_samples(spr_handle *h, int32_t samples) {
     if (!h) return SPR_ERR_INVALID_ARG;
     drop_graph(h);
-    if (samples != 8 && samples != 16 && samples != 32) return SPR_ERR_INVALID_ARG;
+    if (samples != 8 && samples != 16 && samples != 32 && samples != 256) return SPR_ERR_INVALID_ARG;
+    if (samples == 256 && !h->cfg.ms_output) return SPR_ERR_INVALID_ARG;
     cudaSetDevice(h->cfg.device);
     h->cfg.samples = samples;
     h->frame_valid = false;
@@ -344,6 +365,7 @@ int spr_set_samples(spr_handle *h, int32_t samples) {
 int spr_set_multisample_output(spr_handle *h, int32_t enable) {
     if (!h) return SPR_ERR_INVALID_ARG;
     drop_graph(h);
+    if (!enable && h->cfg.samples == 256) return SPR_ERR_INVALID_ARG;
     h->cfg.ms_output = enable ? 1 : 0;
     return SPR_OK;
 }
@@ -490,6 +512,11 @@ struct DiffCall {
     float *grad_fill;         // 4 per path (backward)
     float *grad_vertex;       // 2 per input vertex (backward)
     float *grad_affine;       // 6 per path, or null (backward)
+    // pass `pass` of `passes` (256-sample frames: 8 passes, each weighted
+    // `scale`; the forward adds its image to the earlier passes', the
+    // backward sums the passes' gradients and maps vertices after the last)
+    int pass = 0, passes = 1;
+    float scale = 1.f;
 };
 
 int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint32_t *pv, const uint32_t *bstart,
@@ -527,6 +554,8 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
     FrameCounters *ctr = h->counters.as<FrameCounters>();
     d.queue = &ctr->bin_queue;
     d.status = &ctr->status;
+    d.out_scale = dc.scale;
+    d.accumulate = dc.pass > 0 ? 1 : 0;
     if (!dc.backward) {
         *L += launch_diff_forward(a, d, s);
         return cuda_status();
@@ -535,6 +564,13 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
     if (st) return st;
     if ((st = ensure(h->chain, 16 * (size_t)std::max<int64_t>(h->nf, 1) + 16))) return st;
     d.grad_tvert = h->grad_tvert.as<float2>();
+    const bool multi = dc.passes > 1;  // the pass's gradients go to staging buffers first
+    if (multi) {
+        if ((st = ensure(h->gfill_pass, 16 * (size_t)std::max<uint32_t>(h->P, 1))) ||
+            (st = ensure(h->gtvert_total, 8 * (size_t)std::max<uint32_t>(h->V, 1))))
+            return st;
+        d.grad_fill = h->gfill_pass.as<float4>();
+    }
     d.chain = h->chain.as<float4>() + 1;
     d.n_chain = reinterpret_cast<uint32_t *>(h->chain.p);
     for (int depth = h->tape_depth;; depth *= 2) {
@@ -545,7 +581,7 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
         d.tape = h->tape.as<float4>();
         d.tape_rec = h->tape_rec.as<float4>();
         d.tape_depth = depth;
-        cudaMemsetAsync(dc.grad_fill, 0, 16 * (size_t)h->P, s);
+        cudaMemsetAsync(d.grad_fill, 0, 16 * (size_t)h->P, s);
         cudaMemsetAsync(h->grad_tvert.p, 0, 8 * (size_t)h->V, s);
         cudaMemsetAsync(&ctr->status, 0, 4, s);
         cudaMemsetAsync(d.n_chain, 0, 4, s);
@@ -559,8 +595,17 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
         }
         if (depth >= (1 << 16)) return SPR_ERR_CAPACITY_EXCEEDED;
     }
+    const float2 *gt = h->grad_tvert.as<float2>();
+    if (multi) {
+        *L += launch_accumulate(dc.grad_fill, reinterpret_cast<float *>(d.grad_fill), 4 * (int64_t)h->P, dc.pass == 0,
+                                s);
+        *L += launch_accumulate(h->gtvert_total.as<float>(), h->grad_tvert.as<float>(), 2 * (int64_t)h->V,
+                                dc.pass == 0, s);
+        if (dc.pass + 1 < dc.passes) return cuda_status();
+        gt = h->gtvert_total.as<float2>();
+    }
     if (dc.grad_affine) cudaMemsetAsync(dc.grad_affine, 0, 24 * (size_t)h->P, s);
-    *L += launch_diff_vertex(a, h->grad_tvert.as<float2>(), h->vmap.as<uint32_t>(),
+    *L += launch_diff_vertex(a, gt, h->vmap.as<uint32_t>(),
                              reinterpret_cast<float2 *>(dc.grad_vertex), dc.grad_affine, s);
     return cuda_status();
 }
@@ -788,12 +833,64 @@ int backward_of_held_frame(spr_handle *h, void *stream, const DiffCall &dc) {
     return st ? st : cuda_status();
 }
 
+// A 256-sample frame: 8 passes of 32 samples (pass g: rows 8j + g of the
+// 256-row pattern, geometry moved by -pass_shift_256(g)), each a whole
+// frame.  Plain frames add the passes' exact fixed-point sample sums and
+// encode once; differentiable frames add the passes' images and gradients
+// with weight 1/8.  Launch, host-read and step-time figures are the passes'
+// totals; the element counts and stage dumps are the last pass's.
+int render_passes(spr_handle *h, void *stream, const DiffCall *dc) {
+    if (!h->has_scene) return SPR_ERR_NO_SCENE;
+    cudaSetDevice(h->cfg.device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t npix = frame_pixels(h);
+    int st = SPR_OK;
+    if (!dc) {
+        if ((st = ensure(h->sums, 32 * (size_t)npix))) return st;
+        cudaMemsetAsync(h->sums.p, 0, 32 * (size_t)npix, s);
+    }
+    int launches = 0, syncs = 0;
+    double ms[kSteps] = {};
+    for (int g = 0; g < kPasses256 && !st; ++g) {
+        h->pass = g;
+        if (dc) {
+            DiffCall pc = *dc;
+            pc.pass = g;
+            pc.passes = kPasses256;
+            pc.scale = 1.f / (float)kPasses256;
+            st = render_frame(h, stream, &pc);
+        } else {
+            st = render_frame(h, stream, nullptr);
+        }
+        launches += h->launches;
+        syncs += h->host_syncs;
+        for (int i = 0; i < kSteps; ++i) ms[i] += h->step_ms[i];
+    }
+    h->pass = 0;
+    h->diff_ready = false;  // the buffers hold the last pass only
+    if (st) {
+        h->frame_valid = false;
+        return st;
+    }
+    if (!dc) launches += launch_encode_sums(make_args(h), h->sums.as<long long>(), h->image.as<uint32_t>(), npix, s);
+    h->launches = launches;
+    h->host_syncs = syncs;
+    if (h->timing) std::memcpy(h->step_ms, ms, sizeof(ms));
+    return cuda_status();
+}
+
+// One frame of any sample count.
+int frame(spr_handle *h, void *stream, const DiffCall *dc) {
+    if (h->cfg.samples == 256) return render_passes(h, stream, dc);
+    return render_frame(h, stream, dc);
+}
+
 // A backward: after a differentiable forward of the same inputs (and with
 // step timing off) the held frame's buffers are reused, else every stage is
 // recomputed.
 int backward_frame(spr_handle *h, void *stream, const DiffCall &dc) {
     if (h->diff_ready && !h->timing) return backward_of_held_frame(h, stream, dc);
-    return render_frame(h, stream, &dc);
+    return frame(h, stream, &dc);
 }
 
 }  // namespace
@@ -802,7 +899,7 @@ extern "C" {
 
 int spr_render(spr_handle *h, void *stream) {
     if (!h) return SPR_ERR_INVALID_ARG;
-    if (!h->graph_mode || h->timing || !h->has_scene) return render_frame(h, stream, nullptr);
+    if (!h->graph_mode || h->timing || !h->has_scene || h->cfg.samples == 256) return frame(h, stream, nullptr);
     cudaSetDevice(h->cfg.device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (h->gexec && h->gexec_gen != g_alloc_gen.load()) drop_graph(h);  // a buffer moved
@@ -882,7 +979,7 @@ int spr_diff_render(spr_handle *h, const float *fill_rgba, float *image, void *s
     if (!h || !fill_rgba || !image) return SPR_ERR_INVALID_ARG;
     if (h->n_scenes > 0) return SPR_ERR_UNSUPPORTED;
     const DiffCall dc{false, fill_rgba, nullptr, image, nullptr, nullptr, nullptr};
-    return render_frame(h, stream, &dc);
+    return frame(h, stream, &dc);
 }
 
 int spr_diff_backward(spr_handle *h, const float *fill_rgba, const float *grad_image, float *grad_fill,
@@ -961,7 +1058,8 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d,
                             &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
                             &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
-                      &h->eval[1],     &h->sc_vpos,    &h->sc_type,   &h->sc_pid,    &h->sc_w,      &h->scene_flags};
+                      &h->eval[1],     &h->sc_vpos,    &h->sc_type,   &h->sc_pid,    &h->sc_w,      &h->scene_flags, &h->sums, &h->gfill_pass,
+                      &h->gtvert_total};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;
@@ -1268,7 +1366,7 @@ int spr_batch_diff_render(spr_batch *b, const float *fill_rgba, float *image, vo
     if (!h) return SPR_ERR_UNSUPPORTED;
     b->rendered = false;
     const DiffCall dc{false, fill_rgba, nullptr, image, nullptr, nullptr, nullptr};
-    return render_frame(h, stream, &dc);
+    return frame(h, stream, &dc);
 }
 
 int spr_batch_diff_backward(spr_batch *b, const float *fill_rgba, const float *grad_image, float *grad_fill,

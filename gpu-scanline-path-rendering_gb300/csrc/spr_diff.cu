@@ -612,14 +612,19 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff(FrameArgs a, DiffArgs 
                 sum.w += __shfl_xor_sync(0xffffffffu, sum.w, o);
             }
             if (valid && sub == 0) {
-                const float inv = 1.f / (float)S;
-                d.image[pix] = make_float4(sum.x * inv, sum.y * inv, sum.z * inv, sum.w * inv);
+                const float inv = d.out_scale / (float)S;
+                float4 v = make_float4(sum.x * inv, sum.y * inv, sum.z * inv, sum.w * inv);
+                if (d.accumulate) {
+                    const float4 o = d.image[pix];
+                    v = make_float4(o.x + v.x, o.y + v.y, o.z + v.z, o.w + v.w);
+                }
+                d.image[pix] = v;
             }
             continue;
         }
         // ---- reverse sweep (warp-uniform)
         if (ne > d.tape_depth || nsl > d.tape_depth) continue;
-        const float inv = 1.f / (float)S;
+        const float inv = d.out_scale / (float)S;
         const float4 G = valid ? d.grad_image[pix] : make_float4(0.f, 0.f, 0.f, 0.f);
         float4 lam[SPT];
 #pragma unroll
@@ -878,6 +883,17 @@ int64_t diff_tape_words(const FrameArgs &a, int depth) {
 
 int64_t diff_tape_rec_words(const FrameArgs &a, int depth) {
     return diff_blocks(a) * (int64_t)(kDiffThreads / 32) * depth * 3;
+}
+
+__global__ void k_accumulate(float *__restrict__ dst, const float *__restrict__ src, int64_t n, int first) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = first ? src[i] : dst[i] + src[i];
+}
+
+int launch_accumulate(float *dst, const float *src, int64_t n, int first, cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_accumulate<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dst, src, n, first);
+    return 1;
 }
 
 int launch_diff_forward(const FrameArgs &a, const DiffArgs &d, cudaStream_t s) { return launch_diff<false>(a, d, s); }

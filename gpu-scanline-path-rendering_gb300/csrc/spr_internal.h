@@ -54,6 +54,12 @@ struct SceneInfo {
 void build_cell_samples(int samples, float *out);
 // 256x256 half-plane mask table, uint32[65536 * samples/8].
 void build_mask_table(int samples, uint32_t *out);
+// 256-sample frames are 8 passes of 32 samples: pass g covers rows 8j + g of
+// the 256-row pattern with the 32-sample rows and its own mask table
+// (uint32[65536 * 4]), the geometry moved by -pass_shift_256(g) pixel in y.
+constexpr int kPasses256 = 8;
+void build_pass_mask_table_256(int pass, uint32_t *out);
+float pass_shift_256(int pass);
 void build_resolve_tables(ResolveTables *t);
 
 // ---- scan / sort (spr_sort.cu) ----------------------------------------------------
@@ -98,6 +104,11 @@ struct FrameArgs {
     uint32_t *lmask;
     uint32_t *vmask;  // rows between the chord's end points (vertical_mask2)
     uint32_t *item_path;
+    // Passes of a 256-sample frame (else 0 and null): the geometry's shift
+    // down the pixel (subtracted from transformed y), and the per-pixel
+    // fixed-point sample sums (4 per pixel) that the resolve adds its pass to.
+    float pass_dy;
+    long long *sums;
 };
 
 int launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible,
@@ -133,6 +144,8 @@ int launch_bin_bounds(const uint32_t *pair_key, int64_t n_pairs, uint32_t *bin_s
 // more than 8 samples; unused otherwise).
 int64_t resolve_warps(const FrameArgs &a);
 int64_t resolve_overflow_words(const FrameArgs &a);
+// RGBA8 image of a 256-sample frame from the sums its 8 passes accumulated.
+int launch_encode_sums(const FrameArgs &a, const long long *sums, uint32_t *image, int64_t npix, cudaStream_t s);
 int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_mask, const uint32_t *pair_val,
                    const uint32_t *bin_start, const uint32_t *bin_end, uint32_t *image, uint32_t *overflow,
                    FrameCounters *counters, cudaStream_t s);
@@ -180,6 +193,11 @@ struct DiffArgs {
     int tape_depth;
     uint32_t *queue;     // bin queue (zeroed by the launchers)
     uint32_t *status;    // bit 0: a tape overflowed (rerun with a deeper tape); bit 1: chain list full
+    // pixel = out_scale * (mean of the samples), added to the image when
+    // accumulate (the passes of a 256-sample frame: 1/8 each); the backward
+    // takes out_scale * dL/d(pixel) likewise
+    float out_scale;
+    int accumulate;
 };
 int64_t diff_blocks(const FrameArgs &a);
 int64_t diff_tape_words(const FrameArgs &a, int depth);      // float4 count of the sample-state tape
@@ -190,5 +208,7 @@ int launch_diff_backward(const FrameArgs &a, const DiffArgs &d, cudaStream_t s);
 // vmap: stored vertex -> input vertex index (curves reversed on upload).
 int launch_diff_vertex(const FrameArgs &a, const float2 *grad_tvert, const uint32_t *vmap, float2 *grad_vertex,
                        float *grad_affine, cudaStream_t s);
+// dst = src (first) or dst + src, n floats.
+int launch_accumulate(float *dst, const float *src, int64_t n, int first, cudaStream_t s);
 
 }  // namespace spr

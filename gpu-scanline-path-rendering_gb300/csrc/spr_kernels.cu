@@ -98,6 +98,7 @@ __global__ void k_transform(FrameArgs a, float2 *__restrict__ tvert, uint32_t *_
         const float w2 = w * .5f, h2 = h * .5f;
         ov[0] = (ov[0] - w2) * z / (ov[2] + z) + w2;
         ov[1] = (ov[1] - h2) * z / (ov[2] + z) + h2;
+        if (a.pass_dy != 0.f) ov[1] = ov[1] - a.pass_dy;
         const int xf = ov[0] < 0 ? 0 : (ov[0] <= w ? 1 : 2);
         const int yf = ov[1] < 0 ? 0 : (ov[1] <= h ? 1 : 2);
         switch ((yf << 4) | xf) {
@@ -1062,11 +1063,19 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
         } else {
             for (int j = 0; j < n; ++j) add(w.ecol[j][p], __popc(w.emask[j][p]));
         }
+        const int64_t pix = (int64_t)(y0 + py) * W + tx0 + lane;
+        if (a.sums != nullptr) {  // a pass of a 256-sample frame: exact sums, encoded after the last pass
+            longlong2 *q = reinterpret_cast<longlong2 *>(a.sums) + 2 * pix;
+            const longlong2 q0 = q[0], q1 = q[1];
+            q[0] = make_longlong2(q0.x + ir, q0.y + ig);
+            q[1] = make_longlong2(q1.x + ib, q1.y + ia);
+            continue;
+        }
         const float ar = (float)((double)ir * scale), ag = (float)((double)ig * scale);
         const float ab = (float)((double)ib * scale), aa = (float)((double)ia * scale);
         const uint32_t out = enc8<SRGB>(T, ar) | (enc8<SRGB>(T, ag) << 8) | (enc8<SRGB>(T, ab) << 16) |
                              (enc_lin(aa) << 24);
-        image[(int64_t)(y0 + py) * W + tx0 + lane] = out;
+        image[pix] = out;
     }
 }
 
@@ -1106,6 +1115,30 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
         if ((int64_t)b >= a.n_bins) break;
         resolve_bin<S, MS, SRGB, CAP>(a, draw, merged, pval, bstart, bend, image, ovf, T, w, lane, b);
         __syncwarp();
+    }
+}
+
+// The image of a 256-sample frame from its passes' fixed-point sample sums
+// (the same averaging and encoding as the resolve's last step).
+template <bool SRGB>
+__global__ void k_encode_sums(FrameArgs a, const long long *__restrict__ sums, uint32_t *__restrict__ image,
+                              int64_t npix) {
+    __shared__ SmemTables T;
+    {
+        const ResolveTables *rt = a.rtables;
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) T.th[i] = rt->threshold[i];
+        if constexpr (SRGB)
+            for (int i = threadIdx.x; i < 1024; i += blockDim.x)
+                reinterpret_cast<uint32_t *>(T.bin)[i] = reinterpret_cast<const uint32_t *>(rt->bin)[i];
+    }
+    __syncthreads();
+    const double scale = 1.0 / (68719476736.0 * 256.0);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
+        const longlong2 q0 = reinterpret_cast<const longlong2 *>(sums)[2 * i];
+        const longlong2 q1 = reinterpret_cast<const longlong2 *>(sums)[2 * i + 1];
+        const float ar = (float)((double)q0.x * scale), ag = (float)((double)q0.y * scale);
+        const float ab = (float)((double)q1.x * scale), aa = (float)((double)q1.y * scale);
+        image[i] = enc8<SRGB>(T, ar) | (enc8<SRGB>(T, ag) << 8) | (enc8<SRGB>(T, ab) << 16) | (enc_lin(aa) << 24);
     }
 }
 
@@ -1339,6 +1372,14 @@ int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged,
         else if (srgb) resolve_variant<32, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
         else resolve_variant<32, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
     }
+    return 1;
+}
+
+int launch_encode_sums(const FrameArgs &a, const long long *sums, uint32_t *image, int64_t npix, cudaStream_t s) {
+    if (npix <= 0) return 0;
+    const unsigned grid = (unsigned)std::min<int64_t>((npix + 255) / 256, 152 * 8);
+    if (a.srgb) k_encode_sums<true><<<grid, 256, 0, s>>>(a, sums, image, npix);
+    else k_encode_sums<false><<<grid, 256, 0, s>>>(a, sums, image, npix);
     return 1;
 }
 

@@ -21,6 +21,17 @@ namespace {
 const uint8_t kCol32[32] = {0, 50, 24, 74, 12, 62, 38, 84, 6,  54, 30, 80, 18, 68, 42, 92,
                             3, 53, 29, 77, 17, 63, 41, 89, 9,  59, 35, 83, 21, 71, 45, 93};
 
+// Bit reversal of i on its own bit length, as a fraction of 1.
+double radical_inverse(int i) {
+    int x = i, r = 0, bc = 0;
+    while (x) {
+        r = (r << 1) | (x & 1);
+        x >>= 1;
+        ++bc;
+    }
+    return r / (float)(1 << bc);
+}
+
 void pixel_samples(int n, float *xy) {
     if (n == 32) {
         for (int i = 0; i < 32; ++i) {
@@ -30,28 +41,29 @@ void pixel_samples(int n, float *xy) {
         return;
     }
     // 8 samples: row i of 8, column = bit-reversed i (own bit length)
-    // (ras_qm_mask.cu:130-163); 16 samples apply the same rule to 16 rows.
-    // Rows are already in ascending y.
+    // (ras_qm_mask.cu:130-163); 16 and 256 samples apply the same rule to 16
+    // and 256 rows.  Rows are already in ascending y.
     const double gap = 1.0 / n, hgap = gap / 2;
     for (int i = 0; i < n; ++i) {
-        int x = i, r = 0, bc = 0;
-        while (x) {
-            r = (r << 1) | (x & 1);
-            x >>= 1;
-            ++bc;
-        }
-        double f = r / (float)(1 << bc);
-        int col = (int)(f * n);
+        int col = (int)(radical_inverse(i) * n);
         xy[2 * i] = (float)(col * gap + hgap);
         xy[2 * i + 1] = (float)(i * gap + hgap);
     }
 }
 
-}  // namespace
+// Pixel samples of pass g of a 256-sample frame: rows 8j + g of the
+// 256-sample pattern (j < 32), each put on the 32-sample row (2j + 1) / 64;
+// the pass moves the geometry by -pass_shift_256(g) instead.
+void pass_samples_256(int g, float *xy) {
+    std::vector<float> all(2 * 256);
+    pixel_samples(256, all.data());
+    for (int j = 0; j < 32; ++j) {
+        xy[2 * j] = all[2 * (8 * j + g)];
+        xy[2 * j + 1] = (float)((2 * j + 1) / 64.0);
+    }
+}
 
-void build_cell_samples(int n, float *out) {
-    std::vector<float> p(2 * n);
-    pixel_samples(n, p.data());
+void cell_samples_of(const float *p, int n, float *out) {
     const float ox[4] = {0, 0, 1, 1}, oy[4] = {0, 1, 0, 1};
     for (int k = 0; k < 4; ++k)
         for (int i = 0; i < n; ++i) {
@@ -61,9 +73,9 @@ void build_cell_samples(int n, float *out) {
         }
 }
 
-void build_mask_table(int n, uint32_t *out) {
-    std::vector<float> cs(8 * n);
-    build_cell_samples(n, cs.data());
+// QM_Mask_2x2::makeTable (ras_qm_mask.h:432-484) over the cell samples cs
+// (n per pixel).
+void mask_table_of(const float *cs, int n, uint32_t *out) {
     const int words = n / 8;
     for (int i = 0; i < 65536; ++i) {
         const int y = i / 256, x = i - y * 256;
@@ -97,6 +109,29 @@ void build_mask_table(int n, uint32_t *out) {
         }
     }
 }
+
+}  // namespace
+
+void build_cell_samples(int n, float *out) {
+    std::vector<float> p(2 * n);
+    pixel_samples(n, p.data());
+    cell_samples_of(p.data(), n, out);
+}
+
+void build_mask_table(int n, uint32_t *out) {
+    std::vector<float> cs(8 * n);
+    build_cell_samples(n, cs.data());
+    mask_table_of(cs.data(), n, out);
+}
+
+void build_pass_mask_table_256(int g, uint32_t *out) {
+    std::vector<float> p(2 * 32), cs(8 * 32);
+    pass_samples_256(g, p.data());
+    cell_samples_of(p.data(), 32, cs.data());
+    mask_table_of(cs.data(), 32, out);
+}
+
+float pass_shift_256(int g) { return (float)(2 * g - 7) / 512.f; }
 
 void build_resolve_tables(ResolveTables *t) {
     auto s2l = [](double f) { return f <= 0.04045 ? f / 12.92 : std::pow((f + 0.055) / 1.055, 2.4); };

@@ -98,8 +98,15 @@ typedef struct spr_scene_view {
  * width, height : output buffer size, 1..4096 each (resizeOutputBuffer,
  *                 ras_base.cpp:396-402; the reference caps its buffers at
  *                 4096, ras_define.h:17-20).
- * samples       : samples per pixel, 8 or 32 (setSamples), or 16 (an
- *                 extension: the 8-sample bit-reversal pattern on 16 rows).
+ * samples       : samples per pixel, 8 or 32 (setSamples), or 16 or 256 (an
+ *                 extension: the 8-sample bit-reversal pattern on 16 or 256
+ *                 rows).  A 256-sample frame is rendered as 8 passes of 32
+ *                 samples (pass g: rows 8j + g, the geometry moved up by
+ *                 (2g - 7) / 512 pixel so that they fall on the 32-sample
+ *                 rows); its pixels are the exact means of all 256 samples.
+ *                 256 samples need ms_output = 1, and are not available in
+ *                 batches.  Counts and stage dumps of a 256-sample frame are
+ *                 those of its last pass.
  * ms_output     : 1 = per-sample coverage resolve (the reference's
  *                 multisample GL output, setMultisampleOutput); 0 = one colour
  *                 per pixel with alpha scaled by coverage.
@@ -137,9 +144,10 @@ int spr_destroy(spr_handle *h);
 
 /* resizeOutputBuffer (ras_base.cpp:396-402). */
 int spr_resize(spr_handle *h, int32_t width, int32_t height);
-/* setSamples (ras_base.h:185); 8, 16 or 32.  Rebuilds the device tables. */
+/* setSamples (ras_base.h:185); 8, 16, 32 or 256.  Rebuilds the device tables. */
 int spr_set_samples(spr_handle *h, int32_t samples);
-/* setMultisampleOutput (ras_base.h:186). */
+/* setMultisampleOutput (ras_base.h:186); SPR_ERR_INVALID_ARG to turn it off
+ * at 256 samples. */
 int spr_set_multisample_output(spr_handle *h, int32_t enable);
 /* enableSRGBCorrection (ras_base.h:179). */
 int spr_enable_srgb_correction(spr_handle *h, int32_t enable);
@@ -288,9 +296,12 @@ int spr_diff_render(spr_handle *h, const float *fill_rgba, float *image, void *s
  * row contributes (c_left - c_right) dL/dI / samples to dL/dx of the
  * crossing, which moves with the chord's end points (points of the curve on
  * cell lines, or at curve ends and monotone split points) and so with the
- * control points.  Outputs are overwritten.  The frame's stages are
- * recomputed (nothing is kept from spr_diff_render).  The per-sample tape
- * grows by itself (one extra readback per doubling). */
+ * control points.  Outputs are overwritten.  Right after an
+ * spr_diff_render of the same inputs (nothing set or rendered in between,
+ * step timing off) the backward reuses that frame's coverage stages and runs
+ * the adjoint kernels only; otherwise every stage is recomputed.  256-sample
+ * frames always recompute their 8 passes.  The per-sample tape grows by
+ * itself (one extra readback per doubling). */
 int spr_diff_backward(spr_handle *h, const float *fill_rgba, const float *grad_image, float *grad_fill,
                       float *grad_vertex, float *grad_affine, void *stream);
 /* New positions of the scene's vertices (2 floats per vertex, in the scene's

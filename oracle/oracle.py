@@ -47,6 +47,8 @@ def lib() -> C.CDLL:
         L.orc_free.restype = None
         L.orc_sample_positions.argtypes = [C.c_int32, vp]
         L.orc_mask_table.argtypes = [C.c_int32, vp]
+        L.orc_pass_samples_256.argtypes = [C.c_int32, vp]
+        L.orc_pass_mask_table_256.argtypes = [C.c_int32, vp]
         L.orc_srgb_tables.argtypes = [vp, vp, vp]
         f = C.c_float
         L.orc_fetch_pixel_table.argtypes = [C.c_int32, f, f, f, f, vp]
@@ -181,6 +183,22 @@ def time_run(scene: "spr.Scene", width, height, samples=8, ms_output=True, srgb=
 def sample_positions(samples) -> np.ndarray:
     out = np.zeros((4 * samples, 2), dtype=np.float32)
     lib().orc_sample_positions(samples, out.ctypes.data)
+    return out
+
+
+def pass_samples_256(g) -> np.ndarray:
+    out = np.zeros((32, 2), dtype=np.float32)
+    st = lib().orc_pass_samples_256(g, out.ctypes.data)
+    if st != 0:
+        raise spr.SprError(st, "orc_pass_samples_256")
+    return out
+
+
+def pass_mask_table_256(g) -> np.ndarray:
+    out = np.zeros((65536, 4), dtype=np.uint32)
+    st = lib().orc_pass_mask_table_256(g, out.ctypes.data)
+    if st != 0:
+        raise spr.SprError(st, "orc_pass_mask_table_256")
     return out
 
 

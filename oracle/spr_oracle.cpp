@@ -240,9 +240,21 @@ std::vector<F2> pixel_samples(int n) {
     return s;
 }
 
+// 256 samples (an extension) apply the 8-sample rule to 256 rows and are
+// rendered as 8 passes of 32: pass g holds rows 8j + g (j < 32), each moved
+// to the 32-sample row (2j + 1) / 64, and the pass moves the geometry up by
+// (2g - 7) / 512 pixel instead (row 8j + g sits at (16j + 2g + 1) / 512).
+std::vector<F2> pass_samples_256(int g) {
+    std::vector<F2> all = pixel_samples(256), s(32);
+    for (int j = 0; j < 32; ++j) s[j] = F2{all[8 * j + g].x, (float)((2 * j + 1) / 64.0)};
+    return s;
+}
+
+inline float pass_shift_256(int g) { return (float)(2 * g - 7) / 512.f; }
+
 // Samples of the 2x2 cell (init_qm_mask_table, ras_qm_mask.h:734-759).
-std::vector<F2> cell_samples(int n) {
-    std::vector<F2> p = pixel_samples(n);
+std::vector<F2> cell_samples_of(const std::vector<F2> &p) {
+    const int n = (int)p.size();
     std::vector<F2> c(4 * n);
     const float ox[4] = {0, 0, 1, 1}, oy[4] = {0, 1, 0, 1};
     for (int k = 0; k < 4; ++k)
@@ -253,6 +265,8 @@ std::vector<F2> cell_samples(int n) {
     return c;
 }
 
+std::vector<F2> cell_samples(int n) { return cell_samples_of(pixel_samples(n)); }
+
 inline F2 normalize2(F2 v) {
     float inv = 1.0f / std::sqrt(v.x * v.x + v.y * v.y);
     return F2{v.x * inv, v.y * inv};
@@ -260,8 +274,8 @@ inline F2 normalize2(F2 v) {
 
 // QM_Mask_2x2::makeTable (ras_qm_mask.h:432-484), built on the host.  Words
 // per texel: samples/8 (8 spp: one word, 32 spp: four).
-std::vector<uint32_t> build_mask_table(int n) {
-    std::vector<F2> cs = cell_samples(n);
+std::vector<uint32_t> mask_table_of(const std::vector<F2> &cs) {
+    const int n = (int)cs.size() / 4;
     const int words = n / 8;
     std::vector<uint32_t> t((size_t)65536 * words);
     for (int i = 0; i < 65536; ++i) {
@@ -294,6 +308,10 @@ std::vector<uint32_t> build_mask_table(int n) {
     }
     return t;
 }
+
+std::vector<uint32_t> build_mask_table(int n) { return mask_table_of(cell_samples(n)); }
+
+std::vector<uint32_t> build_pass_mask_table_256(int g) { return mask_table_of(cell_samples_of(pass_samples_256(g))); }
 
 // fetchPixelTable (ras_qm_mask.h:519-542) with the texture replaced by an
 // explicit point-sampled, clamped lookup: texel = clamp(floor(uv * 256)).
@@ -485,7 +503,7 @@ int validate(const spr_scene_view *v) {
 
 // ---------------------------------------------------- stage 3: transform --
 // k_transformVertex (cu:36-105), preceded by the optional per-path affine.
-void stage_transform(const Scene &s, const orc_config &cfg, orc_result &r, int threads) {
+void stage_transform(const Scene &s, const orc_config &cfg, orc_result &r, int threads, float pass_dy) {
     const spr_scene_view *v = s.view;
     float m[16];
     if (cfg.has_transform) {
@@ -522,6 +540,7 @@ void stage_transform(const Scene &s, const orc_config &cfg, orc_result &r, int t
             float w2 = w * .5f, h2 = h * .5f;
             ov[0] = (ov[0] - w2) * z / (ov[2] + z) + w2;
             ov[1] = (ov[1] - h2) * z / (ov[2] + z) + h2;
+            if (pass_dy != 0.f) ov[1] = ov[1] - pass_dy;
             int xf = ov[0] < 0 ? 0 : (ov[0] <= w ? 1 : 2);
             int yf = ov[1] < 0 ? 0 : (ov[1] <= h ? 1 : 2);
             uint32_t bit;
@@ -949,19 +968,18 @@ inline uint32_t enc_srgb(const SrgbTables &t, float v) {
 }  // namespace
 
 // ================================================================= API ==
-extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_result **out) {
-    if (!scene || !cfgp || !out) return SPR_ERR_INVALID_ARG;
-    const orc_config cfg = *cfgp;
+namespace {
+
+// One frame (pass < 0), or pass `pass` of a 256-sample frame (cfg.samples
+// 32, the pass's samples and shift; the resolve adds its fixed-point sample
+// sums, 4 per pixel, to `sums` instead of writing the image).
+int run_frame(const spr_scene_view *scene, const orc_config &cfg, int pass, orc_result &r, int64_t *sums) {
     if (cfg.width < 1 || cfg.height < 1 || cfg.width > 4096 || cfg.height > 4096) return SPR_ERR_INVALID_ARG;
     if (cfg.samples != 8 && cfg.samples != 16 && cfg.samples != 32) return SPR_ERR_INVALID_ARG;
     int rc = validate(scene);
     if (rc) return rc;
     int threads = cfg.threads > 0 ? cfg.threads : (int)std::max(1u, std::thread::hardware_concurrency());
     const int stop = cfg.stop_after < 0 ? SPR_STAGE_COUNT_ : cfg.stop_after;
-
-    orc_result *rp = new orc_result();
-    orc_result &r = *rp;
-    *out = rp;
     r.width = cfg.width;
     r.height = cfg.height;
     r.samples = cfg.samples;
@@ -988,7 +1006,7 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
     };
 
     // -- stage 3 ---------------------------------------------------------
-    stage_transform(s, cfg, r, threads);
+    stage_transform(s, cfg, r, threads, pass >= 0 ? pass_shift_256(pass) : 0.f);
     lap(SPR_STAGE_TVERTEX);
     if (stop <= SPR_STAGE_PATH_VISIBLE) return SPR_OK;
 
@@ -1025,7 +1043,7 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
     // -- stage 7: fragments + boundary masks ---------------------------------
     // (the table is built once per renderer in the reference; not timed here)
     auto t_table = clk::now();
-    std::vector<uint32_t> table = build_mask_table(S);
+    std::vector<uint32_t> table = pass >= 0 ? build_pass_mask_table_256(pass) : build_mask_table(S);
     t_prev += clk::now() - t_table;
     r.key.resize(nf);
     r.pid.resize(nf);
@@ -1303,6 +1321,14 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
                         ib += fixed36(dec[(v >> 16) & 0xFF]);
                         ia += fixed36(st.lin_decode[v >> 24]);
                     }
+                    if (sums) {
+                        int64_t *q = sums + ((size_t)yy * W + xx) * 4;
+                        q[0] += ir;
+                        q[1] += ig;
+                        q[2] += ib;
+                        q[3] += ia;
+                        continue;
+                    }
                     const double scale = 1.0 / (68719476736.0 * (double)spp);
                     const float ar = (float)((double)ir * scale), ag = (float)((double)ig * scale);
                     const float ab = (float)((double)ib * scale), aa = (float)((double)ia * scale);
@@ -1322,6 +1348,53 @@ extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_
         }
     });
     lap(SPR_STAGE_IMAGE);
+    return SPR_OK;
+}
+
+}  // namespace
+
+// 256 samples: 8 passes of 32 (their sample sums added exactly, then the
+// resolve's averaging and encoding over all 256); the result holds the last
+// pass's stages and counts.
+extern "C" int orc_run(const spr_scene_view *scene, const orc_config *cfgp, orc_result **out) {
+    if (!scene || !cfgp || !out) return SPR_ERR_INVALID_ARG;
+    orc_result *rp = new orc_result();
+    *out = rp;
+    if (cfgp->samples != 256) return run_frame(scene, *cfgp, -1, *rp, nullptr);
+    if (!cfgp->ms_output) return SPR_ERR_INVALID_ARG;
+    if (cfgp->width < 1 || cfgp->height < 1 || cfgp->width > 4096 || cfgp->height > 4096) return SPR_ERR_INVALID_ARG;
+    orc_config c = *cfgp;
+    c.samples = 32;
+    const int W = c.width, H = c.height;
+    std::vector<int64_t> sums((size_t)W * H * 4, 0);
+    double ms[SPR_STAGE_COUNT_] = {};
+    for (int g = 0; g < 8; ++g) {
+        *rp = orc_result();
+        const int rc = run_frame(scene, c, g, *rp, sums.data());
+        if (rc) return rc;
+        for (int k = 0; k < SPR_STAGE_COUNT_; ++k) ms[k] += rp->stage_ms[k];
+    }
+    if (c.stop_after >= 0 && c.stop_after < SPR_STAGE_IMAGE) return SPR_OK;
+    const SrgbTables st = build_srgb_tables();
+    rp->image.assign((size_t)W * H * 4, 0);
+    const double scale = 1.0 / (68719476736.0 * 256.0);
+    for (size_t i = 0; i < (size_t)W * H; ++i) {
+        const int64_t *q = sums.data() + 4 * i;
+        const float ar = (float)((double)q[0] * scale), ag = (float)((double)q[1] * scale);
+        const float ab = (float)((double)q[2] * scale), aa = (float)((double)q[3] * scale);
+        uint8_t *o = rp->image.data() + 4 * i;
+        if (c.srgb) {
+            o[0] = (uint8_t)enc_srgb(st, ar);
+            o[1] = (uint8_t)enc_srgb(st, ag);
+            o[2] = (uint8_t)enc_srgb(st, ab);
+        } else {
+            o[0] = (uint8_t)enc_lin(ar);
+            o[1] = (uint8_t)enc_lin(ag);
+            o[2] = (uint8_t)enc_lin(ab);
+        }
+        o[3] = (uint8_t)enc_lin(aa);
+    }
+    std::memcpy(rp->stage_ms, ms, sizeof(ms));
     return SPR_OK;
 }
 
@@ -1362,9 +1435,23 @@ extern "C" int orc_stage_ms(const orc_result *r, double *ms, int32_t capacity) {
 extern "C" void orc_free(orc_result *r) { delete r; }
 
 extern "C" int orc_sample_positions(int32_t samples, float *out) {
-    if ((samples != 8 && samples != 16 && samples != 32) || !out) return SPR_ERR_INVALID_ARG;
+    if ((samples != 8 && samples != 16 && samples != 32 && samples != 256) || !out) return SPR_ERR_INVALID_ARG;
     std::vector<F2> c = cell_samples(samples);
     std::memcpy(out, c.data(), c.size() * sizeof(F2));
+    return SPR_OK;
+}
+
+extern "C" int orc_pass_samples_256(int32_t pass, float *out) {
+    if (pass < 0 || pass >= 8 || !out) return SPR_ERR_INVALID_ARG;
+    std::vector<F2> p = pass_samples_256(pass);
+    std::memcpy(out, p.data(), p.size() * sizeof(F2));
+    return SPR_OK;
+}
+
+extern "C" int orc_pass_mask_table_256(int32_t pass, uint32_t *out) {
+    if (pass < 0 || pass >= 8 || !out) return SPR_ERR_INVALID_ARG;
+    std::vector<uint32_t> t = build_pass_mask_table_256(pass);
+    std::memcpy(out, t.data(), t.size() * 4);
     return SPR_OK;
 }
 
@@ -1547,13 +1634,25 @@ extern "C" int orc_diff(const spr_scene_view *scene, const orc_config *cfgp, con
     if (grad_affine && !scene->path_affine) return SPR_ERR_INVALID_ARG;
     orc_config cfg = *cfgp;
     cfg.stop_after = SPR_STAGE_DRAW_LIST;
-    orc_result *rp = nullptr;
-    int rc = orc_run(scene, &cfg, &rp);
-    std::unique_ptr<orc_result> hold(rp);
-    if (rc) return rc;
-    const orc_result &r = *rp;
+    // 256 samples: 8 passes of 32 (their samples and shifts), each pixel the
+    // mean over all passes' samples
+    const int passes = cfg.samples == 256 ? 8 : 1;
+    if (passes > 1) cfg.samples = 32;
     const int W = cfg.width, H = cfg.height, S = cfg.samples, WORDS = S / 8;
+    const int Sd = S * passes;
     const uint32_t P = scene->n_paths, V = scene->n_vertices;
+    std::fill(image, image + 4 * (size_t)W * H, 0.0);
+    std::vector<double> gt;
+    if (grad_image) {
+        std::fill(grad_fill, grad_fill + 4 * (size_t)P, 0.0);
+        gt.assign(2 * (size_t)V, 0.0);
+    }
+    std::unique_ptr<orc_result> hold(new orc_result());
+    for (int pass = 0; pass < passes; ++pass) {
+    *hold = orc_result();
+    const int rc = run_frame(scene, cfg, passes > 1 ? pass : -1, *hold, nullptr);
+    if (rc) return rc;
+    const orc_result &r = *hold;
     const int64_t nf = (int64_t)r.entries.size();
     // items touching each pixel, in draw order
     std::vector<std::vector<int32_t>> items((size_t)W * H);
@@ -1564,12 +1663,6 @@ extern "C" int orc_diff(const spr_scene_view *scene, const orc_config *cfgp, con
         for (int Y = y; Y < y + 2; ++Y)
             for (int X = x; X < x + len; ++X)
                 if (X >= 0 && X < W && Y >= 0 && Y < H) items[(size_t)Y * W + X].push_back((int32_t)it);
-    }
-    std::fill(image, image + 4 * (size_t)W * H, 0.0);
-    std::vector<double> gt;
-    if (grad_image) {
-        std::fill(grad_fill, grad_fill + 4 * (size_t)P, 0.0);
-        gt.assign(2 * (size_t)V, 0.0);
     }
     struct Tape {
         int32_t it;
@@ -1583,7 +1676,7 @@ extern "C" int orc_diff(const spr_scene_view *scene, const orc_config *cfgp, con
             const int pxc = X & 1, pyc = Y & 1, k4 = pxc * 2 + pyc;
             double G[4] = {0, 0, 0, 0};
             if (grad_image)
-                for (int c = 0; c < 4; ++c) G[c] = grad_image[4 * ((size_t)Y * W + X) + c] / S;
+                for (int c = 0; c < 4; ++c) G[c] = grad_image[4 * ((size_t)Y * W + X) + c] / Sd;
             for (int i = 0; i < S; ++i) {
                 double col[4] = {1, 1, 1, 1};
                 tape.clear();
@@ -1607,7 +1700,7 @@ extern "C" int orc_diff(const spr_scene_view *scene, const orc_config *cfgp, con
                         col[3] = a * a + col[3] * om;
                     }
                 }
-                for (int c = 0; c < 4; ++c) image[4 * ((size_t)Y * W + X) + c] += col[c] / S;
+                for (int c = 0; c < 4; ++c) image[4 * ((size_t)Y * W + X) + c] += col[c] / Sd;
                 if (!grad_image) continue;
                 double lam[4] = {G[0], G[1], G[2], G[3]};
                 const int rrow = pyc * S + i;
@@ -1707,6 +1800,8 @@ extern "C" int orc_diff(const spr_scene_view *scene, const orc_config *cfgp, con
                 }
             }
         }
+    }  // passes
+    const orc_result &r = *hold;
     if (!grad_image) return SPR_OK;
     // transformed vertex -> input vertex and path affine
     float m[16];

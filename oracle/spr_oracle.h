@@ -19,7 +19,7 @@ extern "C" {
 typedef struct orc_config {
     int32_t width;
     int32_t height;
-    int32_t samples;   /* 8, 16 or 32 */
+    int32_t samples;   /* 8, 16, 32 or 256 (8 passes of 32) */
     int32_t ms_output; /* 1 = per-sample resolve */
     int32_t srgb;      /* 1 = sRGB blending */
     int32_t threads;   /* host threads; <= 0 = all hardware threads */
@@ -46,6 +46,11 @@ void orc_free(orc_result *r);
  *   sRGB decode LUT float[256], encode thresholds float[255],
  *   encode bin base uint8[4096]. */
 int orc_sample_positions(int32_t samples, float *out);
+/* 256 samples per pixel render as 8 passes of 32: pass g's pixel samples
+ * (float2[32], rows 8j + g of the 256-row pattern on the 32-sample rows) and
+ * its half-plane table (uint32[65536 * 4]). */
+int orc_pass_samples_256(int32_t pass, float *out);
+int orc_pass_mask_table_256(int32_t pass, uint32_t *out);
 int orc_mask_table(int32_t samples, uint32_t *out);
 int orc_srgb_tables(float *decode256, float *thresholds255, uint8_t *bins4096);
 

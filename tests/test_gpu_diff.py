@@ -128,6 +128,21 @@ def test_many_paths():
     assert rel(gf, ref["fill"]) < REL_TOL and rel(gv, ref["vertex"]) < REL_TOL
 
 
+def test_256_samples_against_reference_gradient():
+    """256 samples per pixel (8 passes of 32, each weighted 1/8): image and
+    gradients against the oracle's passes."""
+    W, H = 96, 80
+    sc = spr.Scene.generate(spr.SCENE_MIXED, seed=67, width=W, height=H, n_paths=12, n_large=2, seg_min=4,
+                            seg_max=10, with_rational=True, with_affine=True)
+    fill = fills(sc.n_paths, 17)
+    G = np.random.default_rng(18).normal(size=(H, W, 4)).astype(np.float32)
+    img, gf, gv, ga = gpu_diff(sc, W, H, fill, G, 256)
+    ref_img, ref = oracle.diff(sc, W, H, fill, grad_image=G, samples=256)
+    assert np.abs(img - ref_img).max() < 1e-5
+    assert rel(gf, ref["fill"]) < REL_TOL and rel(gv, ref["vertex"]) < REL_TOL
+    assert rel(ga, ref["affine"]) < REL_TOL
+
+
 def test_empty_scene_and_errors():
     empty = spr.Scene(np.zeros((0, 2), np.float32), [], [], [], [], [], [], [])
     with spr.VGRasterizer(48, 40, samples=16) as r:
@@ -149,20 +164,22 @@ def test_empty_scene_and_errors():
         assert e.value.status == spr.ERR_INVALID_ARG
 
 
-def test_finite_differences_on_jittered_renders():
+@pytest.mark.parametrize("samples,n_jit", [(16, 64), (256, 4)])
+def test_finite_differences_on_jittered_renders(samples, n_jit):
     """dL/d(vertex) against central differences (h = 0.1 px) of the rendered
-    loss, both averaged over 64 sub-pixel translations; coincident endpoint
+    loss, both averaged over sub-pixel translations (1024 samples per pixel
+    in all: 16 spp x 64 translations, or 256 spp x 4); coincident endpoint
     copies of a contour move together (one contour point)."""
     W = H = 96
     sc = spr.Scene.generate(spr.SCENE_CUBICS, seed=5, width=W, height=H, n_paths=6, seg_min=4, seg_max=6)
     fill = fills(sc.n_paths, 1)
     G = smooth_weights(W, H)
     rng = np.random.default_rng(2)
-    jit = [np.eye(4, dtype=np.float32) for _ in range(64)]
+    jit = [np.eye(4, dtype=np.float32) for _ in range(n_jit)]
     for t in jit:
         t[0, 3], t[1, 3] = rng.uniform(0, 1), rng.uniform(0, 1)
     Gt = torch.tensor(G, device="cuda")
-    with spr.VGRasterizer(W, H, samples=16) as r:
+    with spr.VGRasterizer(W, H, samples=samples) as r:
         f = torch.tensor(fill, device="cuda")
         img = torch.empty((H, W, 4), device="cuda")
 

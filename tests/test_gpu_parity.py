@@ -273,3 +273,37 @@ def test_shared_vertex_ranges():
                          np.array(cpid2, np.uint32), w, rule, fill)
     check_parity(shared, 200, 200, samples=32)
     check_parity(disjoint, 200, 200, samples=32)
+
+
+@pytest.mark.parametrize("name", ["random", "cubics", "mixed", "oddsize", "handmade"])
+def test_256_samples(name):
+    """256 samples per pixel, rendered as 8 passes of 32 (each with its own
+    samples and geometry shift): the last pass's stages and the image (the
+    exact mean over all 256 samples) match the oracle's passes."""
+    scene, W, H, tf, _, _ = load_golden(name)
+    check_parity(scene, W, H, samples=256, transform=tf)
+
+
+@pytest.mark.parametrize("srgb", [True, False])
+def test_256_samples_modes_and_limits(srgb):
+    scene = spr.Scene.generate(spr.SCENE_MIXED, seed=23, width=160, height=120, n_paths=30, n_large=3,
+                               with_rational=True)
+    check_parity(scene, 160, 120, 256, True, srgb)
+    with render(scene, 160, 120, 256, True, srgb) as r:
+        st = r.frame_stats()
+        assert st["host_syncs"] == 8 * 3  # three size reads per pass
+        r.set_samples(32)  # and back: the tables follow the sample count
+        r.rasterize()
+        assert np.array_equal(r.read_image().reshape(-1),
+                              oracle.run(scene, 160, 120, samples=32, srgb=srgb)["IMAGE"])
+        r.set_multisample_output(False)
+        with pytest.raises(spr.SprError):
+            r.set_samples(256)
+    with pytest.raises(spr.SprError):
+        spr.VGRasterizer(64, 64, samples=256, ms_output=False)
+    with spr.VGRasterizer(64, 64, samples=256) as r:
+        with pytest.raises(spr.SprError):
+            r.set_multisample_output(False)
+    with spr.Batch() as b:
+        with pytest.raises(spr.SprError):
+            b.set_scenes([(scene, 64, 64, 256)])

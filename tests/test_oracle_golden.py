@@ -126,3 +126,64 @@ def test_intersections_live_reference(kind, size, seed):
     counts, entries = oracle.ref_intersections(scene, r["TVERTEX"].reshape(-1, 2), r["PATH_VISIBLE"], size, size)
     assert np.array_equal(r["CURVE_COUNT"], counts)
     assert np.array_equal(r["INTERSECTION"].reshape(-1, 2), entries)
+
+
+def test_256_sample_pattern_and_passes():
+    """256 samples per pixel (an extension): the 8-sample construction on 256
+    rows, row i at (2i+1)/512 and column = bit-reversed i on 8 bits.  It is
+    rendered as 8 passes of 32 samples: pass g holds rows 8j + g on the
+    32-sample rows (2j+1)/64, and moving those rows down by (2g-7)/512 (the
+    pass moves the geometry up by as much) gives back exactly the pattern's
+    rows; the union of the passes is the whole pattern."""
+    cell = oracle.sample_positions(256)
+    p = (cell[:256] * 2).astype(np.float64)
+    assert np.allclose(p[:, 1], (2 * np.arange(256) + 1) / 512)
+    cols = np.round(p[:, 0] * 256 - 0.5).astype(int)
+    rev8 = [int(f"{i:08b}"[::-1], 2) for i in range(256)]
+    assert cols.tolist() == rev8 and sorted(cols) == list(range(256))
+    union = []
+    for g in range(8):
+        q = oracle.pass_samples_256(g).astype(np.float64)
+        assert np.allclose(q[:, 1], (2 * np.arange(32) + 1) / 64)
+        assert np.array_equal(q[:, 0], p[8 * np.arange(32) + g, 0])
+        union.append(np.c_[q[:, 0], q[:, 1] + (2 * g - 7) / 512])
+    union = np.concatenate(union)
+    union = union[np.lexsort((union[:, 0], union[:, 1]))]
+    assert np.allclose(union, p, atol=1e-9)
+
+
+def test_256_pass_tables_and_frame():
+    """Each pass has its own half-plane table (the 32-sample construction over
+    that pass's samples).  A 256-sample frame averages all 256 samples: a
+    black square with edges inside pixels, on white without sRGB, gives edge
+    pixels whose red channel is the share of the 256 pattern's samples
+    outside the square."""
+    t = [oracle.pass_mask_table_256(g) for g in range(8)]
+    assert all(x.shape == (65536, 4) for x in t)
+    assert not np.array_equal(t[0], t[1])
+    W = H = 24
+    lo, hi = 4.3, 19.7
+    pts = [(lo, lo), (hi, lo), (hi, hi), (lo, hi)]
+    vert = np.array([p for i in range(4) for p in (pts[i], pts[(i + 1) % 4])], np.float32)
+    sc = spr.Scene(vert, [0] * 8, [0, 2, 4, 6], [spr.CURVE_LINEAR] * 4, [0] * 4, [-1.0] * 4, [0],
+                   [0xFF000000])
+    img = oracle.run(sc, W, H, samples=256, srgb=False)["IMAGE"].reshape(H, W, 4)
+    p = (oracle.sample_positions(256)[:256] * 2).astype(np.float64)
+    fx, fy = np.float32(lo) - 4, np.float32(hi) - 19
+    inside_l = p[:, 0] > fx          # pixel column 4: right of the left edge
+    inside_r = p[:, 0] < fy          # pixel column 19: left of the right edge
+    inside_t = p[:, 1] > fx          # pixel row 4: below the top edge
+
+    def red(cover):
+        return int((256 - int(cover.sum())) / 256 * 255 + 0.5)
+
+    # within two samples (the half-plane table classifies samples within
+    # about 1/256 pixel of an edge approximately); 32 samples land elsewhere
+    img32 = oracle.run(sc, W, H, samples=32, srgb=False)["IMAGE"].reshape(H, W, 4)
+    for (y, x), cover in (((10, 4), inside_l), ((10, 19), inside_r), ((4, 10), inside_t),
+                          ((4, 4), inside_l & inside_t)):
+        assert abs(int(img[y, x, 0]) - red(cover)) <= 2, (y, x)
+        assert img32[y, x, 0] != img[y, x, 0]
+    assert img[10, 10, 0] == 0 and img[1, 1, 0] == 255 and img[10, 10, 3] == 255
+    with pytest.raises(spr.SprError):
+        oracle.run(sc, W, H, samples=256, ms_output=False)
