@@ -11,10 +11,13 @@ MPVG documents are not available).  One step = one frame through the C ABI
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-The line also carries "batched" (256 uneven scenes: one batched render
-against one launch sequence per scene, scenes/s) and "differentiable"
-(1024x1024, 256 cubic paths, 16 spp: forward, forward + L2 gradient +
-backward, and the plain RGBA8 frame, ms) unless --no-extras.
+The line also carries, unless --no-extras: "batched" (256 uneven scenes:
+one batched render against one launch sequence per scene, scenes/s),
+"differentiable" (1024x1024, 256 cubic paths, 16 spp: forward, forward + L2
+gradient + backward, and the plain RGBA8 frame, ms), "batched_differentiable"
+(64 scenes of 512^2-1024^2 fitted by gradient descent: forward and forward +
+backward per scene) and "samples_256" (the 1024x1024 scene at 256 samples
+per pixel beside 32).
 
 --impl reference times the CPU oracle -- the C++ restatement of the
 reference pipeline (its own GPU code needs OpenGL, unavailable on this machine)
@@ -477,6 +480,40 @@ def run_batched_diff(dev, stream, steps=None):
             "peak_hbm_bytes": int(peak), "graph": "no: sizes change as the geometry moves (read back per step)"}
 
 
+def run_spp256(dev, stream, steps=5):
+    """256 samples per pixel (8 passes of 32, exact mean of all samples)
+    beside 32 on the differentiable workload's scene: plain RGBA8 frames, and
+    the differentiable forward + backward."""
+    import numpy as np
+    import torch
+
+    import spr
+
+    W, H = DIFF["width"], DIFF["height"]
+    sc = spr.Scene.generate(spr.SCENE_CUBICS, seed=DIFF["seed"], width=W, height=H, n_paths=DIFF["n_paths"],
+                            seg_min=DIFF["seg_min"], seg_max=DIFF["seg_max"])
+    sp = stream.cuda_stream
+    fill = torch.tensor(np.random.default_rng(DIFF["seed"]).uniform(0.2, 1.0, (sc.n_paths, 4)).astype(np.float32),
+                        device=dev)
+    img = torch.empty((H, W, 4), device=dev)
+    g = torch.ones_like(img)
+    gf = torch.empty_like(fill)
+    gv = torch.empty((sc.n_vertices, 2), device=dev)
+    out = {"workload": f"{W}x{H}, {DIFF['n_paths']} closed paths of 16-64 cubic segments"}
+    for smp in (32, 256):
+        with spr.VGRasterizer(W, H, samples=smp, device=dev.index) as r:
+            r.add_vg(sc)
+            plain = _timed(dev, stream, lambda: r.rasterize(sp), steps)
+
+            def fb():
+                r.diff_render(fill.data_ptr(), img.data_ptr(), sp)
+                r.diff_backward(fill.data_ptr(), g.data_ptr(), gf.data_ptr(), gv.data_ptr(), None, sp)
+
+            out[f"spp{smp}"] = {"plain_ms": plain, "fwd_bwd_ms": _timed(dev, stream, fb, steps)}
+    out["plain_256_over_32"] = out["spp256"]["plain_ms"] / out["spp32"]["plain_ms"]
+    return out
+
+
 # ------------------------------------------------------------- GPU arm --
 def run_ours(args, rank, world, local_rank):
     import numpy as np
@@ -606,6 +643,7 @@ def run_ours(args, rank, world, local_rank):
         line["batched"] = run_batched(dev, stream)
         line["differentiable"] = run_diff(dev, stream)
         line["batched_differentiable"] = run_batched_diff(dev, stream)
+        line["samples_256"] = run_spp256(dev, stream)
     print(json.dumps(line), flush=True)
 
 
@@ -641,7 +679,7 @@ def main():
                     help="skip the batched-scenes and differentiable-render measurements")
     ap.add_argument("--profile", action="store_true",
                     help="timed GPU frames only (no end-to-end or CPU legs), for profiler runs")
-    ap.add_argument("--part", choices=["all", "batched", "diff", "batched_diff"], default="all",
+    ap.add_argument("--part", choices=["all", "batched", "diff", "batched_diff", "spp256"], default="all",
                     help="run only the batched or the differentiable measurement (one JSON object), "
                          "for profiler runs")
     args = ap.parse_args()
@@ -658,7 +696,8 @@ def main():
         dev = torch.device("cuda", local_rank)
         torch.cuda.set_device(dev)
         stream = torch.cuda.current_stream(dev)
-        fn = {"batched": run_batched, "diff": run_diff, "batched_diff": run_batched_diff}[args.part]
+        fn = {"batched": run_batched, "diff": run_diff, "batched_diff": run_batched_diff,
+              "spp256": run_spp256}[args.part]
         print(json.dumps({args.part: fn(dev, stream, steps=max(2, args.steps))}), flush=True)
         return
     if world > 1:
