@@ -682,7 +682,10 @@ def main():
     ap.add_argument("--part", choices=["all", "batched", "diff", "batched_diff", "spp256"], default="all",
                     help="run only the batched or the differentiable measurement (one JSON object), "
                          "for profiler runs")
+    ap.add_argument("--bd-scenes", type=int, default=BDIFF["n_scenes"],
+                    help="scenes of the batched differentiable measurement (smaller cases for profiling)")
     args = ap.parse_args()
+    BDIFF["n_scenes"] = args.bd_scenes
     scale_workload(args.scale)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
