@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/spr.h"
+#include "spr_scene.h"
 
 namespace {
 
@@ -53,41 +54,30 @@ struct P2 {
 
 }  // namespace
 
-struct spr_scene {
-    std::vector<float> vertex;
-    std::vector<uint32_t> vertex_path_id;
-    std::vector<uint32_t> curve_vertex_pos;
-    std::vector<uint8_t> curve_type;
-    std::vector<uint32_t> curve_path_id;
-    std::vector<float> curve_arc_w;
-    std::vector<uint8_t> fill_rule;
-    std::vector<uint32_t> fill_rgba;
-    std::vector<float> affine;
-    bool has_affine = false;
+namespace {
 
-    void add_curve(uint32_t path, int type, const P2 *pts, double w) {
-        curve_vertex_pos.push_back((uint32_t)(vertex.size() / 2));
-        curve_type.push_back((uint8_t)type);
-        curve_path_id.push_back(path);
-        curve_arc_w.push_back(type == SPR_CURVE_RATIONAL ? (float)w : -1.f);
-        for (int i = 0; i < (type & 7); ++i) {
-            vertex.push_back((float)pts[i].x);
-            vertex.push_back((float)pts[i].y);
-            vertex_path_id.push_back(path);
-        }
+void add_curve(spr_scene &s, uint32_t path, int type, const P2 *pts, double w) {
+    float xy[8];
+    for (int i = 0; i < (type & 7); ++i) {
+        xy[2 * i] = (float)pts[i].x;
+        xy[2 * i + 1] = (float)pts[i].y;
     }
-    uint32_t add_path(Rng &rng) {
-        uint32_t id = (uint32_t)fill_rule.size();
-        uint32_t r = (uint32_t)std::lround(rng.uniform() * 255.0);
-        uint32_t g = (uint32_t)std::lround(rng.uniform() * 255.0);
-        uint32_t b = (uint32_t)std::lround(rng.uniform() * 255.0);
-        uint32_t a = (uint32_t)std::lround(rng.uniform(0.5, 1.0) * 255.0);
-        uint32_t c = r | (g << 8) | (b << 16) | (a << 24);
-        fill_rgba.push_back((c & 0xFF000000u) ? c : 0u);
-        fill_rule.push_back(rng.uniform() < 0.5 ? SPR_FILL_NONZERO : SPR_FILL_EVEN_ODD);
-        return id;
-    }
-};
+    s.add_curve(path, type, xy, (float)w);
+}
+
+uint32_t add_path(spr_scene &s, Rng &rng) {
+    uint32_t id = (uint32_t)s.fill_rule.size();
+    uint32_t r = (uint32_t)std::lround(rng.uniform() * 255.0);
+    uint32_t g = (uint32_t)std::lround(rng.uniform() * 255.0);
+    uint32_t b = (uint32_t)std::lround(rng.uniform() * 255.0);
+    uint32_t a = (uint32_t)std::lround(rng.uniform(0.5, 1.0) * 255.0);
+    uint32_t c = r | (g << 8) | (b << 16) | (a << 24);
+    s.fill_rgba.push_back((c & 0xFF000000u) ? c : 0u);
+    s.fill_rule.push_back(rng.uniform() < 0.5 ? SPR_FILL_NONZERO : SPR_FILL_EVEN_ODD);
+    return id;
+}
+
+}  // namespace
 
 namespace {
 
@@ -136,7 +126,7 @@ void closed_contour(spr_scene &s, Rng &rng, uint32_t path, const std::vector<P2>
             cp[3] = b;
             break;
         }
-        s.add_curve(path, type, cp, w);
+        add_curve(s, path, type, cp, w);
     }
 }
 
@@ -144,7 +134,7 @@ void gen_random(spr_scene &s, Rng &rng, const spr_scene_spec &sp) {
     const double W = sp.width, H = sp.height;
     auto rnd_pt = [&]() { return P2{rng.uniform(0.0, W), rng.uniform(0.0, H)}; };
     for (int p = 0; p < sp.n_paths; ++p) {
-        uint32_t id = s.add_path(rng);
+        uint32_t id = add_path(s, rng);
         int n = rng.range(sp.seg_min, sp.seg_max);
         std::vector<P2> pts(n);
         for (auto &q : pts) q = rnd_pt();
@@ -158,7 +148,7 @@ void gen_local(spr_scene &s, Rng &rng, const spr_scene_spec &sp) {
     const double W = sp.width, H = sp.height;
     const double dim = std::fmin(W, H);
     for (int p = 0; p < sp.n_paths; ++p) {
-        uint32_t id = s.add_path(rng);
+        uint32_t id = add_path(s, rng);
         const double side = rng.uniform(dim / 32.0, dim / 4.0);
         const double x0 = rng.uniform(-side * 0.5, W - side * 0.5), y0 = rng.uniform(-side * 0.5, H - side * 0.5);
         auto rnd_pt = [&]() { return P2{x0 + rng.uniform(0.0, side), y0 + rng.uniform(0.0, side)}; };
@@ -195,7 +185,7 @@ void gen_mixed(spr_scene &s, Rng &rng, const spr_scene_spec &sp) {
     for (int p = 0; p < total; ++p) {
         bool large = rng.uniform() * (g_left + l_left) < l_left;
         if (large) --l_left; else --g_left;
-        uint32_t id = s.add_path(rng);
+        uint32_t id = add_path(s, rng);
         if (!large) {
             double size = rng.uniform(8.0, 64.0);
             int n = rng.range(10, 40);
@@ -278,7 +268,7 @@ void gen_mixed(spr_scene &s, Rng &rng, const spr_scene_spec &sp) {
 void gen_cubics(spr_scene &s, Rng &rng, const spr_scene_spec &sp) {
     const double W = sp.width, H = sp.height, dim = std::fmin(W, H);
     for (int p = 0; p < sp.n_paths; ++p) {
-        uint32_t id = s.add_path(rng);
+        uint32_t id = add_path(s, rng);
         int n = rng.range(sp.seg_min, sp.seg_max);
         double r = rng.uniform(0.03, 0.25) * dim;
         std::vector<P2> pts = star(rng, n, r, 0.5);

@@ -87,6 +87,15 @@ class FrameStats(C.Structure):
                 ("resolve_pairs", C.c_int64), ("device_bytes", C.c_int64)]
 
 
+class RvgInfo(C.Structure):
+    _fields_ = [("viewport", C.c_float * 4), ("window", C.c_float * 4), ("width", C.c_int32),
+                ("height", C.c_int32), ("n_elements", C.c_int32), ("n_gradient_paths", C.c_int32)]
+
+    def as_dict(self):
+        return {"viewport": list(self.viewport), "window": list(self.window), "width": self.width,
+                "height": self.height, "n_elements": self.n_elements, "n_gradient_paths": self.n_gradient_paths}
+
+
 class SceneSpec(C.Structure):
     _fields_ = [("kind", C.c_int32), ("seed", C.c_uint64), ("width", C.c_int32),
                 ("height", C.c_int32), ("n_paths", C.c_int32), ("n_large", C.c_int32),
@@ -138,6 +147,8 @@ def lib() -> C.CDLL:
         L.spr_scene_view_of.argtypes = [vp, C.POINTER(SceneView)]
         L.spr_scene_free.argtypes = [vp]
         L.spr_scene_free.restype = None
+        L.spr_rvg_load.argtypes = [C.c_char_p, i32, C.POINTER(vp), C.POINTER(RvgInfo)]
+        L.spr_rvg_parse.argtypes = [C.c_char_p, sz, i32, C.POINTER(vp), C.POINTER(RvgInfo)]
         L.spr_set_graph_replay.argtypes = [vp, i32]
         L.spr_graph_replays.argtypes = [vp, C.POINTER(i32)]
         L.spr_batch_set_graph_replay.argtypes = [vp, i32]
@@ -229,6 +240,26 @@ class Scene:
                          int(with_rational), int(with_affine))
         h = C.c_void_p()
         check(lib().spr_scene_generate(C.byref(spec), C.byref(h)), "spr_scene_generate")
+        return cls._take(h)
+
+    @classmethod
+    def load_rvg(cls, path, a128=False):
+        """An RVG document (RVG::load): returns (scene, info dict)."""
+        h, info = C.c_void_p(), RvgInfo()
+        check(lib().spr_rvg_load(str(path).encode(), int(a128), C.byref(h), C.byref(info)), "spr_rvg_load")
+        return cls._take(h), info.as_dict()
+
+    @classmethod
+    def parse_rvg(cls, text, a128=False):
+        """An RVG document from a string: returns (scene, info dict)."""
+        b = text.encode() if isinstance(text, str) else bytes(text)
+        h, info = C.c_void_p(), RvgInfo()
+        check(lib().spr_rvg_parse(b, len(b), int(a128), C.byref(h), C.byref(info)), "spr_rvg_parse")
+        return cls._take(h), info.as_dict()
+
+    @classmethod
+    def _take(cls, h) -> "Scene":
+        """Copies a library-owned scene into numpy arrays and frees it."""
         try:
             v = SceneView()
             check(lib().spr_scene_view_of(h, C.byref(v)), "spr_scene_view_of")

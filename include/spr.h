@@ -399,6 +399,31 @@ int spr_scene_generate(const spr_scene_spec *spec, spr_scene **out);
 int spr_scene_view_of(const spr_scene *s, spr_scene_view *view);
 void spr_scene_free(spr_scene *s);
 
+/* ---- RVG documents --------------------------------------------------------
+ * RVG::load (rvg.cpp:62-776) followed by the fill conversion of
+ * VGRasterizer::addVg (ras_base.cpp:138-162): the MPVG text format of the
+ * reference's benchmark documents into a host scene (free with
+ * spr_scene_free).  One path per element that adds vertices; M, fL, L, Q,
+ * C, A (rational arcs) and Z commands; per-element dyn_affine transforms
+ * applied to the vertices; solid colours truncated to 8 bits with alpha
+ * times the opacity (a128 != 0: alpha quantized to 7 bits as RVG::setA128).
+ * Linear and radial paints are counted in n_gradient_paths and get the fill
+ * value path + 1 (the reference's gradient index: alpha 0, so they are not
+ * drawn by this renderer).  Relative and shorthand commands return
+ * SPR_ERR_UNSUPPORTED, malformed documents SPR_ERR_INVALID_SCENE, an
+ * unreadable file SPR_ERR_INVALID_ARG. */
+typedef struct spr_rvg_info {
+    float viewport[4];        /* x0, y0, x1, y1 */
+    float window[4];          /* x0, y0, x1, y1 */
+    int32_t width, height;    /* the viewport's far corner as integers (RVG::width/height) */
+    int32_t n_elements;       /* element lines read */
+    int32_t n_gradient_paths; /* paths with a linear or radial paint */
+} spr_rvg_info;
+
+int spr_rvg_load(const char *path, int32_t a128, spr_scene **out, spr_rvg_info *info);
+/* The same from a text buffer of `length` bytes. */
+int spr_rvg_parse(const char *text, size_t length, int32_t a128, spr_scene **out, spr_rvg_info *info);
+
 #ifdef __cplusplus
 }
 #endif
