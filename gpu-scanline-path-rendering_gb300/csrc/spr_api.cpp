@@ -112,6 +112,11 @@ struct spr_handle {
     // sample sums, and a pass's fill gradient / the summed vertex gradient
     int pass = 0;
     DevBuf sums, gfill_pass, gtvert_total;
+    // gradient paints: table entries and ramp texels on the device, and the
+    // reverse transform (pixel -> scene) of their coordinates
+    DevBuf grad_table, grad_ramp;
+    uint32_t n_grad = 0;
+    float rev[13] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
     // raw curve arrays of the device-side scene upload (kept for vertex updates)
     DevBuf sc_vpos, sc_type, sc_pid, sc_w, scene_flags;
     bool scene_on_device = false, scene_has_arcw = false;
@@ -209,6 +214,10 @@ FrameArgs make_args(const spr_handle *h) {
     a.item_path = nullptr;
     a.pass_dy = 0.f;
     a.sums = nullptr;
+    a.grad_table = h->n_grad ? h->grad_table.as<float4>() : nullptr;
+    a.n_grad = h->n_grad;
+    a.grad_ramp = h->grad_ramp.as<uint32_t>();
+    std::memcpy(a.rev, h->rev, sizeof(a.rev));
     if (h->cfg.samples == 256) {  // the current pass of 32 samples
         a.S = 32;
         a.pass_dy = pass_shift_256(h->pass);
@@ -944,6 +953,40 @@ int spr_render(spr_handle *h, void *stream) {
     return SPR_OK;
 }
 
+int spr_set_gradients(spr_handle *h, const uint32_t *table, uint32_t n_entries, const uint32_t *ramp,
+                      uint32_t n_texels) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
+    if (!table || n_entries == 0) {
+        h->n_grad = 0;
+        return SPR_OK;
+    }
+    if (!ramp || n_texels == 0 || n_texels % 1024 != 0 || n_entries > 0x01000000u) return SPR_ERR_INVALID_ARG;
+    // every entry's ramp run must lie inside one 1024-texel row of the ramp
+    for (uint32_t i = 0; i < n_entries; ++i) {
+        const int32_t p = (int32_t)table[12 * i + 6];
+        float scale;
+        std::memcpy(&scale, &table[12 * i + 7], 4);
+        const float n1 = scale * 1024.f;  // ramp length - 1
+        if (!(n1 >= 0.f)) continue;       // solid slot: never sampled
+        if (p < 0 || (uint64_t)p + (uint64_t)n1 >= n_texels || (p & 1023) + (int64_t)n1 > 1023)
+            return SPR_ERR_INVALID_ARG;
+    }
+    cudaSetDevice(h->cfg.device);
+    int st = upload(h->grad_table, table, (size_t)12 * n_entries);
+    if (!st) st = upload(h->grad_ramp, ramp, n_texels);
+    if (st) return st;
+    h->n_grad = n_entries;
+    return SPR_OK;
+}
+
+int spr_set_rev_transform(spr_handle *h, const float ctx[13]) {
+    if (!h || !ctx) return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
+    std::memcpy(h->rev, ctx, sizeof(h->rev));
+    return SPR_OK;
+}
+
 int spr_set_graph_replay(spr_handle *h, int32_t enable) {
     if (!h) return SPR_ERR_INVALID_ARG;
     h->graph_mode = enable != 0;
@@ -1059,7 +1102,7 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
                             &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
                       &h->eval[1],     &h->sc_vpos,    &h->sc_type,   &h->sc_pid,    &h->sc_w,      &h->scene_flags, &h->sums, &h->gfill_pass,
-                      &h->gtvert_total};
+                      &h->gtvert_total, &h->grad_table, &h->grad_ramp};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;

@@ -109,6 +109,13 @@ struct FrameArgs {
     // fixed-point sample sums (4 per pixel) that the resolve adds its pass to.
     float pass_dy;
     long long *sums;
+    // Gradient paints (else null): 3 float4 per entry (fill value - 1), the
+    // RGBA8 ramp texels in rows of 1024, and the reverse transform
+    // (rx, ry, rw, rp, a) from pixel to scene coordinates.
+    const float4 *grad_table;
+    uint32_t n_grad;
+    const uint32_t *grad_ramp;
+    float rev[13];
 };
 
 int launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible,

@@ -674,6 +674,7 @@ __global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, int64_t nf, i
 // ------------------------------------------------------------ resolve --
 constexpr int kTileW = 32;  // pixel columns per resolve bin (one warp)
 constexpr int kResolveWarps = 8;
+constexpr int kResolveBlocksPerSM = 4;  // shared-memory bound: ~50 KB per block
 
 __device__ __forceinline__ void item_cols(const int4 &it, int W, int &x0, int &x1) {
     const int x = (int)((uint32_t)it.x & 0xFFFFu);
@@ -783,6 +784,50 @@ __device__ __forceinline__ uint32_t blend_sample(const SmemTables &t, int lane, 
     return enc8<SRGB>(t, orr) | (enc8<SRGB>(t, og) << 8) | (enc8<SRGB>(t, ob) << 16) | (enc_lin(oa) << 24);
 }
 
+// ---- gradient paints -----------------------------------------------------
+// Gradient coordinate of pixel position (x, y): back to the scene through
+// the reverse transform, then the entry's 2x3 map (ms_output_32.vert.glsl
+// calc_color).
+__device__ __forceinline__ float2 grad_coord(const FrameArgs &a, const float4 &w0, const float4 &w1, float x, float y) {
+    const float rdx = (a.rev[0] * x + a.rev[3] * y) + a.rev[6];
+    const float rdy = (a.rev[1] * x + a.rev[4] * y) + a.rev[7];
+    const float rdz = (a.rev[2] * x + a.rev[5] * y) + a.rev[8];
+    const float k = a.rev[12] / rdz;
+    const float ox = a.rev[9] + k * rdx, oy = a.rev[10] + k * rdy;
+    return make_float2((ox * w0.x + oy * w0.y) + w0.z, (ox * w0.w + oy * w1.x) + w1.y);
+}
+
+// Colour of gradient entry e at the centre of pixel (X, Y) for a draw item
+// starting at column x0, w pixels wide: the coordinate interpolated along
+// the item's row between its ends (the GL line primitive), the focal-point
+// ratio c, and the ramp sampled at c (n - 1) texels past the first with
+// linear filtering (ms_output_32.frag.glsl).  Texels are decoded from sRGB
+// first under sRGB blending.
+template <bool SRGB>
+__device__ __forceinline__ float4 gradient_colour(const FrameArgs &a, const SmemTables &T, uint32_t e, int x0, int w,
+                                                  int X, int Y, int lane) {
+    const float4 w0 = a.grad_table[3 * e], w1 = a.grad_table[3 * e + 1], w2 = a.grad_table[3 * e + 2];
+    const float yr = (float)Y + 0.5f;
+    const float2 g0 = grad_coord(a, w0, w1, (float)x0, yr), g1 = grad_coord(a, w0, w1, (float)(x0 + w), yr);
+    const float t = ((float)X + 0.5f - (float)x0) / (float)w;
+    const float gx = g0.x * (1.f - t) + g1.x * t, gy = g0.y * (1.f - t) + g1.y * t;
+    const float dx = gx - w2.x, dy = gy - w2.y;
+    const float A = dx * dx + dy * dy, B = dx * w2.x + dy * w2.y;
+    const float den = sqrtf(B * B + A * w2.z) - B;
+    const float c = fminf(A * (den > 1e-6f ? 1.f / den : 0.f), 1.f);
+    const int p = __float_as_int(w1.z);
+    const float pos = c * (w1.w * 1024.f);
+    const int i0 = (int)floorf(pos);
+    const float f = pos - (float)i0;
+    const int row = p >> 10, col = min((p & 1023) + i0, 1023), col1 = min(col + 1, 1023);
+    const uint32_t t0 = a.grad_ramp[row * 1024 + col], t1 = a.grad_ramp[row * 1024 + col1];
+    const float u = 1.f - f;
+    return make_float4(dec8<SRGB>(T, t0 & 0xFF, lane) * u + dec8<SRGB>(T, t1 & 0xFF, lane) * f,
+                       dec8<SRGB>(T, (t0 >> 8) & 0xFF, lane) * u + dec8<SRGB>(T, (t1 >> 8) & 0xFF, lane) * f,
+                       dec8<SRGB>(T, (t0 >> 16) & 0xFF, lane) * u + dec8<SRGB>(T, (t1 >> 16) & 0xFF, lane) * f,
+                       lin8(t0 >> 24) * u + lin8(t1 >> 24) * f);
+}
+
 // ---- resolve state -----------------------------------------------------
 // A bin is 2 pixel rows x 32 columns = 64 pixels, pixel p = row * 32 + col.
 // Each pixel keeps its samples as a short list of (sample mask, RGBA8 colour)
@@ -888,7 +933,7 @@ __device__ __forceinline__ void dedup(BinState<CAP> &w, int p) {
 // sets are pairwise disjoint and each batch is applied in one step, each
 // lane updating its own two pixels; then every pixel is averaged over its
 // samples with an exact fixed-point sum.
-template <int S, bool MS, bool SRGB, int CAP>
+template <int S, bool MS, bool SRGB, int CAP, bool GRAD>
 __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__restrict__ draw,
                                             const uint32_t *__restrict__ merged, const uint32_t *__restrict__ pval,
                                             const uint32_t *__restrict__ bstart, const uint32_t *__restrict__ bend,
@@ -965,9 +1010,10 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
             const int4 it = w.it[q];
             const bool frag = it.w != 0;
             const uint32_t c = (uint32_t)it.z;
-            const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
-                        sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
-            const float sa0 = lin8(c >> 24);
+            float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
+                  sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
+            float sa0 = lin8(c >> 24);
+            const bool grad = GRAD && c - 1u < a.n_grad;  // a gradient paint
             const int dx = lane + tx0 - (int)((uint32_t)it.x & 0xFFFFu);
             const uint4 mm = frag ? w.mm[q] : make_uint4(0u, 0u, 0u, 0u);
             // one-entry memo of blend(dst) for this item (same source, same alpha)
@@ -977,6 +1023,15 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
             for (int py = 0; py < 2; ++py) {
                 if (py >= rows) break;
                 const int p = py * 32 + lane;
+                if (grad) {  // this pixel's colour
+                    const float4 gc = gradient_colour<SRGB>(a, T, c - 1u, (int)(int16_t)(it.x & 0xFFFF), it.y,
+                                                            tx0 + lane, y0 + py, lane);
+                    sr = gc.x;
+                    sg = gc.y;
+                    sb = gc.z;
+                    sa0 = gc.w;
+                    memo = false;
+                }
                 uint32_t m = ALL;
                 float sa = sa0;
                 if (frag) {
@@ -1081,8 +1136,8 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
 
 // Persistent resolve: each warp takes bins from the frame's bin queue until
 // it is empty; a warp's overflow slot is reused from bin to bin.
-template <int S, bool MS, bool SRGB>
-__global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
+template <int S, bool MS, bool SRGB, bool GRAD>
+__device__ __forceinline__ void resolve_persistent(const FrameArgs &a, const int4 *__restrict__ draw,
                                                                  const uint32_t *__restrict__ merged,
                                                                  const uint32_t *__restrict__ pval,
                                                                  const uint32_t *__restrict__ bstart,
@@ -1113,9 +1168,32 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
         if (lane == 0) b = atomicAdd(bin_queue, 1u);
         b = __shfl_sync(0xffffffffu, b, 0);
         if ((int64_t)b >= a.n_bins) break;
-        resolve_bin<S, MS, SRGB, CAP>(a, draw, merged, pval, bstart, bend, image, ovf, T, w, lane, b);
+        resolve_bin<S, MS, SRGB, CAP, GRAD>(a, draw, merged, pval, bstart, bend, image, ovf, T, w, lane, b);
         __syncwarp();
     }
+}
+
+template <int S, bool MS, bool SRGB>
+__global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
+                                                                 const uint32_t *__restrict__ merged,
+                                                                 const uint32_t *__restrict__ pval,
+                                                                 const uint32_t *__restrict__ bstart,
+                                                                 const uint32_t *__restrict__ bend,
+                                                                 uint32_t *__restrict__ image,
+                                                                 uint32_t *__restrict__ overflow,
+                                                                 uint32_t *__restrict__ bin_queue) {
+    resolve_persistent<S, MS, SRGB, false>(a, draw, merged, pval, bstart, bend, image, overflow, bin_queue);
+}
+
+// With gradient paints: registers capped so that the grid's blocks stay
+// resident (the per-pixel paint would otherwise take more).
+template <int S, bool MS, bool SRGB>
+__global__ void __launch_bounds__(kResolveWarps * 32, kResolveBlocksPerSM)
+    k_resolve_grad(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ merged,
+                   const uint32_t *__restrict__ pval, const uint32_t *__restrict__ bstart,
+                   const uint32_t *__restrict__ bend, uint32_t *__restrict__ image, uint32_t *__restrict__ overflow,
+                   uint32_t *__restrict__ bin_queue) {
+    resolve_persistent<S, MS, SRGB, true>(a, draw, merged, pval, bstart, bend, image, overflow, bin_queue);
 }
 
 // The image of a 256-sample frame from its passes' fixed-point sample sums
@@ -1228,7 +1306,6 @@ __global__ void k_decode_keys(const uint64_t *__restrict__ skey, int64_t n, int 
     if (i < n) out[i] = key_from_local((uint32_t)(skey[i] & 0xFFFFFFu), nrows);
 }
 
-constexpr int kResolveBlocksPerSM = 4;  // shared-memory bound: ~50 KB per block
 
 int sm_count() {
     static int n = 0;
@@ -1245,15 +1322,28 @@ int64_t resolve_blocks(const FrameArgs &a) {
     return std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sm_count() * kResolveBlocksPerSM));
 }
 
-template <int S, bool MS, bool SRGB>
-void resolve_variant(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
+template <int S, bool MS, bool SRGB, bool GRAD>
+void resolve_variant_g(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
                      const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
                      uint32_t *queue, cudaStream_t s) {
     constexpr int CAP = MS ? kCapMS : 1;
     const size_t smem = sizeof(SmemTables) + (size_t)kResolveWarps * sizeof(BinState<CAP>);
-    cudaFuncSetAttribute(k_resolve<S, MS, SRGB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_resolve<S, MS, SRGB><<<(unsigned)resolve_blocks(a), kResolveWarps * 32, smem, s>>>(
-        a, draw, merged, pval, bstart, bend, image, overflow, queue);
+    auto kern = GRAD ? k_resolve_grad<S, MS, SRGB> : k_resolve<S, MS, SRGB>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<(unsigned)resolve_blocks(a), kResolveWarps * 32, smem, s>>>(a, draw, merged, pval, bstart, bend, image,
+                                                                      overflow, queue);
+}
+
+// Gradient paints get their own instantiations: the per-pixel paint costs
+// registers that plain frames should not pay for.
+template <int S, bool MS, bool SRGB>
+void resolve_variant(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
+                     const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
+                     uint32_t *queue, cudaStream_t s) {
+    if (a.grad_table != nullptr)
+        resolve_variant_g<S, MS, SRGB, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+    else
+        resolve_variant_g<S, MS, SRGB, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
 }
 
 }  // namespace

@@ -20,6 +20,9 @@ struct spr_scene {
     std::vector<uint32_t> fill_rgba;
     std::vector<float> affine;
     bool has_affine = false;
+    // gradient paints (RVG documents): 12 words per path, RGBA8 ramp texels
+    std::vector<uint32_t> grad_table;
+    std::vector<uint32_t> grad_ramp;
 
     // A curve of `type` on path `path` with control points (x, y) pairs xy.
     void add_curve(uint32_t path, int type, const float *xy, float w) {

@@ -38,6 +38,7 @@ ERR_UNSUPPORTED = 8
 
 # ---- curve types / fill rules / stages / scene kinds -----------------------
 CURVE_LINEAR, CURVE_QUADRATIC, CURVE_CUBIC, CURVE_RATIONAL = 0x02, 0x03, 0x04, 0x13
+RVG_A128, RVG_SRGB_RAMPS = 1, 2
 FILL_NONZERO, FILL_EVEN_ODD = 0, 1
 SCENE_RANDOM, SCENE_MIXED, SCENE_CUBICS, SCENE_LOCAL = 0, 1, 2, 3
 
@@ -149,6 +150,10 @@ def lib() -> C.CDLL:
         L.spr_scene_free.restype = None
         L.spr_rvg_load.argtypes = [C.c_char_p, i32, C.POINTER(vp), C.POINTER(RvgInfo)]
         L.spr_rvg_parse.argtypes = [C.c_char_p, sz, i32, C.POINTER(vp), C.POINTER(RvgInfo)]
+        u32p = C.POINTER(C.c_uint32)
+        L.spr_scene_gradients.argtypes = [vp, C.POINTER(vp), u32p, C.POINTER(vp), u32p]
+        L.spr_set_gradients.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32]
+        L.spr_set_rev_transform.argtypes = [vp, C.POINTER(C.c_float)]
         L.spr_set_graph_replay.argtypes = [vp, i32]
         L.spr_graph_replays.argtypes = [vp, C.POINTER(i32)]
         L.spr_batch_set_graph_replay.argtypes = [vp, i32]
@@ -204,6 +209,8 @@ class Scene:
         self.path_fill_rgba = np.ascontiguousarray(path_fill_rgba, dtype=np.uint32)
         self.path_affine = (None if path_affine is None else
                             np.ascontiguousarray(path_affine, dtype=np.float32).reshape(-1, 6))
+        # gradient paints: (table uint32[12 * entries], ramp uint32[texels]) or None
+        self.gradients = None
 
     @property
     def n_paths(self):
@@ -230,8 +237,10 @@ class Scene:
         return lib().spr_validate_scene(C.byref(v))
 
     def copy(self) -> "Scene":
-        return Scene(*[None if getattr(self, f) is None else getattr(self, f).copy()
-                       for f in self.FIELDS])
+        s = Scene(*[None if getattr(self, f) is None else getattr(self, f).copy() for f in self.FIELDS])
+        if self.gradients is not None:
+            s.gradients = tuple(x.copy() for x in self.gradients)
+        return s
 
     @classmethod
     def generate(cls, kind=SCENE_RANDOM, seed=1, width=512, height=512, n_paths=64, n_large=0,
@@ -243,18 +252,21 @@ class Scene:
         return cls._take(h)
 
     @classmethod
-    def load_rvg(cls, path, a128=False):
-        """An RVG document (RVG::load): returns (scene, info dict)."""
+    def load_rvg(cls, path, a128=False, srgb_ramps=True):
+        """An RVG document (RVG::load): returns (scene, info dict); gradient
+        paints in ``scene.gradients``."""
         h, info = C.c_void_p(), RvgInfo()
-        check(lib().spr_rvg_load(str(path).encode(), int(a128), C.byref(h), C.byref(info)), "spr_rvg_load")
+        flags = (RVG_A128 if a128 else 0) | (RVG_SRGB_RAMPS if srgb_ramps else 0)
+        check(lib().spr_rvg_load(str(path).encode(), flags, C.byref(h), C.byref(info)), "spr_rvg_load")
         return cls._take(h), info.as_dict()
 
     @classmethod
-    def parse_rvg(cls, text, a128=False):
+    def parse_rvg(cls, text, a128=False, srgb_ramps=True):
         """An RVG document from a string: returns (scene, info dict)."""
         b = text.encode() if isinstance(text, str) else bytes(text)
         h, info = C.c_void_p(), RvgInfo()
-        check(lib().spr_rvg_parse(b, len(b), int(a128), C.byref(h), C.byref(info)), "spr_rvg_parse")
+        flags = (RVG_A128 if a128 else 0) | (RVG_SRGB_RAMPS if srgb_ramps else 0)
+        check(lib().spr_rvg_parse(b, len(b), flags, C.byref(h), C.byref(info)), "spr_rvg_parse")
         return cls._take(h), info.as_dict()
 
     @classmethod
@@ -278,6 +290,11 @@ class Scene:
                     arr(v.path_fill_rule, v.n_paths, np.uint8),
                     arr(v.path_fill_rgba, v.n_paths, np.uint32),
                     None if not v.path_affine else arr(v.path_affine, 6 * v.n_paths, np.float32))
+            tp, rp, nt, nr = C.c_void_p(), C.c_void_p(), C.c_uint32(), C.c_uint32()
+            check(lib().spr_scene_gradients(h, C.byref(tp), C.byref(nt), C.byref(rp), C.byref(nr)),
+                  "spr_scene_gradients")
+            if nt.value and s.path_fill_rgba.size and np.any(s.path_fill_rgba - 1 < 0x01000000):
+                s.gradients = (arr(tp.value, 12 * nt.value, np.uint32), arr(rp.value, nr.value, np.uint32))
         finally:
             lib().spr_scene_free(h)
         return s
@@ -328,9 +345,26 @@ class VGRasterizer:
 
     # -- scene and frame -----------------------------------------------------
     def add_vg(self, scene: Scene):
+        """The scene, and its gradient paints when it has them."""
         v = scene.view()
         check(lib().spr_set_scene(self._h, C.byref(v)), "spr_set_scene")
         self._scene = scene
+        self.set_gradients(scene.gradients)
+
+    def set_gradients(self, gradients):
+        """(table uint32[12 * entries], ramp uint32[texels]) or None."""
+        if gradients is None:
+            check(lib().spr_set_gradients(self._h, None, 0, None, 0), "spr_set_gradients")
+            self._grad = None
+            return
+        table, ramp = (np.ascontiguousarray(x, dtype=np.uint32) for x in gradients)
+        check(lib().spr_set_gradients(self._h, table.ctypes.data, len(table) // 12, ramp.ctypes.data, len(ramp)),
+              "spr_set_gradients")
+        self._grad = (table, ramp)
+
+    def set_rev_transform(self, ctx):
+        c = np.ascontiguousarray(ctx, dtype=np.float32).reshape(13)
+        check(lib().spr_set_rev_transform(self._h, c.ctypes.data_as(C.POINTER(C.c_float))), "spr_set_rev_transform")
 
     def set_input_transform(self, m):
         m = np.ascontiguousarray(m, dtype=np.float32).reshape(16)

@@ -169,6 +169,29 @@ int spr_validate_scene(const spr_scene_view *scene);
  * (x, y, 0, 1) followed by the reference's perspective fold (cu:36-105). */
 int spr_set_transform(spr_handle *h, const float m[16]);
 
+/* ---- gradient paints (an extension of the fill: the reference draws them
+ * in its GL output shaders, ms_output_32.vert.glsl:58-103 and
+ * .frag.glsl:45-51) ----------------------------------------------------------
+ * A path whose fill value v satisfies 1 <= v <= 0x01000000 is painted with
+ * gradient-table entry v - 1 (the reference's fill index) when a table is
+ * set.  Entry layout (12 words, gradient_table_texture of rvg.cpp):
+ * float tr[6] (scene -> gradient space g = (tr0 x + tr1 y + tr2,
+ * tr3 x + tr4 y + tr5)), int32 first ramp texel, float (n - 1) / 1024
+ * (n = ramp length), float focal[3] (fx, fy, 1 - fx^2 - fy^2 clamped at 0),
+ * one unused word.  Per pixel, at its centre taken back through the reverse
+ * transform (spr_set_rev_transform) and interpolated along the item's row
+ * as the GL line primitive does: d = g - f, A = d.d, B = d.f,
+ * c = min(A / (sqrt(B^2 + A fz) - B), 1) (0 where the denominator is not
+ * above 1e-6), and the colour is the ramp sampled at c (n - 1) texels past
+ * the first with linear filtering, clamped to the texel row, texels decoded
+ * from sRGB first under sRGB blending.  table = NULL clears. */
+int spr_set_gradients(spr_handle *h, const uint32_t *table, uint32_t n_entries, const uint32_t *ramp,
+                      uint32_t n_texels);
+/* setRevTransform (ras_base.cpp:595-611): screen -> scene for gradient
+ * coordinates, ctx = rx[3], ry[3], rw[3], rp[3], a: rd = rx X + ry Y + rw,
+ * scene = rp + (a / rd.z) rd.  Identity by default. */
+int spr_set_rev_transform(spr_handle *h, const float ctx[13]);
+
 /* ---- frame -------------------------------------------------------------- */
 /* rasterize / rasterizeImpl (ras_base.cpp:1131-1195, cu:879-1453): runs the
  * whole pipeline on `stream` and leaves an RGBA8 image (row y = scene
@@ -406,12 +429,14 @@ void spr_scene_free(spr_scene *s);
  * spr_scene_free).  One path per element that adds vertices; M, fL, L, Q,
  * C, A (rational arcs) and Z commands; per-element dyn_affine transforms
  * applied to the vertices; solid colours truncated to 8 bits with alpha
- * times the opacity (a128 != 0: alpha quantized to 7 bits as RVG::setA128).
- * Linear and radial paints are counted in n_gradient_paths and get the fill
- * value path + 1 (the reference's gradient index: alpha 0, so they are not
- * drawn by this renderer).  Relative and shorthand commands return
- * SPR_ERR_UNSUPPORTED, malformed documents SPR_ERR_INVALID_SCENE, an
- * unreadable file SPR_ERR_INVALID_ARG. */
+ * times the opacity (SPR_RVG_A128: alpha quantized to 7 bits as
+ * RVG::setA128).  Linear and radial paints (spread "pad") get the fill value
+ * path + 1 and a gradient-table entry with its ramp (spr_scene_gradients;
+ * SPR_RVG_SRGB_RAMPS: stops interpolated in linear light, for sRGB
+ * rendering, as the reference does under its sRGB setting).  Relative and
+ * shorthand commands return SPR_ERR_UNSUPPORTED, malformed documents
+ * SPR_ERR_INVALID_SCENE, an unreadable file SPR_ERR_INVALID_ARG. */
+enum spr_rvg_flags { SPR_RVG_A128 = 1, SPR_RVG_SRGB_RAMPS = 2 };
 typedef struct spr_rvg_info {
     float viewport[4];        /* x0, y0, x1, y1 */
     float window[4];          /* x0, y0, x1, y1 */
@@ -420,9 +445,14 @@ typedef struct spr_rvg_info {
     int32_t n_gradient_paths; /* paths with a linear or radial paint */
 } spr_rvg_info;
 
-int spr_rvg_load(const char *path, int32_t a128, spr_scene **out, spr_rvg_info *info);
+int spr_rvg_load(const char *path, int32_t flags, spr_scene **out, spr_rvg_info *info);
 /* The same from a text buffer of `length` bytes. */
-int spr_rvg_parse(const char *text, size_t length, int32_t a128, spr_scene **out, spr_rvg_info *info);
+int spr_rvg_parse(const char *text, size_t length, int32_t flags, spr_scene **out, spr_rvg_info *info);
+/* The scene's gradient table (12 words per entry) and ramp texels (RGBA8,
+ * rows of 1024), for spr_set_gradients; zero entries for generated scenes.
+ * Valid until spr_scene_free. */
+int spr_scene_gradients(const spr_scene *s, const uint32_t **table, uint32_t *n_entries, const uint32_t **ramp,
+                        uint32_t *n_texels);
 
 #ifdef __cplusplus
 }

@@ -25,7 +25,26 @@ class OrcConfig(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("samples", C.c_int32),
                 ("ms_output", C.c_int32), ("srgb", C.c_int32), ("threads", C.c_int32),
                 ("has_transform", C.c_int32), ("transform", C.c_float * 16),
-                ("stop_after", C.c_int32)]
+                ("stop_after", C.c_int32), ("grad_table", C.c_void_p), ("n_grad", C.c_uint32),
+                ("grad_ramp", C.c_void_p), ("n_ramp", C.c_uint32), ("has_rev", C.c_int32),
+                ("rev", C.c_float * 13)]
+
+
+def _paints(cfg, scene, rev):
+    """Points cfg at the scene's gradient table and ramp (kept alive by the
+    returned tuple) and at the reverse transform."""
+    keep = ()
+    g = getattr(scene, "gradients", None)
+    if g is not None:
+        table, ramp = (np.ascontiguousarray(x, dtype=np.uint32) for x in g)
+        cfg.grad_table, cfg.n_grad = table.ctypes.data, len(table) // 12
+        cfg.grad_ramp, cfg.n_ramp = ramp.ctypes.data, len(ramp)
+        keep = (table, ramp)
+    if rev is not None:
+        cfg.has_rev = 1
+        for i, v in enumerate(np.asarray(rev, dtype=np.float32).reshape(13)):
+            cfg.rev[i] = float(v)
+    return keep
 
 
 _lib = None
@@ -108,9 +127,10 @@ class Result:
 
 
 def run(scene: "spr.Scene", width, height, samples=8, ms_output=True, srgb=True, threads=0,
-        transform=None, stop_after=-1) -> Result:
+        transform=None, stop_after=-1, rev=None) -> Result:
     cfg = OrcConfig(width, height, samples, int(ms_output), int(srgb), threads,
                     0 if transform is None else 1, (C.c_float * 16)(), stop_after)
+    keep = _paints(cfg, scene, rev)  # noqa: F841 (alive through the call)
     if transform is not None:
         t = np.asarray(transform, dtype=np.float32).reshape(16)
         for i in range(16):

@@ -953,6 +953,49 @@ inline int16_t key_y(uint32_t k) { return (int16_t)(uint16_t)((k >> 16) - 0x7FFF
 // Decoded channel value as an exact 2^-36 fixed-point integer.
 inline int64_t fixed36(float d) { return (int64_t)(d * 68719476736.0f); }
 
+// Gradient paints, restating the renderer's evaluation of the reference's
+// GL shaders (ms_output_32.vert.glsl calc_color, ms_output_32.frag.glsl):
+// the pixel centre back through the reverse transform, the entry's 2x3 map
+// at both ends of the item's row interpolated to the pixel, the focal-point
+// ratio, the ramp linearly filtered (texels decoded by `dec`).
+inline void grad_coord(const float *rev, const float *e, float x, float y, float &gx, float &gy) {
+    const float rdx = (rev[0] * x + rev[3] * y) + rev[6];
+    const float rdy = (rev[1] * x + rev[4] * y) + rev[7];
+    const float rdz = (rev[2] * x + rev[5] * y) + rev[8];
+    const float k = rev[12] / rdz;
+    const float ox = rev[9] + k * rdx, oy = rev[10] + k * rdy;
+    gx = (ox * e[0] + oy * e[1]) + e[2];
+    gy = (ox * e[3] + oy * e[4]) + e[5];
+}
+
+void gradient_colour(const orc_config &cfg, const float *rev, const float *dec, const float *lin, uint32_t entry,
+                     int x0, int w, int X, int Y, float &sr, float &sg, float &sb, float &sa) {
+    float e[12];
+    std::memcpy(e, cfg.grad_table + 12 * (size_t)entry, sizeof(e));
+    const float yr = (float)Y + 0.5f;
+    float g0x, g0y, g1x, g1y;
+    grad_coord(rev, e, (float)x0, yr, g0x, g0y);
+    grad_coord(rev, e, (float)(x0 + w), yr, g1x, g1y);
+    const float t = ((float)X + 0.5f - (float)x0) / (float)w;
+    const float gx = g0x * (1.f - t) + g1x * t, gy = g0y * (1.f - t) + g1y * t;
+    const float dx = gx - e[8], dy = gy - e[9];
+    const float A = dx * dx + dy * dy, B = dx * e[8] + dy * e[9];
+    const float den = std::sqrt(B * B + A * e[10]) - B;
+    const float c = std::min(A * (den > 1e-6f ? 1.f / den : 0.f), 1.f);
+    int32_t p;
+    std::memcpy(&p, &e[6], 4);
+    const float pos = c * (e[7] * 1024.f);
+    const int i0 = (int)std::floor(pos);
+    const float f = pos - (float)i0;
+    const int row = p >> 10, col = std::min((p & 1023) + i0, 1023), col1 = std::min(col + 1, 1023);
+    const uint32_t t0 = cfg.grad_ramp[row * 1024 + col], t1 = cfg.grad_ramp[row * 1024 + col1];
+    const float u = 1.f - f;
+    sr = dec[t0 & 0xFF] * u + dec[t1 & 0xFF] * f;
+    sg = dec[(t0 >> 8) & 0xFF] * u + dec[(t1 >> 8) & 0xFF] * f;
+    sb = dec[(t0 >> 16) & 0xFF] * u + dec[(t1 >> 16) & 0xFF] * f;
+    sa = lin[t0 >> 24] * u + lin[t1 >> 24] * f;
+}
+
 inline uint32_t enc_lin(float v) {
     float c = fmin_r(fmax_r(v, 0.f), 1.f);
     return (uint32_t)cvt_rzi(c * 255.f + 0.5f);
@@ -1246,6 +1289,8 @@ int run_frame(const spr_scene_view *scene, const orc_config &cfg, int pass, orc_
     }
     const int spp = cfg.ms_output ? S : 1;
     const float *dec = cfg.srgb ? st.decode : st.lin_decode;
+    const float rev_identity[13] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
+    const float *rev = cfg.has_rev ? cfg.rev : rev_identity;
     r.image.assign((size_t)W * H * 4, 0);
     parallel_for(threads, nrows, [&](int64_t b, int64_t e) {
         std::vector<uint32_t> state((size_t)2 * W * spp);
@@ -1258,6 +1303,7 @@ int run_frame(const spr_scene_view *scene, const orc_config &cfg, int pass, orc_
                 uint32_t c = (uint32_t)d.z;
                 float sr = dec[c & 0xFF], sg = dec[(c >> 8) & 0xFF], sb = dec[(c >> 16) & 0xFF];
                 float sa = st.lin_decode[c >> 24];
+                const bool grad = cfg.grad_table != nullptr && c - 1u < cfg.n_grad;
                 for (int py = 0; py < 2; ++py) {
                     int yy = ybase + py;
                     if (yy >= H) continue;
@@ -1274,6 +1320,8 @@ int run_frame(const spr_scene_view *scene, const orc_config &cfg, int pass, orc_
                                 m = r.merged_mask[(int64_t)(d.w - 1) * 4 + k];
                         }
                         uint32_t *px = state.data() + ((size_t)py * W + xx) * spp;
+                        if (grad)
+                            gradient_colour(cfg, rev, dec, st.lin_decode, c - 1u, x, d.y, xx, yy, sr, sg, sb, sa);
                         float a = sa;
                         if (!cfg.ms_output) {
                             int cnt = __builtin_popcount(S == 32 ? m : (m & ((1u << S) - 1u)));

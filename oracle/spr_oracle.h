@@ -26,6 +26,13 @@ typedef struct orc_config {
     int32_t has_transform;
     float transform[16]; /* row-major 4x4, used when has_transform */
     int32_t stop_after;  /* run stages up to and including this spr_stage id (-1 = all) */
+    /* gradient paints (as spr_set_gradients / spr_set_rev_transform); n_grad 0 = none */
+    const uint32_t *grad_table;
+    uint32_t n_grad;
+    const uint32_t *grad_ramp;
+    uint32_t n_ramp;
+    int32_t has_rev;
+    float rev[13];
 } orc_config;
 
 typedef struct orc_result orc_result;
