@@ -97,6 +97,11 @@ class RvgInfo(C.Structure):
                 "height": self.height, "n_elements": self.n_elements, "n_gradient_paths": self.n_gradient_paths}
 
 
+class VgInfo(C.Structure):
+    _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("n_contours", C.c_int32)]
+
+
 class SceneSpec(C.Structure):
     _fields_ = [("kind", C.c_int32), ("seed", C.c_uint64), ("width", C.c_int32),
                 ("height", C.c_int32), ("n_paths", C.c_int32), ("n_large", C.c_int32),
@@ -154,6 +159,10 @@ def lib() -> C.CDLL:
         L.spr_scene_gradients.argtypes = [vp, C.POINTER(vp), u32p, C.POINTER(vp), u32p]
         L.spr_set_gradients.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32]
         L.spr_set_rev_transform.argtypes = [vp, C.POINTER(C.c_float)]
+        L.spr_vg_load.argtypes = [C.c_char_p, C.POINTER(vp), C.POINTER(VgInfo)]
+        L.spr_vg_save.argtypes = [vp, i32, i32, C.c_char_p]
+        L.spr_scene_from_view.argtypes = [C.POINTER(SceneView), C.POINTER(vp)]
+        L.spr_scene_set_gradients.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32]
         L.spr_set_graph_replay.argtypes = [vp, i32]
         L.spr_graph_replays.argtypes = [vp, C.POINTER(i32)]
         L.spr_batch_set_graph_replay.argtypes = [vp, i32]
@@ -268,6 +277,26 @@ class Scene:
         flags = (RVG_A128 if a128 else 0) | (RVG_SRGB_RAMPS if srgb_ramps else 0)
         check(lib().spr_rvg_parse(b, len(b), flags, C.byref(h), C.byref(info)), "spr_rvg_parse")
         return cls._take(h), info.as_dict()
+
+    @classmethod
+    def load_vg(cls, path):
+        """A .vgb / .vgt scene file (VGContainer::load): returns (scene, info dict)."""
+        h, info = C.c_void_p(), VgInfo()
+        check(lib().spr_vg_load(str(path).encode(), C.byref(h), C.byref(info)), "spr_vg_load")
+        return cls._take(h), {n: int(getattr(info, n)) for n, _ in VgInfo._fields_}
+
+    def save_vg(self, path, width, height):
+        """Writes the scene as a .vgb / .vgt file (by the suffix)."""
+        h = C.c_void_p()
+        check(lib().spr_scene_from_view(C.byref(self.view()), C.byref(h)), "spr_scene_from_view")
+        try:
+            if self.gradients is not None:
+                t, r = (np.ascontiguousarray(x, dtype=np.uint32) for x in self.gradients)
+                check(lib().spr_scene_set_gradients(h, t.ctypes.data, len(t) // 12, r.ctypes.data, len(r)),
+                      "spr_scene_set_gradients")
+            check(lib().spr_vg_save(h, int(width), int(height), str(path).encode()), "spr_vg_save")
+        finally:
+            lib().spr_scene_free(h)
 
     @classmethod
     def _take(cls, h) -> "Scene":

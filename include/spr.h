@@ -448,6 +448,29 @@ typedef struct spr_rvg_info {
 int spr_rvg_load(const char *path, int32_t flags, spr_scene **out, spr_rvg_info *info);
 /* The same from a text buffer of `length` bytes. */
 int spr_rvg_parse(const char *text, size_t length, int32_t flags, spr_scene **out, spr_rvg_info *info);
+/* ---- the reference's scene files ---------------------------------------------
+ * VGContainer::loadBinary / loadTxt (vg_container.cpp:1667-1911) for .vgb /
+ * .vgt files (chosen by the name's suffix), flattened as VGRasterizer::addVg
+ * does (paths, their contours, their curves in order; fill value = colour,
+ * 0 when its alpha is 0, or path + 1 for gradient fills, whose table and
+ * ramp come along: spr_scene_gradients; vertex path ids numbered curve by
+ * curve as addVg does).  SPR_ERR_INVALID_SCENE for truncated files, indices
+ * out of range, or curves whose vertex counts do not add up to the vertices.
+ * spr_vg_save writes a scene in the same formats (one contour per path; no
+ * per-path affines: SPR_ERR_UNSUPPORTED). */
+typedef struct spr_vg_info {
+    int32_t x, y, width, height; /* the container's placement and size */
+    int32_t n_contours;
+} spr_vg_info;
+
+int spr_vg_load(const char *path, spr_scene **out, spr_vg_info *info);
+int spr_vg_save(const spr_scene *s, int32_t width, int32_t height, const char *path);
+/* A library-owned copy of a scene view (for spr_vg_save), and gradient
+ * paints attached to it (12 words per table entry, ramp in rows of 1024). */
+int spr_scene_from_view(const spr_scene_view *view, spr_scene **out);
+int spr_scene_set_gradients(spr_scene *s, const uint32_t *table, uint32_t n_entries, const uint32_t *ramp,
+                            uint32_t n_texels);
+
 /* The scene's gradient table (12 words per entry) and ramp texels (RGBA8,
  * rows of 1024), for spr_set_gradients; zero entries for generated scenes.
  * Valid until spr_scene_free. */
