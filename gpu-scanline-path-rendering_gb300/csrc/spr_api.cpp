@@ -115,6 +115,7 @@ struct spr_handle {
     // gradient paints: table entries and ramp texels on the device, and the
     // reverse transform (pixel -> scene) of their coordinates
     DevBuf grad_table, grad_ramp;
+    DevBuf path_start;  // first curve of every path (the per-path segment sort)
     uint32_t n_grad = 0;
     float rev[13] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
     // raw curve arrays of the device-side scene upload (kept for vertex updates)
@@ -736,15 +737,15 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     L += launch_fragment(a, h->tvert.as<float2>(), h->entries.as<int2>(), nf, h->key.as<int32_t>(), h->pidw.as<uint32_t>(),
                     h->wn.as<int8_t>(), h->mask.as<uint32_t>(), h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), s);
     rec(h, 3, s);
-    // stage 8: stable sort by (path, cell key)
-    const int key_bits = 24 + bits_for(h->P ? h->P - 1 : 0);
+    // stage 8: stable sort by (path, cell key): the entries arrive grouped by
+    // path, so each path's segment is sorted on its own
+    if ((st = ensure(h->path_start, 4 * ((size_t)h->P + 1)))) return st;
+    L += launch_segment_sort(h->curves.as<CurveDesc>(), h->C, h->P, h->offsets.as<uint32_t>(),
+                             h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), h->skey[1].as<uint64_t>(),
+                             h->sval[1].as<uint32_t>(), h->path_start.as<uint32_t>(), s);
+    h->skey_sorted = h->skey[1].as<uint64_t>();
+    h->perm_sorted = h->sval[1].as<uint32_t>();
     int rl = 0;
-    const bool alt = radix_sort<uint64_t>(h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(),
-                                          h->skey[1].as<uint64_t>(), h->sval[1].as<uint32_t>(), nf, key_bits,
-                                          h->sort_tmp.as<uint32_t>(), s, &rl);
-    L += rl;
-    h->skey_sorted = alt ? h->skey[1].as<uint64_t>() : h->skey[0].as<uint64_t>();
-    h->perm_sorted = alt ? h->sval[1].as<uint32_t>() : h->sval[0].as<uint32_t>();
     rec(h, 4, s);
     // stages 9-12, 14: winding scan, marks, draw list
     cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);
@@ -1102,7 +1103,7 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
                             &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
                       &h->eval[1],     &h->sc_vpos,    &h->sc_type,   &h->sc_pid,    &h->sc_w,      &h->scene_flags, &h->sums, &h->gfill_pass,
-                      &h->gtvert_total, &h->grad_table, &h->grad_ramp};
+                      &h->gtvert_total, &h->grad_table, &h->grad_ramp, &h->path_start};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;

@@ -69,6 +69,13 @@ int scan_exclusive_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *t
 // In-place exclusive scan of a short array by one block; a[n] = total.
 int scan_tiles_inplace(uint32_t *a, int64_t n, cudaStream_t s);
 int64_t radix_tiles(int64_t n);
+// Stable sort of the fragment entries by (path, 24-bit cell key), given that
+// they arrive grouped by path: every path's segment sorted by one block.
+// Reads keys (values are the positions), writes keys_out / vals_out; keys and
+// vals serve as scratch for long segments.  path_start: P + 1 words.
+int launch_segment_sort(const CurveDesc *curves, uint32_t C, uint32_t P, const uint32_t *offsets, uint64_t *keys,
+                        uint32_t *vals, uint64_t *keys_out, uint32_t *vals_out, uint32_t *path_start,
+                        cudaStream_t s);
 int64_t radix_tmp_words(int64_t n);
 // Stable LSD sort on bits [0, key_bits); returns true when the result is in
 // the *_alt buffers.

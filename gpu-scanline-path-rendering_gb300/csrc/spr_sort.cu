@@ -230,7 +230,274 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const K *__rest
     }
 }
 
+// ---- per-path segment sort ---------------------------------------------------
+// The fragment entries arrive grouped by path (curves are in path order and
+// each curve's entries are contiguous), so the stable sort by (path, cell
+// key) is a stable sort of every path's segment by its 24-bit cell key.  One
+// block per path: segments of up to kSegTile entries are sorted in shared
+// memory (three 8-bit passes, a pass skipped when its digit is constant) and
+// written once; longer ones make the same passes over the segment in global
+// memory, chunk by chunk, ping-ponging through the input keys' own range.
+// Ranking inside a chunk is the scatter's (per-warp digit counters, lanes in
+// input order), so equal keys keep their input order.  Inside a segment the
+// keys' path bits are the path's own, so only the 24-bit cell keys move.
+
+constexpr int kSegThreads = 256;
+constexpr int kSegWarps = kSegThreads / 32;
+constexpr int kSegItems = 8;
+constexpr int kSegTile = kSegThreads * kSegItems;
+constexpr int kSegWarpSpan = 32 * kSegItems;
+
+struct SegSmem {
+    uint32_t key[kSegTile];
+    uint32_t val[kSegTile];
+    uint32_t whist[kSegWarps][256];
+    uint32_t lstart[256];  // first position of each digit in the staged chunk
+    uint32_t dstart[256];  // next output position of each digit in the segment (long segments)
+    uint32_t wsum[kSegWarps + 1];
+};
+
+// First curve of every path (curves ascending by path); start[P] = C.
+__global__ void k_path_starts(const CurveDesc *__restrict__ curves, uint32_t C, uint32_t P, uint32_t *__restrict__ start) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > (int64_t)C) return;
+    const uint32_t lo = c == 0 ? 0u : curves[c - 1].pid + 1u;
+    const uint32_t hi = c == (int64_t)C ? P : curves[c].pid;
+    for (uint32_t q = lo; q <= hi && q <= P; ++q) start[q] = (uint32_t)c;
+}
+
+// Ranks one chunk (kk[], count cnt, input order = warp-major, then item,
+// then lane) by digit `shift` and stages it in shared memory ordered by
+// digit; sm.lstart gets each digit's first staged position, the return value
+// through `tot` the per-digit counts of thread d (d = threadIdx.x).
+__device__ __forceinline__ void seg_stage_chunk(SegSmem &sm, const uint32_t (&kk)[kSegItems],
+                                                const uint32_t (&vv)[kSegItems], int cnt, int shift, uint32_t *tot) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < kSegWarps * 256; i += kSegThreads) (&sm.whist[0][0])[i] = 0;
+    __syncthreads();
+    uint32_t rank[kSegItems];
+#pragma unroll
+    for (int r = 0; r < kSegItems; ++r) {
+        if (warp * kSegWarpSpan + r * 32 >= cnt) break;  // the warp's remaining items are past the end
+        const int li = warp * kSegWarpSpan + r * 32 + lane;
+        const bool valid = li < cnt;
+        const uint32_t d = valid ? ((kk[r] >> shift) & 0xFFu) : (256u + lane);
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t before = __popc(peers & ((1u << lane) - 1u));
+        const uint32_t cur = valid ? sm.whist[warp][d] : 0u;
+        __syncwarp();
+        if (valid && before == 0) sm.whist[warp][d] = cur + __popc(peers);
+        __syncwarp();
+        rank[r] = cur + before;
+    }
+    __syncthreads();
+    {
+        // one digit per thread of the first 256: its count and per-warp offsets
+        const int d = threadIdx.x;
+        const bool dig = d < 256;
+        uint32_t t = 0;
+        if (dig) {
+#pragma unroll
+            for (int w = 0; w < kSegWarps; ++w) {
+                const uint32_t c = sm.whist[w][d];
+                sm.whist[w][d] = t;
+                t += c;
+            }
+        }
+        uint32_t inc = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31 && dig) sm.wsum[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {  // the 8 digit warps' totals
+            const uint32_t x = lane < 8 ? sm.wsum[lane] : 0u;
+            uint32_t xi = x;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, xi, o);
+                if (lane >= o) xi += v;
+            }
+            if (lane < 8) sm.wsum[lane] = xi - x;
+        }
+        __syncthreads();
+        if (dig) {
+            const uint32_t ls = sm.wsum[warp] + inc - t;
+            sm.lstart[d] = ls;
+#pragma unroll
+            for (int w = 0; w < kSegWarps; ++w) sm.whist[w][d] += ls;
+        }
+        *tot = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSegItems; ++r) {
+        if (warp * kSegWarpSpan + r * 32 >= cnt) break;
+        const int li = warp * kSegWarpSpan + r * 32 + lane;
+        if (li < cnt) {
+            const uint32_t d = (kk[r] >> shift) & 0xFFu;
+            const uint32_t lp = sm.whist[warp][d] + rank[r];
+            sm.key[lp] = kk[r];
+            sm.val[lp] = vv[r];
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t *__restrict__ keys_in,
+                                                               const uint32_t *__restrict__ start,
+                                                               const uint32_t *__restrict__ offsets,
+                                                               uint64_t *__restrict__ keys_out,
+                                                               uint32_t *__restrict__ vals_out, uint64_t *keys_tmp,
+                                                               uint32_t *vals_tmp) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SegSmem &sm = *reinterpret_cast<SegSmem *>(smem_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t p = blockIdx.x;
+    const uint32_t b = offsets[start[p]], e = offsets[start[p + 1]];
+    if (e <= b) return;
+    const uint32_t n = e - b;
+    const uint64_t hi = (uint64_t)p << 24;  // the segment's path bits
+    if (n <= (uint32_t)kSegTile) {
+        uint32_t kk[kSegItems];
+        uint32_t vv[kSegItems];
+#pragma unroll
+        for (int r = 0; r < kSegItems; ++r) {
+            const uint32_t li = (uint32_t)(warp * kSegWarpSpan + r * 32 + lane);
+            kk[r] = li < n ? (uint32_t)keys_in[b + li] & 0xFFFFFFu : 0u;
+            vv[r] = b + li;
+        }
+        bool staged = false;  // the current order is in shared memory
+        for (int shift = 0; shift < 24; shift += 8) {
+            const uint32_t d0 = (__shfl_sync(0xffffffffu, kk[0], 0) >> shift) & 0xFFu;
+            bool diff = false;
+#pragma unroll
+            for (int r = 0; r < kSegItems; ++r) {
+                const uint32_t li = (uint32_t)(warp * kSegWarpSpan + r * 32 + lane);
+                diff |= li < n && ((kk[r] >> shift) & 0xFFu) != d0;
+            }
+            // warp 0's first key stands for the block: compare across warps too
+            if (warp == 0 && lane == 0) sm.wsum[kSegWarps] = d0;
+            __syncthreads();
+            const uint32_t dblock = sm.wsum[kSegWarps];
+            diff = diff || (n > 0 && ((kk[0] >> shift) & 0xFFu) != dblock &&
+                            (uint32_t)(warp * kSegWarpSpan + lane) < n);
+            if (!__syncthreads_or(diff)) continue;  // one digit throughout: order unchanged
+            uint32_t tot;
+            seg_stage_chunk(sm, kk, vv, (int)n, shift, &tot);
+            staged = true;
+#pragma unroll
+            for (int r = 0; r < kSegItems; ++r) {
+                const uint32_t li = (uint32_t)(warp * kSegWarpSpan + r * 32 + lane);
+                if (li < n) {
+                    kk[r] = sm.key[li];
+                    vv[r] = sm.val[li];
+                }
+            }
+            __syncthreads();
+        }
+        if (!staged) {  // already in order
+#pragma unroll
+            for (int r = 0; r < kSegItems; ++r) {
+                const uint32_t li = (uint32_t)(warp * kSegWarpSpan + r * 32 + lane);
+                if (li < n) {
+                    keys_out[b + li] = hi | kk[r];
+                    vals_out[b + li] = vv[r];
+                }
+            }
+            return;
+        }
+        for (uint32_t i = threadIdx.x; i < n; i += kSegThreads) {
+            keys_out[b + i] = hi | sm.key[i];
+            vals_out[b + i] = sm.val[i];
+        }
+        return;
+    }
+    // long segment: chunked passes through global memory
+    int cur = 0;  // data in: 0 keys_in (values = positions), 1 *_out, 2 *_tmp
+    for (int shift = 0; shift < 24; shift += 8) {
+        const uint64_t *ksrc = cur == 0 ? keys_in : (cur == 1 ? keys_out : keys_tmp);
+        const uint32_t *vsrc = cur == 1 ? vals_out : vals_tmp;
+        uint64_t *kdst = cur == 1 ? keys_tmp : keys_out;
+        uint32_t *vdst = cur == 1 ? vals_tmp : vals_out;
+        // digit histogram of the segment
+        const bool dig = threadIdx.x < 256;
+        if (dig) sm.dstart[threadIdx.x] = 0;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += kSegThreads)
+            atomicAdd(&sm.dstart[(uint32_t)(ksrc[b + i] >> shift) & 0xFFu], 1u);
+        __syncthreads();
+        const uint32_t cnt_d = dig ? sm.dstart[threadIdx.x] : 0u;
+        if (__syncthreads_or(cnt_d == n)) continue;  // one digit throughout
+        {
+            uint32_t inc = cnt_d;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            if (lane == 31 && dig) sm.wsum[warp] = inc;
+            __syncthreads();
+            if (warp == 0) {
+                const uint32_t x = lane < 8 ? sm.wsum[lane] : 0u;
+                uint32_t xi = x;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(0xffffffffu, xi, o);
+                    if (lane >= o) xi += v;
+                }
+                if (lane < 8) sm.wsum[lane] = xi - x;
+            }
+            __syncthreads();
+            if (dig) sm.dstart[threadIdx.x] = b + sm.wsum[warp] + inc - cnt_d;
+            __syncthreads();
+        }
+        for (uint32_t c0 = 0; c0 < n; c0 += kSegTile) {
+            const int cnt = (int)min((uint32_t)kSegTile, n - c0);
+            uint32_t kk[kSegItems];
+            uint32_t vv[kSegItems];
+#pragma unroll
+            for (int r = 0; r < kSegItems; ++r) {
+                const int li = warp * kSegWarpSpan + r * 32 + lane;
+                const bool valid = li < cnt;
+                kk[r] = valid ? (uint32_t)ksrc[b + c0 + li] & 0xFFFFFFu : 0u;
+                vv[r] = valid ? (cur == 0 ? b + c0 + (uint32_t)li : vsrc[b + c0 + li]) : 0u;
+            }
+            uint32_t tot;
+            seg_stage_chunk(sm, kk, vv, cnt, shift, &tot);
+            for (int i = threadIdx.x; i < cnt; i += kSegThreads) {
+                const uint32_t k = sm.key[i];
+                const uint32_t d = (k >> shift) & 0xFFu;
+                const uint32_t pos = sm.dstart[d] + (uint32_t)i - sm.lstart[d];
+                kdst[pos] = hi | k;
+                vdst[pos] = sm.val[i];
+            }
+            __syncthreads();
+            if (threadIdx.x < 256) sm.dstart[threadIdx.x] += tot;
+            __syncthreads();
+        }
+        cur = cur == 1 ? 2 : 1;
+    }
+    if (cur == 1) return;
+    for (uint32_t i = threadIdx.x; i < n; i += kSegThreads) {  // into the output arrays
+        keys_out[b + i] = cur == 0 ? keys_in[b + i] : keys_tmp[b + i];
+        vals_out[b + i] = cur == 0 ? b + i : vals_tmp[b + i];
+    }
+}
+
 }  // namespace
+
+int launch_segment_sort(const CurveDesc *curves, uint32_t C, uint32_t P, const uint32_t *offsets, uint64_t *keys,
+                        uint32_t *vals, uint64_t *keys_out, uint32_t *vals_out, uint32_t *path_start,
+                        cudaStream_t s) {
+    if (P == 0) return 0;
+    k_path_starts<<<(unsigned)(((int64_t)C + 1 + 255) / 256), 256, 0, s>>>(curves, C, P, path_start);
+    cudaFuncSetAttribute(k_segment_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem));
+    k_segment_sort<<<P, kSegThreads, sizeof(SegSmem), s>>>(keys, path_start, offsets, keys_out, vals_out, keys, vals);
+    return 2;
+}
 
 int64_t scan_tmp_words(int64_t n) { return (n + kScanTile - 1) / kScanTile + 2; }
 
