@@ -307,3 +307,13 @@ def test_256_samples_modes_and_limits(srgb):
     with spr.Batch() as b:
         with pytest.raises(spr.SprError):
             b.set_scenes([(scene, 64, 64, 256)])
+
+
+def test_long_path_segments():
+    """Paths of 145k-338k entries each: the fragment sort's long-segment
+    passes (chunked through global memory) against the oracle's stable
+    sort, every stage exact."""
+    for W in (1024, 2048):
+        sc = spr.Scene.generate(spr.SCENE_RANDOM, seed=77, width=W, height=W, n_paths=4, seg_min=300, seg_max=400)
+        counts, _ = check_parity(sc, W, W, samples=8)
+        assert counts["curve_fragment"] > 500_000
