@@ -1194,6 +1194,9 @@ struct spr_batch {
     int device = 0, ms_output = 1, srgb = 1;
     bool timing = false, graph = false;
     spr_handle *group[3] = {nullptr, nullptr, nullptr};  // samples 8, 16, 32
+    // graph replays of the groups run side by side, one stream each
+    cudaStream_t gstream[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t gdone[3] = {nullptr, nullptr, nullptr}, gstart = nullptr;
     struct Entry {
         int group;
         int64_t image_off;
@@ -1301,6 +1304,11 @@ int spr_batch_destroy(spr_batch *b) {
         spr_destroy(h);
         h = nullptr;
     }
+    for (int g = 0; g < 3; ++g) {
+        if (b->gstream[g]) cudaStreamDestroy(b->gstream[g]);
+        if (b->gdone[g]) cudaEventDestroy(b->gdone[g]);
+    }
+    if (b->gstart) cudaEventDestroy(b->gstart);
     delete b;
     return SPR_OK;
 }
@@ -1339,10 +1347,52 @@ int spr_batch_set_scenes(spr_batch *b, const spr_batch_scene *scenes, int32_t n)
     return SPR_OK;
 }
 
+namespace {
+// Graph replay of every group at once: each group's captured frame on its
+// own stream, ordered after the caller's stream and joined back into it.
+// Returns false (nothing launched) unless every group has a current graph.
+bool replay_groups_concurrently(spr_batch *b, cudaStream_t s) {
+    int n = 0;
+    for (spr_handle *h : b->group) {
+        if (!h) continue;
+        if (!h->graph_mode || h->timing || !h->gexec || h->gexec_gen != g_alloc_gen.load()) return false;
+        ++n;
+    }
+    if (n < 2) return false;
+    cudaSetDevice(b->device);
+    if (!b->gstart && cudaEventCreateWithFlags(&b->gstart, cudaEventDisableTiming) != cudaSuccess) return false;
+    for (int g = 0; g < 3; ++g) {
+        if (!b->group[g]) continue;
+        if (!b->gstream[g] && cudaStreamCreateWithFlags(&b->gstream[g], cudaStreamNonBlocking) != cudaSuccess)
+            return false;
+        if (!b->gdone[g] && cudaEventCreateWithFlags(&b->gdone[g], cudaEventDisableTiming) != cudaSuccess) return false;
+    }
+    cudaEventRecord(b->gstart, s);
+    for (int g = 0; g < 3; ++g) {
+        spr_handle *h = b->group[g];
+        if (!h) continue;
+        cudaStreamWaitEvent(b->gstream[g], b->gstart, 0);
+        cudaGraphLaunch(h->gexec, b->gstream[g]);
+        cudaEventRecord(b->gdone[g], b->gstream[g]);
+        cudaStreamWaitEvent(s, b->gdone[g], 0);
+        h->host_syncs = 0;
+        h->frame_valid = true;
+        ++h->graph_replays;
+    }
+    return true;
+}
+}  // namespace
+
 int spr_batch_render(spr_batch *b, void *stream) {
     if (!b) return SPR_ERR_INVALID_ARG;
     if (b->entries.empty()) return SPR_ERR_NO_SCENE;
     b->rendered = false;
+    if (b->graph && replay_groups_concurrently(b, static_cast<cudaStream_t>(stream))) {
+        const int st = cuda_status();
+        if (st) return st;
+        b->rendered = true;
+        return SPR_OK;
+    }
     for (spr_handle *h : b->group) {
         if (!h) continue;
         int st = spr_render(h, stream);
