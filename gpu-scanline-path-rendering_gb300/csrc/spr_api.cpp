@@ -1190,13 +1190,15 @@ const char *spr_status_string(int32_t status) {
 // concatenation of its scenes (path, curve and vertex ids offset) plus the
 // per-scene table, and renders all of them in one launch sequence.
 
+constexpr int kGroups = 4;  // batch groups by sample count: 8, 16, 32, 256
+
 struct spr_batch {
     int device = 0, ms_output = 1, srgb = 1;
     bool timing = false, graph = false;
-    spr_handle *group[3] = {nullptr, nullptr, nullptr};  // samples 8, 16, 32
+    spr_handle *group[kGroups] = {};  // samples 8, 16, 32, 256
     // graph replays of the groups run side by side, one stream each
-    cudaStream_t gstream[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t gdone[3] = {nullptr, nullptr, nullptr}, gstart = nullptr;
+    cudaStream_t gstream[kGroups] = {};
+    cudaEvent_t gdone[kGroups] = {}, gstart = nullptr;
     struct Entry {
         int group;
         int64_t image_off;
@@ -1208,7 +1210,7 @@ struct spr_batch {
 
 namespace {
 
-int group_of(int samples) { return samples == 8 ? 0 : (samples == 16 ? 1 : 2); }
+int group_of(int samples) { return samples == 8 ? 0 : (samples == 16 ? 1 : (samples == 32 ? 2 : 3)); }
 
 // Concatenates the scenes `idx` of `in` into one scene and uploads it to h,
 // with the per-scene table and the scene of every path.
@@ -1304,7 +1306,7 @@ int spr_batch_destroy(spr_batch *b) {
         spr_destroy(h);
         h = nullptr;
     }
-    for (int g = 0; g < 3; ++g) {
+    for (int g = 0; g < kGroups; ++g) {
         if (b->gstream[g]) cudaStreamDestroy(b->gstream[g]);
         if (b->gdone[g]) cudaEventDestroy(b->gdone[g]);
     }
@@ -1318,16 +1320,17 @@ int spr_batch_set_scenes(spr_batch *b, const spr_batch_scene *scenes, int32_t n)
     for (int i = 0; i < n; ++i) {
         const spr_batch_scene &s = scenes[i];
         if (s.width < 1 || s.height < 1 || s.width > 4096 || s.height > 4096) return SPR_ERR_INVALID_ARG;
-        if (s.samples != 8 && s.samples != 16 && s.samples != 32) return SPR_ERR_INVALID_ARG;
+        if (s.samples != 8 && s.samples != 16 && s.samples != 32 && s.samples != 256) return SPR_ERR_INVALID_ARG;
+        if (s.samples == 256 && !b->ms_output) return SPR_ERR_INVALID_ARG;
         int st = validate_scene(&s.scene);
         if (st) return st;
     }
     cudaSetDevice(b->device);
     b->rendered = false;
     b->entries.assign(n, spr_batch::Entry{0, 0, 0, 0});
-    std::vector<int> idx[3];
+    std::vector<int> idx[kGroups];
     for (int i = 0; i < n; ++i) idx[group_of(scenes[i].samples)].push_back(i);
-    for (int g = 0; g < 3; ++g) {
+    for (int g = 0; g < kGroups; ++g) {
         if (idx[g].empty()) {
             spr_destroy(b->group[g]);
             b->group[g] = nullptr;
@@ -1361,14 +1364,14 @@ bool replay_groups_concurrently(spr_batch *b, cudaStream_t s) {
     if (n < 2) return false;
     cudaSetDevice(b->device);
     if (!b->gstart && cudaEventCreateWithFlags(&b->gstart, cudaEventDisableTiming) != cudaSuccess) return false;
-    for (int g = 0; g < 3; ++g) {
+    for (int g = 0; g < kGroups; ++g) {
         if (!b->group[g]) continue;
         if (!b->gstream[g] && cudaStreamCreateWithFlags(&b->gstream[g], cudaStreamNonBlocking) != cudaSuccess)
             return false;
         if (!b->gdone[g] && cudaEventCreateWithFlags(&b->gdone[g], cudaEventDisableTiming) != cudaSuccess) return false;
     }
     cudaEventRecord(b->gstart, s);
-    for (int g = 0; g < 3; ++g) {
+    for (int g = 0; g < kGroups; ++g) {
         spr_handle *h = b->group[g];
         if (!h) continue;
         cudaStreamWaitEvent(b->gstream[g], b->gstart, 0);

@@ -945,6 +945,7 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
     // the bin's scene: viewport, first bin, image
     int W = a.W, H = a.H;
     uint32_t lb = b;
+    int64_t image_off = 0;
     if (a.scenes != nullptr) {
         int lo = 0, hi = a.n_scenes - 1;  // last scene whose bin_off <= b
         while (lo < hi) {
@@ -956,7 +957,8 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
         W = sc->W;
         H = sc->H;
         lb = b - sc->bin_off;
-        image += sc->image_off;
+        image_off = sc->image_off;
+        image += image_off;
     }
     const int ntx = (W + kTileW - 1) / kTileW;
     const int row = (int)(lb / ntx), tile = (int)(lb % ntx);
@@ -1120,7 +1122,7 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
         }
         const int64_t pix = (int64_t)(y0 + py) * W + tx0 + lane;
         if (a.sums != nullptr) {  // a pass of a 256-sample frame: exact sums, encoded after the last pass
-            longlong2 *q = reinterpret_cast<longlong2 *>(a.sums) + 2 * pix;
+            longlong2 *q = reinterpret_cast<longlong2 *>(a.sums) + 2 * (image_off + pix);
             const longlong2 q0 = q[0], q1 = q[1];
             q[0] = make_longlong2(q0.x + ir, q0.y + ig);
             q[1] = make_longlong2(q1.x + ib, q1.y + ia);

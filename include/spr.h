@@ -104,9 +104,8 @@ typedef struct spr_scene_view {
  *                 samples (pass g: rows 8j + g, the geometry moved up by
  *                 (2g - 7) / 512 pixel so that they fall on the 32-sample
  *                 rows); its pixels are the exact means of all 256 samples.
- *                 256 samples need ms_output = 1, and are not available in
- *                 batches.  Counts and stage dumps of a 256-sample frame are
- *                 those of its last pass.
+ *                 256 samples need ms_output = 1.  Counts and stage dumps of
+ *                 a 256-sample frame are those of its last pass.
  * ms_output     : 1 = per-sample coverage resolve (the reference's
  *                 multisample GL output, setMultisampleOutput); 0 = one colour
  *                 per pixel with alpha scaled by coverage.

@@ -95,3 +95,19 @@ def test_batch_rejects_bad_input():
         b.set_scenes([(sc, 64, 64, 8)])
         b.render()
         assert np.array_equal(b.read_image(0), single(sc, 64, 64, 8)[0])
+
+
+def test_batch_with_256_samples():
+    """256-sample scenes in a batch (their own group, 8 passes of 32) next to
+    8- and 32-sample ones: each scene byte-identical to its single render."""
+    items = []
+    for i, (W, H, smp) in enumerate([(96, 80, 256), (128, 64, 32), (50, 70, 256), (64, 64, 8)]):
+        sc = spr.Scene.generate(spr.SCENE_MIXED, seed=300 + i, width=W, height=H, n_paths=12, n_large=2,
+                                with_rational=True)
+        items.append((sc, W, H, smp))
+    with spr.Batch() as b:
+        b.set_scenes(items)
+        b.render()
+        for i, (sc, W, H, smp) in enumerate(items):
+            exp, _ = single(sc, W, H, smp)
+            assert np.array_equal(b.read_image(i), exp), f"scene {i} ({smp} spp)"

@@ -304,7 +304,7 @@ def test_256_samples_modes_and_limits(srgb):
     with spr.VGRasterizer(64, 64, samples=256) as r:
         with pytest.raises(spr.SprError):
             r.set_multisample_output(False)
-    with spr.Batch() as b:
+    with spr.Batch(ms_output=False) as b:
         with pytest.raises(spr.SprError):
             b.set_scenes([(scene, 64, 64, 256)])
 
