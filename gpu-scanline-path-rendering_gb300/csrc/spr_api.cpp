@@ -620,6 +620,12 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
     return cuda_status();
 }
 
+// Fragment sort choice: one block per path needs enough paths to fill the
+// GPU and segments short enough for shared memory (longer ones are sorted by
+// a single block, chunk by chunk).
+constexpr int64_t kSegmentSortMinPaths = 1024;
+constexpr int64_t kSegmentSortMaxMean = 2048;  // mean entries per path
+
 int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     if (!h) return SPR_ERR_INVALID_ARG;
     if (!h->has_scene) return SPR_ERR_NO_SCENE;
@@ -737,15 +743,27 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     L += launch_fragment(a, h->tvert.as<float2>(), h->entries.as<int2>(), nf, h->key.as<int32_t>(), h->pidw.as<uint32_t>(),
                     h->wn.as<int8_t>(), h->mask.as<uint32_t>(), h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), s);
     rec(h, 3, s);
-    // stage 8: stable sort by (path, cell key): the entries arrive grouped by
-    // path, so each path's segment is sorted on its own
-    if ((st = ensure(h->path_start, 4 * ((size_t)h->P + 1)))) return st;
-    L += launch_segment_sort(h->curves.as<CurveDesc>(), h->C, h->P, h->offsets.as<uint32_t>(),
-                             h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), h->skey[1].as<uint64_t>(),
-                             h->sval[1].as<uint32_t>(), h->path_start.as<uint32_t>(), s);
-    h->skey_sorted = h->skey[1].as<uint64_t>();
-    h->perm_sorted = h->sval[1].as<uint32_t>();
+    // stage 8: stable sort by (path, cell key).  The entries arrive grouped by
+    // path, so with enough paths to fill the GPU each path's segment is
+    // sorted on its own by one block; frames of few (hence long) paths take
+    // the device-wide LSD radix sort, whose work does not depend on them.
     int rl = 0;
+    if (h->P >= kSegmentSortMinPaths && nf / std::max<int64_t>(h->P, 1) <= kSegmentSortMaxMean) {
+        if ((st = ensure(h->path_start, 4 * ((size_t)h->P + 1)))) return st;
+        L += launch_segment_sort(h->curves.as<CurveDesc>(), h->C, h->P, h->offsets.as<uint32_t>(),
+                                 h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), h->skey[1].as<uint64_t>(),
+                                 h->sval[1].as<uint32_t>(), h->path_start.as<uint32_t>(), s);
+        h->skey_sorted = h->skey[1].as<uint64_t>();
+        h->perm_sorted = h->sval[1].as<uint32_t>();
+    } else {
+        const int key_bits = 24 + bits_for(h->P ? h->P - 1 : 0);
+        const bool alt = radix_sort<uint64_t>(h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(),
+                                              h->skey[1].as<uint64_t>(), h->sval[1].as<uint32_t>(), nf, key_bits,
+                                              h->sort_tmp.as<uint32_t>(), s, &rl);
+        L += rl;
+        h->skey_sorted = alt ? h->skey[1].as<uint64_t>() : h->skey[0].as<uint64_t>();
+        h->perm_sorted = alt ? h->sval[1].as<uint32_t>() : h->sval[0].as<uint32_t>();
+    }
     rec(h, 4, s);
     // stages 9-12, 14: winding scan, marks, draw list
     cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);

@@ -309,11 +309,30 @@ def test_256_samples_modes_and_limits(srgb):
             b.set_scenes([(scene, 64, 64, 256)])
 
 
+def concat(a, b):
+    """Scene a's paths followed by scene b's."""
+    P, V = a.n_paths, a.n_vertices
+    return spr.Scene(np.concatenate([a.vertex, b.vertex]), np.concatenate([a.vertex_path_id, b.vertex_path_id + P]),
+                     np.concatenate([a.curve_vertex_pos, b.curve_vertex_pos + V]),
+                     np.concatenate([a.curve_type, b.curve_type]),
+                     np.concatenate([a.curve_path_id, b.curve_path_id + P]),
+                     np.concatenate([a.curve_arc_w, b.curve_arc_w]),
+                     np.concatenate([a.path_fill_rule, b.path_fill_rule]),
+                     np.concatenate([a.path_fill_rgba, b.path_fill_rgba]))
+
+
 def test_long_path_segments():
-    """Paths of 145k-338k entries each: the fragment sort's long-segment
-    passes (chunked through global memory) against the oracle's stable
-    sort, every stage exact."""
+    """The fragment sort on long paths, against the oracle's stable sort with
+    every stage exact: a frame of a few paths of 145k-338k entries each (the
+    device-wide radix sort), and 1,100 short paths with three of 29k-36k
+    entries (one block per path; the long ones chunked through global
+    memory)."""
     for W in (1024, 2048):
         sc = spr.Scene.generate(spr.SCENE_RANDOM, seed=77, width=W, height=W, n_paths=4, seg_min=300, seg_max=400)
         counts, _ = check_parity(sc, W, W, samples=8)
         assert counts["curve_fragment"] > 500_000
+    many = spr.Scene.generate(spr.SCENE_MIXED, seed=91, width=1024, height=1024, n_paths=1100, n_large=12)
+    longp = spr.Scene.generate(spr.SCENE_RANDOM, seed=5, width=1024, height=1024, n_paths=3, seg_min=60, seg_max=90)
+    sc = concat(many, longp)
+    counts, _ = check_parity(sc, 1024, 1024, samples=8)
+    assert counts["path"] > 1024 and counts["curve_fragment"] > 550_000
