@@ -116,6 +116,10 @@ struct spr_handle {
     // reverse transform (pixel -> scene) of their coordinates
     DevBuf grad_table, grad_ramp;
     DevBuf path_start;  // first curve of every path (the per-path segment sort)
+    // launch choices (spr_autotune; -1 / 0 = the built-in rule): fragment
+    // sort (0 device-wide radix, 1 per-path segments), curve-emission order
+    // (0 off, 1 on), resolve blocks per SM
+    int tune_sort = -1, tune_emit = -1, tune_bps = 0;
     uint32_t n_grad = 0;
     float rev[13] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
     // raw curve arrays of the device-side scene upload (kept for vertex updates)
@@ -219,6 +223,7 @@ FrameArgs make_args(const spr_handle *h) {
     a.n_grad = h->n_grad;
     a.grad_ramp = h->grad_ramp.as<uint32_t>();
     std::memcpy(a.rev, h->rev, sizeof(a.rev));
+    a.resolve_bps = h->tune_bps;
     if (h->cfg.samples == 256) {  // the current pass of 32 samples
         a.S = 32;
         a.pass_dy = pass_shift_256(h->pass);
@@ -725,7 +730,7 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     rec(h, 2, s);
     // emission order: curves sorted by estimated cost (16-bit keys, two passes)
     const uint32_t *order = nullptr;
-    if (h->C >= 4096) {
+    if (h->tune_emit >= 0 ? h->tune_emit == 1 : h->C >= 4096) {
         if ((st = ensure(h->ekey[0], 4 * (size_t)h->C)) || (st = ensure(h->ekey[1], 4 * (size_t)h->C)) ||
             (st = ensure(h->eval[0], 4 * (size_t)h->C)) || (st = ensure(h->eval[1], 4 * (size_t)h->C)) ||
             (st = ensure(h->sort_tmp, 4 * (size_t)std::max(radix_tmp_words(nf), radix_tmp_words(h->C)))))
@@ -748,7 +753,10 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     // sorted on its own by one block; frames of few (hence long) paths take
     // the device-wide LSD radix sort, whose work does not depend on them.
     int rl = 0;
-    if (h->P >= kSegmentSortMinPaths && nf / std::max<int64_t>(h->P, 1) <= kSegmentSortMaxMean) {
+    const bool segment_sort = h->tune_sort >= 0 ? h->tune_sort == 1
+                                                : h->P >= kSegmentSortMinPaths &&
+                                                      nf / std::max<int64_t>(h->P, 1) <= kSegmentSortMaxMean;
+    if (segment_sort && h->P > 0) {
         if ((st = ensure(h->path_start, 4 * ((size_t)h->P + 1)))) return st;
         L += launch_segment_sort(h->curves.as<CurveDesc>(), h->C, h->P, h->offsets.as<uint32_t>(),
                                  h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), h->skey[1].as<uint64_t>(),
@@ -1003,6 +1011,86 @@ int spr_set_rev_transform(spr_handle *h, const float ctx[13]) {
     if (!h || !ctx) return SPR_ERR_INVALID_ARG;
     drop_graph(h);
     std::memcpy(h->rev, ctx, sizeof(h->rev));
+    return SPR_OK;
+}
+
+namespace {
+// Mean device time of `frames` frames (after one untimed frame).
+int time_frames(spr_handle *h, void *stream, int frames, float *ms) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int st = frame(h, stream, nullptr);
+    if (st) return st;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return cuda_status();
+    cudaEventRecord(e0, s);
+    for (int i = 0; i < frames && !st; ++i) st = frame(h, stream, nullptr);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / (float)frames;
+    return st ? st : cuda_status();
+}
+}  // namespace
+
+int spr_autotune(spr_handle *h, int32_t frames, void *stream, spr_tune *out) {
+    if (!h || frames < 1) return SPR_ERR_INVALID_ARG;
+    if (!h->has_scene) return SPR_ERR_NO_SCENE;
+    cudaSetDevice(h->cfg.device);
+    drop_graph(h);
+    const bool timing = h->timing;
+    h->timing = false;
+    h->tune_sort = h->tune_emit = -1;
+    h->tune_bps = 0;
+    float base = 0.f;
+    int st = time_frames(h, stream, frames, &base);
+    // one choice at a time, the others at their best so far
+    int best_sort = -1, best_emit = -1, best_bps = 0;
+    float best = base;
+    for (int v = 0; v <= 1 && !st; ++v) {
+        h->tune_sort = v;
+        float t = 0.f;
+        if ((st = time_frames(h, stream, frames, &t))) break;
+        if (t < best) best = t, best_sort = v;
+    }
+    h->tune_sort = best_sort;
+    for (int v = 0; v <= 1 && !st; ++v) {
+        h->tune_emit = v;
+        float t = 0.f;
+        if ((st = time_frames(h, stream, frames, &t))) break;
+        if (t < best) best = t, best_emit = v;
+    }
+    h->tune_emit = best_emit;
+    for (int v = 2; v <= 3 && !st; ++v) {  // 4 is the default
+        h->tune_bps = v;
+        float t = 0.f;
+        if ((st = time_frames(h, stream, frames, &t))) break;
+        if (t < best) best = t, best_bps = v;
+    }
+    h->tune_bps = best_bps;
+    h->timing = timing;
+    if (st) return st;
+    if (out) {
+        out->sort = best_sort;
+        out->emit_order = best_emit;
+        out->resolve_bps = best_bps;
+        out->frame_ms = best;
+        out->default_ms = base;
+    }
+    return SPR_OK;
+}
+
+int spr_set_tuning(spr_handle *h, const spr_tune *t) {
+    if (!h || !t) return SPR_ERR_INVALID_ARG;
+    if (t->sort < -1 || t->sort > 1 || t->emit_order < -1 || t->emit_order > 1 || t->resolve_bps < 0 ||
+        t->resolve_bps > 4)
+        return SPR_ERR_INVALID_ARG;
+    drop_graph(h);
+    h->tune_sort = t->sort;
+    h->tune_emit = t->emit_order;
+    h->tune_bps = t->resolve_bps;
     return SPR_OK;
 }
 

@@ -123,6 +123,7 @@ struct FrameArgs {
     uint32_t n_grad;
     const uint32_t *grad_ramp;
     float rev[13];
+    int resolve_bps;  // resolve blocks per SM (1..4; 0 = the default 4)
 };
 
 int launch_transform(const FrameArgs &a, float2 *tvert, uint32_t *path_flags, uint8_t *path_visible,

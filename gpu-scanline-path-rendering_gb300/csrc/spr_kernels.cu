@@ -1321,7 +1321,8 @@ int sm_count() {
 
 int64_t resolve_blocks(const FrameArgs &a) {
     const int64_t need = (a.n_bins + kResolveWarps - 1) / kResolveWarps;
-    return std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sm_count() * kResolveBlocksPerSM));
+    const int bps = a.resolve_bps >= 1 && a.resolve_bps <= kResolveBlocksPerSM ? a.resolve_bps : kResolveBlocksPerSM;
+    return std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sm_count() * bps));
 }
 
 template <int S, bool MS, bool SRGB, bool GRAD>

@@ -97,6 +97,14 @@ class RvgInfo(C.Structure):
                 "height": self.height, "n_elements": self.n_elements, "n_gradient_paths": self.n_gradient_paths}
 
 
+class Tune(C.Structure):
+    _fields_ = [("sort", C.c_int32), ("emit_order", C.c_int32), ("resolve_bps", C.c_int32),
+                ("frame_ms", C.c_float), ("default_ms", C.c_float)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class VgInfo(C.Structure):
     _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
                 ("n_contours", C.c_int32)]
@@ -159,6 +167,8 @@ def lib() -> C.CDLL:
         L.spr_scene_gradients.argtypes = [vp, C.POINTER(vp), u32p, C.POINTER(vp), u32p]
         L.spr_set_gradients.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32]
         L.spr_set_rev_transform.argtypes = [vp, C.POINTER(C.c_float)]
+        L.spr_autotune.argtypes = [vp, i32, vp, C.POINTER(Tune)]
+        L.spr_set_tuning.argtypes = [vp, C.POINTER(Tune)]
         L.spr_vg_load.argtypes = [C.c_char_p, C.POINTER(vp), C.POINTER(VgInfo)]
         L.spr_vg_save.argtypes = [vp, i32, i32, C.c_char_p]
         L.spr_scene_from_view.argtypes = [C.POINTER(SceneView), C.POINTER(vp)]
@@ -390,6 +400,16 @@ class VGRasterizer:
         check(lib().spr_set_gradients(self._h, table.ctypes.data, len(table) // 12, ramp.ctypes.data, len(ramp)),
               "spr_set_gradients")
         self._grad = (table, ramp)
+
+    def autotune(self, frames=3, stream=None) -> dict:
+        """Times the launch choices on the current scene and keeps the fastest."""
+        t = Tune()
+        check(lib().spr_autotune(self._h, int(frames), stream, C.byref(t)), "spr_autotune")
+        return t.as_dict()
+
+    def set_tuning(self, sort=-1, emit_order=-1, resolve_bps=0):
+        t = Tune(sort, emit_order, resolve_bps, 0.0, 0.0)
+        check(lib().spr_set_tuning(self._h, C.byref(t)), "spr_set_tuning")
 
     def set_rev_transform(self, ctx):
         c = np.ascontiguousarray(ctx, dtype=np.float32).reshape(13)

@@ -186,6 +186,28 @@ int spr_set_transform(spr_handle *h, const float m[16]);
  * from sRGB first under sRGB blending.  table = NULL clears. */
 int spr_set_gradients(spr_handle *h, const uint32_t *table, uint32_t n_entries, const uint32_t *ramp,
                       uint32_t n_texels);
+/* ---- launch tuning (an extension) --------------------------------------------
+ * Launch choices that change speed, never results: the fragment sort (0 =
+ * device-wide LSD radix, 1 = one block per path segment), the curve-emission
+ * order by estimated cost (0 off, 1 on) and the resolve's blocks per SM
+ * (1-4).  -1 / 0 select the built-in rule (segment sort for frames of at
+ * least 1,024 paths averaging at most 2,048 entries; emission order from
+ * 4,096 curves; 4 blocks per SM).  spr_autotune times `frames` frames of
+ * the handle's scene under each choice, one choice at a time with the
+ * others at their best so far, keeps the fastest (built-in rules on ties)
+ * and reports it with the built-in rules' time.  Both drop a captured
+ * graph. */
+typedef struct spr_tune {
+    int32_t sort;
+    int32_t emit_order;
+    int32_t resolve_bps;
+    float frame_ms;   /* spr_autotune: the kept choices' mean frame time */
+    float default_ms; /* spr_autotune: the built-in rules' mean frame time */
+} spr_tune;
+
+int spr_autotune(spr_handle *h, int32_t frames, void *stream, spr_tune *out);
+int spr_set_tuning(spr_handle *h, const spr_tune *t);
+
 /* setRevTransform (ras_base.cpp:595-611): screen -> scene for gradient
  * coordinates, ctx = rx[3], ry[3], rw[3], rp[3], a: rd = rx X + ry Y + rw,
  * scene = rp + (a / rd.z) rd.  Identity by default. */

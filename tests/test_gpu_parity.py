@@ -336,3 +336,29 @@ def test_long_path_segments():
     sc = concat(many, longp)
     counts, _ = check_parity(sc, 1024, 1024, samples=8)
     assert counts["path"] > 1024 and counts["curve_fragment"] > 550_000
+
+
+def test_tuning_changes_speed_not_results():
+    """Every launch choice (fragment sort, emission order, resolve blocks per
+    SM) gives the same image and stages; spr_autotune keeps one no slower
+    than the built-in rules."""
+    W = H = 384
+    sc = spr.Scene.generate(spr.SCENE_MIXED, seed=17, width=W, height=H, n_paths=1500, n_large=6,
+                            with_rational=True)
+    with render(sc, W, H, 32) as r:
+        ref = r.read_image().copy()
+        perm = r.dump("SORT_PERM").copy()
+        for sort in (0, 1):
+            for emit in (0, 1):
+                for bps in (1, 3):
+                    r.set_tuning(sort, emit, bps)
+                    r.rasterize()
+                    assert np.array_equal(r.read_image(), ref), (sort, emit, bps)
+                    assert np.array_equal(r.dump("SORT_PERM"), perm)
+        t = r.autotune(frames=2)
+        assert t["sort"] in (-1, 0, 1) and t["emit_order"] in (-1, 0, 1) and t["resolve_bps"] in (0, 2, 3)
+        assert 0 < t["frame_ms"] <= t["default_ms"]
+        r.rasterize()
+        assert np.array_equal(r.read_image(), ref)
+        with pytest.raises(spr.SprError):
+            r.set_tuning(2, 0, 0)
