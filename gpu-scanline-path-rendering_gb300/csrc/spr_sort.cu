@@ -346,6 +346,91 @@ __device__ __forceinline__ void seg_stage_chunk(SegSmem &sm, const uint32_t (&kk
     __syncthreads();
 }
 
+// Segments of up to kWarpSeg entries: one warp each, three 8-bit passes in
+// the warp's own shared memory (no block barriers).  Lane l ranks entry
+// 32c + l of every chunk c; the warp's digit counters make the ranks stable.
+constexpr int kWarpSeg = 256;
+constexpr int kSmallWarps = 8;
+
+__global__ void __launch_bounds__(kSmallWarps * 32) k_segment_sort_small(const uint64_t *__restrict__ keys_in,
+                                                                        const uint32_t *__restrict__ start,
+                                                                        const uint32_t *__restrict__ offsets,
+                                                                        uint32_t P, uint64_t *__restrict__ keys_out,
+                                                                        uint32_t *__restrict__ vals_out) {
+    __shared__ uint32_t skey[kSmallWarps][2][kWarpSeg], sval[kSmallWarps][2][kWarpSeg], shist[kSmallWarps][256];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t p = blockIdx.x * kSmallWarps + w;
+    if (p >= P) return;
+    const uint32_t b = offsets[start[p]], e = offsets[start[p + 1]];
+    if (e <= b || e - b > (uint32_t)kWarpSeg) return;
+    const int n = (int)(e - b);
+    const uint64_t hi = (uint64_t)p << 24;
+    for (int i = lane; i < n; i += 32) {
+        skey[w][0][i] = (uint32_t)keys_in[b + i] & 0xFFFFFFu;
+        sval[w][0][i] = b + (uint32_t)i;
+    }
+    __syncwarp();
+    int cur = 0;
+    const int nch = (n + 31) >> 5;
+    for (int shift = 0; shift < 24; shift += 8) {
+        const uint32_t d0 = (skey[w][cur][0] >> shift) & 0xFFu;
+        bool diff = false;
+        for (int i = lane; i < n; i += 32) diff |= ((skey[w][cur][i] >> shift) & 0xFFu) != d0;
+        if (!__any_sync(0xffffffffu, diff)) continue;  // one digit throughout
+        for (int i = lane; i < 256; i += 32) shist[w][i] = 0u;
+        __syncwarp();
+        uint32_t rk[kWarpSeg / 32];
+#pragma unroll
+        for (int c = 0; c < kWarpSeg / 32; ++c) {
+            if (c >= nch) break;
+            const int i = c * 32 + lane;
+            const bool valid = i < n;
+            const uint32_t d = valid ? (skey[w][cur][i] >> shift) & 0xFFu : 256u + lane;
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            const uint32_t before = __popc(peers & ((1u << lane) - 1u));
+            const uint32_t old = valid ? shist[w][d] : 0u;
+            __syncwarp();
+            if (valid && before == 0) shist[w][d] = old + __popc(peers);
+            __syncwarp();
+            rk[c] = old + before;
+        }
+        // exclusive scan of the 256 digit counts: lane owns digits 8l .. 8l + 7
+        uint32_t loc[8], sum = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            loc[q] = sum;
+            sum += shist[w][lane * 8 + q];
+        }
+        uint32_t inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 8; ++q) shist[w][lane * 8 + q] = inc - sum + loc[q];
+        __syncwarp();
+#pragma unroll
+        for (int c = 0; c < kWarpSeg / 32; ++c) {
+            if (c >= nch) break;
+            const int i = c * 32 + lane;
+            if (i < n) {
+                const uint32_t k = skey[w][cur][i];
+                const uint32_t pos = shist[w][(k >> shift) & 0xFFu] + rk[c];
+                skey[w][cur ^ 1][pos] = k;
+                sval[w][cur ^ 1][pos] = sval[w][cur][i];
+            }
+        }
+        __syncwarp();
+        cur ^= 1;
+    }
+    for (int i = lane; i < n; i += 32) {
+        keys_out[b + i] = hi | skey[w][cur][i];
+        vals_out[b + i] = sval[w][cur][i];
+    }
+}
+
 __global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t *__restrict__ keys_in,
                                                                const uint32_t *__restrict__ start,
                                                                const uint32_t *__restrict__ offsets,
@@ -357,7 +442,7 @@ __global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t p = blockIdx.x;
     const uint32_t b = offsets[start[p]], e = offsets[start[p + 1]];
-    if (e <= b) return;
+    if (e - b <= (uint32_t)kWarpSeg) return;  // empty, or a warp's (k_segment_sort_small)
     const uint32_t n = e - b;
     const uint64_t hi = (uint64_t)p << 24;  // the segment's path bits
     if (n <= (uint32_t)kSegTile) {
@@ -495,8 +580,10 @@ int launch_segment_sort(const CurveDesc *curves, uint32_t C, uint32_t P, const u
     if (P == 0) return 0;
     k_path_starts<<<(unsigned)(((int64_t)C + 1 + 255) / 256), 256, 0, s>>>(curves, C, P, path_start);
     cudaFuncSetAttribute(k_segment_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem));
+    k_segment_sort_small<<<(P + kSmallWarps - 1) / kSmallWarps, kSmallWarps * 32, 0, s>>>(keys, path_start, offsets, P,
+                                                                                      keys_out, vals_out);
     k_segment_sort<<<P, kSegThreads, sizeof(SegSmem), s>>>(keys, path_start, offsets, keys_out, vals_out, keys, vals);
-    return 2;
+    return 3;
 }
 
 int64_t scan_tmp_words(int64_t n) { return (n + kScanTile - 1) / kScanTile + 2; }
