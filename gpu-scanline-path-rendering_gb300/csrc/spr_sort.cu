@@ -349,8 +349,8 @@ __device__ __forceinline__ void seg_stage_chunk(SegSmem &sm, const uint32_t (&kk
 // Segments of up to kWarpSeg entries: one warp each, three 8-bit passes in
 // the warp's own shared memory (no block barriers).  Lane l ranks entry
 // 32c + l of every chunk c; the warp's digit counters make the ranks stable.
-constexpr int kWarpSeg = 256;
-constexpr int kSmallWarps = 8;
+constexpr int kWarpSeg = 512;
+constexpr int kSmallWarps = 4;
 
 __global__ void __launch_bounds__(kSmallWarps * 32) k_segment_sort_small(const uint64_t *__restrict__ keys_in,
                                                                         const uint32_t *__restrict__ start,
