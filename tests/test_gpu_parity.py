@@ -362,3 +362,30 @@ def test_tuning_changes_speed_not_results():
         assert np.array_equal(r.read_image(), ref)
         with pytest.raises(spr.SprError):
             r.set_tuning(2, 0, 0)
+
+
+def test_random_configurations():
+    """Seeded sweep: scene kind, size, path count, sample count (8/16/32/256),
+    output modes, rational segments, per-path affines and a random affine or
+    projective input transform, every stage and the image exact."""
+    rng = np.random.default_rng(2026)
+    kinds = [spr.SCENE_RANDOM, spr.SCENE_MIXED, spr.SCENE_CUBICS, spr.SCENE_LOCAL]
+    for case in range(24):
+        W, H = int(rng.integers(16, 300)), int(rng.integers(16, 300))
+        kind = kinds[case % 4]
+        samples = [8, 16, 32, 256][int(rng.integers(0, 4))]
+        ms = bool(rng.integers(0, 2)) or samples == 256
+        srgb = bool(rng.integers(0, 2))
+        sc = spr.Scene.generate(kind, seed=int(rng.integers(1, 1 << 30)), width=W, height=H,
+                                n_paths=int(rng.integers(1, 80)), n_large=int(rng.integers(0, 3)),
+                                seg_min=3, seg_max=int(rng.integers(4, 24)), with_rational=bool(rng.integers(0, 2)),
+                                with_affine=bool(rng.integers(0, 2)))
+        tf = None
+        if rng.integers(0, 2):
+            tf = np.eye(4, dtype=np.float32)
+            tf[0, :2] = rng.uniform(-1.3, 1.3, 2)
+            tf[1, :2] = rng.uniform(-1.3, 1.3, 2)
+            tf[0, 3], tf[1, 3] = rng.uniform(-20, 60, 2)
+            if rng.integers(0, 3) == 0:
+                tf[3, :2] = rng.uniform(-4e-4, 4e-4, 2)
+        check_parity(sc, W, H, samples, ms, srgb, tf)
