@@ -110,6 +110,15 @@ class VgInfo(C.Structure):
                 ("n_contours", C.c_int32)]
 
 
+class StrokeInfo(C.Structure):
+    _fields_ = [("n_fill_paths", C.c_uint32), ("n_stroke_paths", C.c_uint32), ("n_offset_pieces", C.c_uint32),
+                ("max_depth", C.c_int32)]
+
+
+# spr_stroke_style: one per path
+STROKE_STYLE = np.dtype([("rgba", "<u4"), ("width", "<f4")])
+
+
 class SceneSpec(C.Structure):
     _fields_ = [("kind", C.c_int32), ("seed", C.c_uint64), ("width", C.c_int32),
                 ("height", C.c_int32), ("n_paths", C.c_int32), ("n_large", C.c_int32),
@@ -173,6 +182,7 @@ def lib() -> C.CDLL:
         L.spr_vg_save.argtypes = [vp, i32, i32, C.c_char_p]
         L.spr_scene_from_view.argtypes = [C.POINTER(SceneView), C.POINTER(vp)]
         L.spr_scene_set_gradients.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32]
+        L.spr_stroke_to_fill.argtypes = [C.POINTER(SceneView), vp, C.POINTER(vp), C.POINTER(StrokeInfo)]
         L.spr_set_graph_replay.argtypes = [vp, i32]
         L.spr_graph_replays.argtypes = [vp, C.POINTER(i32)]
         L.spr_batch_set_graph_replay.argtypes = [vp, i32]
@@ -307,6 +317,21 @@ class Scene:
             check(lib().spr_vg_save(h, int(width), int(height), str(path).encode()), "spr_vg_save")
         finally:
             lib().spr_scene_free(h)
+
+    def stroke_to_fill(self, rgba, width):
+        """Stroke-to-fill (spr_stroke_to_fill): rgba and width per path (or
+        one value for all).  Returns (scene, info dict); the gradient paints
+        carry over."""
+        n = self.n_paths
+        st = np.zeros(n, dtype=STROKE_STYLE)
+        st["rgba"] = np.broadcast_to(np.asarray(rgba, dtype=np.uint32), (n,))
+        st["width"] = np.broadcast_to(np.asarray(width, dtype=np.float32), (n,))
+        h, info = C.c_void_p(), StrokeInfo()
+        check(lib().spr_stroke_to_fill(C.byref(self.view()), st.ctypes.data, C.byref(h), C.byref(info)),
+              "spr_stroke_to_fill")
+        out = Scene._take(h)
+        out.gradients = self.gradients
+        return out, {k: int(getattr(info, k)) for k, _ in StrokeInfo._fields_}
 
     @classmethod
     def _take(cls, h) -> "Scene":

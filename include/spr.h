@@ -498,6 +498,38 @@ int spr_scene_set_gradients(spr_scene *s, const uint32_t *table, uint32_t n_entr
 int spr_scene_gradients(const spr_scene *s, const uint32_t **table, uint32_t *n_entries, const uint32_t **ramp,
                         uint32_t *n_texels);
 
+/* ---- stroke-to-fill ------------------------------------------------------ */
+/*
+ * Replaces VGContainer::strokeToOffsetCurve (vg_container.cpp:555-1353) with
+ * the offset-curve approximation of SimpleBezierCurve::segApproxOffsetCurve
+ * (bezier_curve.cpp:548-590): a new library-owned scene in which every input
+ * path with a nonzero fill value keeps its fill path (open contours closed by
+ * a line) and every path with a stroke (rgba != 0, width > 0) is followed by
+ * a nonzero stroke path: per contour, butt caps, the curves offset by
+ * +-width/2 (pieces within 1/32 px at their mid points, at most 128 per curve)
+ * and bevel joins -- the cap and join kinds the reference's code draws.
+ * `rgba` is a fill value like path_fill_rgba (RGBA8 colour, or gradient
+ * entry + 1); width is in the path's own coordinates (per-path affines are
+ * kept).  A contour starts at a path's first curve and wherever a curve's
+ * first vertex differs from the previous curve's last.  styles holds one
+ * entry per input path; a non-finite width is SPR_ERR_INVALID_ARG.  Gradient
+ * tables are not copied: attach them with spr_scene_set_gradients.
+ */
+typedef struct spr_stroke_style {
+    uint32_t rgba;
+    float width;
+} spr_stroke_style;
+
+typedef struct spr_stroke_info {
+    uint32_t n_fill_paths;    /* fill paths kept */
+    uint32_t n_stroke_paths;  /* stroke paths added */
+    uint32_t n_offset_pieces; /* offset curves emitted (caps and joins not counted) */
+    int32_t max_depth;        /* deepest halving level reached (1..8) */
+} spr_stroke_info;
+
+int spr_stroke_to_fill(const spr_scene_view *in, const spr_stroke_style *styles, spr_scene **out,
+                       spr_stroke_info *info);
+
 #ifdef __cplusplus
 }
 #endif
