@@ -47,12 +47,20 @@ __device__ __forceinline__ uint32_t pixel_mask(const uint4 &mm, int S, int k) {
 }
 
 // Bit r of the 2S stacked sample rows of cell column px in a vertical-mask
-// word layout (vertical_mask / vertical_mask2).
+// word layout (vertical_mask / vertical_mask2).  The word is picked by
+// selects: px and r vary by lane, and a lane-dependent array index would
+// put the fragment's masks in local memory.
 template <int S>
 __device__ __forceinline__ uint32_t row_bit(const uint32_t *m, int px, int r) {
-    if constexpr (S == 32) return (m[2 * px + (r >> 5)] >> (r & 31)) & 1u;
-    else if constexpr (S == 16) return (m[px] >> r) & 1u;
-    else return (m[0] >> r) & 1u;
+    if constexpr (S == 32) {
+        const int i = 2 * px + (r >> 5);
+        const uint32_t w = i < 2 ? (i == 0 ? m[0] : m[1]) : (i == 2 ? m[2] : m[3]);
+        return (w >> (r & 31)) & 1u;
+    } else if constexpr (S == 16) {
+        return ((px ? m[1] : m[0]) >> r) & 1u;
+    } else {
+        return (m[0] >> r) & 1u;
+    }
 }
 
 // Curve basis at t: P(t) = sum_j B[j] P_j, and P'(t).
