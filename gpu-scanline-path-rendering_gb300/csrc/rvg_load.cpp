@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "../../include/spr.h"
+#include "gradients.h"
 #include "spr_scene.h"
 
 namespace {
@@ -82,21 +83,144 @@ float srgb_to_linear(float f) { return f <= 0.04045f ? f / 12.92f : std::pow((f 
 
 float linear_to_srgb(float f) { return f <= 0.0031308f ? 12.92f * f : (1.f + 0.055f) * std::pow(f, 1.f / 2.4f) - 0.055f; }
 
-// One painted path's gradient item (TGradientItem, vg_container.h:59-64).
-struct GradItem {
-    float tr[6];
-    int32_t p, n;
-    float focal[4];
-    int32_t mode;
-};
+}  // namespace
+
+namespace spr_grad {
+
+// The paint's gradient item and ramp (rvg.cpp:487-700): the inverse of the
+// paint-to-scene map followed by the gradient's own normalisation, the
+// focal point, and the stops sampled into 2^k texels (16 per smallest stop
+// gap, at most 1024).
+void Builder::paint(bool radial, const float tr[6], float x0, float y0, float x1, float y1, float r,
+                    std::vector<float> k, bool srgb) {
+    float ti[6] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f};
+    float focal[3] = {0.f, 0.f, 0.f};
+    const float det = (float)((double)tr[0] * (double)tr[4] - (double)tr[1] * (double)tr[3]);
+    const float idet = safe_rcp(det);
+    ti[0] = tr[4] * idet;
+    ti[3] = -tr[3] * idet;
+    ti[1] = -tr[1] * idet;
+    ti[4] = tr[0] * idet;
+    ti[2] = -(float)((double)tr[2] * (double)ti[0] + (double)tr[5] * (double)ti[1]);
+    ti[5] = -(float)((double)tr[2] * (double)ti[3] + (double)tr[5] * (double)ti[4]);
+    ti[2] -= x0;
+    ti[5] -= y0;
+    if (radial) {
+        const float ir = safe_rcp(r);
+        for (float &v : ti) v *= ir;
+        focal[0] = (x1 - x0) * ir;
+        focal[1] = (y1 - y0) * ir;
+    } else {
+        float dx = x1 - x0, dy = y1 - y0;
+        const float kk = 2.f / (dx * dx + dy * dy);
+        dx *= kk;
+        dy *= kk;
+        ti[0] = ti[0] * dx + ti[3] * dy;
+        ti[1] = ti[1] * dx + ti[4] * dy;
+        ti[2] = ti[2] * dx + ti[5] * dy;
+        ti[3] = ti[4] = ti[5] = 0.f;
+        ti[2] -= 1.f;
+        focal[0] = -1.f;
+        focal[1] = 0.f;
+    }
+    focal[2] = 1.f - focal[0] * focal[0] - focal[1] * focal[1];
+    if (!(focal[2] > 0.f)) focal[2] = 0.f;
+    if (k.empty()) k.assign(5, 0.f);
+    if (k.size() <= 5) {
+        k.resize(10);
+        std::memcpy(&k[5], &k[0], sizeof(float) * 5);
+        k[0] = 0.f;
+        k[5] = 1.f;
+    }
+    float min_delta = 1.f;
+    for (size_t i = 5; i < k.size(); i += 5) {
+        const float d = k[i] - k[i - 5];
+        if (d > 0.f && d < min_delta) min_delta = d;
+    }
+    int res = (int)(16.f / min_delta);
+    if (res < 1) res = 1;
+    if (res > 1023) res = 1023;
+    res |= res >> 1;
+    res |= res >> 2;
+    res |= res >> 4;
+    res |= res >> 8;
+    res++;
+    Item gi{};
+    std::memcpy(gi.tr, ti, sizeof(ti));
+    std::memcpy(gi.focal, focal, sizeof(focal));
+    gi.mode = radial ? 1 : 0;
+    gi.p = (int32_t)ramp.size();
+    gi.n = res;
+    items.push_back(gi);
+    const float ires = 1.f / (float)(res - 1);
+    size_t pk = 0;
+    for (int i = 0; i < res; ++i) {
+        const float t = (float)i * ires;
+        float t0 = 0.f, t1 = 1.f;
+        while (pk + 10 < k.size()) {
+            t0 = k[pk];
+            t1 = k[pk + 5];
+            if (t > t1 || t0 == t1) pk += 5;
+            else break;
+        }
+        t0 = k[pk];
+        t1 = k[pk + 5];
+        float tl = (t - t0) * safe_rcp(t1 - t0);
+        if (!(tl > 0.f)) tl = 0.f;
+        if (tl > 1.f) tl = 1.f;
+        auto lerp = [](float a, float b, float u) { return a + (b - a) * u; };
+        uint32_t rgba;
+        if (srgb) {  // interpolated in linear light, stored as sRGB
+            auto mix = [](float a, float b, float u) { return a * (1 - u) + b * u; };
+            float c[3];
+            for (int ch = 0; ch < 3; ++ch)
+                c[ch] = linear_to_srgb(mix(srgb_to_linear(k[pk + 1 + ch]), srgb_to_linear(k[pk + 6 + ch]), tl));
+            rgba = f32tou8(c[0]) | (f32tou8(c[1]) << 8) | (f32tou8(c[2]) << 16);
+        } else {
+            rgba = f32tou8(lerp(k[pk + 1], k[pk + 6], tl)) | (f32tou8(lerp(k[pk + 2], k[pk + 7], tl)) << 8) |
+                   (f32tou8(lerp(k[pk + 3], k[pk + 8], tl)) << 16);
+        }
+        rgba += f32tou8(lerp(k[pk + 4], k[pk + 9], tl)) << 24;
+        ramp.push_back(rgba);
+    }
+}
+
+// gradient_table_texture / gradient_ramp_texture: ramps repacked by
+// decreasing length (a ramp of 2^k texels then never crosses a 1024-texel
+// row), 12 words per painted path, (n - 1) / 1024 in word 7.
+void Builder::finish(spr_scene &sc) {
+    const size_t n = items.size();
+    std::vector<size_t> order(n);
+    for (size_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return items[a].n > items[b].n; });
+    sc.grad_ramp.assign((ramp.size() + 1023) / 1024 * 1024, 0u);
+    int32_t pout = 0;
+    for (size_t id : order) {
+        const int32_t p0 = items[id].p;
+        items[id].p = pout;
+        if (items[id].n) {
+            std::memcpy(&sc.grad_ramp[pout], &ramp[p0], sizeof(uint32_t) * items[id].n);
+            pout += items[id].n;
+        }
+    }
+    sc.grad_table.assign(std::max<size_t>(n, 1) * 12, 0u);
+    for (size_t i = 0; i < n; ++i) {
+        std::memcpy(&sc.grad_table[i * 12], &items[i], 12 * sizeof(uint32_t));
+        const float scale = (float)(items[i].n - 1) * (1.f / 1024.f);
+        std::memcpy(&sc.grad_table[i * 12 + 7], &scale, 4);
+    }
+}
+
+}  // namespace spr_grad
+
+namespace {
 
 struct Parser {
     std::istringstream in;
     spr_scene &sc;
     spr_rvg_info &info;
     bool a128, srgb;
-    std::vector<GradItem> items;  // one per painted path
-    std::vector<uint32_t> ramp;   // ramp texels as built, before packing
+    spr_grad::Builder grads;  // one item per painted path
     Parser(const std::string &text, spr_scene &s, spr_rvg_info &i, bool a, bool sr)
         : in(text), sc(s), info(i), a128(a), srgb(sr) {}
 
@@ -115,42 +239,11 @@ struct Parser {
                 line[i] = ' ';
         }
         std::istringstream s0(line.substr(0, ppad)), s1(line.substr(ppad));
-        float tr[6] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f}, ti[6] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f};
-        float focal[3] = {0.f, 0.f, 0.f};
+        float tr[6] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f};
         s1 >> tr[0] >> tr[1] >> tr[2] >> tr[3] >> tr[4] >> tr[5];
-        const float det = (float)((double)tr[0] * (double)tr[4] - (double)tr[1] * (double)tr[3]);
-        const float idet = safe_rcp(det);
-        ti[0] = tr[4] * idet;
-        ti[3] = -tr[3] * idet;
-        ti[1] = -tr[1] * idet;
-        ti[4] = tr[0] * idet;
-        ti[2] = -(float)((double)tr[2] * (double)ti[0] + (double)tr[5] * (double)ti[1]);
-        ti[5] = -(float)((double)tr[2] * (double)ti[3] + (double)tr[5] * (double)ti[4]);
         float x0 = 0.f, y0 = 0.f, x1 = 0.f, y1 = 0.f, r = 0.f;
         s0 >> x0 >> y0 >> x1 >> y1;
-        ti[2] -= x0;
-        ti[5] -= y0;
-        if (radial) {
-            s0 >> r;
-            const float ir = safe_rcp(r);
-            for (float &v : ti) v *= ir;
-            focal[0] = (x1 - x0) * ir;
-            focal[1] = (y1 - y0) * ir;
-        } else {
-            float dx = x1 - x0, dy = y1 - y0;
-            const float k = 2.f / (dx * dx + dy * dy);
-            dx *= k;
-            dy *= k;
-            ti[0] = ti[0] * dx + ti[3] * dy;
-            ti[1] = ti[1] * dx + ti[4] * dy;
-            ti[2] = ti[2] * dx + ti[5] * dy;
-            ti[3] = ti[4] = ti[5] = 0.f;
-            ti[2] -= 1.f;
-            focal[0] = -1.f;
-            focal[1] = 0.f;
-        }
-        focal[2] = 1.f - focal[0] * focal[0] - focal[1] * focal[1];
-        if (!(focal[2] > 0.f)) focal[2] = 0.f;
+        if (radial) s0 >> r;
         // stops: offset and RGBA (alpha times the opacity)
         std::vector<float> k;
         float knot = 0.f;
@@ -159,91 +252,8 @@ struct Parser {
             s0 >> v[0] >> v[1] >> v[2] >> v[3];
             k.insert(k.end(), {knot, v[0], v[1], v[2], v[3] * opacity});
         }
-        if (k.empty()) k.assign(5, 0.f);
-        if (k.size() <= 5) {
-            k.resize(10);
-            std::memcpy(&k[5], &k[0], sizeof(float) * 5);
-            k[0] = 0.f;
-            k[5] = 1.f;
-        }
-        float min_delta = 1.f;
-        for (size_t i = 5; i < k.size(); i += 5) {
-            const float d = k[i] - k[i - 5];
-            if (d > 0.f && d < min_delta) min_delta = d;
-        }
-        int res = (int)(16.f / min_delta);
-        if (res < 1) res = 1;
-        if (res > 1023) res = 1023;
-        res |= res >> 1;
-        res |= res >> 2;
-        res |= res >> 4;
-        res |= res >> 8;
-        res++;
-        GradItem gi{};
-        std::memcpy(gi.tr, ti, sizeof(ti));
-        std::memcpy(gi.focal, focal, sizeof(focal));
-        gi.mode = radial ? 1 : 0;
-        gi.p = (int32_t)ramp.size();
-        gi.n = res;
-        items.push_back(gi);
-        const float ires = 1.f / (float)(res - 1);
-        size_t pk = 0;
-        for (int i = 0; i < res; ++i) {
-            const float t = (float)i * ires;
-            float t0 = 0.f, t1 = 1.f;
-            while (pk + 10 < k.size()) {
-                t0 = k[pk];
-                t1 = k[pk + 5];
-                if (t > t1 || t0 == t1) pk += 5;
-                else break;
-            }
-            t0 = k[pk];
-            t1 = k[pk + 5];
-            float tl = (t - t0) * safe_rcp(t1 - t0);
-            if (!(tl > 0.f)) tl = 0.f;
-            if (tl > 1.f) tl = 1.f;
-            auto lerp = [](float a, float b, float u) { return a + (b - a) * u; };
-            uint32_t rgba;
-            if (srgb) {  // interpolated in linear light, stored as sRGB
-                auto mix = [](float a, float b, float u) { return a * (1 - u) + b * u; };
-                float c[3];
-                for (int ch = 0; ch < 3; ++ch)
-                    c[ch] = linear_to_srgb(mix(srgb_to_linear(k[pk + 1 + ch]), srgb_to_linear(k[pk + 6 + ch]), tl));
-                rgba = f32tou8(c[0]) | (f32tou8(c[1]) << 8) | (f32tou8(c[2]) << 16);
-            } else {
-                rgba = f32tou8(lerp(k[pk + 1], k[pk + 6], tl)) | (f32tou8(lerp(k[pk + 2], k[pk + 7], tl)) << 8) |
-                       (f32tou8(lerp(k[pk + 3], k[pk + 8], tl)) << 16);
-            }
-            rgba += f32tou8(lerp(k[pk + 4], k[pk + 9], tl)) << 24;
-            ramp.push_back(rgba);
-        }
+        grads.paint(radial, tr, x0, y0, x1, y1, r, k, srgb);
         return SPR_OK;
-    }
-
-    // gradient_table_texture / gradient_ramp_texture: ramps repacked by
-    // decreasing length (a ramp of 2^k texels then never crosses a 1024-texel
-    // row), 12 words per painted path, (n - 1) / 1024 in word 7.
-    void finish_gradients() {
-        const size_t n = items.size();
-        std::vector<size_t> order(n);
-        for (size_t i = 0; i < n; ++i) order[i] = i;
-        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return items[a].n > items[b].n; });
-        sc.grad_ramp.assign((ramp.size() + 1023) / 1024 * 1024, 0u);
-        int32_t pout = 0;
-        for (size_t id : order) {
-            const int32_t p0 = items[id].p;
-            items[id].p = pout;
-            if (items[id].n) {
-                std::memcpy(&sc.grad_ramp[pout], &ramp[p0], sizeof(uint32_t) * items[id].n);
-                pout += items[id].n;
-            }
-        }
-        sc.grad_table.assign(std::max<size_t>(n, 1) * 12, 0u);
-        for (size_t i = 0; i < n; ++i) {
-            std::memcpy(&sc.grad_table[i * 12], &items[i], 12 * sizeof(uint32_t));
-            const float scale = (float)(items[i].n - 1) * (1.f / 1024.f);
-            std::memcpy(&sc.grad_table[i * 12 + 7], &scale, 4);
-        }
     }
 
     uint32_t vertex_count() const { return (uint32_t)(sc.vertex.size() / 2); }
@@ -445,7 +455,7 @@ struct Parser {
                 }
                 const uint32_t rgba = to_u8(r) | (to_u8(g) << 8) | (to_u8(b) << 16) | (ca << 24);
                 sc.fill_rgba[path] = (rgba & 0xFF000000u) ? rgba : 0u;
-                items.push_back(GradItem{});  // an empty slot keeps the table indexed by path
+                grads.solid();  // an empty slot keeps the table indexed by path
             } else if (t == "linear" || t == "radial") {
                 const int st = gradient(t == "radial", opacity);
                 if (st) return st;
@@ -455,7 +465,7 @@ struct Parser {
                 return SPR_ERR_INVALID_SCENE;
             }
         }
-        finish_gradients();
+        grads.finish(sc);
         return SPR_OK;
     }
 };

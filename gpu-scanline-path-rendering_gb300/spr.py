@@ -110,6 +110,19 @@ class VgInfo(C.Structure):
                 ("n_contours", C.c_int32)]
 
 
+class SvgInfo(C.Structure):
+    _fields_ = [("view_box", C.c_float * 4), ("width", C.c_int32), ("height", C.c_int32),
+                ("n_paths", C.c_int32), ("n_gradient_paths", C.c_int32), ("n_stroked_paths", C.c_int32)]
+
+    def as_dict(self):
+        return {"view_box": list(self.view_box), "width": self.width, "height": self.height,
+                "n_paths": self.n_paths, "n_gradient_paths": self.n_gradient_paths,
+                "n_stroked_paths": self.n_stroked_paths}
+
+
+SVG_A128, SVG_SRGB_RAMPS, SVG_STROKE_TO_FILL = 1, 2, 4
+
+
 class StrokeInfo(C.Structure):
     _fields_ = [("n_fill_paths", C.c_uint32), ("n_stroke_paths", C.c_uint32), ("n_offset_pieces", C.c_uint32),
                 ("max_depth", C.c_int32)]
@@ -182,6 +195,8 @@ def lib() -> C.CDLL:
         L.spr_vg_save.argtypes = [vp, i32, i32, C.c_char_p]
         L.spr_scene_from_view.argtypes = [C.POINTER(SceneView), C.POINTER(vp)]
         L.spr_scene_set_gradients.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32]
+        L.spr_svg_load.argtypes = [C.c_char_p, i32, C.POINTER(vp), C.POINTER(SvgInfo)]
+        L.spr_svg_parse.argtypes = [C.c_char_p, sz, i32, C.POINTER(vp), C.POINTER(SvgInfo)]
         L.spr_stroke_to_fill.argtypes = [C.POINTER(SceneView), vp, C.POINTER(vp), C.POINTER(StrokeInfo)]
         L.spr_set_graph_replay.argtypes = [vp, i32]
         L.spr_graph_replays.argtypes = [vp, C.POINTER(i32)]
@@ -317,6 +332,28 @@ class Scene:
             check(lib().spr_vg_save(h, int(width), int(height), str(path).encode()), "spr_vg_save")
         finally:
             lib().spr_scene_free(h)
+
+    @staticmethod
+    def _svg_flags(a128, srgb_ramps, stroke_to_fill):
+        return ((SVG_A128 if a128 else 0) | (SVG_SRGB_RAMPS if srgb_ramps else 0) |
+                (SVG_STROKE_TO_FILL if stroke_to_fill else 0))
+
+    @classmethod
+    def load_svg(cls, path, a128=False, srgb_ramps=True, stroke_to_fill=False):
+        """An SVG document (SVG::load + addVg): returns (scene, info dict)."""
+        h, info = C.c_void_p(), SvgInfo()
+        check(lib().spr_svg_load(str(path).encode(), cls._svg_flags(a128, srgb_ramps, stroke_to_fill),
+                                 C.byref(h), C.byref(info)), "spr_svg_load")
+        return cls._take(h), info.as_dict()
+
+    @classmethod
+    def parse_svg(cls, text, a128=False, srgb_ramps=True, stroke_to_fill=False):
+        """An SVG document from a string: returns (scene, info dict)."""
+        b = text.encode() if isinstance(text, str) else bytes(text)
+        h, info = C.c_void_p(), SvgInfo()
+        check(lib().spr_svg_parse(b, len(b), cls._svg_flags(a128, srgb_ramps, stroke_to_fill), C.byref(h),
+                                  C.byref(info)), "spr_svg_parse")
+        return cls._take(h), info.as_dict()
 
     def stroke_to_fill(self, rgba, width):
         """Stroke-to-fill (spr_stroke_to_fill): rgba and width per path (or

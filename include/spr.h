@@ -498,6 +498,38 @@ int spr_scene_set_gradients(spr_scene *s, const uint32_t *table, uint32_t n_entr
 int spr_scene_gradients(const spr_scene *s, const uint32_t **table, uint32_t *n_entries, const uint32_t **ramp,
                         uint32_t *n_texels);
 
+/* ---- SVG documents -------------------------------------------------------- */
+/*
+ * spr_svg_load / spr_svg_parse replace SVG::load (svg_load.cpp:189-1548)
+ * followed by addVg's fill conversion: the top-level <svg> elements' <g>,
+ * <defs>, <path>, <polygon>, <linearGradient>, <radialGradient> and <stop>
+ * elements with inherited fill, fill-rule, fill-opacity, stroke,
+ * stroke-width and transform (matrix, translate, scale; rotate and skew are
+ * ignored as by the reference); path data M L H V C S Q A Z in both cases
+ * with the reference's reading (arcs as cubics); colours rgb(), #rgb,
+ * #rrggbb.  The image is the viewBox's size (width/height when there is no
+ * viewBox) with y flipped.  A stroked path is filled with its stroke colour
+ * (addVg), or with SPR_SVG_STROKE_TO_FILL keeps its fill and gets an outline
+ * path (spr_stroke_to_fill).  Gradient fills get the fill value path + 1 and
+ * a gradient-table entry (spr_scene_gradients), which the reference's SVG
+ * path never builds.  Documents with elements or values the reference cannot
+ * read (rect, circle, ellipse, named colours, rgba(), T commands, style keys
+ * other than stop-color / stop-opacity, objectBoundingBox gradients) return
+ * SPR_ERR_UNSUPPORTED; malformed XML or numbers SPR_ERR_INVALID_SCENE; an
+ * unreadable file SPR_ERR_INVALID_ARG.
+ */
+enum spr_svg_flags { SPR_SVG_A128 = 1, SPR_SVG_SRGB_RAMPS = 2, SPR_SVG_STROKE_TO_FILL = 4 };
+typedef struct spr_svg_info {
+    float view_box[4];         /* x, y, width, height */
+    int32_t width, height;     /* the output size: the viewBox's, as integers */
+    int32_t n_paths;           /* paths in the scene */
+    int32_t n_gradient_paths;  /* paths with a gradient fill */
+    int32_t n_stroked_paths;   /* paths with a stroke colour */
+} spr_svg_info;
+
+int spr_svg_load(const char *path, int32_t flags, spr_scene **out, spr_svg_info *info);
+int spr_svg_parse(const char *text, size_t length, int32_t flags, spr_scene **out, spr_svg_info *info);
+
 /* ---- stroke-to-fill ------------------------------------------------------ */
 /*
  * Replaces VGContainer::strokeToOffsetCurve (vg_container.cpp:555-1353) with
