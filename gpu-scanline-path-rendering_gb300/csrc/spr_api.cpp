@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
@@ -122,6 +123,11 @@ struct spr_handle {
     int tune_sort = -1, tune_emit = -1, tune_bps = 0;
     uint32_t n_grad = 0;
     float rev[13] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
+    // output view (setOutputTransform / enableOutputTransform): the inverse
+    // transform's rows 0, 1, 3 and the view's buffer
+    bool out_tf = false;
+    OutputInverse out_inv{{1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f}};
+    DevBuf output;
     // raw curve arrays of the device-side scene upload (kept for vertex updates)
     DevBuf sc_vpos, sc_type, sc_pid, sc_w, scene_flags;
     bool scene_on_device = false, scene_has_arcw = false;
@@ -1155,6 +1161,74 @@ int spr_read_image(spr_handle *h, uint8_t *host_rgba, void *stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t bytes = 4 * (size_t)h->frame_W * h->frame_H;
     if (cudaMemcpyAsync(host_rgba, h->image.p, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return cuda_status();
+    ++h->host_syncs;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
+    return SPR_OK;
+}
+
+int spr_set_output_transform(spr_handle *h, const float m[16]) {
+    if (!h || !m) return SPR_ERR_INVALID_ARG;
+    // 4x4 inverse by Gauss-Jordan elimination with partial pivoting (double)
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 8; ++c) a[r][c] = c < 4 ? (double)m[4 * r + c] : (c - 4 == r ? 1.0 : 0.0);
+    for (int c = 0; c < 4; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (!(std::fabs(a[piv][c]) > 0.0) || !std::isfinite(a[piv][c])) return SPR_ERR_INVALID_ARG;
+        if (piv != c)
+            for (int k = 0; k < 8; ++k) std::swap(a[c][k], a[piv][k]);
+        const double d = a[c][c];
+        for (int k = 0; k < 8; ++k) a[c][k] /= d;
+        for (int r = 0; r < 4; ++r) {
+            if (r == c) continue;
+            const double f = a[r][c];
+            for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+        }
+    }
+    const int rows[3] = {0, 1, 3}, cols[3] = {0, 1, 3};
+    OutputInverse inv;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            inv.m[3 * i + j] = (float)a[rows[i]][4 + cols[j]];
+            if (!std::isfinite(inv.m[3 * i + j])) return SPR_ERR_INVALID_ARG;
+        }
+    h->out_inv = inv;
+    return SPR_OK;
+}
+
+int spr_enable_output_transform(spr_handle *h, int32_t enable) {
+    if (!h) return SPR_ERR_INVALID_ARG;
+    h->out_tf = enable != 0;
+    return SPR_OK;
+}
+
+int spr_output_device_ptr(spr_handle *h, void **out, void *stream) {
+    if (!h || !out) return SPR_ERR_INVALID_ARG;
+    if (!h->frame_valid) return SPR_ERR_NO_SCENE;
+    if (!h->out_tf) {
+        *out = h->image.p;
+        return SPR_OK;
+    }
+    cudaSetDevice(h->cfg.device);
+    const int64_t n = (int64_t)h->frame_W * h->frame_H;
+    int st = ensure(h->output, 4 * (size_t)std::max<int64_t>(n, 1));
+    if (st) return st;
+    launch_output_view(h->image.as<uint32_t>(), h->output.as<uint32_t>(), h->frame_W, h->frame_H, h->out_inv,
+                       static_cast<cudaStream_t>(stream));
+    *out = h->output.p;
+    return cuda_status();
+}
+
+int spr_read_output(spr_handle *h, uint8_t *host_rgba, void *stream) {
+    if (!h || !host_rgba) return SPR_ERR_INVALID_ARG;
+    void *src = nullptr;
+    int st = spr_output_device_ptr(h, &src, stream);
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t bytes = 4 * (size_t)h->frame_W * h->frame_H;
+    if (cudaMemcpyAsync(host_rgba, src, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return cuda_status();
     ++h->host_syncs;
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
     return SPR_OK;

@@ -160,6 +160,11 @@ int launch_bin_bounds(const uint32_t *pair_key, int64_t n_pairs, uint32_t *bin_s
 int64_t resolve_warps(const FrameArgs &a);
 int64_t resolve_overflow_words(const FrameArgs &a);
 // RGBA8 image of a 256-sample frame from the sums its 8 passes accumulated.
+// Rows 0, 1 and 3 (columns 0, 1, 3) of the output transform's inverse.
+struct OutputInverse {
+    float m[9];
+};
+int launch_output_view(const uint32_t *image, uint32_t *out, int W, int H, const OutputInverse &inv, cudaStream_t s);
 int launch_encode_sums(const FrameArgs &a, const long long *sums, uint32_t *image, int64_t npix, cudaStream_t s);
 int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_mask, const uint32_t *pair_val,
                    const uint32_t *bin_start, const uint32_t *bin_end, uint32_t *image, uint32_t *overflow,

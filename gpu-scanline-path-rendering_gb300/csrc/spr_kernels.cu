@@ -1476,6 +1476,33 @@ int launch_encode_sums(const FrameArgs &a, const long long *sums, uint32_t *imag
     return 1;
 }
 
+// The output view (drawOutputResize with output_scale.{vert,frag}.glsl,
+// ras_base.cpp:760-803): pixel (x, y) shows the image texel nearest to
+// inv * (x + 0.5, y + 0.5, 0, 1) after the divide by w, clamped to the edge
+// (the scale texture's GL_NEAREST / GL_CLAMP_TO_EDGE).  inv holds the
+// inverse transform's rows 0, 1 and 3, columns 0, 1 and 3.
+__global__ void k_output_view(const uint32_t *__restrict__ image, uint32_t *__restrict__ out, int W, int H,
+                              OutputInverse inv) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)W * H) return;
+    const int x = (int)(i % W), y = (int)(i / W);
+    const float px = (float)x + 0.5f, py = (float)y + 0.5f;
+    const float qx = inv.m[0] * px + inv.m[1] * py + inv.m[2];
+    const float qy = inv.m[3] * px + inv.m[4] * py + inv.m[5];
+    const float qw = inv.m[6] * px + inv.m[7] * py + inv.m[8];
+    float u = qx / qw, v = qy / qw;
+    u = fminf(fmaxf(floorf(u), 0.f), (float)(W - 1));  // fmaxf takes 0 for a NaN
+    v = fminf(fmaxf(floorf(v), 0.f), (float)(H - 1));
+    out[i] = image[(int64_t)(int)v * W + (int)u];
+}
+
+int launch_output_view(const uint32_t *image, uint32_t *out, int W, int H, const OutputInverse &inv, cudaStream_t s) {
+    const int64_t n = (int64_t)W * H;
+    if (n <= 0) return 0;
+    k_output_view<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(image, out, W, H, inv);
+    return 1;
+}
+
 int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cudaStream_t s) {
     // non-negative floats up to and a little beyond 1.0, plus the negative zero
     k_selftest_encode<<<4 * 152, 256, 0, s>>>(rt, 0u, 0x3F800100u, bad);

@@ -195,6 +195,10 @@ def lib() -> C.CDLL:
         L.spr_vg_save.argtypes = [vp, i32, i32, C.c_char_p]
         L.spr_scene_from_view.argtypes = [C.POINTER(SceneView), C.POINTER(vp)]
         L.spr_scene_set_gradients.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32]
+        L.spr_set_output_transform.argtypes = [vp, C.POINTER(C.c_float)]
+        L.spr_enable_output_transform.argtypes = [vp, i32]
+        L.spr_output_device_ptr.argtypes = [vp, C.POINTER(vp), vp]
+        L.spr_read_output.argtypes = [vp, vp, vp]
         L.spr_svg_load.argtypes = [C.c_char_p, i32, C.POINTER(vp), C.POINTER(SvgInfo)]
         L.spr_svg_parse.argtypes = [C.c_char_p, sz, i32, C.POINTER(vp), C.POINTER(SvgInfo)]
         L.spr_stroke_to_fill.argtypes = [C.POINTER(SceneView), vp, C.POINTER(vp), C.POINTER(StrokeInfo)]
@@ -498,6 +502,23 @@ class VGRasterizer:
 
     def save_output_to_file(self, path):
         check(lib().spr_save_png(self._h, os.fsencode(str(path))), "spr_save_png")
+
+    def set_output_transform(self, m):
+        """setOutputTransform: row-major 4x4 (the zoomed view, read_output)."""
+        a = np.ascontiguousarray(m, dtype=np.float32).reshape(16)
+        check(lib().spr_set_output_transform(self._h, a.ctypes.data_as(C.POINTER(C.c_float))),
+              "spr_set_output_transform")
+
+    def enable_output_transform(self, f=True):
+        check(lib().spr_enable_output_transform(self._h, int(bool(f))), "spr_enable_output_transform")
+
+    def read_output(self, out=None, stream=None) -> np.ndarray:
+        """The output view of the last image (the image itself when the
+        output transform is off)."""
+        if out is None:
+            out = np.empty((self.height, self.width, 4), dtype=np.uint8)
+        check(lib().spr_read_output(self._h, out.ctypes.data, stream), "spr_read_output")
+        return out
 
     def element_number(self) -> dict:
         e = ElementNumber()

@@ -228,6 +228,23 @@ int spr_image_device_ptr(spr_handle *h, void **out);
  * synchronizes the stream. */
 int spr_read_image(spr_handle *h, uint8_t *host_rgba, void *stream);
 
+/* setOutputTransform / enableOutputTransform (ras_base.cpp:586-593,
+ * ras_base.h:174-175): the reference's zoomed on-screen view of the image
+ * (drawOutputResize, output_scale.{vert,frag}.glsl, ras_base.cpp:760-803).
+ * m is row-major like spr_set_transform; a singular or non-finite inverse is
+ * SPR_ERR_INVALID_ARG.  The view's pixel (x, y) is the image texel nearest to
+ * inverse(m) * (x + 0.5, y + 0.5, 0, 1) after the divide by w, clamped to
+ * the image (GL_NEAREST, GL_CLAMP_TO_EDGE; the coordinate is evaluated per
+ * pixel, which equals GL's interpolation for affine m).  The image itself
+ * (spr_read_image, spr_save_png) stays unzoomed, as saveOutputToFile's.
+ * Off: the view is the image. */
+int spr_set_output_transform(spr_handle *h, const float m[16]);
+int spr_enable_output_transform(spr_handle *h, int32_t enable);
+/* Device pointer of the view of the last image (computed on `stream` when
+ * the transform is on), and its copy to host memory (synchronizes). */
+int spr_output_device_ptr(spr_handle *h, void **out, void *stream);
+int spr_read_output(spr_handle *h, uint8_t *host_rgba, void *stream);
+
 /* saveOutputToFile (ras_base.cpp:1221-1277) without the exit(0): writes the
  * last image as a PNG, flipped vertically and with alpha forced to 255 like
  * the reference. */

@@ -317,3 +317,42 @@ def ref_vertical_mask2(samples, y0, y1) -> np.ndarray:
     out = np.zeros(4, np.int32)
     ref().ref_vertical_mask2(samples, y0, y1, out.ctypes.data)
     return out.view(np.uint32)[: samples // 8]
+
+
+def output_inverse(m):
+    """Rows 0, 1, 3 / columns 0, 1, 3 of the inverse of the row-major 4x4 m,
+    by Gauss-Jordan elimination with partial pivoting in double precision,
+    then rounded to float32 (spr_set_output_transform's arithmetic)."""
+    a = [[float(m[4 * r + c]) for c in range(4)] + [1.0 if k == r else 0.0 for k in range(4)] for r in range(4)]
+    for c in range(4):
+        piv = c
+        for r in range(c + 1, 4):
+            if abs(a[r][c]) > abs(a[piv][c]):
+                piv = r
+        if not abs(a[piv][c]) > 0.0:
+            raise ValueError("singular output transform")
+        a[c], a[piv] = a[piv], a[c]
+        d = a[c][c]
+        a[c] = [v / d for v in a[c]]
+        for r in range(4):
+            if r != c:
+                f = a[r][c]
+                a[r] = [a[r][k] - f * a[c][k] for k in range(8)]
+    return np.array([[a[r][4 + c] for c in (0, 1, 3)] for r in (0, 1, 3)], np.float32)
+
+
+def output_view(image, m):
+    """The output view (drawOutputResize, ras_base.cpp:760-803, with
+    output_scale.vert.glsl / .frag.glsl): pixel (x, y) takes the texel
+    nearest to inverse(m) * (x + 0.5, y + 0.5, 0, 1) / w, clamped to the edge
+    (GL_NEAREST, GL_CLAMP_TO_EDGE).  image: (H, W, 4) uint8."""
+    H, W = image.shape[:2]
+    inv = output_inverse(np.asarray(m, np.float32).reshape(16))
+    py, px = np.meshgrid(np.arange(H, dtype=np.float32) + np.float32(0.5),
+                         np.arange(W, dtype=np.float32) + np.float32(0.5), indexing="ij")
+    q = [(inv[r, 0] * px + inv[r, 1] * py) + inv[r, 2] for r in range(3)]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        u, v = q[0] / q[2], q[1] / q[2]
+    u = np.clip(np.nan_to_num(np.floor(u), nan=0.0), 0, W - 1).astype(np.int64)
+    v = np.clip(np.nan_to_num(np.floor(v), nan=0.0), 0, H - 1).astype(np.int64)
+    return image[v, u]
