@@ -128,6 +128,7 @@ struct spr_handle {
     bool out_tf = false;
     OutputInverse out_inv{{1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f}};
     DevBuf output;
+    DevBuf wn_base;  // batch frames: the winding scan at every scene's first entry
     // raw curve arrays of the device-side scene upload (kept for vertex updates)
     DevBuf sc_vpos, sc_type, sc_pid, sc_w, scene_flags;
     bool scene_on_device = false, scene_has_arcw = false;
@@ -273,6 +274,23 @@ int validate_view(const spr_scene_view *v) {
     return SPR_OK;
 }
 
+// A gradient table and ramp as spr_set_gradients takes them: the ramp in
+// whole 1024-texel rows, every entry's ramp run inside one row.
+int check_gradients(const uint32_t *table, uint32_t n_entries, const uint32_t *ramp, uint32_t n_texels) {
+    if (!table || !ramp || n_texels == 0 || n_texels % 1024 != 0 || n_entries > 0x01000000u)
+        return SPR_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < n_entries; ++i) {
+        const int32_t p = (int32_t)table[12 * i + 6];
+        float scale;
+        std::memcpy(&scale, &table[12 * i + 7], 4);
+        const float n1 = scale * 1024.f;  // ramp length - 1
+        if (!(n1 >= 0.f)) continue;       // solid slot: never sampled
+        if (p < 0 || (uint64_t)p + (uint64_t)n1 >= n_texels || (p & 1023) + (int64_t)n1 > 1023)
+            return SPR_ERR_INVALID_ARG;
+    }
+    return SPR_OK;
+}
+
 int validate_scene(const spr_scene_view *v) {
     int st = validate_view(v);
     if (st) return st;
@@ -349,7 +367,9 @@ int spr_destroy(spr_handle *h) {
                       &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
                       &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
                       &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
-                      &h->eval[1], &h->sc_vpos, &h->sc_type, &h->sc_pid, &h->sc_w, &h->scene_flags};
+                      &h->eval[1], &h->sc_vpos, &h->sc_type, &h->sc_pid, &h->sc_w, &h->scene_flags,
+                      &h->sums, &h->gfill_pass, &h->gtvert_total, &h->grad_table, &h->grad_ramp, &h->path_start,
+                      &h->output, &h->wn_base};
     for (DevBuf *b : bufs) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
@@ -721,7 +741,8 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         (st = ensure(h->wn_scan, (size_t)nf)) || (st = ensure(h->draw, 16 * 2 * (size_t)nf)) ||
         (st = ensure(h->heads, 4 * (size_t)nf)) || (st = ensure(h->flags_tmp, 4 * (size_t)flags_tmp_words(nf))) ||
         (st = ensure(h->merged, 4 * (size_t)WORDS * nf)) ||
-        (batch && (st = ensure(h->item_scene, 4 * 2 * (size_t)nf))))
+        (batch && (st = ensure(h->item_scene, 4 * 2 * (size_t)nf))) ||
+        (batch && (st = ensure(h->wn_base, (size_t)std::max(h->n_scenes, 1)))))
         return st;
     uint32_t *item_scene = batch ? h->item_scene.as<uint32_t>() : nullptr;
     if (dc) {
@@ -783,7 +804,7 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);
     L += launch_scan_mark(a, nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
                      h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, h->counters.as<FrameCounters>(),
-                     h->flags_tmp.as<uint32_t>(), s);
+                     h->flags_tmp.as<uint32_t>(), batch ? h->wn_base.as<int8_t>() : nullptr, s);
     if (!cap) {
         cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
         ++h->host_syncs;
@@ -994,17 +1015,8 @@ int spr_set_gradients(spr_handle *h, const uint32_t *table, uint32_t n_entries, 
         h->n_grad = 0;
         return SPR_OK;
     }
-    if (!ramp || n_texels == 0 || n_texels % 1024 != 0 || n_entries > 0x01000000u) return SPR_ERR_INVALID_ARG;
-    // every entry's ramp run must lie inside one 1024-texel row of the ramp
-    for (uint32_t i = 0; i < n_entries; ++i) {
-        const int32_t p = (int32_t)table[12 * i + 6];
-        float scale;
-        std::memcpy(&scale, &table[12 * i + 7], 4);
-        const float n1 = scale * 1024.f;  // ramp length - 1
-        if (!(n1 >= 0.f)) continue;       // solid slot: never sampled
-        if (p < 0 || (uint64_t)p + (uint64_t)n1 >= n_texels || (p & 1023) + (int64_t)n1 > 1023)
-            return SPR_ERR_INVALID_ARG;
-    }
+    const int chk = check_gradients(table, n_entries, ramp, n_texels);
+    if (chk) return chk;
     cudaSetDevice(h->cfg.device);
     int st = upload(h->grad_table, table, (size_t)12 * n_entries);
     if (!st) st = upload(h->grad_ramp, ramp, n_texels);
@@ -1283,7 +1295,7 @@ int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
                             &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
                             &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
                       &h->eval[1],     &h->sc_vpos,    &h->sc_type,   &h->sc_pid,    &h->sc_w,      &h->scene_flags, &h->sums, &h->gfill_pass,
-                      &h->gtvert_total, &h->grad_table, &h->grad_ramp, &h->path_start};
+                      &h->gtvert_total, &h->grad_table, &h->grad_ramp, &h->path_start, &h->output, &h->wn_base};
     for (const DevBuf *b : bufs) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;
@@ -1409,6 +1421,20 @@ int upload_group(spr_handle *h, const spr_batch_scene *in, const std::vector<int
     std::vector<uint32_t> vpid(V), cvp(C), cpid(C), fill(P), pscene(P);
     std::vector<uint8_t> ctype(C), rule(P);
     std::vector<SceneInfo> info(idx.size());
+    // the scenes' gradient entries and ramps, concatenated: a scene's fill
+    // values 1..n_grad move by the entries before it, its entries' ramp
+    // positions by the texels before it; other values below alpha 1 (which
+    // draw nothing) become 0 so that they do not name another scene's entry
+    std::vector<uint32_t> gtable, gramp;
+    for (int i : idx) {
+        if (!in[i].n_grad) continue;
+        const uint32_t ebase = (uint32_t)(gtable.size() / 12), rbase = (uint32_t)gramp.size();
+        if ((uint64_t)ebase + in[i].n_grad > 0x01000000u) return SPR_ERR_CAPACITY_EXCEEDED;
+        gtable.insert(gtable.end(), in[i].grad_table, in[i].grad_table + 12 * (size_t)in[i].n_grad);
+        for (uint32_t e = 0; e < in[i].n_grad; ++e) gtable[12 * (size_t)(ebase + e) + 6] += rbase;
+        gramp.insert(gramp.end(), in[i].grad_ramp, in[i].grad_ramp + in[i].n_ramp);
+    }
+    uint32_t ebase = 0;
     size_t p0 = 0, c0 = 0, v0 = 0;
     int64_t pix = 0;
     uint32_t bins = 0;
@@ -1426,6 +1452,14 @@ int upload_group(spr_handle *h, const spr_batch_scene *in, const std::vector<int
         if (v.n_paths) {
             std::memcpy(&fill[p0], v.path_fill_rgba, 4 * (size_t)v.n_paths);
             std::memcpy(&rule[p0], v.path_fill_rule, v.n_paths);
+        }
+        if (!gtable.empty()) {
+            for (uint32_t i = 0; i < v.n_paths; ++i) {
+                uint32_t &f = fill[p0 + i];
+                if (f >= 1u && f <= b.n_grad) f += ebase;
+                else if (f < 0x01000000u) f = 0u;
+            }
+            ebase += b.n_grad;
         }
         for (uint32_t i = 0; i < v.n_paths; ++i) {
             pscene[p0 + i] = (uint32_t)k;
@@ -1457,6 +1491,9 @@ int upload_group(spr_handle *h, const spr_batch_scene *in, const std::vector<int
     int st = spr_set_scene(h, &cat);
     if (st) return st;
     if ((st = upload(h->scenes_d, info.data(), info.size())) || (st = upload(h->path_scene, pscene.data(), P)))
+        return st;
+    if ((st = spr_set_gradients(h, gtable.empty() ? nullptr : gtable.data(), (uint32_t)(gtable.size() / 12),
+                                gramp.empty() ? nullptr : gramp.data(), (uint32_t)gramp.size())))
         return st;
     h->scenes_h = info;
     h->n_scenes = (int)info.size();
@@ -1504,6 +1541,7 @@ int spr_batch_set_scenes(spr_batch *b, const spr_batch_scene *scenes, int32_t n)
         if (s.samples == 256 && !b->ms_output) return SPR_ERR_INVALID_ARG;
         int st = validate_scene(&s.scene);
         if (st) return st;
+        if (s.n_grad && (st = check_gradients(s.grad_table, s.n_grad, s.grad_ramp, s.n_ramp))) return st;
     }
     cudaSetDevice(b->device);
     b->rendered = false;

@@ -141,9 +141,11 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
 int64_t flags_tmp_words(int64_t nf);
 // Winding scan, merged-fragment / span marks, draw list and merged heads.
 // item_scene (batch frames only, else null) receives the scene of each draw item.
+// scene_base: n_scenes bytes for batch frames (the winding scan restarts
+// at every scene), else unused.
 int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
                       int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
-                      uint32_t *tmp, cudaStream_t s);
+                      uint32_t *tmp, int8_t *scene_base, cudaStream_t s);
 int launch_stencil(const FrameArgs &a, int64_t nf, int64_t n_merged, const uint64_t *skey, const uint32_t *perm,
                     const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan, const uint32_t *heads,
                     uint32_t *merged_mask, cudaStream_t s);

@@ -1393,20 +1393,55 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
 
 int64_t flags_tmp_words(int64_t nf) { return 2 * ((nf + kFlagTile - 1) / kFlagTile + 2); }
 
+// Batches: the winding scan restarted at every scene's first entry.  A
+// contour left open (the RVG reader's Z adds no segment) leaves a nonzero
+// winding sum on its rows, which the reference's scan carries into the
+// paths after it; across a batch it would also reach the later scenes,
+// which a single-scene render of them does not see.  base[s] = the scan at
+// scene s's first sorted entry (paths, hence scenes, ascend along the
+// sorted entries), then every entry of scene s subtracts it.
+__global__ void k_scene_wn_base(const FrameArgs a, int64_t nf, const uint64_t *__restrict__ skey,
+                                const int8_t *__restrict__ wn_scan, int8_t *__restrict__ base) {
+    const int s = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (s >= a.n_scenes) return;
+    int64_t lo = 0, hi = nf;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if ((int)a.path_scene[(uint32_t)(skey[mid] >> 24)] < s) lo = mid + 1;
+        else hi = mid;
+    }
+    base[s] = lo < nf ? wn_scan[lo] : (int8_t)0;
+}
+
+__global__ void k_wn_rebase(const FrameArgs a, int64_t nf, const uint64_t *__restrict__ skey,
+                            const int8_t *__restrict__ base, int8_t *__restrict__ wn_scan) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x) {
+        const int8_t b = base[a.path_scene[(uint32_t)(skey[i] >> 24)]];
+        if (b) wn_scan[i] = (int8_t)(wn_scan[i] - b);
+    }
+}
+
 int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
                       int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
-                      uint32_t *tmp, cudaStream_t s) {
+                      uint32_t *tmp, int8_t *scene_base, cudaStream_t s) {
     const int64_t ntiles = (nf + kFlagTile - 1) / kFlagTile;
     uint32_t *s0 = tmp, *s1 = tmp + (ntiles + 2);
+    int n = 8;
     k_wn_reduce<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(nf, perm, wn, s0);
     scan_tiles_inplace(s0, ntiles, s);
     k_wn_down<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(nf, perm, wn, s0, wn_scan);
+    if (a.scenes != nullptr && a.n_scenes > 1 && scene_base != nullptr) {
+        k_scene_wn_base<<<grid_for(a.n_scenes), kThreads, 0, s>>>(a, nf, skey, wn_scan, scene_base);
+        k_wn_rebase<<<(unsigned)std::min<int64_t>(grid_for(nf), 152 * 16), kThreads, 0, s>>>(a, nf, skey, scene_base,
+                                                                                          wn_scan);
+        n += 2;
+    }
     k_flags_reduce<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(a, nf, skey, wn_scan, s0, s1);
     scan_tiles_inplace(s0, ntiles, s);
     scan_tiles_inplace(s1, ntiles, s);
     k_flags_down<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(a, nf, ntiles, skey, wn_scan, s0, s1, draw, heads,
                                                             item_scene, counters);
-    return 8;
+    return n;
 }
 
 int launch_stencil(const FrameArgs &a, int64_t nf, int64_t nm, const uint64_t *skey, const uint32_t *perm,

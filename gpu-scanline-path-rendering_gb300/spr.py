@@ -141,7 +141,8 @@ class SceneSpec(C.Structure):
 
 class BatchScene(C.Structure):
     _fields_ = [("scene", SceneView), ("width", C.c_int32), ("height", C.c_int32), ("samples", C.c_int32),
-                ("has_transform", C.c_int32), ("transform", C.c_float * 16)]
+                ("has_transform", C.c_int32), ("transform", C.c_float * 16), ("grad_table", C.c_void_p),
+                ("n_grad", C.c_uint32), ("grad_ramp", C.c_void_p), ("n_ramp", C.c_uint32)]
 
 
 _lib = None
@@ -621,6 +622,11 @@ class Batch:
             tf = it[4] if len(it) > 4 else None
             arr[i].scene = scene.view()
             keep.append(scene)
+            if scene.gradients is not None:
+                t, r = (np.ascontiguousarray(x, dtype=np.uint32) for x in scene.gradients)
+                keep += [t, r]
+                arr[i].grad_table, arr[i].n_grad = t.ctypes.data, len(t) // 12
+                arr[i].grad_ramp, arr[i].n_ramp = r.ctypes.data, len(r)
             arr[i].width, arr[i].height, arr[i].samples = int(w), int(h), int(smp)
             arr[i].has_transform = 0 if tf is None else 1
             if tf is not None:

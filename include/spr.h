@@ -388,6 +388,13 @@ typedef struct spr_batch_scene {
     int32_t samples;       /* 8, 16 or 32                                    */
     int32_t has_transform; /* 1 = transform (row-major 4x4) is applied       */
     float transform[16];
+    /* optional gradient paints of this scene, as spr_set_gradients takes them
+     * (12 words per entry, ramp texels in rows of 1024); n_grad = 0: none.
+     * Fill values 1..n_grad use the scene's own entries. */
+    const uint32_t *grad_table;
+    uint32_t n_grad;
+    const uint32_t *grad_ramp;
+    uint32_t n_ramp;
 } spr_batch_scene;
 /* ms_output and srgb apply to every scene of the batch. */
 int spr_batch_create(int32_t device, int32_t ms_output, int32_t srgb, spr_batch **out);

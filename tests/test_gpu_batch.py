@@ -111,3 +111,46 @@ def test_batch_with_256_samples():
         for i, (sc, W, H, smp) in enumerate(items):
             exp, _ = single(sc, W, H, smp)
             assert np.array_equal(b.read_image(i), exp), f"scene {i} ({smp} spp)"
+
+
+@pytest.mark.parametrize("srgb", [True, False])
+def test_batch_with_gradient_paints(srgb):
+    """Loaded documents with gradient paints (an RVG and an SVG document, the
+    SVG one twice with different sizes) batched with plain scenes, one with
+    alpha-0 fill values that must not pick up another scene's gradient
+    entries: every image byte-identical to its single-scene render."""
+    from test_rvg import DOC as RVG
+    from test_svg import DOC as SVG
+    rvg, ri = spr.Scene.parse_rvg(RVG, srgb_ramps=srgb)
+    svg, si = spr.Scene.parse_svg(SVG, srgb_ramps=srgb)
+    plain = spr.Scene.generate(spr.SCENE_MIXED, seed=4, width=128, height=96, n_paths=20)
+    junk = plain.copy()
+    junk.path_fill_rgba = np.where(np.arange(junk.n_paths) % 2 == 0, np.arange(junk.n_paths) % 5 + 1,
+                                   junk.path_fill_rgba).astype(np.uint32)
+    items = [(rvg, ri["width"], ri["height"], 32, None), (plain, 128, 96, 8, None),
+             (svg, si["width"], si["height"], 8, None), (junk, 128, 96, 32, None),
+             (svg, si["width"], si["height"], 32, None)]
+    with spr.Batch(srgb=srgb) as b:
+        b.set_scenes(items)
+        b.render()
+        for i, (sc, W, H, smp, tf) in enumerate(items):
+            exp, _ = single(sc, W, H, smp, tf, True, srgb)
+            assert np.array_equal(b.read_image(i), exp), i
+
+
+def test_open_contour_does_not_reach_later_scenes():
+    """A contour left open (Z adds no segment in RVG documents) leaves a
+    winding sum on its rows that the single-scene scan carries into later
+    paths of its scene; in a batch it must not reach the next scenes."""
+    L = spr.CURVE_LINEAR
+    opened = spr.Scene(np.array([[5, 5], [40, 5], [40, 5], [40, 40]], np.float32), [0] * 4, [0, 2], [L, L],
+                       [0, 0], [-1, -1], [0], [0xFF0000FF])
+    plain = spr.Scene.generate(spr.SCENE_MIXED, seed=9, width=96, height=64, n_paths=12)
+    items = [(opened, 64, 48, 32, None), (plain, 96, 64, 32, None), (opened, 64, 48, 8, None),
+             (plain, 96, 64, 8, None)]
+    with spr.Batch() as b:
+        b.set_scenes(items)
+        b.render()
+        for i, (sc, W, H, smp, tf) in enumerate(items):
+            exp, _ = single(sc, W, H, smp, tf)
+            assert np.array_equal(b.read_image(i), exp), i
