@@ -154,3 +154,37 @@ def test_open_contour_does_not_reach_later_scenes():
         for i, (sc, W, H, smp, tf) in enumerate(items):
             exp, _ = single(sc, W, H, smp, tf)
             assert np.array_equal(b.read_image(i), exp), i
+
+
+@pytest.mark.parametrize("ms,srgb", [(True, True), (False, False)])
+def test_loaded_documents_across_modes(ms, srgb):
+    """Gradient-painted documents at every sample count of the mode (256 with
+    multisample output only), alone against the oracle and batched against
+    their single renders; and a graph-replayed single frame equal to the
+    eager one."""
+    from test_rvg import DOC as RVG
+    from test_svg import DOC as SVG
+    rvg, ri = spr.Scene.parse_rvg(RVG, srgb_ramps=srgb)
+    svg, si = spr.Scene.parse_svg(SVG, srgb_ramps=srgb, stroke_to_fill=True)
+    counts = (8, 16, 32, 256) if ms else (8, 16, 32)
+    items = []
+    for smp in counts:
+        for sc, info in ((rvg, ri), (svg, si)):
+            W, H = info["width"], info["height"]
+            exp, _ = single(sc, W, H, smp, None, ms, srgb)
+            ref = oracle.run(sc, W, H, samples=smp, ms_output=ms, srgb=srgb)["IMAGE"]
+            assert np.array_equal(exp.reshape(-1), ref), (smp, W)
+            items.append((sc, W, H, smp, None, exp))
+    with spr.Batch(ms_output=ms, srgb=srgb) as b:
+        b.set_scenes([it[:5] for it in items])
+        b.render()
+        for i, it in enumerate(items):
+            assert np.array_equal(b.read_image(i), it[5]), i
+    W, H = ri["width"], ri["height"]
+    with spr.VGRasterizer(W, H, samples=32, ms_output=ms, srgb=srgb) as r:
+        r.add_vg(rvg)
+        r.set_graph_replay(True)
+        for _ in range(3):
+            r.rasterize()
+        assert r.graph_replays() >= 1
+        assert np.array_equal(r.read_image(), items[2 * counts.index(32)][5])
