@@ -389,3 +389,37 @@ def test_random_configurations():
             if rng.integers(0, 3) == 0:
                 tf[3, :2] = rng.uniform(-4e-4, 4e-4, 2)
         check_parity(sc, W, H, samples, ms, srgb, tf)
+
+
+def drop_curves(sc, keep):
+    """The scene with only the curves in `keep` (their vertices stay, so some
+    vertices belong to no curve and some contours are left open)."""
+    keep = np.asarray(keep, bool)
+    out = sc.copy()
+    for f in ("curve_vertex_pos", "curve_type", "curve_path_id", "curve_arc_w"):
+        setattr(out, f, np.ascontiguousarray(getattr(sc, f)[keep]))
+    return out
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_open_contours_and_alpha_zero_fills(seed):
+    """Open contours (winding sums left nonzero on their rows, carried into
+    later paths as the reference's scan does), orphaned vertices and fill
+    values of alpha 0 that are not 0: every stage bit-exact against the
+    oracle, and batched renders equal to the single renders."""
+    rng = np.random.default_rng(seed)
+    sc = spr.Scene.generate(spr.SCENE_MIXED, seed=40 + seed, width=200, height=150, n_paths=30,
+                            with_rational=True, with_affine=seed == 2)
+    sc = drop_curves(sc, rng.random(sc.n_curves) > 0.08)
+    sc.path_fill_rgba = np.where(rng.random(sc.n_paths) < 0.2, rng.integers(1, 0x01000000, sc.n_paths),
+                                 sc.path_fill_rgba).astype(np.uint32)
+    plain = spr.Scene.generate(spr.SCENE_MIXED, seed=50 + seed, width=120, height=90, n_paths=15)
+    for smp, ms in ((8, True), (32, True), (32, False)):
+        check_parity(sc, 200, 150, samples=smp, ms=ms)
+    items = [(sc, 200, 150, 32), (plain, 120, 90, 32), (sc, 200, 150, 8), (plain, 120, 90, 8)]
+    with spr.Batch() as b:
+        b.set_scenes(items)
+        b.render()
+        for i, (s, W, H, smp) in enumerate(items):
+            with render(s, W, H, smp) as r:
+                assert np.array_equal(b.read_image(i), r.read_image()), i
