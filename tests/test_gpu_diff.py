@@ -358,3 +358,20 @@ def test_backward_reuses_the_held_forward_frame():
         r.diff_render(f.data_ptr(), img.data_ptr())
         gf5, gv5, _ = backward(r)
     assert rel(gf4, gf5) < 1e-5 and rel(gv4, gv5) < 1e-5
+
+
+def test_open_contours_against_reference_gradient():
+    """Open contours (winding sums carried past their rows, as in the plain
+    frame) and orphaned vertices: image and gradients against the CPU
+    reference gradient."""
+    from test_gpu_parity import drop_curves
+    W, H = 160, 128
+    sc = spr.Scene.generate(spr.SCENE_MIXED, seed=77, width=W, height=H, n_paths=24, n_large=3, seg_min=6,
+                            seg_max=16, with_rational=True)
+    sc = drop_curves(sc, np.random.default_rng(5).random(sc.n_curves) > 0.1)
+    fill = fills(sc.n_paths, 11)
+    G = np.random.default_rng(12).normal(size=(H, W, 4)).astype(np.float32)
+    img, gf, gv, _ = gpu_diff(sc, W, H, fill, G, 16)
+    ref_img, ref = oracle.diff(sc, W, H, fill, grad_image=G, samples=16)
+    assert np.abs(img - ref_img).max() < 1e-5
+    assert rel(gf, ref["fill"]) < REL_TOL and rel(gv, ref["vertex"]) < REL_TOL
