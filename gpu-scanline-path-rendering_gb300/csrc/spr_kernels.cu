@@ -1047,6 +1047,13 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
                 }
                 const float om = 1.f - sa;
                 int n = w.cnt[p];
+                if (sa == 1.f && m == ALL) {
+                    // opaque over every sample: src * 1 + dst * 0 is the source
+                    // whatever dst holds, so one entry blended once stands for
+                    // all (the per-sample blends and the merge give the same)
+                    n = 1;
+                    w.emask[0][p] = ALL;
+                }
                 if (EXPLICIT && n != kFull && frag) {
                     int splits = 0;
                     for (int j = 0; j < n; ++j) {

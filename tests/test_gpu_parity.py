@@ -423,3 +423,15 @@ def test_open_contours_and_alpha_zero_fills(seed):
         for i, (s, W, H, smp) in enumerate(items):
             with render(s, W, H, smp) as r:
                 assert np.array_equal(b.read_image(i), r.read_image()), i
+
+
+@pytest.mark.parametrize("samples,ms,srgb", [(8, True, True), (16, True, False), (32, True, True), (32, False, True),
+                                             (8, False, False)])
+def test_opaque_fills(samples, ms, srgb):
+    """Opaque fills (alpha 255) mixed with translucent ones, over deep
+    overlap: every stage and the image exact against the oracle."""
+    sc = spr.Scene.generate(spr.SCENE_MIXED, seed=91, width=160, height=120, n_paths=60, n_large=6)
+    rng = np.random.default_rng(4)
+    opaque = rng.random(sc.n_paths) < 0.7
+    sc.path_fill_rgba = np.where(opaque, sc.path_fill_rgba | 0xFF000000, sc.path_fill_rgba).astype(np.uint32)
+    check_parity(sc, 160, 120, samples=samples, ms=ms, srgb=srgb)
