@@ -1016,7 +1016,6 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
                   sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
             float sa0 = lin8(c >> 24);
             const bool grad = GRAD && c - 1u < a.n_grad;  // a gradient paint
-            if (!grad && c < 0x01000000u) continue;      // alpha 0: src * 0 + dst * 1 leaves every sample
             const int dx = lane + tx0 - (int)((uint32_t)it.x & 0xFFFFu);
             const uint4 mm = frag ? w.mm[q] : make_uint4(0u, 0u, 0u, 0u);
             // one-entry memo of blend(dst) for this item (same source, same alpha)
