@@ -36,7 +36,7 @@ enum spr_status {
     SPR_ERR_TIMEOUT = 5,           /* a bounded device wait gave up          */
     SPR_ERR_CUDA = 6,              /* any other CUDA runtime error           */
     SPR_ERR_NO_SCENE = 7,          /* render called before spr_set_scene     */
-    SPR_ERR_UNSUPPORTED = 8        /* option not supported by this build     */
+    SPR_ERR_UNSUPPORTED = 8        /* option not supported by this library   */
 };
 
 /* ---- scene model ------------------------------------------------------- */

@@ -24,7 +24,7 @@ RefDim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1}, gridD
 #define _MOCHIMAZUI_VG_CONTAINER_H_  // vg_container.h needs glm; only CT_* are used
 #include "bezier_curve_type.h"
 // ras_define.h's LAUNCH expands to a <<<...>>> launch; the only use compiled
-// here is the GPU table initialisation, which the driver replaces.
+// here is the GPU table initialisation, which this file replaces with host loops.
 #include "ras_define.h"
 #undef LAUNCH
 #define LAUNCH(kernel, N, NT, args) ((void)0)

@@ -4,7 +4,7 @@
 // copied: ref_driver.cpp includes the reference headers where they lie.
 //
 // The shim supplies: empty CUDA execution-space qualifiers, the launch
-// built-ins (threadIdx/blockIdx/blockDim; the driver runs one "thread" per
+// built-ins (threadIdx/blockIdx/blockDim; ref_driver.cpp runs one "thread" per
 // call), the few device intrinsics the headers use (with CUDA's saturating
 // conversion semantics), a point-sampled stand-in for the removed texture
 // reference API, and a float max() with device fmaxf semantics at global
