@@ -1,0 +1,56 @@
+"""Host document readers on damaged input: seeded byte mutations and
+truncations of the test documents must come back as a status (or a valid
+scene), never a crash; deep nesting is refused."""
+import numpy as np
+import pytest
+
+import spr
+from test_rvg import DOC as RVG
+from test_svg import DOC as SVG
+
+
+def mutations(doc, seed, n):
+    rng = np.random.default_rng(seed)
+    b = bytearray(doc.encode())
+    alphabet = b" <>/=\"',.-+eEMLHVCSQAZmlhvcsqaz0123456789()#;:&x\n\t"
+    for _ in range(n):
+        m = bytearray(b)
+        for _ in range(int(rng.integers(1, 6))):
+            i = int(rng.integers(0, len(m)))
+            op = int(rng.integers(0, 3))
+            if op == 0:
+                m[i] = alphabet[int(rng.integers(0, len(alphabet)))]
+            elif op == 1:
+                del m[i]
+            else:
+                m.insert(i, alphabet[int(rng.integers(0, len(alphabet)))])
+        if rng.random() < 0.2:
+            m = m[:int(rng.integers(0, len(m)))]
+        yield bytes(m)
+
+
+@pytest.mark.parametrize("kind", ["svg", "rvg"])
+def test_mutated_documents(kind):
+    doc, parse = (SVG, spr.Scene.parse_svg) if kind == "svg" else (RVG, spr.Scene.parse_rvg)
+    ok = 0
+    for text in mutations(doc, 17 if kind == "svg" else 18, 400):
+        try:
+            sc, _ = parse(text)
+        except spr.SprError as e:
+            assert e.status in (spr.ERR_INVALID_SCENE, spr.ERR_UNSUPPORTED, spr.ERR_INVALID_ARG)
+            continue
+        ok += 1
+        if sc.n_paths:
+            assert spr.lib().spr_validate_scene(sc.view()) == spr.OK
+            assert np.all(np.isfinite(sc.vertex)) or kind == "rvg"
+    assert ok > 0
+
+
+def test_deep_nesting_is_refused():
+    doc = '<svg viewBox="0 0 9 9">' + "<g>" * 300 + '<path d="M0 0 L1 1"/>' + "</g>" * 300 + "</svg>"
+    with pytest.raises(spr.SprError) as e:
+        spr.Scene.parse_svg(doc)
+    assert e.value.status == spr.ERR_INVALID_SCENE
+    doc = '<svg viewBox="0 0 9 9">' + "<g>" * 100 + '<path d="M0 0 L1 0 L0 1 z"/>' + "</g>" * 100 + "</svg>"
+    sc, _ = spr.Scene.parse_svg(doc)
+    assert sc.n_paths == 1
