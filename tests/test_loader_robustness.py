@@ -54,3 +54,30 @@ def test_deep_nesting_is_refused():
     doc = '<svg viewBox="0 0 9 9">' + "<g>" * 100 + '<path d="M0 0 L1 0 L0 1 z"/>' + "</g>" * 100 + "</svg>"
     sc, _ = spr.Scene.parse_svg(doc)
     assert sc.n_paths == 1
+
+
+@pytest.mark.parametrize("suffix", ["vgb", "vgt"])
+def test_mutated_scene_files(tmp_path, suffix):
+    sc, info = spr.Scene.parse_rvg(RVG)
+    f = tmp_path / f"doc.{suffix}"
+    sc.save_vg(f, info["width"], info["height"])
+    data = f.read_bytes()
+    rng = np.random.default_rng(23)
+    ok = 0
+    for _ in range(300):
+        m = bytearray(data)
+        for _ in range(int(rng.integers(1, 8))):
+            i = int(rng.integers(0, len(m)))
+            m[i] = int(rng.integers(0, 256)) if suffix == "vgb" else b"0123456789 -.e\n"[int(rng.integers(0, 15))]
+        if rng.random() < 0.3:
+            m = m[:int(rng.integers(0, len(m)))]
+        f.write_bytes(bytes(m))
+        try:
+            back, _ = spr.Scene.load_vg(f)
+        except spr.SprError as e:
+            assert e.status in (spr.ERR_INVALID_SCENE, spr.ERR_UNSUPPORTED, spr.ERR_INVALID_ARG,
+                                spr.ERR_OUT_OF_MEMORY)
+            continue
+        ok += 1
+        assert spr.lib().spr_validate_scene(back.view()) == spr.OK
+    assert ok > 0
