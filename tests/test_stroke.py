@@ -230,3 +230,30 @@ def test_gpu_parity_on_stroked_scenes(samples):
             r.add_vg(sc)
             r.rasterize()
             assert np.array_equal(r.read_image().reshape(-1), ref)
+
+
+def test_degenerate_curves():
+    """Zero-length and collinear curves, coincident control points, huge and
+    tiny widths: finite closed outlines (or an error status), never NaN."""
+    rng = np.random.default_rng(31)
+    kinds = [(L, 2), (Q, 3), (CU, 4), (R, 3)]
+    for trial in range(200):
+        curves = []
+        p = rng.integers(0, 4, 2).astype(np.float32) * 5
+        for _ in range(int(rng.integers(1, 5))):
+            k, n = kinds[int(rng.integers(0, 4))]
+            pts = [p] + [rng.integers(0, 4, 2).astype(np.float32) * 5 if rng.random() < 0.6 else p for _ in range(n - 1)]
+            if rng.random() < 0.2:  # collinear
+                d = rng.normal(size=2).astype(np.float32)
+                pts = [p + d * t for t in np.linspace(0, 3, n).astype(np.float32)]
+            curves.append((k, [tuple(map(float, q)) for q in pts], float(rng.uniform(0.2, 3))))
+            p = np.asarray(pts[-1], np.float32)
+        sc = one_path(curves)
+        width = float([1e-3, 0.5, 4.0, 1e4][trial % 4])
+        try:
+            out, _ = sc.stroke_to_fill(RED, width)
+        except spr.SprError as e:
+            assert e.status == spr.ERR_INVALID_SCENE
+            continue
+        assert np.all(np.isfinite(out.vertex))
+        loops(curves_of(out))
