@@ -19,10 +19,16 @@ gradient + backward, and the plain RGBA8 frame, ms), "batched_differentiable"
 backward per scene) and "samples_256" (the 1024x1024 scene at 256 samples
 per pixel beside 32).
 
---impl reference times the CPU oracle -- the C++ restatement of the
+The line's "cpu_baseline" is the CPU oracle -- the C++ restatement of the
 reference pipeline (its own GPU code needs OpenGL, unavailable on this machine)
--- on all host threads, each step a 2048x512 band of the same scene.
-Multi-GPU runs are independent replicas (the path has no exchange step).
+-- rendering the whole 2048x2048 frame once on all host threads.
+
+--impl reference times the same CPU oracle on the same frame with all host
+threads, one 2048x256 row band per step: step k renders rows
+256 (k mod 8) .. 256 (k mod 8) + 255, so every 8 consecutive steps render
+the whole frame once, and the value is the pixels of the timed steps over
+their time.  Multi-GPU runs are independent replicas (the path has no
+exchange step).
 """
 from __future__ import annotations
 
@@ -46,7 +52,7 @@ UNIT = "Mpix/s"
 WORKLOAD = dict(kind=1, seed=20261203, width=2048, height=2048, n_paths=15000, n_large=5000,
                 seg_min=10, seg_max=40, with_rational=False, with_affine=True)
 SAMPLES, MS_OUTPUT, SRGB = 32, True, True
-BAND = (896, 256)  # CPU sample: rows 896..1151
+BAND_ROWS = 256  # rows per step of the reference arm (the frame in 8 bands)
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 
 
@@ -195,37 +201,80 @@ def peaks():
 
 
 # ------------------------------------------------------------- CPU arm --
-def cpu_sample(scene, steps=1, warmup=0, threads=0):
-    """Oracle on the band sample; returns (Mpix/s, mean ms, cores)."""
+def cpu_frame(scene, threads=0):
+    """The oracle on the whole frame, once; returns (Mpix/s, ms, cores)."""
     import oracle
 
     cores = threads or os.cpu_count()
-    y0, bh = BAND
-    W = WORKLOAD["width"]
-    tf = band_transform(y0)
-    for _ in range(warmup):
-        oracle.time_run(scene, W, bh, SAMPLES, MS_OUTPUT, SRGB, threads=cores, transform=tf)
-    ms = []
-    for _ in range(steps):
-        t, _ = oracle.time_run(scene, W, bh, SAMPLES, MS_OUTPUT, SRGB, threads=cores, transform=tf)
-        ms.append(t)
-    mean = sum(ms) / len(ms)
-    return W * bh / (mean / 1e3) / 1e6, mean, cores
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    t, _ = oracle.time_run(scene, W, H, SAMPLES, MS_OUTPUT, SRGB, threads=cores)
+    return W * H / (t / 1e3) / 1e6, t, cores
+
+
+def cpu_bands(scene, steps, warmup, threads=0):
+    """The oracle one row band per step, cycling through the frame's bands
+    (step k: band k mod n_bands, counted from the first warm-up step);
+    returns (Mpix/s over the timed steps, mean ms per step, cores)."""
+    import oracle
+
+    cores = threads or os.cpu_count()
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    nb = (H + BAND_ROWS - 1) // BAND_ROWS
+    pix, ms = 0, []
+    for k in range(warmup + steps):
+        y0 = (k % nb) * BAND_ROWS
+        bh = min(BAND_ROWS, H - y0)
+        t, _ = oracle.time_run(scene, W, bh, SAMPLES, MS_OUTPUT, SRGB, threads=cores,
+                               transform=band_transform(y0))
+        if k >= warmup:
+            ms.append(t)
+            pix += W * bh
+    return pix / (sum(ms) / 1e3) / 1e6, sum(ms) / len(ms), cores
+
+
+SMALL = dict(kind=0, seed=20261203, width=512, height=512, n_paths=64, seg_min=8, seg_max=32, samples=8)
+
+
+def crossing_accuracy(r, scene, W, H):
+    """The FP64 check of the GPU's crossing points: the TVERTEX and
+    INTERSECTION stages of the frame just rendered by handle `r`, measured by
+    the CPU oracle against exact FP64 crossings (errors along the cut line,
+    px)."""
+    import oracle
+
+    e = oracle.intersection_error(scene, r.dump("TVERTEX"), r.dump("INTERSECTION"), W, H)
+    return {"max_intersection_x_err_px": e["max_err_px"], "mean_err_px": e["mean_err_px"],
+            "crossings": e["n_crossings"], "over_1px": e["n_over_1px"], "not_bracketed": e["n_unbracketed"],
+            "entries_not_matching_walk": e["n_mismatched"]}
+
+
+def small_scene_accuracy(dev):
+    """The small plain-path workload (512x512, 8 spp, 64 paths of 8-32
+    segments) rendered on the GPU, its crossings checked in FP64."""
+    import spr
+
+    w = SMALL
+    sc = spr.Scene.generate(w["kind"], seed=w["seed"], width=w["width"], height=w["height"],
+                            n_paths=w["n_paths"], seg_min=w["seg_min"], seg_max=w["seg_max"])
+    with spr.VGRasterizer(w["width"], w["height"], samples=w["samples"], device=dev.index) as r:
+        r.add_vg(sc)
+        r.rasterize()
+        return crossing_accuracy(r, sc, w["width"], w["height"])
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     scene = make_scene()
-    value, mean_ms, cores = cpu_sample(scene, steps=args.steps, warmup=args.warmup)
-    y0, bh = BAND
-    sample = (f"rows {y0}..{y0 + bh - 1} (a {WORKLOAD['width']}x{bh} band) of the 2048x2048 scene "
-              f"per step, all stages, {cores} threads")
+    value, mean_ms, cores = cpu_bands(scene, args.steps, args.warmup)
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    sample = (f"the {W}x{H} frame in {W}x{BAND_ROWS} row bands, one band per step in order (every "
+              f"{(H + BAND_ROWS - 1) // BAND_ROWS} steps render the whole frame), all stages, {cores} threads")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": workload_config({"sample": sample}),
+            "config": workload_config(),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -614,15 +663,17 @@ def run_ours(args, rank, world, local_rank):
     traffic = per_unit * units if (per_unit is not None and units) else None
     frame_bytes = frame_alg_bytes(counts, scene.n_vertices, scene.n_curves, scene.n_paths, W, H, SAMPLES)
 
-    cpu_value, cpu_ms, cores = cpu_sample(scene, steps=1, warmup=0)
-    y0, bh = BAND
+    cpu_value, cpu_ms, cores = cpu_frame(scene)
+    accuracy = {"large_frame": crossing_accuracy(r, scene, W, H), "small_frame": small_scene_accuracy(dev),
+                "what": "GPU crossing points (FP32) vs exact FP64 crossings of the same curves and cut lines, "
+                        "error along the cut line in px, checked by the CPU oracle"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config({"counts": counts, "resolve_pairs": npairs,
-                                   "host_syncs_per_frame": stats["host_syncs"],
-                                   "device_bytes": stats["device_bytes"]}),
+        "config": workload_config(),
+        "frame": {"counts": counts, "resolve_pairs": npairs, "host_syncs_per_frame": stats["host_syncs"],
+                  "device_bytes": stats["device_bytes"]},
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_max, "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo},
@@ -634,9 +685,9 @@ def run_ours(args, rank, world, local_rank):
                            "frac": frame_bytes / (ms_max / 1e3) / 1e9 / peak, "unit": "GB/s"},
         "step_ms": step_mean,
         "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"rows {y0}..{y0 + bh - 1} (a {W}x{bh} band) of the same scene, "
-                                   f"one frame, all stages, {cores} threads",
+                         "sample": f"the whole {W}x{H} frame once, all stages, {cores} threads",
                          "ms": cpu_ms},
+        "intersection_accuracy": accuracy,
     }
     if not args.no_extras:  # the batched and differentiable rows, on this GPU after the plain frames
         del flush

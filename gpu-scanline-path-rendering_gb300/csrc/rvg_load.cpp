@@ -478,8 +478,14 @@ extern "C" int spr_rvg_parse(const char *text, size_t length, int32_t flags, spr
     spr_scene *s = new (std::nothrow) spr_scene();
     if (!s) return SPR_ERR_OUT_OF_MEMORY;
     spr_rvg_info local{};
-    Parser p(std::string(text, length), *s, local, (flags & SPR_RVG_A128) != 0, (flags & SPR_RVG_SRGB_RAMPS) != 0);
-    const int st = p.run();
+    int st;
+    try {  // no C++ exception crosses the C ABI: an allocation failure is a status
+        Parser p(std::string(text, length), *s, local, (flags & SPR_RVG_A128) != 0,
+                 (flags & SPR_RVG_SRGB_RAMPS) != 0);
+        st = p.run();
+    } catch (const std::bad_alloc &) {
+        st = SPR_ERR_OUT_OF_MEMORY;
+    }
     if (st) {
         delete s;
         return st;
@@ -491,12 +497,17 @@ extern "C" int spr_rvg_parse(const char *text, size_t length, int32_t flags, spr
 
 extern "C" int spr_rvg_load(const char *path, int32_t flags, spr_scene **out, spr_rvg_info *info) {
     if (!path || !out) return SPR_ERR_INVALID_ARG;
-    std::ifstream f(path, std::ios::binary);
-    if (!f) return SPR_ERR_INVALID_ARG;
-    std::ostringstream ss;
-    ss << f.rdbuf();
-    const std::string text = ss.str();
-    return spr_rvg_parse(text.data(), text.size(), flags, out, info);
+    *out = nullptr;
+    try {
+        std::ifstream f(path, std::ios::binary);
+        if (!f) return SPR_ERR_INVALID_ARG;
+        std::ostringstream ss;
+        ss << f.rdbuf();
+        const std::string text = ss.str();
+        return spr_rvg_parse(text.data(), text.size(), flags, out, info);
+    } catch (const std::bad_alloc &) {
+        return SPR_ERR_OUT_OF_MEMORY;
+    }
 }
 
 extern "C" int spr_scene_gradients(const spr_scene *s, const uint32_t **table, uint32_t *n_entries,

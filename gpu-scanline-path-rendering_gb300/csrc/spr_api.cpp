@@ -32,11 +32,21 @@ using namespace spr;
 
 namespace {
 
+// Device bytes held by one handle's buffers and the caller's cap on them
+// (0 = none; spr_set_memory_limit), the counterpart of the reference's fixed
+// arena that throws when it is exhausted (cuda_cached_allocator.h:77-82).
+struct Budget {
+    size_t used = 0;
+    size_t limit = 0;
+};
+
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
+    Budget *budget = nullptr;  // the owning handle's, if any
     void release() {
         if (p) cudaFree(p);
+        if (budget) budget->used -= bytes;
         p = nullptr;
         bytes = 0;
     }
@@ -53,16 +63,24 @@ std::atomic<uint64_t> g_alloc_gen{0};
 int ensure(DevBuf &b, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (b.bytes >= bytes) return SPR_OK;
-    g_alloc_gen.fetch_add(1);
-    b.release();
     size_t want = bytes + bytes / 4;
     want = (want + 255) & ~(size_t)255;
+    if (b.budget && b.budget->limit) {
+        // over the cap even at the exact size: refuse, keeping the old buffer
+        const size_t others = b.budget->used - b.bytes;
+        const size_t exact = (bytes + 255) & ~(size_t)255;
+        if (others + exact > b.budget->limit) return SPR_ERR_OUT_OF_MEMORY;
+        want = std::min(want, b.budget->limit - others);
+    }
+    g_alloc_gen.fetch_add(1);
+    b.release();
     if (cudaMalloc(&b.p, want) != cudaSuccess) {
         cudaGetLastError();
         b.p = nullptr;
         return SPR_ERR_OUT_OF_MEMORY;
     }
     b.bytes = want;
+    if (b.budget) b.budget->used += want;
     return SPR_OK;
 }
 
@@ -164,7 +182,28 @@ struct spr_handle {
     bool timing = false;
     cudaEvent_t ev[kSteps + 1] = {};
     double step_ms[kSteps] = {};
+    Budget budget;
 };
+
+namespace {
+
+// Every device buffer of a handle.
+std::vector<DevBuf *> handle_bufs(spr_handle *h) {
+    return {&h->mask_table, &h->rtables, &h->vertex,   &h->vpid,      &h->curves,  &h->rule,
+                      &h->fill,       &h->affine,  &h->tvert,    &h->pflags,    &h->pvis,    &h->counts,
+                      &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
+                      &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
+                      &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
+                      &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
+                      &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
+                      &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
+                      &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
+                      &h->eval[1], &h->sc_vpos, &h->sc_type, &h->sc_pid, &h->sc_w, &h->scene_flags,
+                      &h->sums, &h->gfill_pass, &h->gtvert_total, &h->grad_table, &h->grad_ramp, &h->path_start,
+                      &h->output, &h->wn_base};
+}
+
+}  // namespace
 
 namespace {
 
@@ -335,6 +374,7 @@ int spr_create(const spr_config *config, spr_handle **out) {
     spr_handle *h = new (std::nothrow) spr_handle();
     if (!h) return SPR_ERR_OUT_OF_MEMORY;
     h->cfg = *config;
+    for (DevBuf *b : handle_bufs(h)) b->budget = &h->budget;
     for (int i = 0; i < 16; ++i) h->m[i] = (i % 5 == 0) ? 1.f : 0.f;
     st = build_tables(h);
     if (!st) {
@@ -358,19 +398,7 @@ int spr_destroy(spr_handle *h) {
     cudaSetDevice(h->cfg.device);
     drop_graph(h);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
-    DevBuf *bufs[] = {&h->mask_table, &h->rtables, &h->vertex,   &h->vpid,      &h->curves,  &h->rule,
-                      &h->fill,       &h->affine,  &h->tvert,    &h->pflags,    &h->pvis,    &h->counts,
-                      &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
-                      &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
-                      &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
-                      &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
-                      &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
-                      &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
-                      &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
-                      &h->eval[1], &h->sc_vpos, &h->sc_type, &h->sc_pid, &h->sc_w, &h->scene_flags,
-                      &h->sums, &h->gfill_pass, &h->gtvert_total, &h->grad_table, &h->grad_ramp, &h->path_start,
-                      &h->output, &h->wn_base};
-    for (DevBuf *b : bufs) b->release();
+    for (DevBuf *b : handle_bufs(h)) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
     for (auto &e : h->ev)
@@ -1279,24 +1307,19 @@ int spr_step_timing(spr_handle *h, double *ms, int32_t capacity, int32_t *n_out)
     return SPR_OK;
 }
 
+int spr_set_memory_limit(spr_handle *h, int64_t bytes) {
+    if (!h || bytes < 0) return SPR_ERR_INVALID_ARG;
+    h->budget.limit = (size_t)bytes;
+    return SPR_OK;
+}
+
 int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
     if (!h || !out) return SPR_ERR_INVALID_ARG;
     out->kernel_launches = h->launches;
     out->host_syncs = h->host_syncs;
     out->resolve_pairs = h->npairs;
     size_t total = 0;
-    const DevBuf *bufs[] = {&h->mask_table, &h->rtables, &h->vertex,   &h->vpid,      &h->curves,  &h->rule,
-                            &h->fill,       &h->affine,  &h->tvert,    &h->pflags,    &h->pvis,    &h->counts,
-                            &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
-                            &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
-                            &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
-                            &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
-                            &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d,
-                            &h->path_scene, &h->item_scene, &h->chord,   &h->lmask,     &h->item_path, &h->tape,
-                            &h->tape_rec,   &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
-                      &h->eval[1],     &h->sc_vpos,    &h->sc_type,   &h->sc_pid,    &h->sc_w,      &h->scene_flags, &h->sums, &h->gfill_pass,
-                      &h->gtvert_total, &h->grad_table, &h->grad_ramp, &h->path_start, &h->output, &h->wn_base};
-    for (const DevBuf *b : bufs) total += b->bytes;
+    for (const DevBuf *b : handle_bufs(h)) total += b->bytes;
     out->device_bytes = (int64_t)total;
     return SPR_OK;
 }

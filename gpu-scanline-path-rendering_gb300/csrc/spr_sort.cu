@@ -10,7 +10,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "../../include/spr.h"
 #include "spr_internal.h"
@@ -650,10 +649,7 @@ template bool radix_sort<uint32_t>(uint32_t *, uint32_t *, uint32_t *, uint32_t 
 // and all calls on a device share it.
 namespace {
 constexpr int64_t kNoAllocMaxTiles = 16384;
-constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) uint32_t g_noalloc_tile_sums[kNoAllocMaxTiles + 2];
-std::mutex g_noalloc_mutex;
-uint32_t *g_noalloc_scratch[kNoAllocMaxDevices] = {};
 }  // namespace
 
 }  // namespace spr
@@ -662,26 +658,20 @@ extern "C" int spr_scan_offsets_noalloc(const uint32_t *d_counts, uint32_t *d_of
     using namespace spr;
     if (n < 0 || !d_offsets || (n > 0 && !d_counts)) return SPR_ERR_INVALID_ARG;
     if (n > kNoAllocMaxTiles * (int64_t)kScanTile) return SPR_ERR_CAPACITY_EXCEEDED;
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess) return SPR_ERR_CUDA;
-    if (dev < 0 || dev >= kNoAllocMaxDevices) return SPR_ERR_UNSUPPORTED;
-    uint32_t *scratch = nullptr;
-    {
-        // First call on this device (current now): look up the device address
-        // of the scratch array.  In host code the array's name is only a
-        // host-side stand-in, so kernels are always given this address.
-        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!g_noalloc_scratch[dev]) {
-            void *p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noalloc_tile_sums) != cudaSuccess || !p) {
-                cudaGetLastError();
-                return SPR_ERR_CUDA;
-            }
-            g_noalloc_scratch[dev] = static_cast<uint32_t *>(p);
-        }
-        scratch = g_noalloc_scratch[dev];
+    // An error left pending by the caller's own earlier work is not this
+    // call's: report it without clearing it and launch nothing.
+    if (cudaPeekAtLastError() != cudaSuccess) return SPR_ERR_CUDA;
+    // The device address of the scratch array in the current context.  In
+    // host code the array's name is only a host-side stand-in, so kernels are
+    // always given this address.  It is looked up on every call (a cheap
+    // lookup once the module is loaded; the first call on a device loads it),
+    // so a device reset or a switch of context between calls is followed.
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_tile_sums) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return SPR_ERR_CUDA;
     }
     // Every tile sum is written before it is read, so nothing needs clearing.
-    scan_exclusive_u32(d_counts, d_offsets, n, scratch, static_cast<cudaStream_t>(stream));
+    scan_exclusive_u32(d_counts, d_offsets, n, static_cast<uint32_t *>(p), static_cast<cudaStream_t>(stream));
     return cudaGetLastError() == cudaSuccess ? SPR_OK : SPR_ERR_CUDA;
 }

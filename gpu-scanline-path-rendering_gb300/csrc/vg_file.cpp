@@ -310,6 +310,10 @@ int to_scene(const Container &c, spr_scene &s) {
                     type != SPR_CURVE_RATIONAL)
                     return SPR_ERR_INVALID_SCENE;
                 if ((uint64_t)c.vertex_index[cu] + (type & 7) > nv) return SPR_ERR_INVALID_SCENE;
+                // every curve owns its vertices, so the curves of all paths together
+                // name at most nv of them: stop before paths that share contours
+                // make the arrays grow past the file's own size
+                if (s.vertex_path_id.size() + (size_t)(type & 7) > nv) return SPR_ERR_INVALID_SCENE;
                 s.curve_vertex_pos.push_back(c.vertex_index[cu]);
                 s.curve_type.push_back((uint8_t)type);
                 s.curve_path_id.push_back(p);
@@ -365,9 +369,8 @@ void from_scene(const spr_scene &s, int32_t width, int32_t height, Container &c)
 
 }  // namespace
 
-extern "C" int spr_vg_load(const char *path, spr_scene **out, spr_vg_info *info) {
-    if (!path || !out) return SPR_ERR_INVALID_ARG;
-    *out = nullptr;
+namespace {
+int vg_load(const char *path, spr_scene **out, spr_vg_info *info) {
     const std::string name(path);
     const bool bin = ends_with(name, "vgb"), txt = ends_with(name, "vgt");
     if (!bin && !txt) return SPR_ERR_INVALID_ARG;
@@ -396,8 +399,7 @@ extern "C" int spr_vg_load(const char *path, spr_scene **out, spr_vg_info *info)
     return SPR_OK;
 }
 
-extern "C" int spr_vg_save(const spr_scene *s, int32_t width, int32_t height, const char *path) {
-    if (!s || !path) return SPR_ERR_INVALID_ARG;
+int vg_save(const spr_scene *s, int32_t width, int32_t height, const char *path) {
     const std::string name(path);
     const bool bin = ends_with(name, "vgb"), txt = ends_with(name, "vgt");
     if (!bin && !txt) return SPR_ERR_INVALID_ARG;
@@ -411,13 +413,7 @@ extern "C" int spr_vg_save(const spr_scene *s, int32_t width, int32_t height, co
     return f ? SPR_OK : SPR_ERR_INVALID_ARG;
 }
 
-extern "C" int spr_scene_from_view(const spr_scene_view *v, spr_scene **out) {
-    if (!v || !out) return SPR_ERR_INVALID_ARG;
-    *out = nullptr;
-    const int st = spr_validate_scene(v);
-    if (st) return st;
-    spr_scene *s = new (std::nothrow) spr_scene();
-    if (!s) return SPR_ERR_OUT_OF_MEMORY;
+int scene_from_view(const spr_scene_view *v, spr_scene *s) {
     s->vertex.assign(v->vertex, v->vertex + 2 * (size_t)v->n_vertices);
     s->vertex_path_id.assign(v->vertex_path_id, v->vertex_path_id + v->n_vertices);
     s->curve_vertex_pos.assign(v->curve_vertex_pos, v->curve_vertex_pos + v->n_curves);
@@ -430,6 +426,48 @@ extern "C" int spr_scene_from_view(const spr_scene_view *v, spr_scene **out) {
     if (v->path_affine) {
         s->affine.assign(v->path_affine, v->path_affine + 6 * (size_t)v->n_paths);
         s->has_affine = true;
+    }
+    return SPR_OK;
+}
+}  // namespace
+
+// The C entry points: no C++ exception crosses the ABI (an allocation failure
+// on a large or hostile file is a status, not std::terminate).
+extern "C" int spr_vg_load(const char *path, spr_scene **out, spr_vg_info *info) {
+    if (!path || !out) return SPR_ERR_INVALID_ARG;
+    *out = nullptr;
+    try {
+        return vg_load(path, out, info);
+    } catch (const std::bad_alloc &) {
+        return SPR_ERR_OUT_OF_MEMORY;
+    }
+}
+
+extern "C" int spr_vg_save(const spr_scene *s, int32_t width, int32_t height, const char *path) {
+    if (!s || !path) return SPR_ERR_INVALID_ARG;
+    try {
+        return vg_save(s, width, height, path);
+    } catch (const std::bad_alloc &) {
+        return SPR_ERR_OUT_OF_MEMORY;
+    }
+}
+
+extern "C" int spr_scene_from_view(const spr_scene_view *v, spr_scene **out) {
+    if (!v || !out) return SPR_ERR_INVALID_ARG;
+    *out = nullptr;
+    const int st = spr_validate_scene(v);
+    if (st) return st;
+    spr_scene *s = new (std::nothrow) spr_scene();
+    if (!s) return SPR_ERR_OUT_OF_MEMORY;
+    int r;
+    try {
+        r = scene_from_view(v, s);
+    } catch (const std::bad_alloc &) {
+        r = SPR_ERR_OUT_OF_MEMORY;
+    }
+    if (r) {
+        delete s;
+        return r;
     }
     *out = s;
     return SPR_OK;

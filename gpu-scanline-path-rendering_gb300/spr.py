@@ -174,6 +174,7 @@ def lib() -> C.CDLL:
         L.spr_enable_step_timing.argtypes = [vp, i32]
         L.spr_step_timing.argtypes = [vp, C.POINTER(C.c_double), i32, C.POINTER(i32)]
         L.spr_get_frame_stats.argtypes = [vp, C.POINTER(FrameStats)]
+        L.spr_set_memory_limit.argtypes = [vp, C.c_int64]
         L.spr_step_name.argtypes = [i32]
         L.spr_step_name.restype = C.c_char_p
         L.spr_debug_dump.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
@@ -535,6 +536,12 @@ class VGRasterizer:
         check(lib().spr_step_timing(self._h, buf, 64, C.byref(n)), "spr_step_timing")
         return {lib().spr_step_name(i).decode(): buf[i] for i in range(n.value)}
 
+    def set_memory_limit(self, nbytes: int):
+        """Cap on the handle's device memory (0 = none); a frame that would
+        need more raises SprError(ERR_OUT_OF_MEMORY) and the handle stays
+        usable."""
+        check(lib().spr_set_memory_limit(self._h, int(nbytes)), "spr_set_memory_limit")
+
     def frame_stats(self) -> dict:
         st = FrameStats()
         check(lib().spr_get_frame_stats(self._h, C.byref(st)), "spr_get_frame_stats")
@@ -658,6 +665,12 @@ class Batch:
         e = ElementNumber()
         check(lib().spr_batch_get_counts(self._h, C.byref(e)), "spr_batch_get_counts")
         return e.as_dict()
+
+    def set_memory_limit(self, nbytes: int):
+        """Cap on the handle's device memory (0 = none); a frame that would
+        need more raises SprError(ERR_OUT_OF_MEMORY) and the handle stays
+        usable."""
+        check(lib().spr_set_memory_limit(self._h, int(nbytes)), "spr_set_memory_limit")
 
     def frame_stats(self) -> dict:
         st = FrameStats()

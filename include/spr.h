@@ -279,6 +279,15 @@ typedef struct spr_frame_stats {
     int64_t device_bytes;    /* device memory held by the handle            */
 } spr_frame_stats;
 int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out);
+/* Cap on the device memory the handle's buffers may hold, in bytes (0 = no
+ * cap, the default).  The counterpart of the reference's fixed-size frame
+ * arena, whose allocator throws when it is exhausted
+ * (cuda_cached_allocator.h:40-115, the throw at :77-82).  A call that would
+ * need more returns SPR_ERR_OUT_OF_MEMORY, as a failed device allocation
+ * does; the handle stays usable (its buffers and scene are kept), and a
+ * later call under a higher cap or none renders normally.  Buffers already
+ * held above a lowered cap are kept until they must grow. */
+int spr_set_memory_limit(spr_handle *h, int64_t bytes);
 /* Name of step i of spr_step_timing (static string, NULL if out of range). */
 const char *spr_step_name(int32_t i);
 
@@ -327,11 +336,14 @@ int spr_selftest(spr_handle *h, int64_t *srgb_encode_mismatches);
  * Its scratch is a fixed 64 KB array compiled into the library, which every
  * GPU that loads the library holds until the process exits.  Limit:
  * n <= 33,554,432 (16384 tiles of 2048 counts); larger n returns
- * SPR_ERR_CAPACITY_EXCEEDED and launches nothing.  The first call on each
- * device looks up the array's device address with that device current; make
- * that first call before any stream capture.  All calls on a device share
- * the one array, so calls that overlap on the GPU (other streams, other host
- * threads) race and must be serialized by the caller.
+ * SPR_ERR_CAPACITY_EXCEEDED and launches nothing.  Every call looks up the
+ * array's device address in the current context (so a device reset or a
+ * change of context between calls is followed); the first call on a device
+ * also loads the array, so make that first call before any stream capture.
+ * A CUDA error already pending from the caller's own work is returned as
+ * SPR_ERR_CUDA, left pending, and nothing is launched.  All calls on a device
+ * share the one array, so calls that overlap on the GPU (other streams, other
+ * host threads) race and must be serialized by the caller.
  */
 int spr_scan_offsets_noalloc(const uint32_t *d_counts, uint32_t *d_offsets, int64_t n, void *stream);
 

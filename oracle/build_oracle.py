@@ -10,6 +10,7 @@ matching the CUDA kernels built with --fmad=false.
 """
 from __future__ import annotations
 
+import os
 import pathlib
 import platform
 import shutil
@@ -17,7 +18,11 @@ import subprocess
 import sys
 
 HERE = pathlib.Path(__file__).resolve().parent
-REFERENCE_SRC = pathlib.Path("/root/reference/gpu-scanline/src")
+# The reference's source tree: SPR_REFERENCE_SRC, or the read-only mount of
+# this build's container by default (absent on machines without it, where
+# build_ref() builds nothing).
+DEFAULT_REFERENCE_SRC = "/root/reference/gpu-scanline/src"
+REFERENCE_SRC = pathlib.Path(os.environ.get("SPR_REFERENCE_SRC", DEFAULT_REFERENCE_SRC))
 CXX = shutil.which("g++") or "g++"
 FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 
@@ -51,9 +56,11 @@ def build_oracle(force=False) -> pathlib.Path:
     return out
 
 
-def build_ref(force=False):
-    """Compiles the reference's intersection and mask code; None if absent."""
-    if not (REFERENCE_SRC / "rasterizer" / "shared" / "ras_cut.h").exists():
+def build_ref(force=False, reference_src=None):
+    """Compiles the reference's intersection and mask code from
+    `reference_src` (default REFERENCE_SRC); None if absent."""
+    src = pathlib.Path(reference_src) if reference_src else REFERENCE_SRC
+    if not (src / "rasterizer" / "shared" / "ras_cut.h").exists():
         return None
     outdir = HERE / "_ref"
     outdir.mkdir(exist_ok=True)
@@ -63,12 +70,19 @@ def build_ref(force=False):
     if force or _stale(out, srcs):
         cuda_inc = "/usr/local/cuda/include"
         _run([CXX, *FLAGS, "-w", "-I", str(HERE / "ref" / "shim_include"), "-I", str(HERE / "ref"),
-              "-I", str(REFERENCE_SRC), "-I", str(REFERENCE_SRC / "rasterizer" / "shared"),
+              "-I", str(src), "-I", str(src / "rasterizer" / "shared"),
               "-I", cuda_inc, "-o", str(out), str(HERE / "ref" / "ref_driver.cpp")])
     return out
 
 
 if __name__ == "__main__":
-    force = "--force" in sys.argv
-    print(build_oracle(force))
-    print(build_ref(force))
+    import argparse
+
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--reference-src", default=None,
+                    help=f"the reference's gpu-scanline/src directory (default: $SPR_REFERENCE_SRC or "
+                         f"{DEFAULT_REFERENCE_SRC})")
+    args = ap.parse_args()
+    print(build_oracle(args.force))
+    print(build_ref(args.force, args.reference_src))

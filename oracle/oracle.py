@@ -75,8 +75,32 @@ def lib() -> C.CDLL:
         L.orc_vertical_mask2.argtypes = [C.c_int32, f, f, vp]
         L.orc_fetch_table_selftest.argtypes = [C.c_int32, C.c_int32, vp]
         L.orc_diff.argtypes = [C.POINTER(spr.SceneView), C.POINTER(OrcConfig), vp, vp, vp, vp, vp, vp]
+        L.orc_intersection_error.argtypes = [C.POINTER(spr.SceneView), vp, vp, C.c_int64, C.c_int32, C.c_int32,
+                                             C.c_int32, C.POINTER(XErr)]
         _lib = L
     return _lib
+
+
+class XErr(C.Structure):
+    _fields_ = [("max_err_px", C.c_double), ("mean_err_px", C.c_double), ("max_resid_px", C.c_double),
+                ("n_crossings", C.c_int64), ("n_over_1px", C.c_int64), ("n_unbracketed", C.c_int64),
+                ("n_mismatched", C.c_int64), ("worst_entry", C.c_int64)]
+
+
+def intersection_error(scene: "spr.Scene", tvertex: np.ndarray, entries: np.ndarray, width, height,
+                       threads=0) -> dict:
+    """FP32 crossing points (the entries' t on the FP32 transformed curves)
+    against the exact FP64 crossings with the same cut lines: the error along
+    the cut line in pixels (max, mean), with counts."""
+    tv = np.ascontiguousarray(tvertex, dtype=np.float32).reshape(-1)
+    en = np.ascontiguousarray(entries, dtype=np.int32).reshape(-1)
+    out = XErr()
+    v = scene.view()
+    st = lib().orc_intersection_error(C.byref(v), tv.ctypes.data, en.ctypes.data, len(en) // 2, width, height,
+                                      threads, C.byref(out))
+    if st != 0:
+        raise spr.SprError(st, "orc_intersection_error")
+    return {n: (float(getattr(out, n)) if t is C.c_double else int(getattr(out, n))) for n, t in XErr._fields_}
 
 
 def have_ref() -> bool:

@@ -1910,3 +1910,223 @@ extern "C" int orc_diff(const spr_scene_view *scene, const orc_config *cfgp, con
     }
     return SPR_OK;
 }
+
+// ------------------------------------ FP64 check of the crossing points --
+// For the benchmark spec's accuracy report: how far the FP32 crossing points of
+// the intersection entries (k_make_intersection_impl_1, ras_cut.h:837-1241,
+// as emitted above) lie from the exact crossings of the same curves with the
+// same cut lines.  The curves are the FP32 transformed vertices; the exact
+// crossing t* solves P_side(t) = c in double on the entry's monotone piece
+// (60 bisection steps, then Newton polish), and the error is measured along
+// the cut line: for a crossing of a horizontal line y = c the x error, for a
+// vertical line x = c the y error, of the point the fragment stage uses (the
+// FP32 curve_coord at the entry's t, flag bits cleared).
+namespace {
+
+double coord_d(int type, double w, const float *v, double t) {
+    const double a = v[0], b = v[1], c = v[2], d = v[3], u = 1.0 - t;
+    switch (type) {
+    case kLinear: return a * u + b * t;
+    case kQuad: return a * u * u + 2.0 * b * u * t + c * t * t;
+    case kCubic: return a * u * u * u + 3.0 * b * u * u * t + 3.0 * c * u * t * t + d * t * t * t;
+    default: {  // rational quadratic with weights (1, w, 1); v[1] is the raw middle coordinate
+        const double num = a * u * u + 2.0 * w * b * u * t + c * t * t;
+        const double den = u * u + 2.0 * w * u * t + t * t;
+        return den != 0.0 ? num / den : 0.0;
+    }
+    }
+}
+
+struct CrossingMeta {
+    float t;      // entry t, flag bits cleared
+    float t0, t1; // the monotone piece (flag bits cleared)
+    float c;      // cut-line coordinate
+    int side;     // 0: vertical line x = c, 1: horizontal line y = c
+    bool crossing;
+};
+
+// emit_curve's walk, recording which solve produced each entry.
+int emit_meta(const CurveGeom &g, int W, int H, std::vector<CrossingMeta> &out) {
+    float t0_ms = 0.f;
+    F2 v0{g.px[0], g.py[0]};
+    for (int ms = 0; ms < g.n_pieces; ++ms) {
+        float traw = g.tcut[ms];
+        F2 v1{curve_coord(g.type, g.w, g.px, traw), curve_coord(g.type, g.w, g.py, traw)};
+        uint32_t tb = bits_of(traw) & 0xFFFFFFFCu;
+        float t1_ms = (std::floor(v1.x) == v1.x) ? float_of(tb | 2u) : float_of(tb | 3u);
+        CutRange cr = cut_range(v0, v1, W, H);
+        int nx = cr.nx, ny = cr.ny;
+        const int n_loop = nx + ny + 1;
+        float x = (float)(cr.dx < 0.f ? cr.xe : cr.xb);
+        float y = (float)(cr.dy < 0.f ? cr.ye : cr.yb);
+        float slot[2] = {t0_ms, t0_ms};
+        float slot_c[2] = {0.f, 0.f};
+        bool slot_x[2] = {false, false};
+        const float p0 = float_of(bits_of(t0_ms) & 0xFFFFFFFCu), p1 = float_of(bits_of(t1_ms) & 0xFFFFFFFCu);
+        for (int i = -1; i < n_loop; ++i) {
+            float t_solve = 0.f, c = 0.f, t_min;
+            int side = 0, took = 0;
+            float ntx = slot[0], nty = slot[1];
+            if (i == -1) {
+                t_min = ntx;
+                if (nx == 0) {
+                    t_solve = 2.f;
+                } else if (ny == 0) {
+                    side = 1;
+                    t_solve = 2.f;
+                } else {
+                    nx--;
+                    c = x;
+                    x += cr.dx;
+                }
+            } else if (ntx <= nty) {
+                t_min = ntx;
+                took = 0;
+                if (nx > 0) {
+                    nx--;
+                    c = x;
+                    x += cr.dx;
+                } else {
+                    t_solve = 2.f;
+                }
+            } else {
+                t_min = nty;
+                took = 1;
+                side = 1;
+                if (ny > 0) {
+                    ny--;
+                    c = y;
+                    y += cr.dy;
+                } else {
+                    t_solve = 2.f;
+                }
+            }
+            if (i >= 0) {
+                out.push_back({float_of(bits_of(t_min) & 0xFFFFFFFCu), p0, p1, slot_c[took], took, slot_x[took]});
+            }
+            const bool solved = t_solve < 2.f;
+            if (solved) t_solve = solve_crossing(g, side ? g.py : g.px, c, t_min, t1_ms);
+            slot[side] = float_of((bits_of(t_solve) & 0xFFFFFFFCu) | (uint32_t)side);
+            slot_c[side] = c;
+            slot_x[side] = solved;
+        }
+        t0_ms = t1_ms;
+        v0 = v1;
+    }
+    return (int)out.size();
+}
+
+// Exact root of P(t) = c on [a, b] in double; false without a sign change.
+bool root_d(int type, double w, const float *P, double c, double a, double b, double *t_out) {
+    double fa = coord_d(type, w, P, a) - c, fb = coord_d(type, w, P, b) - c;
+    if (fa == 0.0) return *t_out = a, true;
+    if (fb == 0.0) return *t_out = b, true;
+    if ((fa < 0.0) == (fb < 0.0)) return false;
+    for (int it = 0; it < 60; ++it) {
+        const double m = 0.5 * (a + b), fm = coord_d(type, w, P, m) - c;
+        if (fm == 0.0) return *t_out = m, true;
+        if ((fm < 0.0) == (fa < 0.0)) a = m, fa = fm;
+        else b = m, fb = fm;
+    }
+    *t_out = std::fabs(fa) < std::fabs(fb) ? a : b;
+    return true;
+}
+
+}  // namespace
+
+extern "C" int orc_intersection_error(const spr_scene_view *scene, const float *tvertex, const int32_t *entries,
+                                      int64_t n_entries, int32_t width, int32_t height, int32_t threads,
+                                      orc_xerr *out) {
+    if (!scene || !out || (n_entries > 0 && (!tvertex || !entries))) return SPR_ERR_INVALID_ARG;
+    *out = orc_xerr{};
+    out->worst_entry = -1;
+    const uint32_t C = scene->n_curves;
+    // entries of curve i start at offs[i] (they are grouped by curve id)
+    std::vector<int64_t> offs(C + 1, n_entries);
+    {
+        int64_t j = 0;
+        for (uint32_t i = 0; i <= C; ++i) {
+            while (j < n_entries && (uint32_t)entries[2 * j] < i) ++j;
+            offs[i] = j;
+        }
+    }
+    const int nthreads = threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    struct Acc {
+        double max_err = 0, sum_err = 0, max_resid = 0;
+        int64_t n = 0, mismatched = 0, unbracketed = 0, over_1px = 0, worst = -1;
+    };
+    std::vector<Acc> acc(nthreads);
+    std::atomic<int64_t> next{0};
+    auto work = [&](int tid) {
+        Acc &A = acc[tid];
+        std::vector<CrossingMeta> meta;
+        for (;;) {
+            const int64_t c0 = next.fetch_add(256);
+            if (c0 >= C) break;
+            for (int64_t i = c0; i < std::min<int64_t>(C, c0 + 256); ++i) {
+                CurveGeom g;
+                g.type = scene->curve_type[i];
+                g.w = (g.type == kRational) ? scene->curve_arc_w[i] : 0.f;
+                const uint32_t p = scene->curve_vertex_pos[i];
+                const int nv = g.type & 7;
+                for (int k = 0; k < 4; ++k) {
+                    g.px[k] = k < nv ? tvertex[2 * ((size_t)p + k)] : 0.f;
+                    g.py[k] = k < nv ? tvertex[2 * ((size_t)p + k) + 1] : 0.f;
+                }
+                const int64_t b = offs[i], e = offs[i + 1];
+                if (b == e) continue;
+                monotonize(g, true);
+                meta.clear();
+                emit_meta(g, width, height, meta);
+                if ((int64_t)meta.size() != e - b) {
+                    A.mismatched += e - b;
+                    continue;
+                }
+                for (int64_t k = b; k < e; ++k) {
+                    const CrossingMeta &m = meta[k - b];
+                    const float t = float_of((uint32_t)entries[2 * k + 1] & 0xFFFFFFFCu);
+                    if (bits_of(t) != bits_of(m.t)) {
+                        ++A.mismatched;
+                        continue;
+                    }
+                    if (!m.crossing) continue;
+                    const float *P = m.side ? g.py : g.px;  // the coordinate fixed by the cut line
+                    const float *Q = m.side ? g.px : g.py;  // the coordinate along it
+                    double ts;
+                    if (!root_d(g.type, g.w, P, m.c, m.t0, m.t1, &ts)) {
+                        ++A.unbracketed;
+                        continue;
+                    }
+                    const double q_exact = coord_d(g.type, g.w, Q, ts);
+                    const double q_used = curve_coord(g.type, g.w, Q, t);
+                    const double err = std::fabs(q_used - q_exact);
+                    const double resid = std::fabs((double)curve_coord(g.type, g.w, P, t) - m.c);
+                    ++A.n;
+                    A.sum_err += err;
+                    if (err > 1.0) ++A.over_1px;
+                    if (err > A.max_err) A.max_err = err, A.worst = k;
+                    A.max_resid = std::max(A.max_resid, resid);
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthreads; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto &t : pool) t.join();
+    double sum = 0;
+    for (const Acc &A : acc) {
+        out->n_crossings += A.n;
+        out->n_mismatched += A.mismatched;
+        out->n_unbracketed += A.unbracketed;
+        out->n_over_1px += A.over_1px;
+        sum += A.sum_err;
+        if (A.worst >= 0 && (out->worst_entry < 0 || A.max_err > out->max_err_px)) {
+            out->max_err_px = A.max_err;
+            out->worst_entry = A.worst;
+        }
+        out->max_resid_px = std::max(out->max_resid_px, A.max_resid);
+    }
+    out->mean_err_px = out->n_crossings ? sum / (double)out->n_crossings : 0.0;
+    return SPR_OK;
+}

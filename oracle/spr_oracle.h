@@ -78,6 +78,26 @@ int orc_vertical_mask2(int32_t samples, float y0, float y1, uint32_t *out_words)
 int orc_diff(const spr_scene_view *scene, const orc_config *cfg, const float *fill, const float *grad_image,
              double *image, double *grad_fill, double *grad_vertex, double *grad_affine);
 
+/* Accuracy of the FP32 crossing points against FP64: for every crossing
+ * entry (not piece starts) of entries[2 * n_entries] (curve id, t | flags,
+ * grouped by curve id, as SPR_STAGE_INTERSECTION) of the curves whose FP32
+ * transformed vertices are tvertex[2 * V] (SPR_STAGE_TVERTEX), the distance
+ * along the cut line between the point the fragment stage uses (the FP32
+ * curve point at the entry's t) and the exact crossing of the curve with
+ * the line (FP64 root on the entry's monotone piece). */
+typedef struct orc_xerr {
+    double max_err_px;     /* max |along-line coordinate error|           */
+    double mean_err_px;
+    double max_resid_px;   /* max distance of the FP32 point from its line */
+    int64_t n_crossings;
+    int64_t n_over_1px;    /* crossings more than 1 px off                 */
+    int64_t n_unbracketed; /* no sign change on the piece (not measured)   */
+    int64_t n_mismatched;  /* entries that differ from the oracle's walk   */
+    int64_t worst_entry;   /* index of the max error (-1: none)            */
+} orc_xerr;
+int orc_intersection_error(const spr_scene_view *scene, const float *tvertex, const int32_t *entries,
+                           int64_t n_entries, int32_t width, int32_t height, int32_t threads, orc_xerr *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,13 +44,16 @@ def test_clock_sampler_parsing():
 
 
 def test_reference_arm_json(monkeypatch, capsys):
-    monkeypatch.setattr(bench, "BAND", (1000, 8))
-    args = type("A", (), {"steps": 1, "warmup": 0, "gpus": 1})()
+    monkeypatch.setattr(bench, "BAND_ROWS", 4)
+    args = type("A", (), {"steps": 2, "warmup": 1, "gpus": 1})()
     bench.run_reference(args, rank=0, world=1)
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "Mpix/s" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["higher_is_better"] is True
+    # both arms describe the same workload with the same config object
+    assert line["config"] == bench.workload_config()
+    assert line["metric"] == bench.METRIC
 
 
 def test_reference_arm_silent_on_other_ranks(capsys):

@@ -203,12 +203,68 @@ def test_step_timing_and_stats():
         assert st["kernel_launches"] > 10 and st["host_syncs"] == 3 and st["device_bytes"] > 0
 
 
-def test_benchmark_scene_band():
-    """A 2048x256 band of the benchmark scene (all 20,000 paths), exact."""
+def test_small_scene_as_specified():
+    """The small plain-path workload exactly as specified: 512x512 RGBA8,
+    8 samples per pixel, 64 closed paths of 8-32 segments (40% line, 30%
+    quadratic, 30% cubic, control points uniform in the viewport), identity
+    transform, solid fills (RGB U[0,1], alpha U[0.5,1]), nonzero / even-odd
+    50/50, one seed: every stage and the image exact against the oracle."""
+    scene = spr.Scene.generate(spr.SCENE_RANDOM, seed=20261203, width=512, height=512, n_paths=64, seg_min=8,
+                               seg_max=32)
+    types = scene.curve_type
+    assert np.all(np.isin(types, [spr.CURVE_LINEAR, spr.CURVE_QUADRATIC, spr.CURVE_CUBIC]))
+    for ms in (True, False):
+        counts, diff = check_parity(scene, 512, 512, samples=8, ms=ms)
+        assert counts["path"] == 64 and counts["curve_fragment"] > 100_000 and diff == 0
+
+
+def test_benchmark_scene_full_frame():
+    """The whole 2048x2048, 32-spp benchmark frame (15,000 glyph-like and
+    5,000 large paths): every stage and the image exact against the oracle."""
     import bench
 
     scene = bench.make_scene()
-    y0, bh = bench.BAND
+    counts, diff = check_parity(scene, 2048, 2048, samples=32)
+    assert counts["curve_fragment"] > 10_000_000 and diff == 0
+
+
+def test_memory_limit_refuses_then_recovers():
+    """A cap on the handle's device memory (the reference's fixed arena that
+    throws when exhausted): a frame that needs more fails with
+    ERR_OUT_OF_MEMORY, the handle keeps its scene, and the next frame under a
+    larger cap or none renders exactly."""
+    s = spr.Scene.generate(spr.SCENE_MIXED, seed=58, width=320, height=240, n_paths=300, n_large=12)
+    ref = oracle.run(s, 320, 240, samples=32)
+    with spr.VGRasterizer(320, 240, samples=32) as r:
+        r.add_vg(s)
+        held = r.frame_stats()["device_bytes"]
+        r.set_memory_limit(held + 4096)
+        with pytest.raises(spr.SprError) as e:
+            r.rasterize()
+        assert e.value.status == spr.ERR_OUT_OF_MEMORY
+        assert r.frame_stats()["device_bytes"] <= held + 4096
+        with pytest.raises(spr.SprError):
+            r.read_image()  # no valid frame
+        r.set_memory_limit(0)
+        r.rasterize()
+        assert np.array_equal(r.read_image().reshape(-1), ref["IMAGE"])
+        need = r.frame_stats()["device_bytes"]
+        r.set_memory_limit(need)  # enough for this frame: renders under the cap
+        r.rasterize()
+        assert np.array_equal(r.read_image().reshape(-1), ref["IMAGE"])
+        assert r.frame_stats()["device_bytes"] <= need
+        with pytest.raises(spr.SprError):
+            r.set_memory_limit(-1)
+
+
+def test_benchmark_scene_band():
+    """A 2048x256 band (rows 896-1151) of the benchmark scene, rendered as the
+    CPU arm renders its steps (all 20,000 paths moved by the band's
+    transform), exact."""
+    import bench
+
+    scene = bench.make_scene()
+    y0, bh = 896, bench.BAND_ROWS
     counts, diff = check_parity(scene, 2048, bh, samples=32, transform=bench.band_transform(y0))
     assert counts["curve_fragment"] > 100000 and diff == 0
 

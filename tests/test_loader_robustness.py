@@ -81,3 +81,24 @@ def test_mutated_scene_files(tmp_path, suffix):
         ok += 1
         assert spr.lib().spr_validate_scene(back.view()) == spr.OK
     assert ok > 0
+
+
+def test_scene_file_paths_sharing_one_contour(tmp_path):
+    """A small .vgt whose 4,000 paths all name the same 4,000-curve contour:
+    the flattening would need 16 M curves, far more than the file's 8,000
+    vertices allow, so it must be refused at once (no runaway allocation)."""
+    import time
+
+    n_paths, n_curves = 4000, 4000
+    out = ["0,0,64,64", f"{n_paths},1,{n_curves},{2 * n_curves},0,0"]
+    out += ["0,1,\x00,\x00,4278190335,0"] * n_paths  # contour 0, solid colour, nonzero
+    out += [f"0,{n_curves}"]
+    out += [f"{2 * i},\x02,-1" for i in range(n_curves)]
+    out += [f"{i % 64}.0,{(i * 7) % 64}.0" for i in range(2 * n_curves)]
+    f = tmp_path / "shared.vgt"
+    f.write_bytes(("\n".join(out) + "\n").encode("latin-1"))
+    t0 = time.perf_counter()
+    with pytest.raises(spr.SprError) as e:
+        spr.Scene.load_vg(f)
+    assert e.value.status == spr.ERR_INVALID_SCENE
+    assert time.perf_counter() - t0 < 2.0

@@ -59,10 +59,29 @@ def _noalloc(counts):
 
 
 def test_noalloc_scan_matches_render_offsets_two_calls():
+    """Two calls in a row on the curves of two scenes against the offsets at
+    which spr_render placed each curve's intersection entries."""
     for seed, size in ((11, 256), (12, 384)):
         counts, expected = _render_offsets(seed, size)
         got = _noalloc(counts)
         np.testing.assert_array_equal(got, expected)
+
+
+def _expected(counts):
+    return np.concatenate([[0], np.cumsum(counts, dtype=np.uint64)]).astype(np.uint32)
+
+
+def test_noalloc_scan_synthetic_sizes_in_a_row():
+    """Synthetic counts against np.cumsum, one call after another on the
+    shared scratch: nothing, one count, more than 1,024 tiles of 2,048 counts
+    (the tile-sum scan then carries across its 1,024-tile chunks), a smaller
+    multi-tile input right after it (so stale tile sums of the larger call
+    lie beyond its end), and exactly the maximum size."""
+    rng = np.random.default_rng(5)
+    for n in (0, 1, 2048 * 1100 + 7, 3 * 2048 + 5, MAX_N, 2047):
+        counts = rng.integers(0, 64, n, dtype=np.uint32)  # totals stay below 2^32
+        got = _noalloc(counts)
+        np.testing.assert_array_equal(got, _expected(counts), err_msg=f"n = {n}")
 
 
 def test_noalloc_scan_rejects_oversize():
