@@ -286,7 +286,7 @@ FrameArgs make_args(const spr_handle *h) {
         a.path_scene = nullptr;
         a.scenes = nullptr;
         a.n_scenes = 0;
-        a.n_bins = (int64_t)((a.W + 31) / 32) * ((a.H + 1) / 2);
+        a.n_bins = (int64_t)((a.W + kBinW - 1) / kBinW) * ((a.H + 1) / 2);
     }
     return a;
 }
@@ -1494,7 +1494,7 @@ int upload_group(spr_handle *h, const spr_batch_scene *in, const std::vector<int
         SceneInfo &si = info[k];
         si.W = b.width;
         si.H = b.height;
-        si.ntx = (b.width + 31) / 32;
+        si.ntx = (b.width + kBinW - 1) / kBinW;
         si.nrows = (b.height + 1) / 2;
         si.image_off = pix;
         si.bin_off = bins;

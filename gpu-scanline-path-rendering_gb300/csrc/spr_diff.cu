@@ -38,7 +38,7 @@ namespace {
 constexpr int kDiffThreads = 256;    // 8 warps, each working on its own cells
 constexpr int kDiffPathAcc = 4096;   // paths with shared-memory fill-gradient accumulators (backward)
 constexpr int kDiffCacheSlots = 256; // else: slots of each warp's path-gradient cache
-constexpr int kTileW = 32;
+constexpr int kTileW = kBinW;  // columns of a resolve bin
 
 __device__ __forceinline__ uint32_t pixel_mask(const uint4 &mm, int S, int k) {
     if (S == 32) return k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w));

@@ -36,8 +36,11 @@ struct FrameCounters {
     uint32_t pad[3];
 };
 
+// Pixel columns of a resolve bin (one cell row high, one warp each).
+constexpr int kBinW = 64;
+
 // One scene of a batch frame: its viewport, its resolve bins (ntx columns of
-// 32 pixels x nrows cell rows, numbered from bin_off) and its image (W x H
+// kBinW pixels x nrows cell rows, numbered from bin_off) and its image (W x H
 // pixels from image_off in the frame's image buffer), and its 4x4 input
 // transform (row-major).
 struct SceneInfo {

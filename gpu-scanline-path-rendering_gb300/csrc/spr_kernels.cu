@@ -672,9 +672,9 @@ __global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, int64_t nf, i
 }
 
 // ------------------------------------------------------------ resolve --
-constexpr int kTileW = 32;  // pixel columns per resolve bin (one warp)
+constexpr int kBinCells = kBinW / 2;  // cells per resolve bin: one lane each
 constexpr int kResolveWarps = 8;
-constexpr int kResolveBlocksPerSM = 4;  // shared-memory bound: ~50 KB per block
+constexpr int kResolveMaxBlocksPerSM = 4;
 
 __device__ __forceinline__ void item_cols(const int4 &it, int W, int &x0, int &x1) {
     const int x = (int)((uint32_t)it.x & 0xFFFFu);
@@ -689,7 +689,7 @@ __global__ void k_item_tiles(FrameArgs a, const int4 *__restrict__ draw, const u
     const int W = item_scene != nullptr ? a.scenes[item_scene[i]].W : a.W;
     int x0, x1;
     item_cols(draw[i], W, x0, x1);
-    cnt[i] = x1 > x0 ? (uint32_t)((x1 - 1) / kTileW - x0 / kTileW + 1) : 0u;
+    cnt[i] = x1 > x0 ? (uint32_t)((x1 - 1) / kBinW - x0 / kBinW + 1) : 0u;
 }
 
 __global__ void k_emit_pairs(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
@@ -708,10 +708,10 @@ __global__ void k_emit_pairs(FrameArgs a, const int4 *__restrict__ draw, const u
     int x0, x1;
     item_cols(it, W, x0, x1);
     if (x1 <= x0) return;
-    const int ntx = (W + kTileW - 1) / kTileW;
+    const int ntx = (W + kBinW - 1) / kBinW;
     const int row = (it.x >> 16) / 2;
     uint32_t o = offs[i];
-    for (int t = x0 / kTileW; t <= (x1 - 1) / kTileW; ++t) {
+    for (int t = x0 / kBinW; t <= (x1 - 1) / kBinW; ++t) {
         pkey[o] = bin0 + (uint32_t)(row * ntx + t);
         pval[o] = (uint32_t)i;
         ++o;
@@ -828,119 +828,169 @@ __device__ __forceinline__ float4 gradient_colour(const FrameArgs &a, const Smem
                        lin8(t0 >> 24) * u + lin8(t1 >> 24) * f);
 }
 
-// ---- resolve state -----------------------------------------------------
-// A bin is 2 pixel rows x 32 columns = 64 pixels, pixel p = row * 32 + col.
-// Each pixel keeps its samples as a short list of (sample mask, RGBA8 colour)
-// entries whose masks partition the pixel's samples: equal colours are merged
-// after every blend, so a pixel typically holds 1-3 entries and a blend costs
-// one evaluation per entry instead of one per sample.  A pixel that would
-// need more than kCapMS entries (rare) switches to an explicit per-sample
-// array in a global overflow area owned by the warp resolving its bin
-// (count = kFull) and switches back once it has kCapMS or fewer distinct
-// colours.  Every sample still gets exactly the value the per-sample rule
-// gives.
-constexpr uint8_t kFull = 0xFF;
-constexpr int kCapMS = 8;  // entries per pixel in the multisample modes
+// ---- resolve state -------------------------------------------------------
+// A bin is one cell row (2 pixel rows) x 64 pixel columns = 32 cells of 2x2
+// pixels; lane l of the warp resolving the bin owns cell l.  Every draw item
+// covers whole cells, and the 4 pixels of a cell see the same items in the
+// same order, so a cell keeps its 4 x S samples (pixel k = px.x * 2 + px.y,
+// the merged masks' layout: bits [k S, (k + 1) S) of the cell's mask words)
+// as a short list of (sample mask, RGBA8 colour) entries whose masks
+// partition the samples.  An item blends each entry it touches once,
+// splitting the entries it covers in part, and entries of equal colour are
+// merged after every item: a cell typically holds 1-4 entries, and an entry
+// often spans several pixels, so one blend serves many samples.  Entries
+// 0..kCellCap-1 live in shared memory; a cell that needs more (rare: up to
+// one per sample) keeps the rest in a global area owned by its warp and
+// lane, with the same layout.  Every sample gets exactly the value the
+// per-sample rule gives.
+constexpr int kCellCap = 8;
 
-template <int CAP>
-struct BinState {
-    uint32_t emask[CAP][64];
-    uint32_t ecol[CAP][64];
-    uint8_t cnt[64];
-    int4 it[32];  // staged draw items
-    uint4 mm[32];  // their merged sample masks
+template <int MW, int CAP>
+struct CellState {
+    uint32_t ent[CAP][MW + 1][32];  // entry j of lane l's cell: mask words k < MW, colour at k = MW
+    int4 it[32];                    // staged draw items
+    uint32_t mm[MW][32];            // their merged sample masks
 };
 
-// Columns [c0, c1) of a bin as a bit mask.
-__device__ __forceinline__ uint32_t col_bits(int c0, int c1) {
+// Entry j of lane `lane`'s cell: its first word; word k is at [k * 32].
+template <int MW, int CAP>
+__device__ __forceinline__ uint32_t *entry(CellState<MW, CAP> &w, uint32_t *gx, int j, int lane) {
+    return j < CAP ? &w.ent[j][0][lane] : gx + (size_t)(j - CAP) * (MW + 1) * 32 + lane;
+}
+
+// Cells [c0, c1) of a bin as a lane mask.
+__device__ __forceinline__ uint32_t cell_bits(int c0, int c1) {
+    c0 = max(c0, 0);
+    c1 = min(c1, kBinCells);
     if (c1 <= c0) return 0u;
     const uint32_t hi = c1 >= 32 ? 0xFFFFFFFFu : ((1u << c1) - 1u);
     return hi & ~((1u << c0) - 1u);
 }
 
-// Sample mask of pixel k (= px.x * 2 + px.y) of a merged fragment's cell.
+// Bits of pixel k within mask word `wd` (cell masks of S samples per pixel).
 template <int S>
-__device__ __forceinline__ uint32_t cell_pixel_mask(const uint4 &mm, int k) {
-    if constexpr (S == 32) return k == 0 ? mm.x : (k == 1 ? mm.y : (k == 2 ? mm.z : mm.w));
-    else if constexpr (S == 16) return ((k < 2 ? mm.x : mm.y) >> (16 * (k & 1))) & 0xFFFFu;
-    else return (mm.x >> (8 * k)) & 0xFFu;
-}
-
-// Explicit samples of pixel p of a bin: ovf[p * 32 + s] (global memory).
-__device__ __forceinline__ uint32_t &full_sample(uint32_t *ovf, int p, int s) { return ovf[p * 32 + s]; }
-
-// Entries -> explicit S samples (pixels with more than CAP colours).
-template <int S, int CAP, bool EXPLICIT>
-__device__ void to_full(BinState<CAP> &w, uint32_t *ovf, int p) {
-    if constexpr (EXPLICIT) {
-        const int n = w.cnt[p];
-        for (int smp = 0; smp < S; ++smp) {
-            uint32_t v = 0;
-            for (int j = 0; j < n; ++j)
-                if ((w.emask[j][p] >> smp) & 1u) v = w.ecol[j][p];
-            full_sample(ovf, p, smp) = v;
-        }
-        w.cnt[p] = kFull;
-    }
-}
-
-// Explicit samples -> entries when at most CAP distinct colours remain.
-template <int S, int CAP, bool EXPLICIT>
-__device__ void try_compress(BinState<CAP> &w, uint32_t *ovf, int p) {
-    if constexpr (EXPLICIT) {
-        uint32_t col[CAP], msk[CAP];
-        int n = 0;
-        for (int smp = 0; smp < S; ++smp) {
-            const uint32_t v = full_sample(ovf, p, smp);
-            int j = 0;
-            while (j < n && col[j] != v) ++j;
-            if (j == n) {
-                if (n == CAP) return;  // stays explicit
-                col[n] = v;
-                msk[n] = 0u;
-                ++n;
-            }
-            msk[j] |= 1u << smp;
-        }
-        for (int j = 0; j < n; ++j) w.emask[j][p] = msk[j], w.ecol[j][p] = col[j];
-        w.cnt[p] = (uint8_t)n;
-    }
+__device__ __forceinline__ uint32_t pixel_word_bits(int wd, int k) {
+    if constexpr (S == 32) return wd == k ? 0xFFFFFFFFu : 0u;
+    else if constexpr (S == 16) return wd == (k >> 1) ? (0xFFFFu << (16 * (k & 1))) : 0u;
+    else return 0xFFu << (8 * k);
 }
 
 // Merges entries of equal colour.
-template <int CAP>
-__device__ __forceinline__ void dedup(BinState<CAP> &w, int p) {
-    int n = w.cnt[p];
+template <int MW, int CAP>
+__device__ __forceinline__ void cell_dedup(CellState<MW, CAP> &w, uint32_t *gx, int lane, int &n) {
     for (int j = 1; j < n; ++j) {
-        const uint32_t cj = w.ecol[j][p];
+        uint32_t *ej = entry(w, gx, j, lane);
+        const uint32_t cj = ej[MW * 32];
         for (int i = 0; i < j; ++i) {
-            if (w.ecol[i][p] == cj) {
-                w.emask[i][p] |= w.emask[j][p];
+            uint32_t *ei = entry(w, gx, i, lane);
+            if (ei[MW * 32] == cj) {
                 --n;
-                w.emask[j][p] = w.emask[n][p];
-                w.ecol[j][p] = w.ecol[n][p];
+                uint32_t *en = entry(w, gx, n, lane);
+#pragma unroll
+                for (int k = 0; k < MW; ++k) {
+                    ei[k * 32] |= ej[k * 32];
+                    ej[k * 32] = en[k * 32];
+                }
+                ej[MW * 32] = en[MW * 32];
                 --j;
                 break;
             }
         }
     }
-    w.cnt[p] = (uint8_t)n;
 }
 
-// One warp per bin of (cell row, 32 pixel columns), lane = column (both pixel
-// rows).  Every item covers both rows of its columns, so items (merged
-// fragments and spans, in draw-list order) are taken in batches whose column
-// sets are pairwise disjoint and each batch is applied in one step, each
-// lane updating its own two pixels; then every pixel is averaged over its
-// samples with an exact fixed-point sum.
+// One item (source colour sr, sg, sb with alpha sa) over the samples of mask
+// m of lane `lane`'s cell, in the multisample modes.
+template <int S, bool SRGB, int CAP>
+__device__ __forceinline__ void cell_apply(CellState<S / 8, CAP> &w, uint32_t *gx, int lane, int &n,
+                                           const uint32_t (&m)[S / 8], const SmemTables &T, float sr, float sg,
+                                           float sb, float sa) {
+    constexpr int MW = S / 8;
+    const float om = 1.f - sa;
+    uint32_t full = 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < MW; ++k) full &= m[k];
+    if (sa == 1.f && full == 0xFFFFFFFFu) {
+        // opaque over every sample: src * 1 + dst * 0 is the source whatever
+        // dst holds, so one entry stands for all (the per-sample blends and
+        // the merge give the same)
+        uint32_t *e0 = &w.ent[0][0][lane];
+        e0[MW * 32] = blend_sample<SRGB>(T, lane, 0u, sr, sg, sb, sa, om);
+#pragma unroll
+        for (int k = 0; k < MW; ++k) e0[k * 32] = 0xFFFFFFFFu;
+        n = 1;
+        return;
+    }
+    const int n0 = n;
+    bool changed = false;
+    for (int j = 0; j < n0; ++j) {
+        uint32_t *ej = entry(w, gx, j, lane);
+        uint32_t em[MW], in[MW], any = 0u, part = 0u;
+#pragma unroll
+        for (int k = 0; k < MW; ++k) {
+            em[k] = ej[k * 32];
+            in[k] = em[k] & m[k];
+            any |= in[k];
+            part |= em[k] & ~m[k];
+        }
+        if (!any) continue;
+        const uint32_t r = blend_sample<SRGB>(T, lane, ej[MW * 32], sr, sg, sb, sa, om);
+        changed = true;
+        if (!part) {
+            ej[MW * 32] = r;
+        } else {
+            uint32_t *en = entry(w, gx, n, lane);
+#pragma unroll
+            for (int k = 0; k < MW; ++k) {
+                ej[k * 32] = em[k] & ~m[k];
+                en[k * 32] = in[k];
+            }
+            en[MW * 32] = r;
+            ++n;
+        }
+    }
+    if (changed && n > 1) cell_dedup<MW, CAP>(w, gx, lane, n);
+}
+
+// Sample mask of item q over lane `lane`'s cell: a merged fragment's mask, or
+// every sample for a span.
+template <int S, int CAP>
+__device__ __forceinline__ void item_mask(const CellState<S / 8, CAP> &w, int q, bool frag, uint32_t (&m)[S / 8]) {
+#pragma unroll
+    for (int k = 0; k < S / 8; ++k) m[k] = frag ? w.mm[k][q] : 0xFFFFFFFFu;
+}
+
+// Exact mean of a pixel's samples: every decoded value x 2^36 is an integer,
+// the 64-bit sums are exact, one rounding to float at the end.
+struct PixelSum {
+    long long r = 0, g = 0, b = 0, a = 0;
+};
+template <bool SRGB>
+__device__ __forceinline__ void add_sample(PixelSum &p, const SmemTables &T, int lane, uint32_t v, int weight) {
+    p.r += (long long)weight * (long long)(dec8<SRGB>(T, v & 0xFF, lane) * 68719476736.0f);
+    p.g += (long long)weight * (long long)(dec8<SRGB>(T, (v >> 8) & 0xFF, lane) * 68719476736.0f);
+    p.b += (long long)weight * (long long)(dec8<SRGB>(T, (v >> 16) & 0xFF, lane) * 68719476736.0f);
+    p.a += (long long)weight * (long long)(lin8(v >> 24) * 68719476736.0f);
+}
+
+template <bool SRGB>
+__device__ __forceinline__ uint32_t encode_mean(const SmemTables &T, const PixelSum &p, double scale) {
+    const float ar = (float)((double)p.r * scale), ag = (float)((double)p.g * scale);
+    const float ab = (float)((double)p.b * scale), aa = (float)((double)p.a * scale);
+    return enc8<SRGB>(T, ar) | (enc8<SRGB>(T, ag) << 8) | (enc8<SRGB>(T, ab) << 16) | (enc_lin(aa) << 24);
+}
+
+// One warp per bin.  Items (merged fragments and spans, in draw-list order)
+// are staged 32 at a time; a 32 x 32 ballot transpose of their cell sets
+// gives every lane the staged items covering its cell, which it applies in
+// order.  Then every pixel is averaged over its samples.
 template <int S, bool MS, bool SRGB, int CAP, bool GRAD>
 __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__restrict__ draw,
                                             const uint32_t *__restrict__ merged, const uint32_t *__restrict__ pval,
                                             const uint32_t *__restrict__ bstart, const uint32_t *__restrict__ bend,
-                                            uint32_t *__restrict__ image, uint32_t *__restrict__ ovf,
-                                            const SmemTables &T, BinState<CAP> &w, const int lane, const uint32_t b) {
-    constexpr bool EXPLICIT = MS && S > CAP;  // entries can exceed CAP
-    constexpr uint32_t ALL = MS ? (S == 32 ? 0xFFFFFFFFu : ((1u << S) - 1u)) : 1u;
+                                            uint32_t *__restrict__ image, uint32_t *__restrict__ gx,
+                                            const SmemTables &T, CellState<S / 8, CAP> &w, const int lane,
+                                            const uint32_t b) {
     constexpr int MW = S / 8;
     // the bin's scene: viewport, first bin, image
     int W = a.W, H = a.H;
@@ -960,202 +1010,164 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
         image_off = sc->image_off;
         image += image_off;
     }
-    const int ntx = (W + kTileW - 1) / kTileW;
+    const int ntx = (W + kBinW - 1) / kBinW;
     const int row = (int)(lb / ntx), tile = (int)(lb % ntx);
-    const int tx0 = tile * kTileW;
+    const int tx0 = tile * kBinW;
     const int y0 = row * 2;
-    const int cols = min(kTileW, W - tx0);  // valid columns of this bin
-    const int rows = min(2, H - y0);        // valid pixel rows
+    const int X0 = tx0 + 2 * lane;  // this lane's cell: columns X0, X0 + 1, rows y0, y0 + 1
+    // state: one white entry over every sample (multisample), or one colour
+    // per pixel (single-sample output)
+    int n = 1;
+    uint32_t pc[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    if constexpr (MS) {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int p = lane + 32 * h;
-        w.cnt[p] = 1;
-        w.emask[0][p] = ALL;
-        w.ecol[0][p] = 0xFFFFFFFFu;
+        for (int k = 0; k <= MW; ++k) w.ent[0][k][lane] = 0xFFFFFFFFu;
     }
     const uint32_t beg = bstart[b], fin = bend[b];
     for (uint32_t base = beg; base < fin; base += 32) {
         __syncwarp();
         const int cnt = (int)min(32u, fin - base);
-        uint32_t cm = 0u;  // columns of this lane's staged item
+        uint32_t cm = 0u;  // cells of this lane's staged item
         if (lane < cnt) {
             const int4 it = draw[pval[base + lane]];
             w.it[lane] = it;
-            const int x = (int)((uint32_t)it.x & 0xFFFFu) - tx0;
+            const int x = (int)((uint32_t)it.x & 0xFFFFu);
             if (it.w != 0) {
                 if constexpr (MW == 4) {
-                    w.mm[lane] = __ldg(reinterpret_cast<const uint4 *>(merged) + (it.w - 1));
+                    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(merged) + (it.w - 1));
+                    w.mm[0][lane] = v.x;
+                    w.mm[1][lane] = v.y;
+                    w.mm[2][lane] = v.z;
+                    w.mm[3][lane] = v.w;
                 } else if constexpr (MW == 2) {
                     const uint2 v = __ldg(reinterpret_cast<const uint2 *>(merged) + (it.w - 1));
-                    w.mm[lane] = make_uint4(v.x, v.y, 0u, 0u);
+                    w.mm[0][lane] = v.x;
+                    w.mm[1][lane] = v.y;
                 } else {
-                    w.mm[lane] = make_uint4(__ldg(merged + (it.w - 1)), 0u, 0u, 0u);
+                    w.mm[0][lane] = __ldg(merged + (it.w - 1));
                 }
-                cm = col_bits(max(x, 0), min(x + 2, cols));
+                cm = x < W ? cell_bits((x - tx0) >> 1, ((x - tx0) >> 1) + 1) : 0u;
             } else {
-                cm = col_bits(max(x, 0), min(x + it.y, cols));
+                const int xa = max(x, 0), xb = min(x + it.y, W);
+                cm = xb > xa ? cell_bits((xa - tx0) >> 1, (xb - tx0 + 1) >> 1) : 0u;
             }
         }
         __syncwarp();
-        // mine: bit q = staged item q covers this lane's column (a transpose
-        // of the 32 x 32 bit matrix of column sets)
+        // mine: bit q = staged item q covers this lane's cell (a transpose of
+        // the 32 x 32 bit matrix of cell sets)
         uint32_t mine = 0u;
 #pragma unroll
         for (int L = 0; L < 32; ++L) {
             const uint32_t bm = __ballot_sync(0xffffffffu, (cm >> L) & 1u);
             if (lane == L) mine = bm;
         }
-        // every lane applies its own items in draw order to its two pixels
+        // every lane applies its own items in draw order to its cell
         while (mine) {
             const int q = __ffs(mine) - 1;
             mine &= mine - 1u;
             const int4 it = w.it[q];
             const bool frag = it.w != 0;
             const uint32_t c = (uint32_t)it.z;
-            float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
-                  sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane);
-            float sa0 = lin8(c >> 24);
-            const bool grad = GRAD && c - 1u < a.n_grad;  // a gradient paint
-            const int dx = lane + tx0 - (int)((uint32_t)it.x & 0xFFFFu);
-            const uint4 mm = frag ? w.mm[q] : make_uint4(0u, 0u, 0u, 0u);
-            // one-entry memo of blend(dst) for this item (same source, same alpha)
-            uint32_t memo_d = 0u, memo_r = 0u;
-            bool memo = false;
+            uint32_t m[MW];
+            item_mask<S, CAP>(w, q, frag, m);
+            if (!GRAD || c - 1u >= a.n_grad) {  // a solid colour (else a gradient paint)
+                const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
+                            sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane), sa = lin8(c >> 24);
+                if constexpr (MS) {
+                    cell_apply<S, SRGB, CAP>(w, gx, lane, n, m, T, sr, sg, sb, sa);
+                } else {
+                    // single-sample output: alpha x coverage per pixel
 #pragma unroll
-            for (int py = 0; py < 2; ++py) {
-                if (py >= rows) break;
-                const int p = py * 32 + lane;
-                if (grad) {  // this pixel's colour
-                    const float4 gc = gradient_colour<SRGB>(a, T, c - 1u, (int)(int16_t)(it.x & 0xFFFF), it.y,
-                                                            tx0 + lane, y0 + py, lane);
-                    sr = gc.x;
-                    sg = gc.y;
-                    sb = gc.z;
-                    sa0 = gc.w;
-                    memo = false;
-                }
-                uint32_t m = ALL;
-                float sa = sa0;
-                if (frag) {
-                    m = cell_pixel_mask<S>(mm, dx * 2 + py);
-                    if (m == 0u) continue;
-                    if constexpr (!MS) {
-                        sa = sa0 * ((float)__popc(m) / (float)S);
-                        m = ALL;
-                        memo = false;
+                    for (int k = 0; k < 4; ++k) {
+                        int cov = 0;
+#pragma unroll
+                        for (int wd = 0; wd < MW; ++wd) cov += __popc(m[wd] & pixel_word_bits<S>(wd, k));
+                        if (cov == 0) continue;
+                        const float ak = sa * ((float)cov / (float)S);
+                        pc[k] = blend_sample<SRGB>(T, lane, pc[k], sr, sg, sb, ak, 1.f - ak);
                     }
                 }
-                const float om = 1.f - sa;
-                int n = w.cnt[p];
-                if (sa == 1.f && m == ALL) {
-                    // opaque over every sample: src * 1 + dst * 0 is the source
-                    // whatever dst holds, so one entry blended once stands for
-                    // all (the per-sample blends and the merge give the same)
-                    n = 1;
-                    w.emask[0][p] = ALL;
-                }
-                if (EXPLICIT && n != kFull && frag) {
-                    int splits = 0;
-                    for (int j = 0; j < n; ++j) {
-                        const uint32_t em = w.emask[j][p];
-                        splits += ((em & m) != 0u && (em & ~m) != 0u) ? 1 : 0;
+            } else if constexpr (GRAD) {
+                // a colour per pixel: one application per pixel
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int X = X0 + (k >> 1), Y = y0 + (k & 1);
+                    uint32_t mk[MW];
+                    int cov = 0;
+#pragma unroll
+                    for (int wd = 0; wd < MW; ++wd) {
+                        mk[wd] = m[wd] & pixel_word_bits<S>(wd, k);
+                        cov += __popc(mk[wd]);
                     }
-                    if (n + splits > CAP) {
-                        to_full<S, CAP, EXPLICIT>(w, ovf, p);
-                        n = kFull;
-                    }
-                }
-                if (n == kFull) {
-                    if constexpr (EXPLICIT) {
-                        for (uint32_t mk = m; mk; mk &= mk - 1u) {
-                            uint32_t &v = full_sample(ovf, p, __ffs(mk) - 1);
-                            const uint32_t dv = v;
-                            if (!(memo && dv == memo_d)) {
-                                memo_r = blend_sample<SRGB>(T, lane, dv, sr, sg, sb, sa, om);
-                                memo_d = dv;
-                                memo = true;
-                            }
-                            v = memo_r;
-                        }
-                        try_compress<S, CAP, EXPLICIT>(w, ovf, p);
-                    }
-                    continue;
-                }
-                const int n0 = n;
-                for (int j = 0; j < n0; ++j) {
-                    const uint32_t em = w.emask[j][p];
-                    const uint32_t in = em & m;
-                    if (in == 0u) continue;
-                    const uint32_t dv = w.ecol[j][p];
-                    if (!(memo && dv == memo_d)) {
-                        memo_r = blend_sample<SRGB>(T, lane, dv, sr, sg, sb, sa, om);
-                        memo_d = dv;
-                        memo = true;
-                    }
-                    if (in == em) {
-                        w.ecol[j][p] = memo_r;
+                    if (cov == 0) continue;
+                    const float4 gc = gradient_colour<SRGB>(a, T, c - 1u, (int)(int16_t)(it.x & 0xFFFF), it.y, X, Y,
+                                                            lane);
+                    if constexpr (MS) {
+                        cell_apply<S, SRGB, CAP>(w, gx, lane, n, mk, T, gc.x, gc.y, gc.z, gc.w);
                     } else {
-                        w.emask[j][p] = em & ~m;
-                        w.emask[n][p] = in;
-                        w.ecol[n][p] = memo_r;
-                        ++n;
+                        const float ak = gc.w * ((float)cov / (float)S);
+                        pc[k] = blend_sample<SRGB>(T, lane, pc[k], gc.x, gc.y, gc.z, ak, 1.f - ak);
                     }
                 }
-                w.cnt[p] = (uint8_t)n;
-                if (n > 1) dedup(w, p);
             }
         }
     }
     __syncwarp();
-    if (lane >= cols) return;
+    // per-pixel means: pixel k = px * 2 + py of the cell, at column X0 + px,
+    // row y0 + py
     const double scale = 1.0 / (68719476736.0 * (double)(MS ? S : 1));
+    uint32_t out[4];
 #pragma unroll
-    for (int py = 0; py < 2; ++py) {
-        if (py >= rows) continue;
-        const int p = py * 32 + lane;
-        long long ir = 0, ig = 0, ib = 0, ia = 0;
-        const int n = w.cnt[p];
-        auto add = [&](uint32_t v, int weight) {
-            ir += (long long)weight * (long long)(dec8<SRGB>(T, v & 0xFF, lane) * 68719476736.0f);
-            ig += (long long)weight * (long long)(dec8<SRGB>(T, (v >> 8) & 0xFF, lane) * 68719476736.0f);
-            ib += (long long)weight * (long long)(dec8<SRGB>(T, (v >> 16) & 0xFF, lane) * 68719476736.0f);
-            ia += (long long)weight * (long long)(lin8(v >> 24) * 68719476736.0f);
-        };
-        if (n == kFull) {
-            if constexpr (EXPLICIT)
-                for (int smp = 0; smp < S; ++smp) add(full_sample(ovf, p, smp), 1);
+    for (int k = 0; k < 4; ++k) {
+        PixelSum p;
+        if constexpr (MS) {
+            for (int j = 0; j < n; ++j) {
+                const uint32_t *ej = entry(w, gx, j, lane);
+                int cov = 0;
+#pragma unroll
+                for (int wd = 0; wd < MW; ++wd) cov += __popc(ej[wd * 32] & pixel_word_bits<S>(wd, k));
+                if (cov) add_sample<SRGB>(p, T, lane, ej[MW * 32], cov);
+            }
         } else {
-            for (int j = 0; j < n; ++j) add(w.ecol[j][p], __popc(w.emask[j][p]));
+            add_sample<SRGB>(p, T, lane, pc[k], 1);
         }
-        const int64_t pix = (int64_t)(y0 + py) * W + tx0 + lane;
+        const int X = X0 + (k >> 1), Y = y0 + (k & 1);
         if (a.sums != nullptr) {  // a pass of a 256-sample frame: exact sums, encoded after the last pass
-            longlong2 *q = reinterpret_cast<longlong2 *>(a.sums) + 2 * (image_off + pix);
-            const longlong2 q0 = q[0], q1 = q[1];
-            q[0] = make_longlong2(q0.x + ir, q0.y + ig);
-            q[1] = make_longlong2(q1.x + ib, q1.y + ia);
+            if (X < W && Y < H) {
+                longlong2 *q = reinterpret_cast<longlong2 *>(a.sums) + 2 * (image_off + (int64_t)Y * W + X);
+                const longlong2 q0 = q[0], q1 = q[1];
+                q[0] = make_longlong2(q0.x + p.r, q0.y + p.g);
+                q[1] = make_longlong2(q1.x + p.b, q1.y + p.a);
+            }
             continue;
         }
-        const float ar = (float)((double)ir * scale), ag = (float)((double)ig * scale);
-        const float ab = (float)((double)ib * scale), aa = (float)((double)ia * scale);
-        const uint32_t out = enc8<SRGB>(T, ar) | (enc8<SRGB>(T, ag) << 8) | (enc8<SRGB>(T, ab) << 16) |
-                             (enc_lin(aa) << 24);
-        image[pix] = out;
+        out[k] = encode_mean<SRGB>(T, p, scale);
+    }
+    if (a.sums != nullptr) return;
+#pragma unroll
+    for (int py = 0; py < 2; ++py) {
+        const int Y = y0 + py;
+        if (Y >= H) continue;
+        const int64_t pix = (int64_t)Y * W + X0;
+        if (X0 + 1 < W && (reinterpret_cast<uintptr_t>(image + pix) & 7u) == 0) {
+            *reinterpret_cast<uint2 *>(image + pix) = make_uint2(out[py], out[2 + py]);
+        } else {
+            if (X0 < W) image[pix] = out[py];
+            if (X0 + 1 < W) image[pix + 1] = out[2 + py];
+        }
     }
 }
 
 // Persistent resolve: each warp takes bins from the frame's bin queue until
-// it is empty; a warp's overflow slot is reused from bin to bin.
+// it is empty; a warp's overflow entry area is reused from bin to bin.
 template <int S, bool MS, bool SRGB, bool GRAD>
 __device__ __forceinline__ void resolve_persistent(const FrameArgs &a, const int4 *__restrict__ draw,
-                                                                 const uint32_t *__restrict__ merged,
-                                                                 const uint32_t *__restrict__ pval,
-                                                                 const uint32_t *__restrict__ bstart,
-                                                                 const uint32_t *__restrict__ bend,
-                                                                 uint32_t *__restrict__ image,
-                                                                 uint32_t *__restrict__ overflow,
-                                                                 uint32_t *__restrict__ bin_queue) {
-    constexpr int CAP = MS ? kCapMS : 1;
-    constexpr bool EXPLICIT = MS && S > CAP;
+                                                   const uint32_t *__restrict__ merged,
+                                                   const uint32_t *__restrict__ pval,
+                                                   const uint32_t *__restrict__ bstart,
+                                                   const uint32_t *__restrict__ bend, uint32_t *__restrict__ image,
+                                                   uint32_t *__restrict__ overflow, uint32_t *__restrict__ bin_queue) {
+    constexpr int CAP = MS ? kCellCap : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemTables &T = *reinterpret_cast<SmemTables *>(smem_raw);
     {
@@ -1169,21 +1181,22 @@ __device__ __forceinline__ void resolve_persistent(const FrameArgs &a, const int
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    BinState<CAP> &w = reinterpret_cast<BinState<CAP> *>(smem_raw + sizeof(SmemTables))[warp];
+    CellState<S / 8, CAP> &w = reinterpret_cast<CellState<S / 8, CAP> *>(smem_raw + sizeof(SmemTables))[warp];
     const int64_t slot = (int64_t)blockIdx.x * kResolveWarps + warp;
-    uint32_t *ovf = EXPLICIT ? overflow + slot * 64 * 32 : nullptr;
+    // entries past CAP: up to one per sample of the cell
+    uint32_t *gx = MS ? overflow + slot * (int64_t)(4 * S - CAP) * (S / 8 + 1) * 32 : nullptr;
     for (;;) {
         uint32_t b = 0;
         if (lane == 0) b = atomicAdd(bin_queue, 1u);
         b = __shfl_sync(0xffffffffu, b, 0);
         if ((int64_t)b >= a.n_bins) break;
-        resolve_bin<S, MS, SRGB, CAP, GRAD>(a, draw, merged, pval, bstart, bend, image, ovf, T, w, lane, b);
+        resolve_bin<S, MS, SRGB, CAP, GRAD>(a, draw, merged, pval, bstart, bend, image, gx, T, w, lane, b);
         __syncwarp();
     }
 }
 
 template <int S, bool MS, bool SRGB>
-__global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
+__global__ void __launch_bounds__(kResolveWarps * 32, 3) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
                                                                  const uint32_t *__restrict__ merged,
                                                                  const uint32_t *__restrict__ pval,
                                                                  const uint32_t *__restrict__ bstart,
@@ -1194,10 +1207,10 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(FrameArgs a, con
     resolve_persistent<S, MS, SRGB, false>(a, draw, merged, pval, bstart, bend, image, overflow, bin_queue);
 }
 
-// With gradient paints: registers capped so that the grid's blocks stay
-// resident (the per-pixel paint would otherwise take more).
+// With gradient paints: registers capped so that two blocks stay resident
+// (the per-pixel paint would otherwise take more).
 template <int S, bool MS, bool SRGB>
-__global__ void __launch_bounds__(kResolveWarps * 32, kResolveBlocksPerSM)
+__global__ void __launch_bounds__(kResolveWarps * 32, 2)
     k_resolve_grad(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ merged,
                    const uint32_t *__restrict__ pval, const uint32_t *__restrict__ bstart,
                    const uint32_t *__restrict__ bend, uint32_t *__restrict__ image, uint32_t *__restrict__ overflow,
@@ -1326,22 +1339,41 @@ int sm_count() {
     return n;
 }
 
+// Shared memory of a resolve block: the tables and one cell state per warp.
+size_t resolve_smem(int S, bool ms) {
+    const int MW = S / 8, CAP = ms ? kCellCap : 1;
+    return sizeof(SmemTables) + (size_t)kResolveWarps * ((size_t)CAP * (MW + 1) * 32 * 4 + 32 * 16 + (size_t)MW * 32 * 4);
+}
+
+// Resolve blocks per SM: as many as fit in shared memory (at most 4), or
+// the tuned count if lower.
+int resolve_bps(const FrameArgs &a) {
+    const int fit = std::max(1, std::min<int>(kResolveMaxBlocksPerSM, (int)((227u << 10) / resolve_smem(a.S, a.ms_output))));
+    return a.resolve_bps >= 1 && a.resolve_bps < fit ? a.resolve_bps : fit;
+}
+
 int64_t resolve_blocks(const FrameArgs &a) {
     const int64_t need = (a.n_bins + kResolveWarps - 1) / kResolveWarps;
-    const int bps = a.resolve_bps >= 1 && a.resolve_bps <= kResolveBlocksPerSM ? a.resolve_bps : kResolveBlocksPerSM;
-    return std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sm_count() * bps));
+    return std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sm_count() * resolve_bps(a)));
 }
 
 template <int S, bool MS, bool SRGB, bool GRAD>
 void resolve_variant_g(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
                      const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
                      uint32_t *queue, cudaStream_t s) {
-    constexpr int CAP = MS ? kCapMS : 1;
-    const size_t smem = sizeof(SmemTables) + (size_t)kResolveWarps * sizeof(BinState<CAP>);
+    constexpr int CAP = MS ? kCellCap : 1;
+    const size_t smem = sizeof(SmemTables) + (size_t)kResolveWarps * sizeof(CellState<S / 8, CAP>);
     auto kern = GRAD ? k_resolve_grad<S, MS, SRGB> : k_resolve<S, MS, SRGB>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<(unsigned)resolve_blocks(a), kResolveWarps * 32, smem, s>>>(a, draw, merged, pval, bstart, bend, image,
-                                                                      overflow, queue);
+    // resident blocks per SM (registers or shared memory), so that every
+    // launched block runs at once; never more than resolve_blocks(a), which
+    // sized the overflow entry area
+    int fit = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, kResolveWarps * 32, smem) != cudaSuccess || fit < 1)
+        fit = 1;
+    const int64_t blocks = std::min<int64_t>(resolve_blocks(a), (int64_t)sm_count() * fit);
+    kern<<<(unsigned)blocks, kResolveWarps * 32, smem, s>>>(a, draw, merged, pval, bstart, bend, image, overflow,
+                                                             queue);
 }
 
 // Gradient paints get their own instantiations: the per-pixel paint costs
@@ -1555,8 +1587,9 @@ int launch_selftest_encode(const ResolveTables *rt, unsigned long long *bad, cud
 int64_t resolve_warps(const FrameArgs &a) { return resolve_blocks(a) * kResolveWarps; }
 
 int64_t resolve_overflow_words(const FrameArgs &a) {
-    if (!(a.ms_output && a.S > kCapMS)) return 0;
-    return resolve_warps(a) * 64 * 32;
+    if (!a.ms_output) return 0;
+    const int S = a.S == 256 ? 32 : a.S;
+    return resolve_warps(a) * (int64_t)(4 * S - kCellCap) * (S / 8 + 1) * 32;
 }
 
 int launch_scene_prepare(const uint32_t *cvp, const uint8_t *ctype, const uint32_t *cpid, const float *arcw,
