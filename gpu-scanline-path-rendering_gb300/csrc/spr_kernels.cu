@@ -845,11 +845,16 @@ __device__ __forceinline__ float4 gradient_colour(const FrameArgs &a, const Smem
 // per-sample rule gives.
 constexpr int kCellCap = 8;
 
+// Draw items staged per window: kWin batches of 32.
+constexpr int kWin = 2;
+
 template <int MW, int CAP>
 struct CellState {
     uint32_t ent[CAP][MW + 1][32];  // entry j of lane l's cell: mask words k < MW, colour at k = MW
-    int4 it[32];                    // staged draw items
-    uint32_t mm[MW][32];            // their merged sample masks
+    uint32_t icol[kWin * 32];       // staged items: colour,
+    uint32_t imask[kWin * 32];      // merged mask index + 1 (0: a span),
+    uint32_t ixw[kWin * 32];        // first column | width << 16
+    uint32_t mine[kWin][32];        // per batch, the staged items covering lane l's cell
 };
 
 // Entry j of lane `lane`'s cell: its first word; word k is at [k * 32].
@@ -952,12 +957,21 @@ __device__ __forceinline__ void cell_apply(CellState<S / 8, CAP> &w, uint32_t *g
     if (changed && n > 1) cell_dedup<MW, CAP>(w, gx, lane, n);
 }
 
-// Sample mask of item q over lane `lane`'s cell: a merged fragment's mask, or
-// every sample for a span.
-template <int S, int CAP>
-__device__ __forceinline__ void item_mask(const CellState<S / 8, CAP> &w, int q, bool frag, uint32_t (&m)[S / 8]) {
+// Merged sample mask m (MW words) of fragment record `idx` (merged index + 1).
+template <int MW>
+__device__ __forceinline__ void load_mask(const uint32_t *__restrict__ merged, uint32_t idx, uint32_t (&m)[MW]) {
+    if (idx == 0u) {
 #pragma unroll
-    for (int k = 0; k < S / 8; ++k) m[k] = frag ? w.mm[k][q] : 0xFFFFFFFFu;
+        for (int k = 0; k < MW; ++k) m[k] = 0xFFFFFFFFu;  // a span: every sample
+    } else if constexpr (MW == 4) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(merged) + (idx - 1));
+        m[0] = v.x, m[1] = v.y, m[2] = v.z, m[3] = v.w;
+    } else if constexpr (MW == 2) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(merged) + (idx - 1));
+        m[0] = v.x, m[1] = v.y;
+    } else {
+        m[0] = __ldg(merged + (idx - 1));
+    }
 }
 
 // Exact mean of a pixel's samples: every decoded value x 2^36 is an integer,
@@ -981,9 +995,13 @@ __device__ __forceinline__ uint32_t encode_mean(const SmemTables &T, const Pixel
 }
 
 // One warp per bin.  Items (merged fragments and spans, in draw-list order)
-// are staged 32 at a time; a 32 x 32 ballot transpose of their cell sets
-// gives every lane the staged items covering its cell, which it applies in
-// order.  Then every pixel is averaged over its samples.
+// are staged kWin x 32 at a time; a 32 x 32 ballot transpose of each batch's
+// cell sets gives every lane the staged items covering its cell, which it
+// applies in order, independently of the other lanes until the window ends
+// (a lane's work is the items over its own cell, not the most any lane has
+// in each batch).  The merged mask of the lane's next item is loaded while
+// it applies the current one.  Then every pixel is averaged over its
+// samples.
 template <int S, bool MS, bool SRGB, int CAP, bool GRAD>
 __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__restrict__ draw,
                                             const uint32_t *__restrict__ merged, const uint32_t *__restrict__ pval,
@@ -1024,52 +1042,54 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
         for (int k = 0; k <= MW; ++k) w.ent[0][k][lane] = 0xFFFFFFFFu;
     }
     const uint32_t beg = bstart[b], fin = bend[b];
-    for (uint32_t base = beg; base < fin; base += 32) {
+    for (uint32_t base = beg; base < fin; base += kWin * 32) {
         __syncwarp();
-        const int cnt = (int)min(32u, fin - base);
-        uint32_t cm = 0u;  // cells of this lane's staged item
-        if (lane < cnt) {
-            const int4 it = draw[pval[base + lane]];
-            w.it[lane] = it;
-            const int x = (int)((uint32_t)it.x & 0xFFFFu);
-            if (it.w != 0) {
-                if constexpr (MW == 4) {
-                    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(merged) + (it.w - 1));
-                    w.mm[0][lane] = v.x;
-                    w.mm[1][lane] = v.y;
-                    w.mm[2][lane] = v.z;
-                    w.mm[3][lane] = v.w;
-                } else if constexpr (MW == 2) {
-                    const uint2 v = __ldg(reinterpret_cast<const uint2 *>(merged) + (it.w - 1));
-                    w.mm[0][lane] = v.x;
-                    w.mm[1][lane] = v.y;
+        const int nb = (int)min((uint32_t)kWin, (fin - base + 31) / 32);  // batches in this window
+        for (int c = 0; c < nb; ++c) {
+            const uint32_t p = base + c * 32 + lane;
+            uint32_t cm = 0u;  // cells of this lane's staged item
+            if (p < fin) {
+                const int4 it = draw[pval[p]];
+                const int x = (int)((uint32_t)it.x & 0xFFFFu);
+                w.icol[c * 32 + lane] = (uint32_t)it.z;
+                w.imask[c * 32 + lane] = (uint32_t)it.w;
+                w.ixw[c * 32 + lane] = ((uint32_t)it.x & 0xFFFFu) | ((uint32_t)it.y << 16);
+                if (it.w != 0) {
+                    cm = x < W ? cell_bits((x - tx0) >> 1, ((x - tx0) >> 1) + 1) : 0u;
                 } else {
-                    w.mm[0][lane] = __ldg(merged + (it.w - 1));
+                    const int xa = max(x, 0), xb = min(x + it.y, W);
+                    cm = xb > xa ? cell_bits((xa - tx0) >> 1, (xb - tx0 + 1) >> 1) : 0u;
                 }
-                cm = x < W ? cell_bits((x - tx0) >> 1, ((x - tx0) >> 1) + 1) : 0u;
-            } else {
-                const int xa = max(x, 0), xb = min(x + it.y, W);
-                cm = xb > xa ? cell_bits((xa - tx0) >> 1, (xb - tx0 + 1) >> 1) : 0u;
             }
+            // bit q of lane L's word: staged item q covers cell L (a transpose
+            // of the 32 x 32 bit matrix of cell sets)
+            uint32_t mine = 0u;
+#pragma unroll
+            for (int L = 0; L < 32; ++L) {
+                const uint32_t bm = __ballot_sync(0xffffffffu, (cm >> L) & 1u);
+                if (lane == L) mine = bm;
+            }
+            w.mine[c][lane] = mine;
         }
         __syncwarp();
-        // mine: bit q = staged item q covers this lane's cell (a transpose of
-        // the 32 x 32 bit matrix of cell sets)
-        uint32_t mine = 0u;
-#pragma unroll
-        for (int L = 0; L < 32; ++L) {
-            const uint32_t bm = __ballot_sync(0xffffffffu, (cm >> L) & 1u);
-            if (lane == L) mine = bm;
-        }
-        // every lane applies its own items in draw order to its cell
-        while (mine) {
-            const int q = __ffs(mine) - 1;
-            mine &= mine - 1u;
-            const int4 it = w.it[q];
-            const bool frag = it.w != 0;
-            const uint32_t c = (uint32_t)it.z;
-            uint32_t m[MW];
-            item_mask<S, CAP>(w, q, frag, m);
+        // this lane's items in draw order: batch cw, remaining bits
+        int cw = 0;
+        uint32_t bits = w.mine[0][lane];
+        auto next_item = [&]() -> int {
+            while (bits == 0u && ++cw < nb) bits = w.mine[cw][lane];
+            if (bits == 0u) return -1;
+            const int q = cw * 32 + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            return q;
+        };
+        int q = next_item();
+        uint32_t m[MW];
+        if (q >= 0) load_mask<MW>(merged, w.imask[q], m);
+        while (q >= 0) {
+            const int qn = next_item();
+            uint32_t mn[MW];
+            if (qn >= 0) load_mask<MW>(merged, w.imask[qn], mn);
+            const uint32_t c = w.icol[q];
             if (!GRAD || c - 1u >= a.n_grad) {  // a solid colour (else a gradient paint)
                 const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
                             sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane), sa = lin8(c >> 24);
@@ -1089,6 +1109,7 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
                 }
             } else if constexpr (GRAD) {
                 // a colour per pixel: one application per pixel
+                const uint32_t xw = w.ixw[q];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const int X = X0 + (k >> 1), Y = y0 + (k & 1);
@@ -1100,8 +1121,8 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
                         cov += __popc(mk[wd]);
                     }
                     if (cov == 0) continue;
-                    const float4 gc = gradient_colour<SRGB>(a, T, c - 1u, (int)(int16_t)(it.x & 0xFFFF), it.y, X, Y,
-                                                            lane);
+                    const float4 gc = gradient_colour<SRGB>(a, T, c - 1u, (int)(int16_t)(xw & 0xFFFFu), (int)(xw >> 16),
+                                                            X, Y, lane);
                     if constexpr (MS) {
                         cell_apply<S, SRGB, CAP>(w, gx, lane, n, mk, T, gc.x, gc.y, gc.z, gc.w);
                     } else {
@@ -1110,6 +1131,9 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
                     }
                 }
             }
+            q = qn;
+#pragma unroll
+            for (int k = 0; k < MW; ++k) m[k] = mn[k];
         }
     }
     __syncwarp();
