@@ -146,15 +146,15 @@ struct spr_handle {
     bool out_tf = false;
     OutputInverse out_inv{{1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f}};
     DevBuf output;
-    DevBuf wn_base;  // batch frames: the winding scan at every scene's first entry
     // raw curve arrays of the device-side scene upload (kept for vertex updates)
     DevBuf sc_vpos, sc_type, sc_pid, sc_w, scene_flags;
     bool scene_on_device = false, scene_has_arcw = false;
     int tape_depth = 128;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
-        wn_scan, draw, heads, flags_tmp, merged, tiles, pair_off, pkey[2], pval[2], bins, image, counters, dump_tmp,
-        overflow;
+        wn_scan, draw, heads, merged, tiles, pair_off, pkey[2], pval[2], bins, image, counters, dump_tmp, overflow;
+    // look-back tile words of the frame's scans: entry offsets, scan-mark, pair offsets
+    DevBuf lb_off, lb_mark, lb_pair;
     uint64_t *skey_sorted = nullptr;
     uint32_t *perm_sorted = nullptr;
     const uint32_t *pv_sorted = nullptr;  // resolve pairs in bin order
@@ -170,13 +170,32 @@ struct spr_handle {
     bool frame_valid = false;
     int launches = 0, host_syncs = 0;
     int frame_W = 0, frame_H = 0, frame_S = 8;
-    // graph replay of unchanged frames: the launch sequence of the last eager
-    // frame, captured with its sizes (no host reads)
+    // Buffer capacities of the frame (intersection entries, draw items,
+    // resolve pairs).  A "sized" frame reads its sizes back as it goes and
+    // sets them with headroom; while they hold (caps_ok), frames run without
+    // host reads, taking their sizes from the device counters, and a frame
+    // whose sizes outgrow them is rendered again (sized) before anything
+    // reads it.
+    int64_t cap_nf = 0, cap_items = 0, cap_pairs = 0;
+    bool caps_ok = false;
+    // a frame rendered without host reads whose counters have not been read
+    // yet (their copy in h_counters is complete once done_ev is); stale:
+    // the inputs changed after it was enqueued (it cannot be rendered again)
+    bool pending = false, pending_stale = false;
+    cudaStream_t pending_stream = nullptr;
+    cudaEvent_t done_ev = nullptr;
+    // bounded waits of the look-back scans: polls before giving up, and (for
+    // tests of the timeout) a tile of the entry-offset scan that never
+    // publishes (-1: none)
+    uint32_t lb_spin_cap = kLbSpinCap;
+    int64_t lb_hold_tile = -1;
+    // graph replay of unchanged frames: the launch sequence of a frame
+    // rendered without host reads, captured once (it depends on the
+    // capacities, not on the sizes)
     bool graph_mode = false, capturing = false, graph_failed = false;
     cudaGraphExec_t gexec = nullptr;
     uint64_t gexec_gen = 0;
     cudaStream_t cap_stream = nullptr;
-    int64_t cap_nf = 0, cap_nm = 0, cap_ns = 0, cap_np = 0;
     int graph_replays = 0;
     // timing
     bool timing = false;
@@ -193,22 +212,25 @@ std::vector<DevBuf *> handle_bufs(spr_handle *h) {
                       &h->fill,       &h->affine,  &h->tvert,    &h->pflags,    &h->pvis,    &h->counts,
                       &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
                       &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
-                      &h->wn_scan,    &h->draw,    &h->heads,    &h->flags_tmp, &h->merged,  &h->tiles,
+                      &h->wn_scan,    &h->draw,    &h->heads,    &h->lb_off,    &h->merged,  &h->tiles,
                       &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
                       &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
                       &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
                       &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
                       &h->eval[1], &h->sc_vpos, &h->sc_type, &h->sc_pid, &h->sc_w, &h->scene_flags,
                       &h->sums, &h->gfill_pass, &h->gtvert_total, &h->grad_table, &h->grad_ramp, &h->path_start,
-                      &h->output, &h->wn_base};
+                      &h->output, &h->lb_mark, &h->lb_pair};
 }
 
 }  // namespace
 
 namespace {
 
-void drop_graph(spr_handle *h) {
-    h->diff_ready = false;  // every caller changes the frame's inputs
+void drop_graph(spr_handle *h, bool inputs_changed = true) {
+    if (inputs_changed) {
+        h->diff_ready = false;
+        if (h->pending) h->pending_stale = true;
+    }
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
     h->graph_failed = false;
@@ -398,6 +420,7 @@ int spr_destroy(spr_handle *h) {
     cudaSetDevice(h->cfg.device);
     drop_graph(h);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    if (h->done_ev) cudaEventDestroy(h->done_ev);
     for (DevBuf *b : handle_bufs(h)) b->release();
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->h_u32) cudaFreeHost(h->h_u32);
@@ -410,6 +433,7 @@ int spr_destroy(spr_handle *h) {
 int spr_resize(spr_handle *h, int32_t width, int32_t height) {
     if (!h) return SPR_ERR_INVALID_ARG;
     drop_graph(h);
+    h->caps_ok = false;
     spr_config c = h->cfg;
     c.width = width;
     c.height = height;
@@ -423,6 +447,7 @@ int spr_resize(spr_handle *h, int32_t width, int32_t height) {
 int spr_set_samples(spr_handle *h, int32_t samples) {
     if (!h) return SPR_ERR_INVALID_ARG;
     drop_graph(h);
+    h->caps_ok = false;
     if (samples != 8 && samples != 16 && samples != 32 && samples != 256) return SPR_ERR_INVALID_ARG;
     if (samples == 256 && !h->cfg.ms_output) return SPR_ERR_INVALID_ARG;
     cudaSetDevice(h->cfg.device);
@@ -507,6 +532,7 @@ extern "C" {
 int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     if (!h) return SPR_ERR_INVALID_ARG;
     drop_graph(h);
+    h->caps_ok = false;
     int st = validate_view(v);
     if (st) return st;
     cudaSetDevice(h->cfg.device);
@@ -622,7 +648,7 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
     d.nf = h->nf;
     FrameCounters *ctr = h->counters.as<FrameCounters>();
     d.queue = &ctr->bin_queue;
-    d.status = &ctr->status;
+    d.status = &ctr->diff_status;
     d.out_scale = dc.scale;
     d.accumulate = dc.pass > 0 ? 1 : 0;
     if (!dc.backward) {
@@ -652,10 +678,10 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
         d.tape_depth = depth;
         cudaMemsetAsync(d.grad_fill, 0, 16 * (size_t)h->P, s);
         cudaMemsetAsync(h->grad_tvert.p, 0, 8 * (size_t)h->V, s);
-        cudaMemsetAsync(&ctr->status, 0, 4, s);
+        cudaMemsetAsync(&ctr->diff_status, 0, 4, s);
         cudaMemsetAsync(d.n_chain, 0, 4, s);
         *L += launch_diff_backward(a, d, s);
-        cudaMemcpyAsync(h->h_u32, &ctr->status, 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(h->h_u32, &ctr->diff_status, 4, cudaMemcpyDeviceToHost, s);
         ++h->host_syncs;
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
         if (!(h->h_u32[0] & 1u)) {
@@ -679,12 +705,76 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
     return cuda_status();
 }
 
+// Headroom of the capacities a sized frame sets, so that frames whose sizes
+// drift a little (an animation, a fitting loop) keep fitting.
+int64_t with_headroom(int64_t n) { return n + n / 8 + 256; }
+
+// The counters of a frame rendered without host reads, once complete:
+// sizes to the host, or the frame rendered again (sized) if it outgrew its
+// buffers.  Every call that reads a frame's results settles it first.
+int render_frame(spr_handle *h, void *stream, const DiffCall *dc);
+
+// Queues the copy of a frame's counters to the host and the event after it
+// (a frame rendered without host reads).
+int mark_pending(spr_handle *h, cudaStream_t s) {
+    if (!h->done_ev && cudaEventCreateWithFlags(&h->done_ev, cudaEventDisableTiming) != cudaSuccess)
+        return cuda_status();
+    cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
+    cudaEventRecord(h->done_ev, s);
+    h->pending = true;
+    h->pending_stale = false;
+    h->pending_stream = s;
+    return SPR_OK;
+}
+
+int settle(spr_handle *h) {
+    if (!h->pending) return SPR_OK;
+    h->pending = false;
+    if (cudaEventSynchronize(h->done_ev) != cudaSuccess) return cuda_status();
+    const FrameCounters c = *h->h_counters;
+    if (c.status & kStatusTimeout) {
+        h->frame_valid = false;
+        return SPR_ERR_TIMEOUT;
+    }
+    if (c.status & kStatusOverflow) {
+        h->caps_ok = false;
+        if (h->pending_stale) {  // its inputs are gone: it cannot be rendered again
+            h->frame_valid = false;
+            return SPR_ERR_CAPACITY_EXCEEDED;
+        }
+        return render_frame(h, h->pending_stream, nullptr);
+    }
+    h->nf = c.nf;
+    h->nm = c.n_merged;
+    h->ns = c.n_span;
+    h->npairs = c.n_pairs;
+    h->en.curve_fragment = (int32_t)c.nf;
+    h->en.merged_fragment = (int32_t)c.n_merged;
+    h->en.span = (int32_t)c.n_span;
+    return SPR_OK;
+}
+
+// A pending frame that a new frame supersedes: its overflow, if it is known
+// already, still teaches the capacities (no waiting).
+void supersede(spr_handle *h) {
+    if (!h->pending) return;
+    h->pending = false;
+    if (cudaEventQuery(h->done_ev) == cudaSuccess && (h->h_counters->status & kStatusOverflow)) h->caps_ok = false;
+    cudaGetLastError();  // (cudaErrorNotReady)
+}
+
 // Fragment sort choice: one block per path needs enough paths to fill the
 // GPU and segments short enough for shared memory (longer ones are sorted by
 // a single block, chunk by chunk).
 constexpr int64_t kSegmentSortMinPaths = 1024;
 constexpr int64_t kSegmentSortMaxMean = 2048;  // mean entries per path
 
+// One frame.  Sized (differentiable frames, and the first frame after a
+// change of scene, viewport or sample count): the entry count and then the
+// pair count are read back as they are known, and the buffers and their
+// capacities set from them.  Otherwise no host reads: every kernel takes
+// its size from the device counters and its grid from the capacities, and
+// the counters are copied to the host for settle().
 int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     if (!h) return SPR_ERR_INVALID_ARG;
     if (!h->has_scene) return SPR_ERR_NO_SCENE;
@@ -692,6 +782,7 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     int st = build_tables(h);
     if (st) return st;
+    supersede(h);
     h->frame_valid = false;
     h->diff_ready = false;
     int L = 0;  // kernels launched by this frame
@@ -700,95 +791,73 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     const int W = a.W, H = a.H, WORDS = a.S / 8;
     const bool batch = h->n_scenes > 0;
     const int64_t npix = frame_pixels(h);
+    // (the passes of a 256-sample frame are sized: they add up into one image)
+    const bool sized = (dc != nullptr || !h->caps_ok || h->cfg.samples == 256) && !h->capturing;
     if (h->timing) {
         for (auto &e : h->ev)
             if (!e) cudaEventCreate(&e);
     }
+    FrameCounters *ctr = h->counters.as<FrameCounters>();
+    const int64_t nbins = a.n_bins;
     // stage 3: transform + visibility
     if ((st = ensure(h->tvert, sizeof(float2) * h->V)) || (st = ensure(h->pflags, 4 * (size_t)h->P)) ||
-        (st = ensure(h->pvis, h->P)) || (st = ensure(h->counts, 4 * (size_t)h->C + 4)) ||
-        (st = ensure(h->offsets, 4 * ((size_t)h->C + 1))) ||
-        (st = ensure(h->scan_tmp, 4 * (size_t)scan_tmp_words(std::max<int64_t>(h->C, 1)))) ||
-        (st = ensure(h->image, 4 * (size_t)npix)))
+        (st = ensure(h->pvis, h->P)) || (st = ensure(h->counts, 4 * (size_t)h->C + 16)) ||
+        (st = ensure(h->offsets, 4 * ((size_t)h->C + 1) + 16)) ||
+        (st = ensure(h->lb_off, 8 * (size_t)lookback_words(h->C))) || (st = ensure(h->image, 4 * (size_t)npix)) ||
+        (st = ensure(h->bins, 8 * (size_t)nbins)) ||
+        (st = ensure(h->overflow, 4 * (size_t)std::max<int64_t>(resolve_overflow_words(a), 1))))
         return st;
+    cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);
     rec(h, 0, s);
     L += launch_transform(a, h->tvert.as<float2>(), h->pflags.as<uint32_t>(), h->pvis.as<uint8_t>(), s);
     rec(h, 1, s);
-    // stages 4-5: monotone pieces, entry counts, exclusive scan
+    // stages 4-5: monotone pieces, entry counts, offsets (single-pass scan)
     L += launch_curve_count(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->counts.as<uint32_t>(), s);
-    L += scan_exclusive_u32(h->counts.as<uint32_t>(), h->offsets.as<uint32_t>(), h->C, h->scan_tmp.as<uint32_t>(), s);
-    // under capture the sizes are those of the eager frame just rendered
-    const bool cap = h->capturing;
-    const int64_t cap_nm = h->cap_nm, cap_ns = h->cap_ns, cap_np = h->cap_np;
-    if (!cap) {
-        cudaMemcpyAsync(h->h_u32, h->offsets.as<uint32_t>() + h->C, 4, cudaMemcpyDeviceToHost, s);
+    cudaMemsetAsync(h->lb_off.p, 0, 8 * (size_t)lookback_words(h->C), s);
+    L += scan_lookback_u32(h->counts.as<uint32_t>(), h->offsets.as<uint32_t>(), nullptr, h->C, h->lb_off.as<uint64_t>(),
+                           &ctr->tiles[0], h->lb_spin_cap, &ctr->status, &ctr->need_nf, s, h->lb_hold_tile);
+    if (sized) {
+        cudaMemcpyAsync(h->h_u32, &ctr->need_nf, 4, cudaMemcpyDeviceToHost, s);
         ++h->host_syncs;
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
         if ((st = cuda_status())) return st;
+        const int64_t need = h->h_u32[0];
+        if (need > INT32_MAX) return SPR_ERR_CAPACITY_EXCEEDED;
+        h->cap_nf = dc ? std::max<int64_t>(need, 1) : with_headroom(need);
+        h->cap_items = 2 * h->cap_nf;
     }
-    const int64_t nf = cap ? h->cap_nf : h->h_u32[0];
-    if (nf > INT32_MAX) return SPR_ERR_CAPACITY_EXCEEDED;
-    h->nf = nf;
-    h->en.path = (int32_t)h->P;
-    h->en.curve = (int32_t)h->C;
-    h->en.vertex = (int32_t)h->V;
-    h->en.curve_fragment = (int32_t)nf;
-    h->en.merged_fragment = 0;
-    h->en.span = 0;
-    h->nm = h->ns = h->npairs = 0;
-    const int64_t nbins = a.n_bins;
-    if ((st = ensure(h->bins, 8 * (size_t)nbins))) return st;
-    if ((st = ensure(h->overflow, 4 * (size_t)std::max<int64_t>(resolve_overflow_words(a), 1)))) return st;
-    uint32_t *bin_start = h->bins.as<uint32_t>(), *bin_end = bin_start + nbins;
-    if (nf == 0) {
-        cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
-        for (int i = 2; i <= 6; ++i) rec(h, i, s);
-        if (dc) {
-            if ((st = diff_stage(h, a, *dc, nullptr, bin_start, bin_end, s, &L))) return st;
-        } else {
-            L += launch_resolve(a, nullptr, nullptr, nullptr, bin_start, bin_end, h->image.as<uint32_t>(),
-                                h->overflow.as<uint32_t>(), h->counters.as<FrameCounters>(), s);
-        }
-        rec(h, 7, s);
-        rec(h, 8, s);
-        h->launches = L;
-        h->pv_sorted = nullptr;
-        h->diff_ready = dc && !dc->backward;
-        h->frame_valid = true;
-        h->frame_W = W;
-        h->frame_H = H;
-        h->frame_S = a.S;
-        return cuda_status();
-    }
+    const int64_t cap_nf = h->cap_nf, cap_items = h->cap_items;
     // stages 6-7: entries, fragments, boundary masks
-    if ((st = ensure(h->entries, 8 * (size_t)nf)) || (st = ensure(h->key, 4 * (size_t)nf)) ||
-        (st = ensure(h->pidw, 4 * (size_t)nf)) || (st = ensure(h->wn, (size_t)nf)) ||
-        (st = ensure(h->mask, 4 * (size_t)WORDS * nf)) || (st = ensure(h->skey[0], 8 * (size_t)nf)) ||
-        (st = ensure(h->skey[1], 8 * (size_t)nf)) || (st = ensure(h->sval[0], 4 * (size_t)nf)) ||
-        (st = ensure(h->sval[1], 4 * (size_t)nf)) || (st = ensure(h->sort_tmp, 4 * (size_t)radix_tmp_words(nf))) ||
-        (st = ensure(h->wn_scan, (size_t)nf)) || (st = ensure(h->draw, 16 * 2 * (size_t)nf)) ||
-        (st = ensure(h->heads, 4 * (size_t)nf)) || (st = ensure(h->flags_tmp, 4 * (size_t)flags_tmp_words(nf))) ||
-        (st = ensure(h->merged, 4 * (size_t)WORDS * nf)) ||
-        (batch && (st = ensure(h->item_scene, 4 * 2 * (size_t)nf))) ||
-        (batch && (st = ensure(h->wn_base, (size_t)std::max(h->n_scenes, 1)))))
+    if ((st = ensure(h->entries, 8 * (size_t)cap_nf)) || (st = ensure(h->key, 4 * (size_t)cap_nf)) ||
+        (st = ensure(h->pidw, 4 * (size_t)cap_nf)) || (st = ensure(h->wn, (size_t)cap_nf)) ||
+        (st = ensure(h->mask, 4 * (size_t)WORDS * cap_nf)) || (st = ensure(h->skey[0], 8 * (size_t)cap_nf)) ||
+        (st = ensure(h->skey[1], 8 * (size_t)cap_nf)) || (st = ensure(h->sval[0], 4 * (size_t)cap_nf)) ||
+        (st = ensure(h->sval[1], 4 * (size_t)cap_nf)) || (st = ensure(h->wn_scan, (size_t)cap_nf)) ||
+        (st = ensure(h->draw, 16 * (size_t)cap_items)) || (st = ensure(h->heads, 4 * (size_t)cap_nf)) ||
+        (st = ensure(h->lb_mark, 8 * (size_t)scan_mark_status_words(cap_nf))) ||
+        (st = ensure(h->merged, 4 * (size_t)WORDS * cap_nf)) ||
+        (st = ensure(h->tiles, 4 * (size_t)cap_items + 16)) || (st = ensure(h->pair_off, 4 * (size_t)cap_items + 16)) ||
+        (st = ensure(h->lb_pair, 8 * (size_t)lookback_words(cap_items))) ||
+        (batch && (st = ensure(h->item_scene, 4 * (size_t)cap_items))))
         return st;
     uint32_t *item_scene = batch ? h->item_scene.as<uint32_t>() : nullptr;
     if (dc) {
-        if ((st = ensure(h->chord, 16 * (size_t)nf)) || (st = ensure(h->lmask, 4 * (size_t)WORDS * nf)) ||
-            (st = ensure(h->vmask, 4 * (size_t)WORDS * nf)) || (st = ensure(h->item_path, 4 * 2 * (size_t)nf)))
+        if ((st = ensure(h->chord, 16 * (size_t)cap_nf)) || (st = ensure(h->lmask, 4 * (size_t)WORDS * cap_nf)) ||
+            (st = ensure(h->vmask, 4 * (size_t)WORDS * cap_nf)) || (st = ensure(h->item_path, 4 * (size_t)cap_items)))
             return st;
         a.chord = h->chord.as<float4>();
         a.lmask = h->lmask.as<uint32_t>();
         a.vmask = h->vmask.as<uint32_t>();
         a.item_path = h->item_path.as<uint32_t>();
     }
+    L += launch_admit(&ctr->need_nf, &ctr->nf, (uint32_t)std::min<int64_t>(cap_nf, INT32_MAX), &ctr->status, s);
     rec(h, 2, s);
     // emission order: curves sorted by estimated cost (16-bit keys, two passes)
     const uint32_t *order = nullptr;
     if (h->tune_emit >= 0 ? h->tune_emit == 1 : h->C >= 4096) {
         if ((st = ensure(h->ekey[0], 4 * (size_t)h->C)) || (st = ensure(h->ekey[1], 4 * (size_t)h->C)) ||
             (st = ensure(h->eval[0], 4 * (size_t)h->C)) || (st = ensure(h->eval[1], 4 * (size_t)h->C)) ||
-            (st = ensure(h->sort_tmp, 4 * (size_t)std::max(radix_tmp_words(nf), radix_tmp_words(h->C)))))
+            (st = ensure(h->sort_tmp, 4 * (size_t)radix_tmp_words(std::max<int64_t>(cap_nf, h->C)))))
             return st;
         L += launch_emit_keys(a, h->counts.as<uint32_t>(), h->ekey[0].as<uint32_t>(), h->eval[0].as<uint32_t>(), s);
         int el = 0;
@@ -799,9 +868,10 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         order = ealt ? h->eval[1].as<uint32_t>() : h->eval[0].as<uint32_t>();
     }
     L += launch_curve_emit(a, h->tvert.as<float2>(), h->pvis.as<uint8_t>(), h->offsets.as<uint32_t>(), order,
-                           h->entries.as<int2>(), s);
-    L += launch_fragment(a, h->tvert.as<float2>(), h->entries.as<int2>(), nf, h->key.as<int32_t>(), h->pidw.as<uint32_t>(),
-                    h->wn.as<int8_t>(), h->mask.as<uint32_t>(), h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), s);
+                           h->entries.as<int2>(), ctr, s);
+    L += launch_fragment(a, h->tvert.as<float2>(), h->entries.as<int2>(), cap_nf, ctr, h->key.as<int32_t>(),
+                         h->pidw.as<uint32_t>(), h->wn.as<int8_t>(), h->mask.as<uint32_t>(),
+                         h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), s);
     rec(h, 3, s);
     // stage 8: stable sort by (path, cell key).  The entries arrive grouped by
     // path, so with enough paths to fill the GPU each path's segment is
@@ -810,79 +880,86 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     int rl = 0;
     const bool segment_sort = h->tune_sort >= 0 ? h->tune_sort == 1
                                                 : h->P >= kSegmentSortMinPaths &&
-                                                      nf / std::max<int64_t>(h->P, 1) <= kSegmentSortMaxMean;
+                                                      cap_nf / std::max<int64_t>(h->P, 1) <= kSegmentSortMaxMean;
     if (segment_sort && h->P > 0) {
         if ((st = ensure(h->path_start, 4 * ((size_t)h->P + 1)))) return st;
         L += launch_segment_sort(h->curves.as<CurveDesc>(), h->C, h->P, h->offsets.as<uint32_t>(),
                                  h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(), h->skey[1].as<uint64_t>(),
-                                 h->sval[1].as<uint32_t>(), h->path_start.as<uint32_t>(), s);
+                                 h->sval[1].as<uint32_t>(), h->path_start.as<uint32_t>(), ctr, s);
         h->skey_sorted = h->skey[1].as<uint64_t>();
         h->perm_sorted = h->sval[1].as<uint32_t>();
     } else {
+        if ((st = ensure(h->sort_tmp, 4 * (size_t)radix_tmp_words(std::max<int64_t>(cap_nf, h->C))))) return st;
         const int key_bits = 24 + bits_for(h->P ? h->P - 1 : 0);
         const bool alt = radix_sort<uint64_t>(h->skey[0].as<uint64_t>(), h->sval[0].as<uint32_t>(),
-                                              h->skey[1].as<uint64_t>(), h->sval[1].as<uint32_t>(), nf, key_bits,
-                                              h->sort_tmp.as<uint32_t>(), s, &rl);
+                                              h->skey[1].as<uint64_t>(), h->sval[1].as<uint32_t>(), cap_nf, key_bits,
+                                              h->sort_tmp.as<uint32_t>(), s, &rl, &ctr->nf);
         L += rl;
         h->skey_sorted = alt ? h->skey[1].as<uint64_t>() : h->skey[0].as<uint64_t>();
         h->perm_sorted = alt ? h->sval[1].as<uint32_t>() : h->sval[0].as<uint32_t>();
     }
     rec(h, 4, s);
-    // stages 9-12, 14: winding scan, marks, draw list
-    cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);
-    L += launch_scan_mark(a, nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
-                     h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, h->counters.as<FrameCounters>(),
-                     h->flags_tmp.as<uint32_t>(), batch ? h->wn_base.as<int8_t>() : nullptr, s);
-    if (!cap) {
+    // stages 9-12, 14: winding scan, marks, draw list (one look-back pass)
+    cudaMemsetAsync(h->lb_mark.p, 0, 8 * (size_t)scan_mark_status_words(cap_nf), s);
+    L += launch_scan_mark(a, cap_nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
+                          h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, ctr, h->lb_mark.as<uint64_t>(),
+                          h->lb_spin_cap, s);
+    rec(h, 5, s);
+    // stage 13: merged sample masks
+    L += launch_stencil(a, cap_nf, ctr, h->skey_sorted, h->perm_sorted, h->pidw.as<uint32_t>(), h->mask.as<uint32_t>(),
+                        h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), s);
+    rec(h, 6, s);
+    // stage 15: bin draw items by (cell row, 64-column tile), resolve
+    L += launch_item_tiles(a, h->draw.as<int4>(), item_scene, cap_items, ctr, h->tiles.as<uint32_t>(), s);
+    cudaMemsetAsync(h->lb_pair.p, 0, 8 * (size_t)lookback_words(cap_items), s);
+    L += scan_lookback_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), &ctr->n_items, cap_items,
+                           h->lb_pair.as<uint64_t>(), &ctr->tiles[2], h->lb_spin_cap, &ctr->status, &ctr->need_pairs,
+                           s);
+    if (sized) {
         cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
         ++h->host_syncs;
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
         if ((st = cuda_status())) return st;
+        if (h->h_counters->status & kStatusTimeout) return SPR_ERR_TIMEOUT;
+        h->nf = h->h_counters->nf;
+        h->nm = h->h_counters->n_merged;
+        h->ns = h->h_counters->n_span;
+        h->npairs = h->h_counters->need_pairs;
+        h->cap_pairs = dc ? std::max<int64_t>(h->npairs, 1) : with_headroom(h->npairs);
     }
-    h->nm = cap ? cap_nm : h->h_counters->n_merged;
-    h->ns = cap ? cap_ns : h->h_counters->n_span;
-    h->en.merged_fragment = (int32_t)h->nm;
-    h->en.span = (int32_t)h->ns;
-    rec(h, 5, s);
-    // stage 13: merged sample masks
-    L += launch_stencil(a, nf, h->nm, h->skey_sorted, h->perm_sorted, h->pidw.as<uint32_t>(), h->mask.as<uint32_t>(),
-                   h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), s);
-    rec(h, 6, s);
-    // stage 15: bin draw items by (cell row, 32-column tile), resolve
-    const int64_t items = h->nm + h->ns;
-    if ((st = ensure(h->tiles, 4 * ((size_t)items + 1))) || (st = ensure(h->pair_off, 4 * ((size_t)items + 1))))
+    const int64_t cap_pairs = h->cap_pairs;
+    if ((st = ensure(h->pkey[0], 4 * (size_t)cap_pairs)) || (st = ensure(h->pkey[1], 4 * (size_t)cap_pairs)) ||
+        (st = ensure(h->pval[0], 4 * (size_t)cap_pairs)) || (st = ensure(h->pval[1], 4 * (size_t)cap_pairs)) ||
+        (st = ensure(h->sort_tmp, 4 * (size_t)radix_tmp_words(std::max<int64_t>({cap_pairs, cap_nf, (int64_t)h->C})))))
         return st;
-    if ((st = ensure(h->scan_tmp, 4 * (size_t)scan_tmp_words(std::max<int64_t>({items, (int64_t)h->C, 1}))))) return st;
-    L += launch_item_tiles(a, h->draw.as<int4>(), item_scene, items, h->tiles.as<uint32_t>(), s);
-    L += scan_exclusive_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), items, h->scan_tmp.as<uint32_t>(), s);
-    if (!cap) {
-        cudaMemcpyAsync(h->h_u32, h->pair_off.as<uint32_t>() + items, 4, cudaMemcpyDeviceToHost, s);
-        ++h->host_syncs;
-        if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status();
-    }
-    const int64_t npairs = cap ? cap_np : h->h_u32[0];
-    h->npairs = npairs;
-    if ((st = ensure(h->pkey[0], 4 * (size_t)npairs)) || (st = ensure(h->pkey[1], 4 * (size_t)npairs)) ||
-        (st = ensure(h->pval[0], 4 * (size_t)npairs)) || (st = ensure(h->pval[1], 4 * (size_t)npairs)) ||
-        (st = ensure(h->sort_tmp, 4 * (size_t)std::max(radix_tmp_words(npairs), radix_tmp_words(nf)))))
-        return st;
-    L += launch_emit_pairs(a, h->draw.as<int4>(), item_scene, items, h->pair_off.as<uint32_t>(),
+    L += launch_admit(&ctr->need_pairs, &ctr->n_pairs, (uint32_t)std::min<int64_t>(cap_pairs, INT32_MAX),
+                      &ctr->status, s);
+    L += launch_emit_pairs(a, h->draw.as<int4>(), item_scene, cap_items, ctr, h->pair_off.as<uint32_t>(),
                            h->pkey[0].as<uint32_t>(), h->pval[0].as<uint32_t>(), s);
     const bool palt = radix_sort<uint32_t>(h->pkey[0].as<uint32_t>(), h->pval[0].as<uint32_t>(),
-                                           h->pkey[1].as<uint32_t>(), h->pval[1].as<uint32_t>(), npairs,
+                                           h->pkey[1].as<uint32_t>(), h->pval[1].as<uint32_t>(), cap_pairs,
                                            std::max(bits_for((uint64_t)nbins - 1), 1), h->sort_tmp.as<uint32_t>(), s,
-                                           &rl);
+                                           &rl, &ctr->n_pairs);
     L += rl;
     const uint32_t *pk = palt ? h->pkey[1].as<uint32_t>() : h->pkey[0].as<uint32_t>();
     const uint32_t *pv = palt ? h->pval[1].as<uint32_t>() : h->pval[0].as<uint32_t>();
+    uint32_t *bin_start = h->bins.as<uint32_t>(), *bin_end = bin_start + nbins;
     cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
-    L += launch_bin_bounds(pk, npairs, bin_start, bin_end, s);
+    L += launch_bin_bounds(pk, cap_pairs, ctr, bin_start, bin_end, s);
     rec(h, 7, s);
+    h->en.path = (int32_t)h->P;
+    h->en.curve = (int32_t)h->C;
+    h->en.vertex = (int32_t)h->V;
+    if (sized) {
+        h->en.curve_fragment = (int32_t)h->nf;
+        h->en.merged_fragment = (int32_t)h->nm;
+        h->en.span = (int32_t)h->ns;
+    }
     if (dc) {
         if ((st = diff_stage(h, a, *dc, pv, bin_start, bin_end, s, &L))) return st;
     } else {
         L += launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end,
-                            h->image.as<uint32_t>(), h->overflow.as<uint32_t>(), h->counters.as<FrameCounters>(), s);
+                            h->image.as<uint32_t>(), h->overflow.as<uint32_t>(), ctr, s);
     }
     rec(h, 8, s);
     if ((st = cuda_status())) return st;
@@ -894,6 +971,11 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
             h->step_ms[i] = ms;
         }
     }
+    if (sized) {
+        h->caps_ok = true;
+    } else if (!h->capturing) {
+        if ((st = mark_pending(h, s))) return st;  // the counters come back on their own; settle() reads them
+    }
     h->launches = L;
     h->pv_sorted = pv;
     h->diff_ready = dc && !dc->backward;
@@ -901,7 +983,7 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     h->frame_W = W;
     h->frame_H = H;
     h->frame_S = a.S;
-    return SPR_OK;
+    return cuda_status();
 }
 
 // Backward of the differentiable forward frame still held in the buffers
@@ -993,25 +1075,29 @@ int spr_render(spr_handle *h, void *stream) {
     if (!h->graph_mode || h->timing || !h->has_scene || h->cfg.samples == 256) return frame(h, stream, nullptr);
     cudaSetDevice(h->cfg.device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (h->gexec && h->gexec_gen != g_alloc_gen.load()) drop_graph(h);  // a buffer moved
+    if (h->gexec && (h->gexec_gen != g_alloc_gen.load() || !h->caps_ok)) drop_graph(h, false);  // buffers moved
+    int st0 = SPR_OK;
     if (h->gexec) {
+        supersede(h);
         if (cudaGraphLaunch(h->gexec, s) != cudaSuccess) return cuda_status();
+        if ((st0 = mark_pending(h, s))) return st0;
         h->host_syncs = 0;
         h->frame_valid = true;
         ++h->graph_replays;
         return cuda_status();
     }
+    // render this frame (sized if the capacities are not known), then
+    // capture the launch sequence of a frame without host reads: it depends
+    // on the capacities only, so replays stay valid while the sizes fit
     int st = render_frame(h, stream, nullptr);
     if (st || h->graph_failed) return st;
-    // capture this frame's launch sequence with its sizes
+    if ((st = settle(h))) return st;
     if (!h->cap_stream && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
         return cuda_status();
     const uint64_t gen = g_alloc_gen.load();
-    h->cap_nf = h->nf;
-    h->cap_nm = h->nm;
-    h->cap_ns = h->ns;
-    h->cap_np = h->npairs;
     const int host_syncs = h->host_syncs, launches = h->launches;
+    const spr_element_number en = h->en;
+    const int64_t nf = h->nf, nm = h->nm, ns = h->ns, npairs = h->npairs;
     cudaGraph_t g = nullptr;
     bool ok = cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
     if (ok) {
@@ -1031,6 +1117,8 @@ int spr_render(spr_handle *h, void *stream) {
     h->gexec_gen = gen;
     h->host_syncs = host_syncs;
     h->launches = launches;
+    h->en = en;
+    h->nf = nf, h->nm = nm, h->ns = ns, h->npairs = npairs;
     h->frame_valid = true;
     return SPR_OK;
 }
@@ -1085,7 +1173,7 @@ int spr_autotune(spr_handle *h, int32_t frames, void *stream, spr_tune *out) {
     if (!h || frames < 1) return SPR_ERR_INVALID_ARG;
     if (!h->has_scene) return SPR_ERR_NO_SCENE;
     cudaSetDevice(h->cfg.device);
-    drop_graph(h);
+    drop_graph(h, false);
     const bool timing = h->timing;
     h->timing = false;
     h->tune_sort = h->tune_emit = -1;
@@ -1133,7 +1221,7 @@ int spr_set_tuning(spr_handle *h, const spr_tune *t) {
     if (t->sort < -1 || t->sort > 1 || t->emit_order < -1 || t->emit_order > 1 || t->resolve_bps < 0 ||
         t->resolve_bps > 4)
         return SPR_ERR_INVALID_ARG;
-    drop_graph(h);
+    drop_graph(h, false);
     h->tune_sort = t->sort;
     h->tune_emit = t->emit_order;
     h->tune_bps = t->resolve_bps;
@@ -1143,7 +1231,7 @@ int spr_set_tuning(spr_handle *h, const spr_tune *t) {
 int spr_set_graph_replay(spr_handle *h, int32_t enable) {
     if (!h) return SPR_ERR_INVALID_ARG;
     h->graph_mode = enable != 0;
-    if (!h->graph_mode) drop_graph(h);
+    if (!h->graph_mode) drop_graph(h, false);
     return SPR_OK;
 }
 
@@ -1158,7 +1246,12 @@ int spr_update_vertices(spr_handle *h, const float *vertex, void *stream) {
     if (!h->has_scene) return SPR_ERR_NO_SCENE;
     if (!h->scene_on_device) return SPR_ERR_UNSUPPORTED;
     cudaSetDevice(h->cfg.device);
-    drop_graph(h);
+    // a captured frame reads the vertices from device memory and takes its
+    // sizes from the device counters, so it stays valid for the moved
+    // geometry: only the held differentiable frame and a pending frame's
+    // inputs are gone
+    h->diff_ready = false;
+    if (h->pending) h->pending_stale = true;
     h->frame_valid = false;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (h->V && cudaMemcpyAsync(h->vertex.p, vertex, 8 * (size_t)h->V, cudaMemcpyDefault, s) != cudaSuccess)
@@ -1190,6 +1283,9 @@ int spr_diff_backward(spr_handle *h, const float *fill_rgba, const float *grad_i
 int spr_image_device_ptr(spr_handle *h, void **out) {
     if (!h || !out) return SPR_ERR_INVALID_ARG;
     if (!h->frame_valid) return SPR_ERR_NO_SCENE;
+    cudaSetDevice(h->cfg.device);
+    const int st = settle(h);
+    if (st) return st;
     *out = h->image.p;
     return SPR_OK;
 }
@@ -1198,6 +1294,8 @@ int spr_read_image(spr_handle *h, uint8_t *host_rgba, void *stream) {
     if (!h || !host_rgba) return SPR_ERR_INVALID_ARG;
     if (!h->frame_valid) return SPR_ERR_NO_SCENE;
     cudaSetDevice(h->cfg.device);
+    const int st = settle(h);
+    if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t bytes = 4 * (size_t)h->frame_W * h->frame_H;
     if (cudaMemcpyAsync(host_rgba, h->image.p, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return cuda_status();
@@ -1247,6 +1345,8 @@ int spr_enable_output_transform(spr_handle *h, int32_t enable) {
 int spr_output_device_ptr(spr_handle *h, void **out, void *stream) {
     if (!h || !out) return SPR_ERR_INVALID_ARG;
     if (!h->frame_valid) return SPR_ERR_NO_SCENE;
+    cudaSetDevice(h->cfg.device);
+    if (int sst = settle(h)) return sst;
     if (!h->out_tf) {
         *out = h->image.p;
         return SPR_OK;
@@ -1289,6 +1389,10 @@ int spr_save_png(spr_handle *h, const char *path) {
 
 int spr_get_counts(spr_handle *h, spr_element_number *out) {
     if (!h || !out) return SPR_ERR_INVALID_ARG;
+    if (h->pending) {
+        cudaSetDevice(h->cfg.device);
+        if (int st = settle(h)) return st;
+    }
     *out = h->en;
     return SPR_OK;
 }
@@ -1307,6 +1411,14 @@ int spr_step_timing(spr_handle *h, double *ms, int32_t capacity, int32_t *n_out)
     return SPR_OK;
 }
 
+int spr_debug_set_lookback(spr_handle *h, uint32_t spin_cap, int64_t hold_tile) {
+    if (!h || spin_cap == 0) return SPR_ERR_INVALID_ARG;
+    drop_graph(h, false);
+    h->lb_spin_cap = spin_cap;
+    h->lb_hold_tile = hold_tile < 0 ? -1 : hold_tile;
+    return SPR_OK;
+}
+
 int spr_set_memory_limit(spr_handle *h, int64_t bytes) {
     if (!h || bytes < 0) return SPR_ERR_INVALID_ARG;
     h->budget.limit = (size_t)bytes;
@@ -1315,6 +1427,10 @@ int spr_set_memory_limit(spr_handle *h, int64_t bytes) {
 
 int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out) {
     if (!h || !out) return SPR_ERR_INVALID_ARG;
+    if (h->pending) {
+        cudaSetDevice(h->cfg.device);
+        if (int st = settle(h)) return st;
+    }
     out->kernel_launches = h->launches;
     out->host_syncs = h->host_syncs;
     out->resolve_pairs = h->npairs;
@@ -1330,6 +1446,7 @@ int spr_debug_dump(spr_handle *h, int32_t stage, void *dst, size_t capacity, siz
     if (!h || !needed) return SPR_ERR_INVALID_ARG;
     if (!h->frame_valid) return SPR_ERR_NO_SCENE;
     cudaSetDevice(h->cfg.device);
+    if (int st = settle(h)) return st;
     const int64_t nf = h->nf;
     const int WORDS = h->frame_S / 8;
     const void *src = nullptr;
@@ -1599,7 +1716,7 @@ bool replay_groups_concurrently(spr_batch *b, cudaStream_t s) {
     int n = 0;
     for (spr_handle *h : b->group) {
         if (!h) continue;
-        if (!h->graph_mode || h->timing || !h->gexec || h->gexec_gen != g_alloc_gen.load()) return false;
+        if (!h->graph_mode || h->timing || !h->gexec || h->gexec_gen != g_alloc_gen.load() || !h->caps_ok) return false;
         ++n;
     }
     if (n < 2) return false;
@@ -1616,7 +1733,9 @@ bool replay_groups_concurrently(spr_batch *b, cudaStream_t s) {
         spr_handle *h = b->group[g];
         if (!h) continue;
         cudaStreamWaitEvent(b->gstream[g], b->gstart, 0);
+        supersede(h);
         cudaGraphLaunch(h->gexec, b->gstream[g]);
+        mark_pending(h, b->gstream[g]);
         cudaEventRecord(b->gdone[g], b->gstream[g]);
         cudaStreamWaitEvent(s, b->gdone[g], 0);
         h->host_syncs = 0;
@@ -1646,9 +1765,21 @@ int spr_batch_render(spr_batch *b, void *stream) {
     return SPR_OK;
 }
 
+namespace {
+// Every group's frame settled (see settle()).
+int settle_batch(spr_batch *b) {
+    cudaSetDevice(b->device);
+    for (spr_handle *h : b->group)
+        if (h && h->pending)
+            if (int st = settle(h)) return st;
+    return SPR_OK;
+}
+}  // namespace
+
 int spr_batch_image_device_ptr(spr_batch *b, int32_t scene, void **out) {
     if (!b || !out || scene < 0 || scene >= (int32_t)b->entries.size()) return SPR_ERR_INVALID_ARG;
     if (!b->rendered) return SPR_ERR_NO_SCENE;
+    if (int st = settle_batch(b)) return st;
     const spr_batch::Entry &e = b->entries[scene];
     *out = b->group[e.group]->image.as<uint32_t>() + e.image_off;
     return SPR_OK;
@@ -1657,6 +1788,7 @@ int spr_batch_image_device_ptr(spr_batch *b, int32_t scene, void **out) {
 int spr_batch_read_image(spr_batch *b, int32_t scene, uint8_t *host_rgba, void *stream) {
     if (!b || !host_rgba || scene < 0 || scene >= (int32_t)b->entries.size()) return SPR_ERR_INVALID_ARG;
     if (!b->rendered) return SPR_ERR_NO_SCENE;
+    if (int st = settle_batch(b)) return st;
     cudaSetDevice(b->device);
     const spr_batch::Entry &e = b->entries[scene];
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1669,6 +1801,7 @@ int spr_batch_read_image(spr_batch *b, int32_t scene, uint8_t *host_rgba, void *
 
 int spr_batch_get_counts(spr_batch *b, spr_element_number *total) {
     if (!b || !total) return SPR_ERR_INVALID_ARG;
+    if (int st = settle_batch(b)) return st;
     spr_element_number t{};
     for (spr_handle *h : b->group) {
         if (!h) continue;

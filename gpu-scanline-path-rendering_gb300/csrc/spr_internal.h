@@ -26,13 +26,31 @@ struct ResolveTables {
     uint8_t bin[4096];
 };
 
-// Frame-level counters written by the kernels (device memory).
+// Frame status bits (FrameCounters::status).
+constexpr uint32_t kStatusOverflow = 1u;  // a frame size exceeded its buffers
+constexpr uint32_t kStatusTimeout = 2u;   // a bounded device wait gave up
+// Polls of a look-back window before it gives up: about a second of waiting
+// (each poll sleeps 64 ns at least), far beyond any real wait.
+constexpr uint32_t kLbSpinCap = 1u << 24;
+
+// Frame-level sizes and flags written by the kernels (device memory): a
+// frame's kernels read their sizes here, so no size has to come back to the
+// host.  A size is "admitted" once it is known to fit its buffers; one that
+// does not fit is admitted as 0 (the rest of the frame then does nothing)
+// and sets kStatusOverflow, and the frame is rendered again with larger
+// buffers before anything reads it.
 struct FrameCounters {
-    uint32_t n_merged;
-    uint32_t n_span;
-    uint32_t n_pairs;
-    uint32_t status;     // nonzero: capacity overflow detected on the device
-    uint32_t bin_queue;  // next resolve bin to hand out (persistent resolve)
+    uint32_t n_merged;     // merged fragments (draw items with sample masks)
+    uint32_t n_span;       // spans
+    uint32_t n_pairs;      // resolve pairs, admitted
+    uint32_t status;       // kStatusOverflow | kStatusTimeout
+    uint32_t bin_queue;    // next resolve bin to hand out (persistent resolve)
+    uint32_t nf;           // intersection entries, admitted
+    uint32_t need_nf;      // intersection entries of the frame
+    uint32_t need_pairs;   // resolve pairs of the frame
+    uint32_t n_items;      // n_merged + n_span
+    uint32_t tiles[3];     // look-back tile counters: entry offsets, scan-mark, pair offsets
+    uint32_t diff_status;  // differentiable frames: bit 0 tape too short, bit 1 chain too short
     uint32_t pad[3];
 };
 
@@ -67,6 +85,22 @@ void build_resolve_tables(ResolveTables *t);
 
 // ---- scan / sort (spr_sort.cu) ----------------------------------------------------
 int64_t scan_tmp_words(int64_t n);
+// Single-pass exclusive scan (decoupled look-back) of n u32 values:
+// out[0..n) = exclusive prefix sums, out[n] = total, *total_out = total when
+// given.  n = *n_dev when n_dev is given (at most n_cap: the grid is sized
+// for n_cap), else n_cap.  tile_status holds lookback_words(n_cap) words and
+// *tile_ctr one word, both zero before the call.  A wait longer than
+// spin_cap polls sets kStatusTimeout in *frame_status.  in and out must be
+// 16-byte aligned.  hold_tile >= 0 (tests of the timeout only): that tile
+// never publishes, so the tiles after it wait until spin_cap runs out.
+int64_t lookback_words(int64_t n);
+int scan_lookback_u32(const uint32_t *in, uint32_t *out, const uint32_t *n_dev, int64_t n_cap, uint64_t *tile_status,
+                      uint32_t *tile_ctr, uint32_t spin_cap, uint32_t *frame_status, uint32_t *total_out,
+                      cudaStream_t s, int64_t hold_tile = -1);
+// Admits a size: *admitted = *need if *need <= cap, else 0 and
+// kStatusOverflow in *status; 0 as well after a timeout (the size may be
+// wrong then).
+int launch_admit(const uint32_t *need, uint32_t *admitted, uint32_t cap, uint32_t *status, cudaStream_t s);
 // out[0..n) = exclusive prefix sums of in, out[n] = total.
 int scan_exclusive_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp, cudaStream_t s);
 // In-place exclusive scan of a short array by one block; a[n] = total.
@@ -76,16 +110,18 @@ int64_t radix_tiles(int64_t n);
 // they arrive grouped by path: every path's segment sorted by one block.
 // Reads keys (values are the positions), writes keys_out / vals_out; keys and
 // vals serve as scratch for long segments.  path_start: P + 1 words.
+// Nothing is sorted when the frame's entries were not admitted (ctr->nf 0).
 int launch_segment_sort(const CurveDesc *curves, uint32_t C, uint32_t P, const uint32_t *offsets, uint64_t *keys,
                         uint32_t *vals, uint64_t *keys_out, uint32_t *vals_out, uint32_t *path_start,
-                        cudaStream_t s);
+                        const FrameCounters *ctr, cudaStream_t s);
 int64_t radix_tmp_words(int64_t n);
 // Stable LSD sort on bits [0, key_bits); returns true when the result is in
 // the *_alt buffers.
 // *launches receives the number of kernels launched.
+// n = *n_dev when n_dev is given (at most n: the grids are sized for n).
 template <class K>
 bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_t n, int key_bits, uint32_t *tmp,
-                cudaStream_t s, int *launches);
+                cudaStream_t s, int *launches, const uint32_t *n_dev = nullptr);
 
 // ---- pipeline kernels (spr_kernels.cu); each launcher returns its kernel count --
 struct FrameArgs {
@@ -136,28 +172,33 @@ int launch_curve_count(const FrameArgs &a, const float2 *tvert, const uint8_t *p
 // Sort keys of the emission order (curves by decreasing estimated cost).
 int launch_emit_keys(const FrameArgs &a, const uint32_t *counts, uint32_t *key, uint32_t *val, cudaStream_t s);
 // order: curve processed by thread i (null = identity); outputs do not depend on it.
+// The kernels below read the frame's sizes from the counters (ctr); their
+// grids are sized for the buffers' capacities (cap_*).
 int launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *path_visible,
-                       const uint32_t *offsets, const uint32_t *order, int2 *entries, cudaStream_t s);
-int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t nf, int32_t *key,
-                     uint32_t *pidw, int8_t *wn, uint32_t *mask, uint64_t *sort_key, uint32_t *sort_val,
-                     cudaStream_t s);
-int64_t flags_tmp_words(int64_t nf);
-// Winding scan, merged-fragment / span marks, draw list and merged heads.
-// item_scene (batch frames only, else null) receives the scene of each draw item.
-// scene_base: n_scenes bytes for batch frames (the winding scan restarts
-// at every scene), else unused.
-int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                      int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
-                      uint32_t *tmp, int8_t *scene_base, cudaStream_t s);
-int launch_stencil(const FrameArgs &a, int64_t nf, int64_t n_merged, const uint64_t *skey, const uint32_t *perm,
-                    const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan, const uint32_t *heads,
-                    uint32_t *merged_mask, cudaStream_t s);
-int launch_item_tiles(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t n_items,
-                       uint32_t *tile_counts, cudaStream_t s);
-int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t n_items,
-                       const uint32_t *pair_offsets, uint32_t *pair_key, uint32_t *pair_val, cudaStream_t s);
-int launch_bin_bounds(const uint32_t *pair_key, int64_t n_pairs, uint32_t *bin_start, uint32_t *bin_end,
-                       cudaStream_t s);
+                      const uint32_t *offsets, const uint32_t *order, int2 *entries, const FrameCounters *ctr,
+                      cudaStream_t s);
+int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t cap_nf,
+                    const FrameCounters *ctr, int32_t *key, uint32_t *pidw, int8_t *wn, uint32_t *mask,
+                    uint64_t *sort_key, uint32_t *sort_val, cudaStream_t s);
+// Look-back words of launch_scan_mark (zero before the launch).
+int64_t scan_mark_status_words(int64_t cap_nf);
+// Winding scan, merged-fragment / span marks, draw list and merged heads in
+// one pass (decoupled look-back); writes the item counts to the counters.
+// item_scene (batch frames only, else null) receives the scene of each draw
+// item; in batch frames the winding scan restarts at every scene.
+int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
+                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
+                     uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s);
+int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr, const uint64_t *skey,
+                   const uint32_t *perm, const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan,
+                   const uint32_t *heads, uint32_t *merged_mask, cudaStream_t s);
+int launch_item_tiles(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
+                      const FrameCounters *ctr, uint32_t *tile_counts, cudaStream_t s);
+int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
+                      const FrameCounters *ctr, const uint32_t *pair_offsets, uint32_t *pair_key, uint32_t *pair_val,
+                      cudaStream_t s);
+int launch_bin_bounds(const uint32_t *pair_key, int64_t cap_pairs, const FrameCounters *ctr, uint32_t *bin_start,
+                      uint32_t *bin_end, cudaStream_t s);
 // The resolve is persistent: resolve_warps(a) warps take bins from
 // counters->bin_queue (zeroed by launch_resolve).  overflow: 64 * 32 words
 // per warp for pixels that need explicit samples (multisample modes with

@@ -21,6 +21,7 @@
 
 #include "spr_device.cuh"
 #include "spr_internal.h"
+#include "spr_lookback.cuh"
 
 namespace spr {
 
@@ -173,9 +174,11 @@ __global__ void k_emit_keys(FrameArgs a, const uint32_t *__restrict__ counts, ui
 
 __global__ void k_curve_emit(FrameArgs a, const float2 *__restrict__ tv, const uint8_t *__restrict__ vis,
                              const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ order,
-                             int2 *__restrict__ entries) {
+                             int2 *__restrict__ entries, const FrameCounters *__restrict__ ctr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.C) return;
+    // entries not admitted (the buffers are too small), or the offsets not
+    // to be trusted (a scan gave up waiting): nothing is written
+    if (i >= a.C || ctr->status != 0u || ctr->nf != ctr->need_nf) return;
     const int cid = order != nullptr ? (int)order[i] : i;
     const CurveDesc d = a.curves[cid];
     CurveGeom g;
@@ -263,11 +266,13 @@ __global__ void k_curve_emit(FrameArgs a, const float2 *__restrict__ tv, const u
 // ---------------------------------------------------------- fragments --
 template <int S>
 __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2 *__restrict__ tv,
-                                                       const int2 *__restrict__ entries, int64_t nf,
+                                                       const int2 *__restrict__ entries,
+                                                       const FrameCounters *__restrict__ ctr,
                                                        int32_t *__restrict__ key_out, uint32_t *__restrict__ pid_out,
                                                        int8_t *__restrict__ wn_out, uint32_t *__restrict__ mask_out,
                                                        uint64_t *__restrict__ sort_key, uint32_t *__restrict__ sort_val) {
     constexpr int WORDS = S / 8;
+    const int64_t nf = ctr->nf;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nf) return;
     const int2 e0 = entries[i];
@@ -411,9 +416,10 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
 }
 
 // --------------------------------------------- winding scan + marks --
-constexpr int kFlagThreads = 256;
-constexpr int kFlagItems = 8;
-constexpr int kFlagTile = kFlagThreads * kFlagItems;
+constexpr int kMarkThreads = 256;
+constexpr int kMarkItems = 8;
+constexpr int kMarkTile = kMarkThreads * kMarkItems;
+constexpr uint64_t kSegBit = 1ull << 32;  // winding look-back: a scene starts in the tile (batches)
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
     const int lane = threadIdx.x & 31;
@@ -426,7 +432,7 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
 }
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *sw, uint32_t *total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int W = kFlagThreads / 32;
+    constexpr int W = kMarkThreads / 32;
     uint32_t inc = warp_incl_scan(v);
     if (lane == 31) sw[warp] = inc;
     __syncthreads();
@@ -443,56 +449,53 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *sw, ui
     return r;
 }
 
-__global__ void __launch_bounds__(kFlagThreads) k_wn_reduce(int64_t nf, const uint32_t *__restrict__ perm,
-                                                            const int8_t *__restrict__ wn, uint32_t *__restrict__ sums) {
-    __shared__ uint32_t sw[kFlagThreads / 32 + 1];
-    const int64_t base = (int64_t)blockIdx.x * kFlagTile + (int64_t)threadIdx.x * kFlagItems;
-    uint32_t s = 0;
-#pragma unroll
-    for (int k = 0; k < kFlagItems; ++k) {
-        const int64_t i = base + k;
-        if (i < nf) s += (uint32_t)(int32_t)wn[perm[i]];
-    }
-    uint32_t total;
-    block_excl_scan(s, sw, &total);
-    if (threadIdx.x == 0) sums[blockIdx.x] = total;
-}
+// Segmented sums: (s, f) where f = a segment starts inside; a then b.
+struct SegSum {
+    uint32_t s, f;
+};
+__device__ __forceinline__ SegSum seg_then(SegSum a, SegSum b) { return SegSum{b.f ? b.s : a.s + b.s, a.f | b.f}; }
 
-__global__ void __launch_bounds__(kFlagThreads) k_wn_down(int64_t nf, const uint32_t *__restrict__ perm,
-                                                          const int8_t *__restrict__ wn,
-                                                          const uint32_t *__restrict__ sums,
-                                                          int8_t *__restrict__ wn_scan) {
-    __shared__ uint32_t sw[kFlagThreads / 32 + 1];
-    const int64_t base = (int64_t)blockIdx.x * kFlagTile + (int64_t)threadIdx.x * kFlagItems;
-    uint32_t v[kFlagItems];
-    uint32_t s = 0;
+__device__ __forceinline__ SegSum block_excl_segscan(SegSum v, uint32_t *ss, uint32_t *sf, SegSum *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int W = kMarkThreads / 32;
+    SegSum inc = v;
 #pragma unroll
-    for (int k = 0; k < kFlagItems; ++k) {
-        const int64_t i = base + k;
-        v[k] = i < nf ? (uint32_t)(int32_t)wn[perm[i]] : 0u;
-        s += v[k];
+    for (int o = 1; o < 32; o <<= 1) {
+        const SegSum up{__shfl_up_sync(0xffffffffu, inc.s, o), __shfl_up_sync(0xffffffffu, inc.f, o)};
+        if (lane >= o) inc = seg_then(up, inc);
     }
-    uint32_t total;
-    uint32_t p = block_excl_scan(s, sw, &total) + sums[blockIdx.x];
+    SegSum prev{__shfl_up_sync(0xffffffffu, inc.s, 1), __shfl_up_sync(0xffffffffu, inc.f, 1)};
+    if (lane == 0) prev = SegSum{0u, 0u};
+    if (lane == 31) ss[warp] = inc.s, sf[warp] = inc.f;
+    __syncthreads();
+    if (warp == 0) {
+        SegSum t = lane < W ? SegSum{ss[lane], sf[lane]} : SegSum{0u, 0u};
 #pragma unroll
-    for (int k = 0; k < kFlagItems; ++k) {
-        const int64_t i = base + k;
-        if (i < nf) wn_scan[i] = (int8_t)(uint8_t)p;
-        p += v[k];
+        for (int o = 1; o < 32; o <<= 1) {
+            const SegSum up{__shfl_up_sync(0xffffffffu, t.s, o), __shfl_up_sync(0xffffffffu, t.f, o)};
+            if (lane >= o) t = seg_then(up, t);
+        }
+        SegSum ex{__shfl_up_sync(0xffffffffu, t.s, 1), __shfl_up_sync(0xffffffffu, t.f, 1)};
+        if (lane == 0) ex = SegSum{0u, 0u};
+        if (lane < W) ss[lane] = ex.s, sf[lane] = ex.f;
+        if (lane == W - 1) ss[W] = t.s, sf[W] = t.f;
     }
+    __syncthreads();
+    const SegSum r = seg_then(SegSum{ss[warp], sf[warp]}, prev);
+    *total = SegSum{ss[W], sf[W]};
+    __syncthreads();
+    return r;
 }
 
 struct Mark {
     uint32_t ff, sf;
 };
 
-// k_mark_merged_fragment_and_span (cu:462-535) on sorted position i.
-__device__ __forceinline__ Mark mark_at(int64_t i, const uint64_t *__restrict__ skey, const int8_t *__restrict__ wn_scan,
-                                        const FrameArgs &a) {
-    const uint64_t k1 = skey[i];
+// k_mark_merged_fragment_and_span (cu:462-535) on sorted position i with
+// keys k0 (position i - 1) and k1 (position i) and scanned winding w.
+__device__ __forceinline__ Mark mark_of(int64_t i, uint64_t k0, uint64_t k1, int8_t w, const FrameArgs &a) {
     const Dim dm = dim_of(a, (uint32_t)(k1 >> 24));
     const int W = dm.W, H = dm.H, nrows = (H + 1) / 2;
-    const uint8_t *__restrict__ rule = a.fill_rule;
     const uint32_t key1 = (uint32_t)key_from_local((uint32_t)(k1 & 0xFFFFFFu), nrows);
     const int x1 = key_x(key1), y1 = key_y(key1);
     const bool oob = x1 < 0 || y1 < 0 || x1 >= W || y1 >= H;
@@ -501,69 +504,155 @@ __device__ __forceinline__ Mark mark_at(int64_t i, const uint64_t *__restrict__ 
         m.ff = oob ? 0u : 1u;
         return m;
     }
-    const uint64_t k0 = skey[i - 1];
     const uint32_t p0 = (uint32_t)(k0 >> 24), p1 = (uint32_t)(k1 >> 24);
     const uint32_t key0 = (uint32_t)key_from_local((uint32_t)(k0 & 0xFFFFFFu), nrows);
     const int x0 = key_x(key0), y0 = key_y(key0);
     m.ff = oob ? 0u : ((p0 != p1 || key0 != key1) ? 1u : 0u);
-    const uint8_t fr = rule[p1];
-    const int8_t w = wn_scan[i];
+    const uint8_t fr = a.fill_rule[p1];
     const bool wf = (fr == 0 && w != 0) || (fr == 1 && (w & 1));
     m.sf = (y0 == y1 && (x0 + 2) < x1 && p0 == p1 && wf) ? 1u : 0u;
     return m;
 }
 
-__global__ void __launch_bounds__(kFlagThreads) k_flags_reduce(FrameArgs a, int64_t nf, const uint64_t *__restrict__ skey,
-                                                               const int8_t *__restrict__ wn_scan,
-                                                               uint32_t *__restrict__ fsum, uint32_t *__restrict__ ssum) {
-    __shared__ uint32_t sw[kFlagThreads / 32 + 1];
-    const int64_t base = (int64_t)blockIdx.x * kFlagTile + (int64_t)threadIdx.x * kFlagItems;
-    uint32_t s = 0;
+// Stages 9-12 and 14 in one pass over the sorted entries (thrust's int8
+// scan of the shuffled windings, cu:1099-1101; the marks, cu:462-535; their
+// inclusive scans, cu:1139-1157; the draw list, cu:789-868).  Per tile:
+// the windings gathered through the sort permutation and scanned (int8
+// arithmetic: only the low 8 bits are kept), with the tile's prefix from a
+// decoupled look-back (restarting at every scene of a batch, so that each
+// scene sees the scan a single-scene render gives it); then the merged and
+// span marks, scanned with a second look-back, and the draw items written.
+// The last tile writes the item counts.  Sorted keys and positions are read
+// 128 bits at a time.
+__global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const uint64_t *__restrict__ skey,
+                                                            const uint32_t *__restrict__ perm,
+                                                            const int8_t *__restrict__ wn, int8_t *__restrict__ wn_scan,
+                                                            int4 *__restrict__ draw, uint32_t *__restrict__ heads,
+                                                            uint32_t *__restrict__ item_scene,
+                                                            FrameCounters *__restrict__ ctr,
+                                                            uint64_t *__restrict__ st_wn, uint64_t *__restrict__ st_fl,
+                                                            uint32_t spin_cap) {
+    __shared__ uint32_t ss[kMarkThreads / 32 + 1], sf[kMarkThreads / 32 + 1];
+    __shared__ uint32_t s_tile;
+    __shared__ uint64_t s_pre;
+    const int64_t nf = ctr->nf;
+    const int64_t ntiles = (nf + kMarkTile - 1) / kMarkTile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&ctr->tiles[1], 1u);
+    __syncthreads();
+    const int64_t t = s_tile;
+    if (t >= ntiles) {
+        if (t == 0 && threadIdx.x == 0) ctr->n_merged = ctr->n_span = ctr->n_items = 0u;
+        return;
+    }
+    const int64_t base = t * kMarkTile + (int64_t)threadIdx.x * kMarkItems;
+    const int64_t left = nf - base;
+    const int cnt = left <= 0 ? 0 : (left >= kMarkItems ? kMarkItems : (int)left);
+    uint64_t k[kMarkItems + 1];  // sorted keys at base - 1 .. base + 7
+    uint32_t pm[kMarkItems];
+    if (cnt == kMarkItems) {
+        const uint4 *kp = reinterpret_cast<const uint4 *>(skey + base);
 #pragma unroll
-    for (int k = 0; k < kFlagItems; ++k) {
-        const int64_t i = base + k;
-        if (i < nf) {
-            const Mark m = mark_at(i, skey, wn_scan, a);
-            s += m.ff | (m.sf << 16);
+        for (int q = 0; q < kMarkItems / 2; ++q) {
+            const uint4 v = kp[q];
+            k[1 + 2 * q] = (uint64_t)v.x | ((uint64_t)v.y << 32);
+            k[2 + 2 * q] = (uint64_t)v.z | ((uint64_t)v.w << 32);
+        }
+        const uint4 p0 = reinterpret_cast<const uint4 *>(perm + base)[0];
+        const uint4 p1 = reinterpret_cast<const uint4 *>(perm + base)[1];
+        pm[0] = p0.x, pm[1] = p0.y, pm[2] = p0.z, pm[3] = p0.w, pm[4] = p1.x, pm[5] = p1.y, pm[6] = p1.z, pm[7] = p1.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < kMarkItems; ++j) {
+            k[1 + j] = j < cnt ? skey[base + j] : 0ull;
+            pm[j] = j < cnt ? perm[base + j] : 0u;
         }
     }
-    uint32_t total;
-    block_excl_scan(s, sw, &total);
-    if (threadIdx.x == 0) {
-        fsum[blockIdx.x] = total & 0xFFFFu;
-        ssum[blockIdx.x] = total >> 16;
-    }
-}
-
-__global__ void __launch_bounds__(kFlagThreads) k_flags_down(FrameArgs a, int64_t nf, int64_t ntiles,
-                                                             const uint64_t *__restrict__ skey,
-                                                             const int8_t *__restrict__ wn_scan,
-                                                             const uint32_t *__restrict__ fsum,
-                                                             const uint32_t *__restrict__ ssum, int4 *__restrict__ draw,
-                                                             uint32_t *__restrict__ heads,
-                                                             uint32_t *__restrict__ item_scene,
-                                                             FrameCounters *__restrict__ counters) {
-    __shared__ uint32_t sw[kFlagThreads / 32 + 1];
-    const int64_t base = (int64_t)blockIdx.x * kFlagTile + (int64_t)threadIdx.x * kFlagItems;
-    Mark mk[kFlagItems];
-    uint32_t s = 0;
+    k[0] = (cnt > 0 && base > 0) ? skey[base - 1] : 0ull;
+    // windings in sorted order, and the scene starts of a batch
+    const bool batch = a.scenes != nullptr && a.n_scenes > 1;
+    int32_t v[kMarkItems];
+    uint32_t seg = 0u;  // bit j: a scene starts at base + j
+    SegSum agg{0u, 0u};
 #pragma unroll
-    for (int k = 0; k < kFlagItems; ++k) {
-        const int64_t i = base + k;
-        mk[k] = i < nf ? mark_at(i, skey, wn_scan, a) : Mark{0u, 0u};
-        s += mk[k].ff | (mk[k].sf << 16);
+    for (int j = 0; j < kMarkItems; ++j) {
+        v[j] = j < cnt ? (int32_t)wn[pm[j]] : 0;
+        if (batch && j < cnt &&
+            (base + j == 0 || a.path_scene[(uint32_t)(k[j + 1] >> 24)] != a.path_scene[(uint32_t)(k[j] >> 24)]))
+            seg |= 1u << j;
+        agg = seg_then(agg, SegSum{(uint32_t)v[j], (seg >> j) & 1u});
     }
-    uint32_t total;
-    const uint32_t pre = block_excl_scan(s, sw, &total);
-    uint32_t nfb = fsum[blockIdx.x] + (pre & 0xFFFFu);
-    uint32_t nsb = ssum[blockIdx.x] + (pre >> 16);
+    SegSum tot;
+    const SegSum tpre = block_excl_segscan(agg, ss, sf, &tot);
+    if (threadIdx.x < 32) {
+        uint64_t pre = 0;
+        if (t > 0) {
+            if (threadIdx.x == 0) lb_store(st_wn + t, kLbAggregate | (tot.f ? kSegBit : 0ull) | tot.s);
+            pre = lb_walk(st_wn, t, kSegBit, spin_cap, &ctr->status);
+        }
+        if (threadIdx.x == 0) {
+            lb_store(st_wn + t, kLbInclusive | (uint32_t)(tot.f ? tot.s : (uint32_t)pre + tot.s));
+            s_pre = pre;
+        }
+    }
+    __syncthreads();
+    // scanned windings (exclusive, restarting at scene starts)
+    SegSum run = seg_then(SegSum{(uint32_t)s_pre, 0u}, tpre);
+    int8_t ws[kMarkItems];
 #pragma unroll
-    for (int k = 0; k < kFlagItems; ++k) {
-        const int64_t i = base + k;
-        if (i >= nf) break;
-        const uint32_t ff = mk[k].ff, sf = mk[k].sf;
-        if (ff | sf) {
-            const uint64_t k1 = skey[i];
+    for (int j = 0; j < kMarkItems; ++j) {
+        if ((seg >> j) & 1u) run.s = 0u;
+        ws[j] = (int8_t)(uint8_t)run.s;
+        run.s += (uint32_t)v[j];
+    }
+    if (cnt == kMarkItems) {
+        uint2 packed;
+        packed.x = (uint32_t)(uint8_t)ws[0] | ((uint32_t)(uint8_t)ws[1] << 8) | ((uint32_t)(uint8_t)ws[2] << 16) |
+                   ((uint32_t)(uint8_t)ws[3] << 24);
+        packed.y = (uint32_t)(uint8_t)ws[4] | ((uint32_t)(uint8_t)ws[5] << 8) | ((uint32_t)(uint8_t)ws[6] << 16) |
+                   ((uint32_t)(uint8_t)ws[7] << 24);
+        *reinterpret_cast<uint2 *>(wn_scan + base) = packed;
+    } else {
+#pragma unroll
+        for (int j = 0; j < kMarkItems; ++j)
+            if (j < cnt) wn_scan[base + j] = ws[j];
+    }
+    // marks and their scans
+    Mark mk[kMarkItems];
+    uint32_t fs = 0;
+#pragma unroll
+    for (int j = 0; j < kMarkItems; ++j) {
+        mk[j] = j < cnt ? mark_of(base + j, k[j], k[j + 1], ws[j], a) : Mark{0u, 0u};
+        fs += mk[j].ff | (mk[j].sf << 16);
+    }
+    uint32_t ftot;
+    const uint32_t fpre = block_excl_scan(fs, ss, &ftot);
+    const uint64_t ftot_w = ((uint64_t)(ftot & 0xFFFFu) << 31) | (uint64_t)(ftot >> 16);
+    if (threadIdx.x < 32) {
+        uint64_t pre = 0;
+        if (t > 0) {
+            if (threadIdx.x == 0) lb_store(st_fl + t, kLbAggregate | ftot_w);
+            pre = lb_walk(st_fl, t, 0ull, spin_cap, &ctr->status);
+        }
+        if (threadIdx.x == 0) {
+            lb_store(st_fl + t, kLbInclusive | ((pre + ftot_w) & kLbPayload));
+            s_pre = pre;
+            if (t == ntiles - 1) {  // the frame's item counts
+                const uint64_t all = pre + ftot_w;
+                const uint32_t nm = (uint32_t)(all >> 31) & 0x7FFFFFFFu, ns = (uint32_t)all & 0x7FFFFFFFu;
+                ctr->n_merged = nm;
+                ctr->n_span = ns;
+                ctr->n_items = nm + ns;
+            }
+        }
+    }
+    __syncthreads();
+    uint32_t nfb = (uint32_t)(s_pre >> 31) + (fpre & 0xFFFFu);
+    uint32_t nsb = (uint32_t)(s_pre & 0x7FFFFFFFu) + (fpre >> 16);
+#pragma unroll
+    for (int j = 0; j < kMarkItems; ++j) {
+        const uint32_t ff = mk[j].ff, sfl = mk[j].sf;
+        if (ff | sfl) {
+            const uint64_t k1 = k[j + 1];
             const uint32_t p = (uint32_t)(k1 >> 24);
             const int32_t fill = (int32_t)a.fill_rgba[p];
             const int nrows = (dim_of(a, p).H + 1) / 2;
@@ -571,19 +660,19 @@ __global__ void __launch_bounds__(kFlagThreads) k_flags_down(FrameArgs a, int64_
             if (item_scene != nullptr) {
                 const uint32_t sc = a.path_scene[p];
                 if (ff) item_scene[nfb + nsb] = sc;
-                if (sf) item_scene[nfb + nsb + ff] = sc;
+                if (sfl) item_scene[nfb + nsb + ff] = sc;
             }
             if (a.item_path != nullptr) {
                 if (ff) a.item_path[nfb + nsb] = p;
-                if (sf) a.item_path[nfb + nsb + ff] = p;
+                if (sfl) a.item_path[nfb + nsb + ff] = p;
             }
             if (ff) {
                 const int32_t pos = (int32_t)(((uint32_t)key_y(key1) << 16) | (uint32_t)key_x(key1));
                 draw[nfb + nsb] = make_int4(pos, 2, fill, (int)(nfb + 1));
-                heads[nfb] = (uint32_t)i;
+                heads[nfb] = (uint32_t)(base + j);
             }
-            if (sf) {
-                const uint32_t key0 = (uint32_t)key_from_local((uint32_t)(skey[i - 1] & 0xFFFFFFu), nrows);
+            if (sfl) {
+                const uint32_t key0 = (uint32_t)key_from_local((uint32_t)(k[j] & 0xFFFFFFu), nrows);
                 const int y0 = key_y(key0);
                 int x0 = (int16_t)(key_x(key0) + 2);
                 const int x1 = key_x(key1);
@@ -593,11 +682,7 @@ __global__ void __launch_bounds__(kFlagThreads) k_flags_down(FrameArgs a, int64_
             }
         }
         nfb += ff;
-        nsb += sf;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        counters->n_merged = fsum[ntiles];
-        counters->n_span = ssum[ntiles];
+        nsb += sfl;
     }
 }
 
@@ -607,7 +692,7 @@ __global__ void __launch_bounds__(kFlagThreads) k_flags_down(FrameArgs a, int64_
 // mask bit (the reference's packed counters), reduced to the 7-bit winding
 // number and tested against the fill rule.
 template <int S>
-__global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, int64_t nf, int64_t nm,
+__global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, const FrameCounters *__restrict__ ctr,
                                                       const uint64_t *__restrict__ skey,
                                                       const uint32_t *__restrict__ perm,
                                                       const uint32_t *__restrict__ pidw,
@@ -616,6 +701,7 @@ __global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, int64_t nf, i
                                                       const uint32_t *__restrict__ heads,
                                                       uint32_t *__restrict__ merged) {
     constexpr int WORDS = S / 8;
+    const int64_t nf = ctr->nf, nm = ctr->n_merged;
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nm) return;
     const int64_t h = heads[g];
@@ -683,9 +769,9 @@ __device__ __forceinline__ void item_cols(const int4 &it, int W, int &x0, int &x
 }
 
 __global__ void k_item_tiles(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
-                             int64_t n, uint32_t *__restrict__ cnt) {
+                             const FrameCounters *__restrict__ ctr, uint32_t *__restrict__ cnt) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= (int64_t)ctr->n_items) return;
     const int W = item_scene != nullptr ? a.scenes[item_scene[i]].W : a.W;
     int x0, x1;
     item_cols(draw[i], W, x0, x1);
@@ -693,10 +779,11 @@ __global__ void k_item_tiles(FrameArgs a, const int4 *__restrict__ draw, const u
 }
 
 __global__ void k_emit_pairs(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
-                             int64_t n, const uint32_t *__restrict__ offs, uint32_t *__restrict__ pkey,
-                             uint32_t *__restrict__ pval) {
+                             const FrameCounters *__restrict__ ctr, const uint32_t *__restrict__ offs,
+                             uint32_t *__restrict__ pkey, uint32_t *__restrict__ pval) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    // (pairs not admitted: the pair buffers are too small; or a scan gave up)
+    if (i >= (int64_t)ctr->n_items || ctr->status != 0u || ctr->n_pairs != ctr->need_pairs) return;
     const int4 it = draw[i];
     int W = a.W;
     uint32_t bin0 = 0;
@@ -718,8 +805,9 @@ __global__ void k_emit_pairs(FrameArgs a, const int4 *__restrict__ draw, const u
     }
 }
 
-__global__ void k_bin_bounds(const uint32_t *__restrict__ key, int64_t n, uint32_t *__restrict__ start,
-                             uint32_t *__restrict__ end) {
+__global__ void k_bin_bounds(const uint32_t *__restrict__ key, const FrameCounters *__restrict__ ctr,
+                             uint32_t *__restrict__ start, uint32_t *__restrict__ end) {
+    const int64_t n = ctr->n_pairs;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t k = key[i];
@@ -1435,108 +1523,70 @@ int launch_emit_keys(const FrameArgs &a, const uint32_t *counts, uint32_t *key, 
 }
 
 int launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *vis, const uint32_t *offsets,
-                       const uint32_t *order, int2 *entries, cudaStream_t s) {
+                       const uint32_t *order, int2 *entries, const FrameCounters *ctr, cudaStream_t s) {
     if (a.C <= 0) return 0;
-    k_curve_emit<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, offsets, order, entries);
+    k_curve_emit<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, offsets, order, entries, ctr);
     return 1;
 }
 
-int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t nf, int32_t *key,
-                     uint32_t *pidw, int8_t *wn, uint32_t *mask, uint64_t *sort_key, uint32_t *sort_val,
-                     cudaStream_t s) {
-    if (nf <= 0) return 0;
+int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries, int64_t cap_nf,
+                    const FrameCounters *ctr, int32_t *key, uint32_t *pidw, int8_t *wn, uint32_t *mask,
+                    uint64_t *sort_key, uint32_t *sort_val, cudaStream_t s) {
+    if (cap_nf <= 0) return 0;
+    const unsigned g = grid_for(cap_nf);
     if (a.S == 8)
-        k_fragment<8><<<grid_for(nf), kThreads, 0, s>>>(a, tvert, entries, nf, key, pidw, wn, mask, sort_key, sort_val);
+        k_fragment<8><<<g, kThreads, 0, s>>>(a, tvert, entries, ctr, key, pidw, wn, mask, sort_key, sort_val);
     else if (a.S == 16)
-        k_fragment<16><<<grid_for(nf), kThreads, 0, s>>>(a, tvert, entries, nf, key, pidw, wn, mask, sort_key, sort_val);
+        k_fragment<16><<<g, kThreads, 0, s>>>(a, tvert, entries, ctr, key, pidw, wn, mask, sort_key, sort_val);
     else
-        k_fragment<32><<<grid_for(nf), kThreads, 0, s>>>(a, tvert, entries, nf, key, pidw, wn, mask, sort_key, sort_val);
+        k_fragment<32><<<g, kThreads, 0, s>>>(a, tvert, entries, ctr, key, pidw, wn, mask, sort_key, sort_val);
     return 1;
 }
 
-int64_t flags_tmp_words(int64_t nf) { return 2 * ((nf + kFlagTile - 1) / kFlagTile + 2); }
+int64_t scan_mark_status_words(int64_t cap_nf) { return 2 * std::max<int64_t>(1, (cap_nf + kMarkTile - 1) / kMarkTile); }
 
-// Batches: the winding scan restarted at every scene's first entry.  A
-// contour left open (the RVG reader's Z adds no segment) leaves a nonzero
-// winding sum on its rows, which the reference's scan carries into the
-// paths after it; across a batch it would also reach the later scenes,
-// which a single-scene render of them does not see.  base[s] = the scan at
-// scene s's first sorted entry (paths, hence scenes, ascend along the
-// sorted entries), then every entry of scene s subtracts it.
-__global__ void k_scene_wn_base(const FrameArgs a, int64_t nf, const uint64_t *__restrict__ skey,
-                                const int8_t *__restrict__ wn_scan, int8_t *__restrict__ base) {
-    const int s = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (s >= a.n_scenes) return;
-    int64_t lo = 0, hi = nf;
-    while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if ((int)a.path_scene[(uint32_t)(skey[mid] >> 24)] < s) lo = mid + 1;
-        else hi = mid;
-    }
-    base[s] = lo < nf ? wn_scan[lo] : (int8_t)0;
+int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
+                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
+                     uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s) {
+    const int64_t words = scan_mark_status_words(cap_nf);
+    k_scan_mark<<<(unsigned)(words / 2), kMarkThreads, 0, s>>>(a, skey, perm, wn, wn_scan, draw, heads, item_scene,
+                                                               counters, tile_status, tile_status + words / 2,
+                                                               spin_cap);
+    return 1;
 }
 
-__global__ void k_wn_rebase(const FrameArgs a, int64_t nf, const uint64_t *__restrict__ skey,
-                            const int8_t *__restrict__ base, int8_t *__restrict__ wn_scan) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x) {
-        const int8_t b = base[a.path_scene[(uint32_t)(skey[i] >> 24)]];
-        if (b) wn_scan[i] = (int8_t)(wn_scan[i] - b);
-    }
-}
-
-int launch_scan_mark(const FrameArgs &a, int64_t nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                      int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
-                      uint32_t *tmp, int8_t *scene_base, cudaStream_t s) {
-    const int64_t ntiles = (nf + kFlagTile - 1) / kFlagTile;
-    uint32_t *s0 = tmp, *s1 = tmp + (ntiles + 2);
-    int n = 8;
-    k_wn_reduce<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(nf, perm, wn, s0);
-    scan_tiles_inplace(s0, ntiles, s);
-    k_wn_down<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(nf, perm, wn, s0, wn_scan);
-    if (a.scenes != nullptr && a.n_scenes > 1 && scene_base != nullptr) {
-        k_scene_wn_base<<<grid_for(a.n_scenes), kThreads, 0, s>>>(a, nf, skey, wn_scan, scene_base);
-        k_wn_rebase<<<(unsigned)std::min<int64_t>(grid_for(nf), 152 * 16), kThreads, 0, s>>>(a, nf, skey, scene_base,
-                                                                                          wn_scan);
-        n += 2;
-    }
-    k_flags_reduce<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(a, nf, skey, wn_scan, s0, s1);
-    scan_tiles_inplace(s0, ntiles, s);
-    scan_tiles_inplace(s1, ntiles, s);
-    k_flags_down<<<(unsigned)ntiles, kFlagThreads, 0, s>>>(a, nf, ntiles, skey, wn_scan, s0, s1, draw, heads,
-                                                            item_scene, counters);
-    return n;
-}
-
-int launch_stencil(const FrameArgs &a, int64_t nf, int64_t nm, const uint64_t *skey, const uint32_t *perm,
-                    const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan, const uint32_t *heads,
-                    uint32_t *merged, cudaStream_t s) {
-    if (nm <= 0) return 0;
+int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr, const uint64_t *skey,
+                   const uint32_t *perm, const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan,
+                   const uint32_t *heads, uint32_t *merged, cudaStream_t s) {
+    if (cap_nf <= 0) return 0;
+    const unsigned g = grid_for(cap_nf);
     if (a.S == 8)
-        k_stencil<8><<<grid_for(nm), kThreads, 0, s>>>(a, nf, nm, skey, perm, pidw, mask, wn_scan, heads, merged);
+        k_stencil<8><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, pidw, mask, wn_scan, heads, merged);
     else if (a.S == 16)
-        k_stencil<16><<<grid_for(nm), kThreads, 0, s>>>(a, nf, nm, skey, perm, pidw, mask, wn_scan, heads, merged);
+        k_stencil<16><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, pidw, mask, wn_scan, heads, merged);
     else
-        k_stencil<32><<<grid_for(nm), kThreads, 0, s>>>(a, nf, nm, skey, perm, pidw, mask, wn_scan, heads, merged);
+        k_stencil<32><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, pidw, mask, wn_scan, heads, merged);
     return 1;
 }
 
-int launch_item_tiles(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t n, uint32_t *cnt,
-                      cudaStream_t s) {
-    if (n <= 0) return 0;
-    k_item_tiles<<<grid_for(n), kThreads, 0, s>>>(a, draw, item_scene, n, cnt);
+int launch_item_tiles(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
+                      const FrameCounters *ctr, uint32_t *cnt, cudaStream_t s) {
+    if (cap_items <= 0) return 0;
+    k_item_tiles<<<grid_for(cap_items), kThreads, 0, s>>>(a, draw, item_scene, ctr, cnt);
     return 1;
 }
 
-int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t n,
-                      const uint32_t *offs, uint32_t *pkey, uint32_t *pval, cudaStream_t s) {
-    if (n <= 0) return 0;
-    k_emit_pairs<<<grid_for(n), kThreads, 0, s>>>(a, draw, item_scene, n, offs, pkey, pval);
+int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
+                      const FrameCounters *ctr, const uint32_t *offs, uint32_t *pkey, uint32_t *pval, cudaStream_t s) {
+    if (cap_items <= 0) return 0;
+    k_emit_pairs<<<grid_for(cap_items), kThreads, 0, s>>>(a, draw, item_scene, ctr, offs, pkey, pval);
     return 1;
 }
 
-int launch_bin_bounds(const uint32_t *key, int64_t n, uint32_t *start, uint32_t *end, cudaStream_t s) {
-    if (n <= 0) return 0;
-    k_bin_bounds<<<grid_for(n), kThreads, 0, s>>>(key, n, start, end);
+int launch_bin_bounds(const uint32_t *key, int64_t cap_pairs, const FrameCounters *ctr, uint32_t *start,
+                      uint32_t *end, cudaStream_t s) {
+    if (cap_pairs <= 0) return 0;
+    k_bin_bounds<<<grid_for(cap_pairs), kThreads, 0, s>>>(key, ctr, start, end);
     return 1;
 }
 

@@ -1,18 +1,22 @@
-// spr_sort.cu -- device-wide exclusive scan and stable LSD radix sort.
+// spr_sort.cu -- device-wide exclusive scans and stable LSD radix sort.
 //
-// Both are reduce-then-scan designs: every kernel reads its own tile and
-// global prefixes come from a separate small scan, so no thread block ever
-// waits on another one (no spin loops anywhere).  The radix scatter ranks
-// keys stably inside a tile with warp-level __match_any_sync and per-warp
-// digit counters, so equal keys keep their input order across the whole
-// array (the segmented sort of the reference is stable).
+// The frame's scans of sizes (entry offsets, resolve-pair offsets) are
+// single-pass decoupled look-back scans (spr_lookback.cuh) whose sizes may
+// come from device memory.  The radix sort's digit scans, which run over
+// sizes known on the host, and the allocation-free scan are reduce-then-scan
+// designs in which no block waits on another.  The radix scatter ranks keys
+// stably inside a tile with warp-level __match_any_sync and per-warp digit
+// counters, so equal keys keep their input order across the whole array
+// (the segmented sort of the reference is stable).
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "../../include/spr.h"
 #include "spr_internal.h"
+#include "spr_lookback.cuh"
 
 namespace spr {
 
@@ -113,8 +117,9 @@ __global__ void k_scan_down(const uint32_t *__restrict__ in, uint32_t *__restric
 }
 
 template <class K>
-__global__ void k_radix_hist(const K *__restrict__ keys, int64_t n, int shift, uint32_t *__restrict__ counts,
-                             int64_t ntiles) {
+__global__ void k_radix_hist(const K *__restrict__ keys, int64_t n_cap, const uint32_t *__restrict__ n_dev, int shift,
+                             uint32_t *__restrict__ counts, int64_t ntiles) {
+    const int64_t n = n_dev ? min((int64_t)*n_dev, n_cap) : n_cap;
     __shared__ uint32_t hist[256];
     hist[threadIdx.x] = 0;
     __syncthreads();
@@ -142,10 +147,13 @@ struct ScatterSmem {
 
 template <class K>
 __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const K *__restrict__ keys,
-                                                                  const uint32_t *__restrict__ vals, int64_t n,
-                                                                  int shift, const uint32_t *__restrict__ offsets,
+                                                                  const uint32_t *__restrict__ vals, int64_t n_cap,
+                                                                  const uint32_t *__restrict__ n_dev, int shift,
+                                                                  const uint32_t *__restrict__ offsets,
                                                                   int64_t ntiles, K *__restrict__ keys_out,
                                                                   uint32_t *__restrict__ vals_out) {
+    const int64_t n = n_dev ? min((int64_t)*n_dev, n_cap) : n_cap;
+    if ((int64_t)blockIdx.x * kRadixTile >= n) return;  // a tile past the end (nothing to move)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ScatterSmem<K> &sm = *reinterpret_cast<ScatterSmem<K> *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -355,11 +363,12 @@ __global__ void __launch_bounds__(kSmallWarps * 32) k_segment_sort_small(const u
                                                                         const uint32_t *__restrict__ start,
                                                                         const uint32_t *__restrict__ offsets,
                                                                         uint32_t P, uint64_t *__restrict__ keys_out,
-                                                                        uint32_t *__restrict__ vals_out) {
+                                                                        uint32_t *__restrict__ vals_out,
+                                                                        const FrameCounters *__restrict__ ctr) {
     __shared__ uint32_t skey[kSmallWarps][2][kWarpSeg], sval[kSmallWarps][2][kWarpSeg], shist[kSmallWarps][256];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t p = blockIdx.x * kSmallWarps + w;
-    if (p >= P) return;
+    if (p >= P || ctr->status != 0u || ctr->nf != ctr->need_nf) return;  // (entries not admitted: nothing to sort)
     const uint32_t b = offsets[start[p]], e = offsets[start[p + 1]];
     if (e <= b || e - b > (uint32_t)kWarpSeg) return;
     const int n = (int)(e - b);
@@ -435,11 +444,12 @@ __global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t 
                                                                const uint32_t *__restrict__ offsets,
                                                                uint64_t *__restrict__ keys_out,
                                                                uint32_t *__restrict__ vals_out, uint64_t *keys_tmp,
-                                                               uint32_t *vals_tmp) {
+                                                               uint32_t *vals_tmp, const FrameCounters *__restrict__ ctr) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SegSmem &sm = *reinterpret_cast<SegSmem *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t p = blockIdx.x;
+    if (ctr->status != 0u || ctr->nf != ctr->need_nf) return;  // entries not admitted: nothing to sort
     const uint32_t b = offsets[start[p]], e = offsets[start[p + 1]];
     if (e - b <= (uint32_t)kWarpSeg) return;  // empty, or a warp's (k_segment_sort_small)
     const uint32_t n = e - b;
@@ -575,17 +585,113 @@ __global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t 
 
 int launch_segment_sort(const CurveDesc *curves, uint32_t C, uint32_t P, const uint32_t *offsets, uint64_t *keys,
                         uint32_t *vals, uint64_t *keys_out, uint32_t *vals_out, uint32_t *path_start,
-                        cudaStream_t s) {
+                        const FrameCounters *ctr, cudaStream_t s) {
     if (P == 0) return 0;
     k_path_starts<<<(unsigned)(((int64_t)C + 1 + 255) / 256), 256, 0, s>>>(curves, C, P, path_start);
     cudaFuncSetAttribute(k_segment_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem));
     k_segment_sort_small<<<(P + kSmallWarps - 1) / kSmallWarps, kSmallWarps * 32, 0, s>>>(keys, path_start, offsets, P,
-                                                                                      keys_out, vals_out);
-    k_segment_sort<<<P, kSegThreads, sizeof(SegSmem), s>>>(keys, path_start, offsets, keys_out, vals_out, keys, vals);
+                                                                                      keys_out, vals_out, ctr);
+    k_segment_sort<<<P, kSegThreads, sizeof(SegSmem), s>>>(keys, path_start, offsets, keys_out, vals_out, keys, vals,
+                                                           ctr);
     return 3;
 }
 
+// ---- single-pass scans of frame sizes ------------------------------------------
+// One tile of kScanTile counts per block; tiles are taken in launch order.
+__global__ void __launch_bounds__(kScanThreads) k_scan_lb(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
+                                                           const uint32_t *__restrict__ n_dev, int64_t n_cap,
+                                                           uint64_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
+                                                           uint32_t spin_cap, uint32_t *__restrict__ frame_status,
+                                                           uint32_t *__restrict__ total_out, int64_t hold_tile) {
+    __shared__ uint32_t sw[kScanThreads / 32 + 1];
+    __shared__ uint32_t s_tile, s_prefix;
+    const int64_t n = n_dev ? min((int64_t)*n_dev, n_cap) : n_cap;
+    const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
+    __syncthreads();
+    const int64_t t = s_tile;
+    if (t >= ntiles) {
+        if (t == 0 && threadIdx.x == 0) {  // nothing to scan
+            out[0] = 0u;
+            if (total_out) *total_out = 0u;
+        }
+        return;
+    }
+    const int64_t base = t * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    if (base + kScanItems <= n) {  // two 128-bit loads
+        const uint4 a = reinterpret_cast<const uint4 *>(in + base)[0], b = reinterpret_cast<const uint4 *>(in + base)[1];
+        v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) v[k] = base + k < n ? in[base + k] : 0u;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    uint32_t total;
+    const uint32_t ex = block_excl_scan<kScanThreads>(sum, sw, &total);
+    if (threadIdx.x < 32) {
+        const bool publish = t != hold_tile;  // (a held tile's successors wait until they give up)
+        uint64_t pre = 0;
+        if (t > 0) {
+            if (threadIdx.x == 0 && publish) lb_store(status + t, kLbAggregate | total);
+            pre = lb_walk(status, t, 0ull, spin_cap, frame_status);
+        }
+        if (threadIdx.x == 0) {
+            if (publish) lb_store(status + t, kLbInclusive | (uint32_t)(pre + total));
+            s_prefix = (uint32_t)pre;
+        }
+    }
+    __syncthreads();
+    uint32_t p = s_prefix + ex;
+    uint32_t o[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        o[k] = p;
+        p += v[k];
+    }
+    if (base + kScanItems <= n) {
+        reinterpret_cast<uint4 *>(out + base)[0] = make_uint4(o[0], o[1], o[2], o[3]);
+        reinterpret_cast<uint4 *>(out + base)[1] = make_uint4(o[4], o[5], o[6], o[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < n) out[base + k] = o[k];
+    }
+    if (t == ntiles - 1 && threadIdx.x == 0) {
+        out[n] = s_prefix + total;
+        if (total_out) *total_out = s_prefix + total;
+    }
+}
+
+__global__ void k_admit(const uint32_t *__restrict__ need, uint32_t *__restrict__ admitted, uint32_t cap,
+                        uint32_t *__restrict__ status) {
+    const uint32_t v = *need;
+    if (v <= cap && !(*status & kStatusTimeout)) {  // (after a timeout the size itself may be wrong)
+        *admitted = v;
+    } else {
+        *admitted = 0u;
+        atomicOr(status, kStatusOverflow);
+    }
+}
+
 int64_t scan_tmp_words(int64_t n) { return (n + kScanTile - 1) / kScanTile + 2; }
+
+int64_t lookback_words(int64_t n) { return std::max<int64_t>(1, (n + kScanTile - 1) / kScanTile); }
+
+int scan_lookback_u32(const uint32_t *in, uint32_t *out, const uint32_t *n_dev, int64_t n_cap, uint64_t *tile_status,
+                      uint32_t *tile_ctr, uint32_t spin_cap, uint32_t *frame_status, uint32_t *total_out,
+                      cudaStream_t s, int64_t hold_tile) {
+    k_scan_lb<<<(unsigned)lookback_words(n_cap), kScanThreads, 0, s>>>(in, out, n_dev, n_cap, tile_status, tile_ctr,
+                                                                     spin_cap, frame_status, total_out, hold_tile);
+    return 1;
+}
+
+int launch_admit(const uint32_t *need, uint32_t *admitted, uint32_t cap, uint32_t *status, cudaStream_t s) {
+    k_admit<<<1, 1, 0, s>>>(need, admitted, cap, status);
+    return 1;
+}
 
 int scan_exclusive_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp, cudaStream_t s) {
     int64_t ntiles = (n + kScanTile - 1) / kScanTile;
@@ -613,9 +719,10 @@ int64_t radix_tmp_words(int64_t n) {
 
 template <class K>
 bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_t n, int key_bits, uint32_t *tmp,
-                cudaStream_t s, int *launches) {
+                cudaStream_t s, int *launches, const uint32_t *n_dev) {
     *launches = 0;
-    if (n <= 1) return false;
+    if (n <= 1 && !n_dev) return false;
+    if (n <= 0) n = 1;
     const int64_t ntiles = radix_tiles(n);
     const int64_t c = 256 * ntiles;
     uint32_t *counts = tmp;
@@ -628,19 +735,19 @@ bool radix_sort(K *keys, uint32_t *vals, K *keys_alt, uint32_t *vals_alt, int64_
         const uint32_t *vi = alt ? vals_alt : vals;
         K *ko = alt ? keys : keys_alt;
         uint32_t *vo = alt ? vals : vals_alt;
-        k_radix_hist<K><<<(unsigned)ntiles, kRadixThreads, 0, s>>>(ki, n, shift, counts, ntiles);
+        k_radix_hist<K><<<(unsigned)ntiles, kRadixThreads, 0, s>>>(ki, n, n_dev, shift, counts, ntiles);
         *launches += 2 + scan_exclusive_u32(counts, offsets, c, scan_tmp, s);
-        k_radix_scatter<K><<<(unsigned)ntiles, kRadixThreads, sizeof(ScatterSmem<K>), s>>>(ki, vi, n, shift, offsets,
-                                                                                       ntiles, ko, vo);
+        k_radix_scatter<K><<<(unsigned)ntiles, kRadixThreads, sizeof(ScatterSmem<K>), s>>>(ki, vi, n, n_dev, shift,
+                                                                                       offsets, ntiles, ko, vo);
         alt = !alt;
     }
     return alt;
 }
 
 template bool radix_sort<uint64_t>(uint64_t *, uint32_t *, uint64_t *, uint32_t *, int64_t, int, uint32_t *,
-                                   cudaStream_t, int *);
+                                   cudaStream_t, int *, const uint32_t *);
 template bool radix_sort<uint32_t>(uint32_t *, uint32_t *, uint32_t *, uint32_t *, int64_t, int, uint32_t *,
-                                   cudaStream_t, int *);
+                                   cudaStream_t, int *, const uint32_t *);
 
 // ---- allocation-free exclusive scan ------------------------------------------
 // Scratch of spr_scan_offsets_noalloc: the per-tile partial sums of one scan

@@ -175,6 +175,7 @@ def lib() -> C.CDLL:
         L.spr_step_timing.argtypes = [vp, C.POINTER(C.c_double), i32, C.POINTER(i32)]
         L.spr_get_frame_stats.argtypes = [vp, C.POINTER(FrameStats)]
         L.spr_set_memory_limit.argtypes = [vp, C.c_int64]
+        L.spr_debug_set_lookback.argtypes = [vp, C.c_uint32, C.c_int64]
         L.spr_step_name.argtypes = [i32]
         L.spr_step_name.restype = C.c_char_p
         L.spr_debug_dump.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
@@ -536,6 +537,11 @@ class VGRasterizer:
         check(lib().spr_step_timing(self._h, buf, 64, C.byref(n)), "spr_step_timing")
         return {lib().spr_step_name(i).decode(): buf[i] for i in range(n.value)}
 
+    def debug_set_lookback(self, spin_cap=1 << 24, hold_tile=-1):
+        """Test hook of the bounded look-back waits: polls before a wait gives
+        up, and a tile of the entry-offset scan that never publishes."""
+        check(lib().spr_debug_set_lookback(self._h, int(spin_cap), int(hold_tile)), "spr_debug_set_lookback")
+
     def set_memory_limit(self, nbytes: int):
         """Cap on the handle's device memory (0 = none); a frame that would
         need more raises SprError(ERR_OUT_OF_MEMORY) and the handle stays
@@ -665,6 +671,11 @@ class Batch:
         e = ElementNumber()
         check(lib().spr_batch_get_counts(self._h, C.byref(e)), "spr_batch_get_counts")
         return e.as_dict()
+
+    def debug_set_lookback(self, spin_cap=1 << 24, hold_tile=-1):
+        """Test hook of the bounded look-back waits: polls before a wait gives
+        up, and a tile of the entry-offset scan that never publishes."""
+        check(lib().spr_debug_set_lookback(self._h, int(spin_cap), int(hold_tile)), "spr_debug_set_lookback")
 
     def set_memory_limit(self, nbytes: int):
         """Cap on the handle's device memory (0 = none); a frame that would

@@ -217,8 +217,16 @@ int spr_set_rev_transform(spr_handle *h, const float ctx[13]);
 /* rasterize / rasterizeImpl (ras_base.cpp:1131-1195, cu:879-1453): runs the
  * whole pipeline on `stream` and leaves an RGBA8 image (row y = scene
  * y in [y, y+1), row-major, 4*width bytes per row) in device memory.  Returns
- * after the work is enqueued; the element counts are read back once per frame
- * to size the work buffers. */
+ * after the work is enqueued.  The reference reads the fragment counts back
+ * twice per frame (cu:980, 1139-1157); here only the first frame after a
+ * change of scene, viewport or sample count does (to size the buffers, with
+ * headroom).  Later frames make no host reads: their kernels take their sizes
+ * from device memory, and a frame that outgrows the buffers is rendered again
+ * with larger ones when its results are first read (spr_read_image,
+ * spr_image_device_ptr, spr_get_counts, spr_get_frame_stats, stage dumps).
+ * Inputs changed between such a frame and that read make it
+ * SPR_ERR_CAPACITY_EXCEEDED there; a bounded device wait that gave up makes it
+ * SPR_ERR_TIMEOUT. */
 int spr_render(spr_handle *h, void *stream);
 
 /* Device pointer of the image written by the last spr_render. */
@@ -279,6 +287,13 @@ typedef struct spr_frame_stats {
     int64_t device_bytes;    /* device memory held by the handle            */
 } spr_frame_stats;
 int spr_get_frame_stats(spr_handle *h, spr_frame_stats *out);
+/* Test hook of the bounded device waits (no counterpart in the reference):
+ * the single-pass scans of a frame give up a look-back wait after spin_cap
+ * polls (default 2^24, about a second) and the frame then fails with
+ * SPR_ERR_TIMEOUT; hold_tile >= 0 makes that tile of the entry-offset scan
+ * never publish its sum, so that the tiles after it wait until the limit
+ * runs out (-1: none).  The handle stays usable. */
+int spr_debug_set_lookback(spr_handle *h, uint32_t spin_cap, int64_t hold_tile);
 /* Cap on the device memory the handle's buffers may hold, in bytes (0 = no
  * cap, the default).  The counterpart of the reference's fixed-size frame
  * arena, whose allocator throws when it is exhausted

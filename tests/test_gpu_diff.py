@@ -343,7 +343,7 @@ def test_backward_reuses_the_held_forward_frame():
         gf2, gv2, st2 = backward(r)  # still held
         r.rasterize()
         gf3, gv3, st3 = backward(r)  # recomputed
-        assert st1["host_syncs"] == 1 and st2["host_syncs"] == 1 and st3["host_syncs"] == 4
+        assert st1["host_syncs"] == 1 and st2["host_syncs"] == 1 and st3["host_syncs"] == 3
         assert st1["kernel_launches"] < st3["kernel_launches"]
         for a, b in ((gf1, gf2), (gf1, gf3), (gv1, gv2), (gv1, gv3)):
             assert rel(a, b) < 1e-5
@@ -352,7 +352,7 @@ def test_backward_reuses_the_held_forward_frame():
         vdev = torch.tensor(moved.vertex, device="cuda")
         r.update_vertices(vdev.data_ptr())
         gf4, gv4, st4 = backward(r)
-        assert st4["host_syncs"] == 4
+        assert st4["host_syncs"] == 3
     with spr.VGRasterizer(W, H, samples=16) as r:
         r.add_vg(moved)
         r.diff_render(f.data_ptr(), img.data_ptr())

@@ -26,7 +26,7 @@ def test_replay_matches_and_skips_host_reads():
         r.set_graph_replay(True)
         r.add_vg(sc)
         r.rasterize()  # renders normally, then captures
-        assert r.graph_replays() == 0 and r.frame_stats()["host_syncs"] == 3
+        assert r.graph_replays() == 0 and r.frame_stats()["host_syncs"] == 2  # the sized first frame
         assert np.array_equal(r.read_image(), ref)
         for k in range(3):
             r.rasterize()
@@ -66,7 +66,7 @@ def test_changes_drop_the_graph():
         assert n >= 4
         r.set_graph_replay(False)
         r.rasterize()
-        assert r.graph_replays() == n and r.frame_stats()["host_syncs"] == 3
+        assert r.graph_replays() == n and r.frame_stats()["host_syncs"] == 0  # sized already
 
 
 def test_batch_replay():
