@@ -830,9 +830,9 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     // stages 6-7: entries, fragments, boundary masks
     if ((st = ensure(h->entries, 8 * (size_t)cap_nf)) || (st = ensure(h->key, 4 * (size_t)cap_nf)) ||
         (st = ensure(h->pidw, 4 * (size_t)cap_nf)) || (st = ensure(h->wn, (size_t)cap_nf)) ||
-        (st = ensure(h->mask, 4 * (size_t)WORDS * cap_nf)) || (st = ensure(h->skey[0], 8 * (size_t)cap_nf)) ||
-        (st = ensure(h->skey[1], 8 * (size_t)cap_nf)) || (st = ensure(h->sval[0], 4 * (size_t)cap_nf)) ||
-        (st = ensure(h->sval[1], 4 * (size_t)cap_nf)) || (st = ensure(h->wn_scan, (size_t)cap_nf)) ||
+        (st = ensure(h->mask, 4 * (size_t)WORDS * cap_nf)) || (st = ensure(h->skey[0], 8 * (size_t)cap_nf + 64)) ||
+        (st = ensure(h->skey[1], 8 * (size_t)cap_nf + 64)) || (st = ensure(h->sval[0], 4 * (size_t)cap_nf + 64)) ||
+        (st = ensure(h->sval[1], 4 * (size_t)cap_nf + 64)) || (st = ensure(h->wn_scan, (size_t)cap_nf)) ||
         (st = ensure(h->draw, 16 * (size_t)cap_items)) || (st = ensure(h->heads, 4 * (size_t)cap_nf)) ||
         (st = ensure(h->lb_mark, 8 * (size_t)scan_mark_status_words(cap_nf))) ||
         (st = ensure(h->merged, 4 * (size_t)WORDS * cap_nf)) ||

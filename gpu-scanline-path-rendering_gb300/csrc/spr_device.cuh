@@ -224,6 +224,59 @@ __device__ __forceinline__ int monotonize(const CurveGeom &g, bool visible, floa
     return n;
 }
 
+// monotonize() in registers: the same cut points as its insertion sort
+// (equal values are interchangeable, so a sorting network gives the same
+// array), q[0..n) followed by q[n] = 1, q[k > n] = 0.
+__device__ __forceinline__ void cas(float &a, float &b) {
+    const float lo = fminf(a, b), hi = fmaxf(a, b);  // (no NaN: candidates lie in (0, 1), unused ones are 2)
+    a = lo;
+    b = hi;
+}
+__device__ __forceinline__ int monotonize_r(const CurveGeom &g, bool visible, float (&q)[5]) {
+    q[0] = q[1] = q[2] = q[3] = q[4] = 0.f;
+    if (!visible) return 0;
+    float c[4] = {2.f, 2.f, 2.f, 2.f};  // x roots, then y roots; 2 = none
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float *P = k == 0 ? g.px : g.py;
+        float r0 = 2.f, r1 = 2.f;
+        if (g.type == kQuad) {
+            float b = (P[0] - P[1]) + (P[2] - P[1]);
+            if (!(fabsf(b) < 1e-6f)) {
+                float t = (P[0] - P[1]) / b;
+                if (t > 0.f && t < 1.f) r0 = t;
+            }
+        } else if (g.type == kCubic || g.type == kRational) {
+            float a0 = 0.f, a1 = 0.f;
+            if (g.type == kCubic) {
+                solve_quad_eq((P[3] - P[0]) + 3.f * (P[1] - P[2]), 2.f * ((P[0] - P[1]) + (P[2] - P[1])), P[1] - P[0],
+                              &a0, &a1);
+            } else {
+                float w0 = 1.f, w1 = g.w, w2 = 1.f;
+                float p0 = w0 * P[0], p1 = w1 * P[1], p2 = w2 * P[2];
+                float pw01 = p0 * w1 - p1 * w0;
+                float pw12 = p1 * w2 - p2 * w1;
+                float pw20 = p2 * w0 - p0 * w2;
+                solve_quad_eq(pw01 + pw12 + pw20, -(2.f * pw01 + pw20), pw01, &a0, &a1);
+            }
+            if (a0 > 0.f && a0 < 1.f) r0 = a0;
+            if (a1 > 0.f && a1 < 1.f && a1 != a0) r1 = a1;
+        }
+        c[2 * k] = r0;
+        c[2 * k + 1] = r1;
+    }
+    cas(c[0], c[1]);
+    cas(c[2], c[3]);
+    cas(c[0], c[2]);
+    cas(c[1], c[3]);
+    cas(c[1], c[2]);
+    const int n = (c[0] < 2.f) + (c[1] < 2.f) + (c[2] < 2.f) + (c[3] < 2.f);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q[k] = k < n ? c[k] : (k == n ? 1.f : 0.f);
+    q[4] = n == 4 ? 1.f : 0.f;
+    return n + 1;
+}
+
 // Crossing of coordinate P(t) = c on [tmin, tmax].
 __device__ __forceinline__ float solve_crossing(const CurveGeom &g, const float *P, float c, float tmin, float tmax) {
     if (g.type == kLinear) {

@@ -140,11 +140,13 @@ __global__ void k_curve_count(FrameArgs a, const float2 *__restrict__ tv, const 
     CurveGeom g;
     load_geom(d, tv, g);
     float q[5];
-    const int np = monotonize(g, vis[d.pid] != 0, q);
+    const int np = monotonize_r(g, vis[d.pid] != 0, q);
     const Dim dm = dim_of(a, d.pid);
     float v0x = g.px[0], v0y = g.py[0];
     uint32_t p = 0;
-    for (int i = 0; i < np; ++i) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        if (i >= np) break;
         const float t1 = q[i];
         const float v1x = curve_coord(g.type, g.w, g.px, t1), v1y = curve_coord(g.type, g.w, g.py, t1);
         const CutRange cr = cut_range(v0x, v0y, v1x, v1y, dm.W, dm.H);
@@ -172,94 +174,197 @@ __global__ void k_emit_keys(FrameArgs a, const uint32_t *__restrict__ counts, ui
     val[c] = (uint32_t)c;
 }
 
-__global__ void k_curve_emit(FrameArgs a, const float2 *__restrict__ tv, const uint8_t *__restrict__ vis,
-                             const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ order,
-                             int2 *__restrict__ entries, const FrameCounters *__restrict__ ctr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Entries of one monotone piece, whose chain starts from the piece's own
+// t0 and is solved crossing by crossing (k_make_intersection_impl_1,
+// ras_cut.h:837-1241): every piece is an independent work item.
+struct PieceState {
+    CurveGeom g;
+    int2 *out;
+    int cid, p, i, n_loop, nx, ny;
+    float x, y, dx, dy, slot0, slot1, t1_ms;
+    uint32_t last;
+};
+
+// Sets up piece ms of a curve (v0, v1: its end points; t0_ms: the previous
+// piece's end parameter with its flags, 0 for the first).
+__device__ __forceinline__ void piece_begin(PieceState &st, const Dim &dm, float t0_ms, float traw, float v0x,
+                                            float v0y, float v1x, float v1y) {
+    const uint32_t tb = fbits(traw) & 0xFFFFFFFCu;
+    st.t1_ms = (floorf(v1x) == v1x) ? ffrom(tb | 2u) : ffrom(tb | 3u);
+    const CutRange cr = cut_range(v0x, v0y, v1x, v1y, dm.W, dm.H);
+    st.nx = cr.nx;
+    st.ny = cr.ny;
+    st.n_loop = cr.nx + cr.ny + 1;
+    st.x = (float)(cr.dx < 0.f ? cr.xe : cr.xb);
+    st.y = (float)(cr.dy < 0.f ? cr.ye : cr.yb);
+    st.dx = cr.dx;
+    st.dy = cr.dy;
+    st.slot0 = st.slot1 = t0_ms;
+    st.last = fbits(-1.f);
+    st.p = 0;
+    st.i = -1;
+}
+
+// One step of a piece: the entry at the nearer of the two chains' current
+// crossings (the piece start first), then the next crossing of that chain.
+// Returns false once the piece is done.
+__device__ __forceinline__ bool piece_step(PieceState &st) {
+    float t_solve = 0.f, c = 0.f, t_min;
+    int side = 0;
+    if (st.i == -1) {
+        t_min = st.slot0;
+        if (st.nx == 0) {
+            side = 0;
+            t_solve = 2.f;
+        } else if (st.ny == 0) {
+            side = 1;
+            t_solve = 2.f;
+        } else {
+            side = 0;
+            st.nx--;
+            c = st.x;
+            st.x += st.dx;
+        }
+    } else if (st.slot0 <= st.slot1) {
+        t_min = st.slot0;
+        side = 0;
+        if (st.nx > 0) {
+            st.nx--;
+            c = st.x;
+            st.x += st.dx;
+        } else {
+            t_solve = 2.f;
+        }
+    } else {
+        t_min = st.slot1;
+        side = 1;
+        if (st.ny > 0) {
+            st.ny--;
+            c = st.y;
+            st.y += st.dy;
+        } else {
+            t_solve = 2.f;
+        }
+    }
+    if (st.i >= 0) {
+        uint32_t ob = fbits(t_min);
+        if ((ob & 0xFFFFFFFCu) == (st.last & 0xFFFFFFFCu)) {  // coincident t: both entries get both flags
+            ob |= st.last;
+            st.out[st.p - 1] = make_int2(st.cid, (int)ob);
+        }
+        st.out[st.p] = make_int2(st.cid, (int)ob);
+        st.last = ob;
+        st.p++;
+    }
+    if (t_solve < 2.f) t_solve = solve_crossing(st.g, side ? st.g.py : st.g.px, c, t_min, st.t1_ms);
+    const float sv = ffrom((fbits(t_solve) & 0xFFFFFFFCu) | (uint32_t)side);
+    if (side) st.slot1 = sv;
+    else st.slot0 = sv;
+    return ++st.i < st.n_loop;
+}
+
+// Per warp: its 32 curves (in emission order), their monotone cut points
+// and the output position of every piece.
+constexpr int kEmitWarps = 4;
+struct EmitStash {
+    float px[4][32], py[4][32], w[32], q[5][32];
+    uint32_t type[32], cid[32], poff[5][32];
+    uint32_t item[5 * 32];  // warp item k: lane | piece << 8
+};
+
+// One warp per 32 curves.  Each lane expands its curve into its monotone
+// pieces; the warp's pieces form one list, and a lane whose piece is done
+// takes the next one (a ballot ranks the lanes asking), so the lanes stay
+// busy until the list runs out instead of waiting for the curve with the
+// most crossings.  Curves come in emission order (grouped by type), so a
+// warp's pieces mostly run the same solver.
+__global__ void __launch_bounds__(kEmitWarps * 32) k_curve_emit(FrameArgs a, const float2 *__restrict__ tv,
+                                                                const uint8_t *__restrict__ vis,
+                                                                const uint32_t *__restrict__ offsets,
+                                                                const uint32_t *__restrict__ order,
+                                                                int2 *__restrict__ entries,
+                                                                const FrameCounters *__restrict__ ctr) {
+    __shared__ EmitStash stash[kEmitWarps];
     // entries not admitted (the buffers are too small), or the offsets not
     // to be trusted (a scan gave up waiting): nothing is written
-    if (i >= a.C || ctr->status != 0u || ctr->nf != ctr->need_nf) return;
-    const int cid = order != nullptr ? (int)order[i] : i;
-    const CurveDesc d = a.curves[cid];
-    CurveGeom g;
-    load_geom(d, tv, g);
-    float q[5];
-    const int np = monotonize(g, vis[d.pid] != 0, q);
-    const Dim dm = dim_of(a, d.pid);
-    int2 *out = entries + offsets[cid];
-    float t0_ms = 0.f;
-    float v0x = g.px[0], v0y = g.py[0];
-    int p = 0;
-    for (int ms = 0; ms < np; ++ms) {
-        const float traw = q[ms];
-        const float v1x = curve_coord(g.type, g.w, g.px, traw), v1y = curve_coord(g.type, g.w, g.py, traw);
-        const uint32_t tb = fbits(traw) & 0xFFFFFFFCu;
-        const float t1_ms = (floorf(v1x) == v1x) ? ffrom(tb | 2u) : ffrom(tb | 3u);
-        const CutRange cr = cut_range(v0x, v0y, v1x, v1y, dm.W, dm.H);
-        int nx = cr.nx, ny = cr.ny;
-        const int n_loop = nx + ny + 1;
-        float x = (float)(cr.dx < 0.f ? cr.xe : cr.xb);
-        float y = (float)(cr.dy < 0.f ? cr.ye : cr.yb);
-        float slot0 = t0_ms, slot1 = t0_ms;
-        uint32_t last = fbits(-1.f);
-        for (int i = -1; i < n_loop; ++i) {
-            float t_solve = 0.f, c = 0.f, t_min;
-            int side = 0;
-            if (i == -1) {
-                t_min = slot0;
-                if (nx == 0) {
-                    side = 0;
-                    t_solve = 2.f;
-                } else if (ny == 0) {
-                    side = 1;
-                    t_solve = 2.f;
-                } else {
-                    side = 0;
-                    nx--;
-                    c = x;
-                    x += cr.dx;
-                }
-            } else if (slot0 <= slot1) {
-                t_min = slot0;
-                side = 0;
-                if (nx > 0) {
-                    nx--;
-                    c = x;
-                    x += cr.dx;
-                } else {
-                    t_solve = 2.f;
-                }
-            } else {
-                t_min = slot1;
-                side = 1;
-                if (ny > 0) {
-                    ny--;
-                    c = y;
-                    y += cr.dy;
-                } else {
-                    t_solve = 2.f;
-                }
+    if (ctr->status != 0u || ctr->nf != ctr->need_nf) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    EmitStash &S = stash[warp];
+    const int i = (blockIdx.x * kEmitWarps + warp) * 32 + lane;
+    int np = 0;
+    if (i < a.C) {
+        const int cid = order != nullptr ? (int)order[i] : i;
+        const CurveDesc d = a.curves[cid];
+        CurveGeom g;
+        load_geom(d, tv, g);
+        float q[5];
+        np = monotonize_r(g, vis[d.pid] != 0, q);
+        const Dim dm = dim_of(a, d.pid);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) S.px[k][lane] = g.px[k], S.py[k][lane] = g.py[k];
+        S.w[lane] = g.w;
+        S.type[lane] = (uint32_t)g.type;
+        S.cid[lane] = (uint32_t)cid;
+        uint32_t run = offsets[cid];
+        float v0x = g.px[0], v0y = g.py[0];
+#pragma unroll
+        for (int ms = 0; ms < 5; ++ms) {
+            S.q[ms][lane] = q[ms];
+            S.poff[ms][lane] = run;
+            if (ms < np) {
+                const float v1x = curve_coord(g.type, g.w, g.px, q[ms]), v1y = curve_coord(g.type, g.w, g.py, q[ms]);
+                const CutRange cr = cut_range(v0x, v0y, v1x, v1y, dm.W, dm.H);
+                run += 1 + cr.nx + cr.ny;
+                v0x = v1x;
+                v0y = v1y;
             }
-            if (i >= 0) {
-                uint32_t ob = fbits(t_min);
-                if ((ob & 0xFFFFFFFCu) == (last & 0xFFFFFFFCu)) {
-                    ob |= last;
-                    out[p - 1] = make_int2(cid, (int)ob);
-                }
-                out[p] = make_int2(cid, (int)ob);
-                last = ob;
-                p++;
-            }
-            if (t_solve < 2.f) t_solve = solve_crossing(g, side ? g.py : g.px, c, t_min, t1_ms);
-            const float st = ffrom((fbits(t_solve) & 0xFFFFFFFCu) | (uint32_t)side);
-            if (side)
-                slot1 = st;
-            else
-                slot0 = st;
         }
-        t0_ms = t1_ms;
-        v0x = v1x;
-        v0y = v1y;
+    }
+    // the warp's piece list
+    uint32_t pre = (uint32_t)np;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= o) pre += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+    pre -= (uint32_t)np;
+    for (int ms = 0; ms < np; ++ms) S.item[pre + ms] = (uint32_t)lane | ((uint32_t)ms << 8);
+    __syncwarp();
+    PieceState st;
+    bool active = false;
+    uint32_t next = 0;
+    for (;;) {
+        const uint32_t want = __ballot_sync(0xffffffffu, !active);
+        if (!active) {
+            const uint32_t k = next + __popc(want & ((1u << lane) - 1u));
+            if (k < total) {
+                const uint32_t it = S.item[k];
+                const int L = (int)(it & 0xFFu), ms = (int)(it >> 8);
+                st.g.type = (int)S.type[L];
+                st.g.w = S.w[L];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) st.g.px[c] = S.px[c][L], st.g.py[c] = S.py[c][L];
+                st.cid = (int)S.cid[L];
+                st.out = entries + S.poff[ms][L];
+                const float tq = S.q[ms][L];
+                const float v1x = curve_coord(st.g.type, st.g.w, st.g.px, tq),
+                            v1y = curve_coord(st.g.type, st.g.w, st.g.py, tq);
+                float t0_ms = 0.f, v0x = st.g.px[0], v0y = st.g.py[0];
+                if (ms > 0) {  // the previous piece's end: its parameter with its flags
+                    const float tp = S.q[ms - 1][L];
+                    v0x = curve_coord(st.g.type, st.g.w, st.g.px, tp);
+                    v0y = curve_coord(st.g.type, st.g.w, st.g.py, tp);
+                    const uint32_t tb = fbits(tp) & 0xFFFFFFFCu;
+                    t0_ms = (floorf(v0x) == v0x) ? ffrom(tb | 2u) : ffrom(tb | 3u);
+                }
+                piece_begin(st, dim_of(a, a.curves[st.cid].pid), t0_ms, tq, v0x, v0y, v1x, v1y);
+                active = true;
+            }
+        }
+        next += __popc(want);
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) active = piece_step(st);
     }
 }
 
@@ -1525,7 +1630,8 @@ int launch_emit_keys(const FrameArgs &a, const uint32_t *counts, uint32_t *key, 
 int launch_curve_emit(const FrameArgs &a, const float2 *tvert, const uint8_t *vis, const uint32_t *offsets,
                        const uint32_t *order, int2 *entries, const FrameCounters *ctr, cudaStream_t s) {
     if (a.C <= 0) return 0;
-    k_curve_emit<<<grid_for(a.C), kThreads, 0, s>>>(a, tvert, vis, offsets, order, entries, ctr);
+    k_curve_emit<<<grid_for(a.C, kEmitWarps * 32), kEmitWarps * 32, 0, s>>>(a, tvert, vis, offsets, order, entries,
+                                                                           ctr);
     return 1;
 }
 
