@@ -662,6 +662,19 @@ def run_ours(args, rank, world, local_rank):
     units = {"fragment": counts["curve_fragment"], "pixel": W * H}.get(unit_name or "", None)
     traffic = per_unit * units if (per_unit is not None and units) else None
     frame_bytes = frame_alg_bytes(counts, scene.n_vertices, scene.n_curves, scene.n_paths, W, H, SAMPLES)
+    # the dominant step's instruction-issue roofline: warp instructions per
+    # unit from the committed ncu capture (scaled by the frame's units) over
+    # the step's time, against one instruction per scheduler per cycle
+    inst_unit, inst_unit_name = read_traffic(dom + "_warp_instructions")
+    issue = None
+    if inst_unit is not None and clk.get("sm_mhz"):
+        n_units = {"pixel": W * H}.get(inst_unit_name, 0)
+        inst = inst_unit * n_units
+        peak_inst = torch.cuda.get_device_properties(dev).multi_processor_count * 4 * clk["sm_mhz"] * 1e6
+        issue = {"bound": "issue", "warp_instructions": inst, "achieved": inst / (step_mean[dom] / 1e3),
+                 "peak": peak_inst, "unit": "warp instructions/s", "frac": inst / (step_mean[dom] / 1e3) / peak_inst,
+                 "source": f"ncu warp instructions per {inst_unit_name} (profiles/roofline.md) x the frame's units; "
+                           "peak = SMs x 4 schedulers x median SM clock"}
 
     cpu_value, cpu_ms, cores = cpu_frame(scene)
     accuracy = {"large_frame": crossing_accuracy(r, scene, W, H), "small_frame": small_scene_accuracy(dev),
@@ -680,7 +693,7 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "alg_bytes": sb[dom], "ms": step_mean[dom]},
+                     "traffic": traffic, "alg_bytes": sb[dom], "ms": step_mean[dom], "issue": issue},
         "frame_roofline": {"alg_bytes": frame_bytes, "achieved": frame_bytes / (ms_max / 1e3) / 1e9,
                            "frac": frame_bytes / (ms_max / 1e3) / 1e9 / peak, "unit": "GB/s"},
         "step_ms": step_mean,
