@@ -902,7 +902,8 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     // stages 9-12, 14: winding scan, marks, draw list (one look-back pass)
     cudaMemsetAsync(h->lb_mark.p, 0, 8 * (size_t)scan_mark_status_words(cap_nf), s);
     L += launch_scan_mark(a, cap_nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
-                          h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, ctr, h->lb_mark.as<uint64_t>(),
+                          h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, h->tiles.as<uint32_t>(), ctr,
+                          h->lb_mark.as<uint64_t>(),
                           h->lb_spin_cap, s);
     rec(h, 5, s);
     // stage 13: merged sample masks
@@ -910,7 +911,6 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
                         h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), s);
     rec(h, 6, s);
     // stage 15: bin draw items by (cell row, 64-column tile), resolve
-    L += launch_item_tiles(a, h->draw.as<int4>(), item_scene, cap_items, ctr, h->tiles.as<uint32_t>(), s);
     cudaMemsetAsync(h->lb_pair.p, 0, 8 * (size_t)lookback_words(cap_items), s);
     L += scan_lookback_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), &ctr->n_items, cap_items,
                            h->lb_pair.as<uint64_t>(), &ctr->tiles[2], h->lb_spin_cap, &ctr->status, &ctr->need_pairs,

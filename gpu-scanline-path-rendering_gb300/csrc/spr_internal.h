@@ -183,17 +183,16 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
 // Look-back words of launch_scan_mark (zero before the launch).
 int64_t scan_mark_status_words(int64_t cap_nf);
 // Winding scan, merged-fragment / span marks, draw list and merged heads in
-// one pass (decoupled look-back); writes the item counts to the counters.
-// item_scene (batch frames only, else null) receives the scene of each draw
-// item; in batch frames the winding scan restarts at every scene.
+// one pass (decoupled look-back); writes the item counts to the counters
+// and the resolve bins each item covers to item_tile_count.  item_scene
+// (batch frames only, else null) receives the scene of each draw item; in
+// batch frames the winding scan restarts at every scene.
 int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
-                     uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s);
+                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *item_tile_count,
+                     FrameCounters *counters, uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s);
 int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr, const uint64_t *skey,
                    const uint32_t *perm, const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan,
                    const uint32_t *heads, uint32_t *merged_mask, cudaStream_t s);
-int launch_item_tiles(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
-                      const FrameCounters *ctr, uint32_t *tile_counts, cudaStream_t s);
 int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
                       const FrameCounters *ctr, const uint32_t *pair_offsets, uint32_t *pair_key, uint32_t *pair_val,
                       cudaStream_t s);

@@ -10,7 +10,7 @@
 //   k_mark_merged_fragment_and_span + scans +
 //   k_gen_gl_merged_fragment_and_span (cu:462-868)   -> k_flags_reduce / k_flags_down
 //   k_gen_stencil_cuda_sm + block boundary (cu:554)  -> k_stencil
-//   OpenGL draw + multisample resolve (cu:1312-1433) -> k_item_tiles, k_emit_pairs,
+//   OpenGL draw + multisample resolve (cu:1312-1433) -> k_scan_lb, k_emit_pairs,
 //                                                       radix_sort, k_bin_bounds, k_resolve
 // ("cu" = gpu-scanline/src/rasterizer/R_cut_A_mask_comb_scanline/ras_cut_mask_comb_scanline.cu)
 
@@ -596,6 +596,21 @@ struct Mark {
     uint32_t ff, sf;
 };
 
+// Columns [x0, x1) of draw item `it` in a viewport W wide (its first column
+// read as unsigned 16 bits: cells at x = -2 cover nothing).
+__device__ __forceinline__ void item_cols(const int4 &it, int W, int &x0, int &x1) {
+    const int x = (int)((uint32_t)it.x & 0xFFFFu);
+    x0 = max(x, 0);
+    x1 = min(x + it.y, W);
+}
+
+// Resolve bins (64-column tiles of its cell row) that draw item `it` covers.
+__device__ __forceinline__ uint32_t item_tiles(const int4 &it, int W) {
+    int x0, x1;
+    item_cols(it, W, x0, x1);
+    return x1 > x0 ? (uint32_t)((x1 - 1) / kBinW - x0 / kBinW + 1) : 0u;
+}
+
 // k_mark_merged_fragment_and_span (cu:462-535) on sorted position i with
 // keys k0 (position i - 1) and k1 (position i) and scanned winding w.
 __device__ __forceinline__ Mark mark_of(int64_t i, uint64_t k0, uint64_t k1, int8_t w, const FrameArgs &a) {
@@ -634,6 +649,7 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
                                                             const int8_t *__restrict__ wn, int8_t *__restrict__ wn_scan,
                                                             int4 *__restrict__ draw, uint32_t *__restrict__ heads,
                                                             uint32_t *__restrict__ item_scene,
+                                                            uint32_t *__restrict__ item_tile_count,
                                                             FrameCounters *__restrict__ ctr,
                                                             uint64_t *__restrict__ st_wn, uint64_t *__restrict__ st_fl,
                                                             uint32_t spin_cap) {
@@ -760,7 +776,8 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
             const uint64_t k1 = k[j + 1];
             const uint32_t p = (uint32_t)(k1 >> 24);
             const int32_t fill = (int32_t)a.fill_rgba[p];
-            const int nrows = (dim_of(a, p).H + 1) / 2;
+            const Dim dp = dim_of(a, p);
+            const int nrows = (dp.H + 1) / 2;
             const uint32_t key1 = (uint32_t)key_from_local((uint32_t)(k1 & 0xFFFFFFu), nrows);
             if (item_scene != nullptr) {
                 const uint32_t sc = a.path_scene[p];
@@ -773,7 +790,9 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
             }
             if (ff) {
                 const int32_t pos = (int32_t)(((uint32_t)key_y(key1) << 16) | (uint32_t)key_x(key1));
-                draw[nfb + nsb] = make_int4(pos, 2, fill, (int)(nfb + 1));
+                const int4 it = make_int4(pos, 2, fill, (int)(nfb + 1));
+                draw[nfb + nsb] = it;
+                item_tile_count[nfb + nsb] = item_tiles(it, dp.W);
                 heads[nfb] = (uint32_t)(base + j);
             }
             if (sfl) {
@@ -783,7 +802,9 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
                 const int x1 = key_x(key1);
                 x0 = max(0, x0);
                 const int32_t pos = (int32_t)(((uint32_t)y0 << 16) | (uint32_t)x0);
-                draw[nfb + nsb + ff] = make_int4(pos, x1 - x0, fill, 0);
+                const int4 it = make_int4(pos, x1 - x0, fill, 0);
+                draw[nfb + nsb + ff] = it;
+                item_tile_count[nfb + nsb + ff] = item_tiles(it, dp.W);
             }
         }
         nfb += ff;
@@ -867,22 +888,6 @@ constexpr int kBinCells = kBinW / 2;  // cells per resolve bin: one lane each
 constexpr int kResolveWarps = 8;
 constexpr int kResolveMaxBlocksPerSM = 4;
 
-__device__ __forceinline__ void item_cols(const int4 &it, int W, int &x0, int &x1) {
-    const int x = (int)((uint32_t)it.x & 0xFFFFu);
-    x0 = max(x, 0);
-    x1 = min(x + it.y, W);
-}
-
-__global__ void k_item_tiles(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
-                             const FrameCounters *__restrict__ ctr, uint32_t *__restrict__ cnt) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (int64_t)ctr->n_items) return;
-    const int W = item_scene != nullptr ? a.scenes[item_scene[i]].W : a.W;
-    int x0, x1;
-    item_cols(draw[i], W, x0, x1);
-    cnt[i] = x1 > x0 ? (uint32_t)((x1 - 1) / kBinW - x0 / kBinW + 1) : 0u;
-}
-
 __global__ void k_emit_pairs(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
                              const FrameCounters *__restrict__ ctr, const uint32_t *__restrict__ offs,
                              uint32_t *__restrict__ pkey, uint32_t *__restrict__ pval) {
@@ -921,10 +926,10 @@ __global__ void k_bin_bounds(const uint32_t *__restrict__ key, const FrameCounte
 }
 
 // Shared-memory tables of the resolve.  The sRGB decode table is replicated
-// 8 times (entry k of lane l at k * 8 + l % 8) so that data-dependent lookups
-// of a warp rarely collide in a bank.
+// twice (entry k of lane l at k * 2 + l % 2), which measures as fast as more
+// replicas and leaves the room for 4 resolve blocks per SM.
 struct SmemTables {
-    float dec8r[256 * 8];
+    float dec8r[256 * 2];
     float th[256];
     uint8_t bin[4096];  // number of thresholds <= b / 4096
 };
@@ -954,7 +959,7 @@ __device__ __forceinline__ uint32_t enc_srgb(const SmemTables &t, float v) {
 
 template <bool SRGB>
 __device__ __forceinline__ float dec8(const SmemTables &t, uint32_t k, int lane) {
-    if constexpr (SRGB) return t.dec8r[k * 8 + (lane & 7)];
+    if constexpr (SRGB) return t.dec8r[k * 2 + (lane & 1)];
     else return lin8(k);
 }
 
@@ -1390,7 +1395,7 @@ __device__ __forceinline__ void resolve_persistent(const FrameArgs &a, const int
     {
         const ResolveTables *rt = a.rtables;
         if constexpr (SRGB)
-            for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) T.dec8r[i] = rt->srgb_dec[i >> 3];
+            for (int i = threadIdx.x; i < 256 * 2; i += blockDim.x) T.dec8r[i] = rt->srgb_dec[i >> 1];
         for (int i = threadIdx.x; i < 256; i += blockDim.x) T.th[i] = rt->threshold[i];
         if constexpr (SRGB)
             for (int i = threadIdx.x; i < 1024; i += blockDim.x)
@@ -1413,7 +1418,7 @@ __device__ __forceinline__ void resolve_persistent(const FrameArgs &a, const int
 }
 
 template <int S, bool MS, bool SRGB>
-__global__ void __launch_bounds__(kResolveWarps * 32, 3) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
+__global__ void __launch_bounds__(kResolveWarps * 32, 4) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
                                                                  const uint32_t *__restrict__ merged,
                                                                  const uint32_t *__restrict__ pval,
                                                                  const uint32_t *__restrict__ bstart,
@@ -1652,11 +1657,11 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
 int64_t scan_mark_status_words(int64_t cap_nf) { return 2 * std::max<int64_t>(1, (cap_nf + kMarkTile - 1) / kMarkTile); }
 
 int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, FrameCounters *counters,
-                     uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s) {
+                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *item_tile_count,
+                     FrameCounters *counters, uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s) {
     const int64_t words = scan_mark_status_words(cap_nf);
     k_scan_mark<<<(unsigned)(words / 2), kMarkThreads, 0, s>>>(a, skey, perm, wn, wn_scan, draw, heads, item_scene,
-                                                               counters, tile_status, tile_status + words / 2,
+                                                               item_tile_count, counters, tile_status, tile_status + words / 2,
                                                                spin_cap);
     return 1;
 }
@@ -1672,13 +1677,6 @@ int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr,
         k_stencil<16><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, pidw, mask, wn_scan, heads, merged);
     else
         k_stencil<32><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, pidw, mask, wn_scan, heads, merged);
-    return 1;
-}
-
-int launch_item_tiles(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
-                      const FrameCounters *ctr, uint32_t *cnt, cudaStream_t s) {
-    if (cap_items <= 0) return 0;
-    k_item_tiles<<<grid_for(cap_items), kThreads, 0, s>>>(a, draw, item_scene, ctr, cnt);
     return 1;
 }
 
