@@ -152,7 +152,7 @@ struct spr_handle {
     int tape_depth = 128;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
-        wn_scan, draw, heads, merged, tiles, pair_off, pkey[2], pval[2], bins, image, counters, dump_tmp, overflow;
+        wn_scan, draw, heads, merged, pval, bins, image, counters, dump_tmp, overflow;
     // look-back tile words of the frame's scans: entry offsets, scan-mark, pair offsets
     DevBuf lb_off, lb_mark, lb_pair;
     uint64_t *skey_sorted = nullptr;
@@ -212,8 +212,8 @@ std::vector<DevBuf *> handle_bufs(spr_handle *h) {
                       &h->fill,       &h->affine,  &h->tvert,    &h->pflags,    &h->pvis,    &h->counts,
                       &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
                       &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
-                      &h->wn_scan,    &h->draw,    &h->heads,    &h->lb_off,    &h->merged,  &h->tiles,
-                      &h->pair_off,   &h->pkey[0], &h->pkey[1],  &h->pval[0],   &h->pval[1], &h->bins,
+                      &h->wn_scan,    &h->draw,    &h->heads,    &h->lb_off,    &h->merged,  &h->pval,
+                      &h->bins,
                       &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
                       &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
                       &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
@@ -705,6 +705,11 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
     return cuda_status();
 }
 
+// Words of the bin arrays: offsets (n_bins + 1), counts, fill counters, each
+// padded to 16 bytes.
+int64_t bin_stride(int64_t nbins) { return (nbins + 1 + 3) & ~int64_t(3); }
+int64_t bin_words(int64_t nbins) { return 3 * bin_stride(nbins); }
+
 // Headroom of the capacities a sized frame sets, so that frames whose sizes
 // drift a little (an animation, a fitting loop) keep fitting.
 int64_t with_headroom(int64_t n) { return n + n / 8 + 256; }
@@ -804,7 +809,8 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         (st = ensure(h->pvis, h->P)) || (st = ensure(h->counts, 4 * (size_t)h->C + 16)) ||
         (st = ensure(h->offsets, 4 * ((size_t)h->C + 1) + 16)) ||
         (st = ensure(h->lb_off, 8 * (size_t)lookback_words(h->C))) || (st = ensure(h->image, 4 * (size_t)npix)) ||
-        (st = ensure(h->bins, 8 * (size_t)nbins)) ||
+        (st = ensure(h->bins, 4 * (size_t)bin_words(nbins))) ||
+        (st = ensure(h->lb_pair, 8 * (size_t)lookback_words(nbins))) ||
         (st = ensure(h->overflow, 4 * (size_t)std::max<int64_t>(resolve_overflow_words(a), 1))))
         return st;
     cudaMemsetAsync(h->counters.p, 0, sizeof(FrameCounters), s);
@@ -836,8 +842,7 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         (st = ensure(h->draw, 16 * (size_t)cap_items)) || (st = ensure(h->heads, 4 * (size_t)cap_nf)) ||
         (st = ensure(h->lb_mark, 8 * (size_t)scan_mark_status_words(cap_nf))) ||
         (st = ensure(h->merged, 4 * (size_t)WORDS * cap_nf)) ||
-        (st = ensure(h->tiles, 4 * (size_t)cap_items + 16)) || (st = ensure(h->pair_off, 4 * (size_t)cap_items + 16)) ||
-        (st = ensure(h->lb_pair, 8 * (size_t)lookback_words(cap_items))) ||
+
         (batch && (st = ensure(h->item_scene, 4 * (size_t)cap_items))))
         return st;
     uint32_t *item_scene = batch ? h->item_scene.as<uint32_t>() : nullptr;
@@ -899,10 +904,14 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         h->perm_sorted = alt ? h->sval[1].as<uint32_t>() : h->sval[0].as<uint32_t>();
     }
     rec(h, 4, s);
-    // stages 9-12, 14: winding scan, marks, draw list (one look-back pass)
+    // stages 9-12, 14: winding scan, marks, draw list (one look-back pass),
+    // with the pairs of each resolve bin counted
+    uint32_t *bin_off = h->bins.as<uint32_t>(), *bin_count = bin_off + bin_stride(nbins),
+             *bin_fill = bin_count + bin_stride(nbins);
+    cudaMemsetAsync(bin_count, 0, 8 * (size_t)bin_stride(nbins), s);
     cudaMemsetAsync(h->lb_mark.p, 0, 8 * (size_t)scan_mark_status_words(cap_nf), s);
     L += launch_scan_mark(a, cap_nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
-                          h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, h->tiles.as<uint32_t>(), ctr,
+                          h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, bin_count, ctr,
                           h->lb_mark.as<uint64_t>(),
                           h->lb_spin_cap, s);
     rec(h, 5, s);
@@ -910,11 +919,11 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     L += launch_stencil(a, cap_nf, ctr, h->skey_sorted, h->perm_sorted, h->pidw.as<uint32_t>(), h->mask.as<uint32_t>(),
                         h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), s);
     rec(h, 6, s);
-    // stage 15: bin draw items by (cell row, 64-column tile), resolve
-    cudaMemsetAsync(h->lb_pair.p, 0, 8 * (size_t)lookback_words(cap_items), s);
-    L += scan_lookback_u32(h->tiles.as<uint32_t>(), h->pair_off.as<uint32_t>(), &ctr->n_items, cap_items,
-                           h->lb_pair.as<uint64_t>(), &ctr->tiles[2], h->lb_spin_cap, &ctr->status, &ctr->need_pairs,
-                           s);
+    // stage 15: draw items binned by (cell row, 64-column tile): bin offsets
+    // from the counts, then the items placed and sorted per bin; resolve
+    cudaMemsetAsync(h->lb_pair.p, 0, 8 * (size_t)lookback_words(nbins), s);
+    L += scan_lookback_u32(bin_count, bin_off, nullptr, nbins, h->lb_pair.as<uint64_t>(), &ctr->tiles[2],
+                           h->lb_spin_cap, &ctr->status, &ctr->need_pairs, s);
     if (sized) {
         cudaMemcpyAsync(h->h_counters, h->counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s);
         ++h->host_syncs;
@@ -928,24 +937,14 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         h->cap_pairs = dc ? std::max<int64_t>(h->npairs, 1) : with_headroom(h->npairs);
     }
     const int64_t cap_pairs = h->cap_pairs;
-    if ((st = ensure(h->pkey[0], 4 * (size_t)cap_pairs)) || (st = ensure(h->pkey[1], 4 * (size_t)cap_pairs)) ||
-        (st = ensure(h->pval[0], 4 * (size_t)cap_pairs)) || (st = ensure(h->pval[1], 4 * (size_t)cap_pairs)) ||
-        (st = ensure(h->sort_tmp, 4 * (size_t)radix_tmp_words(std::max<int64_t>({cap_pairs, cap_nf, (int64_t)h->C})))))
-        return st;
+    if ((st = ensure(h->pval, 4 * (size_t)cap_pairs))) return st;
     L += launch_admit(&ctr->need_pairs, &ctr->n_pairs, (uint32_t)std::min<int64_t>(cap_pairs, INT32_MAX),
                       &ctr->status, s);
-    L += launch_emit_pairs(a, h->draw.as<int4>(), item_scene, cap_items, ctr, h->pair_off.as<uint32_t>(),
-                           h->pkey[0].as<uint32_t>(), h->pval[0].as<uint32_t>(), s);
-    const bool palt = radix_sort<uint32_t>(h->pkey[0].as<uint32_t>(), h->pval[0].as<uint32_t>(),
-                                           h->pkey[1].as<uint32_t>(), h->pval[1].as<uint32_t>(), cap_pairs,
-                                           std::max(bits_for((uint64_t)nbins - 1), 1), h->sort_tmp.as<uint32_t>(), s,
-                                           &rl, &ctr->n_pairs);
-    L += rl;
-    const uint32_t *pk = palt ? h->pkey[1].as<uint32_t>() : h->pkey[0].as<uint32_t>();
-    const uint32_t *pv = palt ? h->pval[1].as<uint32_t>() : h->pval[0].as<uint32_t>();
-    uint32_t *bin_start = h->bins.as<uint32_t>(), *bin_end = bin_start + nbins;
-    cudaMemsetAsync(h->bins.p, 0, 8 * (size_t)nbins, s);
-    L += launch_bin_bounds(pk, cap_pairs, ctr, bin_start, bin_end, s);
+    L += launch_bin_scatter(a, h->draw.as<int4>(), item_scene, cap_items, ctr, bin_off, bin_fill,
+                            h->pval.as<uint32_t>(), s);
+    L += launch_bin_sort(bin_off, nbins, h->pval.as<uint32_t>(), ctr, s);
+    const uint32_t *pv = h->pval.as<uint32_t>();
+    uint32_t *bin_start = bin_off, *bin_end = bin_off + 1;
     rec(h, 7, s);
     h->en.path = (int32_t)h->P;
     h->en.curve = (int32_t)h->C;
@@ -1000,8 +999,8 @@ int backward_of_held_frame(spr_handle *h, void *stream, const DiffCall &dc) {
     }
     int L = 0;
     h->host_syncs = 0;
-    uint32_t *bin_start = h->bins.as<uint32_t>();
-    const int st = diff_stage(h, a, dc, h->pv_sorted, bin_start, bin_start + a.n_bins, s, &L);
+    uint32_t *bin_start = h->bins.as<uint32_t>();  // (bin b's items end where bin b + 1's start)
+    const int st = diff_stage(h, a, dc, h->pv_sorted, bin_start, bin_start + 1, s, &L);
     h->launches = L;
     return st ? st : cuda_status();
 }

@@ -184,20 +184,22 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
 int64_t scan_mark_status_words(int64_t cap_nf);
 // Winding scan, merged-fragment / span marks, draw list and merged heads in
 // one pass (decoupled look-back); writes the item counts to the counters
-// and the resolve bins each item covers to item_tile_count.  item_scene
-// (batch frames only, else null) receives the scene of each draw item; in
-// batch frames the winding scan restarts at every scene.
+// and adds every item's pairs to bin_count (n_bins words, zero before).
+// item_scene (batch frames only, else null) receives the scene of each draw
+// item; in batch frames the winding scan restarts at every scene.
 int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *item_tile_count,
+                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *bin_count,
                      FrameCounters *counters, uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s);
 int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr, const uint64_t *skey,
                    const uint32_t *perm, const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan,
                    const uint32_t *heads, uint32_t *merged_mask, cudaStream_t s);
-int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
-                      const FrameCounters *ctr, const uint32_t *pair_offsets, uint32_t *pair_key, uint32_t *pair_val,
-                      cudaStream_t s);
-int launch_bin_bounds(const uint32_t *pair_key, int64_t cap_pairs, const FrameCounters *ctr, uint32_t *bin_start,
-                      uint32_t *bin_end, cudaStream_t s);
+// The draw items of every resolve bin in draw order: bin b's are
+// pval[bin_off[b] .. bin_off[b + 1]) (bin_off: the exclusive scan of the
+// bin counts; bin_fill: n_bins words, zero before).
+int launch_bin_scatter(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
+                       const FrameCounters *ctr, const uint32_t *bin_off, uint32_t *bin_fill, uint32_t *pval,
+                       cudaStream_t s);
+int launch_bin_sort(const uint32_t *bin_off, int64_t nbins, uint32_t *pval, const FrameCounters *ctr, cudaStream_t s);
 // The resolve is persistent: resolve_warps(a) warps take bins from
 // counters->bin_queue (zeroed by launch_resolve).  overflow: 64 * 32 words
 // per warp for pixels that need explicit samples (multisample modes with

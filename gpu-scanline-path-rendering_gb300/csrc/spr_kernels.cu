@@ -10,8 +10,9 @@
 //   k_mark_merged_fragment_and_span + scans +
 //   k_gen_gl_merged_fragment_and_span (cu:462-868)   -> k_flags_reduce / k_flags_down
 //   k_gen_stencil_cuda_sm + block boundary (cu:554)  -> k_stencil
-//   OpenGL draw + multisample resolve (cu:1312-1433) -> k_scan_lb, k_emit_pairs,
-//                                                       radix_sort, k_bin_bounds, k_resolve
+//   OpenGL draw + multisample resolve (cu:1312-1433) -> bin counts (k_scan_mark),
+//                                                       k_scan_lb, k_bin_scatter,
+//                                                       k_bin_sort, k_resolve
 // ("cu" = gpu-scanline/src/rasterizer/R_cut_A_mask_comb_scanline/ras_cut_mask_comb_scanline.cu)
 
 #include <cuda_runtime.h>
@@ -604,11 +605,25 @@ __device__ __forceinline__ void item_cols(const int4 &it, int W, int &x0, int &x
     x1 = min(x + it.y, W);
 }
 
-// Resolve bins (64-column tiles of its cell row) that draw item `it` covers.
-__device__ __forceinline__ uint32_t item_tiles(const int4 &it, int W) {
+// Resolve bins of draw item `it` (64-column tiles of its cell row) in a
+// viewport W x H whose bins are numbered from bin0: *first and the count.
+__device__ __forceinline__ int item_bins(const int4 &it, int W, int H, uint32_t bin0, uint32_t *first) {
     int x0, x1;
     item_cols(it, W, x0, x1);
-    return x1 > x0 ? (uint32_t)((x1 - 1) / kBinW - x0 / kBinW + 1) : 0u;
+    const int row = (it.x >> 16) / 2;
+    if (x1 <= x0 || row < 0 || row >= (H + 1) / 2) return 0;
+    const int ntx = (W + kBinW - 1) / kBinW;
+    *first = bin0 + (uint32_t)(row * ntx + x0 / kBinW);
+    return (x1 - 1) / kBinW - x0 / kBinW + 1;
+}
+
+// Counts item `it`'s pairs in its bins.
+__device__ __forceinline__ void count_bins(const FrameArgs &a, const int4 &it, const Dim &dp, uint32_t p,
+                                           uint32_t *__restrict__ bin_count) {
+    const uint32_t bin0 = a.scenes != nullptr ? a.scenes[a.path_scene[p]].bin_off : 0u;
+    uint32_t b0 = 0;
+    const int nb = item_bins(it, dp.W, dp.H, bin0, &b0);
+    for (int t = 0; t < nb; ++t) atomicAdd(bin_count + b0 + t, 1u);
 }
 
 // k_mark_merged_fragment_and_span (cu:462-535) on sorted position i with
@@ -649,7 +664,7 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
                                                             const int8_t *__restrict__ wn, int8_t *__restrict__ wn_scan,
                                                             int4 *__restrict__ draw, uint32_t *__restrict__ heads,
                                                             uint32_t *__restrict__ item_scene,
-                                                            uint32_t *__restrict__ item_tile_count,
+                                                            uint32_t *__restrict__ bin_count,
                                                             FrameCounters *__restrict__ ctr,
                                                             uint64_t *__restrict__ st_wn, uint64_t *__restrict__ st_fl,
                                                             uint32_t spin_cap) {
@@ -792,7 +807,7 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
                 const int32_t pos = (int32_t)(((uint32_t)key_y(key1) << 16) | (uint32_t)key_x(key1));
                 const int4 it = make_int4(pos, 2, fill, (int)(nfb + 1));
                 draw[nfb + nsb] = it;
-                item_tile_count[nfb + nsb] = item_tiles(it, dp.W);
+                count_bins(a, it, dp, p, bin_count);
                 heads[nfb] = (uint32_t)(base + j);
             }
             if (sfl) {
@@ -804,7 +819,7 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
                 const int32_t pos = (int32_t)(((uint32_t)y0 << 16) | (uint32_t)x0);
                 const int4 it = make_int4(pos, x1 - x0, fill, 0);
                 draw[nfb + nsb + ff] = it;
-                item_tile_count[nfb + nsb + ff] = item_tiles(it, dp.W);
+                count_bins(a, it, dp, p, bin_count);
             }
         }
         nfb += ff;
@@ -888,41 +903,96 @@ constexpr int kBinCells = kBinW / 2;  // cells per resolve bin: one lane each
 constexpr int kResolveWarps = 8;
 constexpr int kResolveMaxBlocksPerSM = 4;
 
-__global__ void k_emit_pairs(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
-                             const FrameCounters *__restrict__ ctr, const uint32_t *__restrict__ offs,
-                             uint32_t *__restrict__ pkey, uint32_t *__restrict__ pval) {
+// The draw items of every resolve bin, in draw order: each item's index is
+// placed in its bins' ranges (bin offsets from the scan of the counts that
+// k_scan_mark took) by warp-aggregated atomic slots, and every bin's range
+// is then sorted (item indices are the draw order).
+__global__ void k_bin_scatter(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
+                              const FrameCounters *__restrict__ ctr, const uint32_t *__restrict__ bin_off,
+                              uint32_t *__restrict__ bin_fill, uint32_t *__restrict__ pval) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    // (pairs not admitted: the pair buffers are too small; or a scan gave up)
-    if (i >= (int64_t)ctr->n_items || ctr->status != 0u || ctr->n_pairs != ctr->need_pairs) return;
-    const int4 it = draw[i];
-    int W = a.W;
-    uint32_t bin0 = 0;
-    if (item_scene != nullptr) {
-        const SceneInfo *sc = a.scenes + item_scene[i];
-        W = sc->W;
-        bin0 = sc->bin_off;
+    const int lane = threadIdx.x & 31;
+    // (pairs not admitted: the pair buffer is too small; or a scan gave up)
+    const bool ok = ctr->status == 0u && ctr->n_pairs == ctr->need_pairs;
+    int nb = 0;
+    uint32_t b0 = 0;
+    if (ok && i < (int64_t)ctr->n_items) {
+        const int4 it = draw[i];
+        int W = a.W, H = a.H;
+        uint32_t bin0 = 0;
+        if (item_scene != nullptr) {
+            const SceneInfo *sc = a.scenes + item_scene[i];
+            W = sc->W;
+            H = sc->H;
+            bin0 = sc->bin_off;
+        }
+        nb = item_bins(it, W, H, bin0, &b0);
     }
-    int x0, x1;
-    item_cols(it, W, x0, x1);
-    if (x1 <= x0) return;
-    const int ntx = (W + kBinW - 1) / kBinW;
-    const int row = (it.x >> 16) / 2;
-    uint32_t o = offs[i];
-    for (int t = x0 / kBinW; t <= (x1 - 1) / kBinW; ++t) {
-        pkey[o] = bin0 + (uint32_t)(row * ntx + t);
-        pval[o] = (uint32_t)i;
-        ++o;
+    const int most = __reduce_max_sync(0xffffffffu, nb);
+    for (int t = 0; t < most; ++t) {
+        const bool act = t < nb;
+        const uint32_t bin = act ? b0 + (uint32_t)t : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, bin);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (act && lane == leader) base = atomicAdd(bin_fill + bin, (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (act) pval[bin_off[bin] + base + __popc(peers & ((1u << lane) - 1u))] = (uint32_t)i;
     }
 }
 
-__global__ void k_bin_bounds(const uint32_t *__restrict__ key, const FrameCounters *__restrict__ ctr,
-                             uint32_t *__restrict__ start, uint32_t *__restrict__ end) {
-    const int64_t n = ctr->n_pairs;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t k = key[i];
-    if (i == 0 || key[i - 1] != k) start[k] = (uint32_t)i;
-    if (i == n - 1 || key[i + 1] != k) end[k] = (uint32_t)(i + 1);
+// One warp per bin: its item indices sorted ascending by a bitonic network
+// that compares in one direction only (stage k compares each element with
+// its mirror in the k-block, then the half-cleaners), so that the missing
+// elements past n behave as +infinity.  Bins of up to kBinSortSmem items are
+// sorted in shared memory, larger ones in place.
+constexpr int kBinSortWarps = 4;
+constexpr int kBinSortSmem = 1024;
+__global__ void __launch_bounds__(kBinSortWarps * 32) k_bin_sort(const uint32_t *__restrict__ bin_off, int64_t nbins,
+                                                                 uint32_t *__restrict__ pval,
+                                                                 const FrameCounters *__restrict__ ctr) {
+    __shared__ uint32_t sk[kBinSortWarps][kBinSortSmem];
+    if (ctr->status != 0u || ctr->n_pairs != ctr->need_pairs) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t b = (int64_t)blockIdx.x * kBinSortWarps + warp;
+    if (b >= nbins) return;
+    const uint32_t beg = bin_off[b], n = bin_off[b + 1] - beg;
+    if (n <= 1u) return;
+    const bool in_smem = n <= (uint32_t)kBinSortSmem;
+    uint32_t *k = in_smem ? sk[warp] : pval + beg;
+    if (in_smem) {
+        for (uint32_t i = lane; i < n; i += 32) k[i] = pval[beg + i];
+        __syncwarp();
+    }
+    int lp = 1;
+    while ((1u << lp) < n) ++lp;  // 2^lp >= n
+    const uint32_t half = 1u << (lp - 1);
+    for (int lk = 1; lk <= lp; ++lk) {
+        for (int lj = lk - 1; lj >= 0; --lj) {
+            const uint32_t j = 1u << lj;
+            for (uint32_t i = lane; i < half; i += 32) {
+                uint32_t x, y;
+                if (lj == lk - 1) {  // mirror within the 2j-block
+                    const uint32_t blk = (i >> lj) << lk, off = i & (j - 1u);
+                    x = blk + off;
+                    y = blk + (2u * j - 1u) - off;
+                } else {
+                    x = ((i >> lj) << (lj + 1)) + (i & (j - 1u));
+                    y = x + j;
+                }
+                if (y < n) {
+                    const uint32_t u = k[x], v = k[y];
+                    if (u > v) {
+                        k[x] = v;
+                        k[y] = u;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    if (in_smem)
+        for (uint32_t i = lane; i < n; i += 32) pval[beg + i] = k[i];
 }
 
 // Shared-memory tables of the resolve.  The sRGB decode table is replicated
@@ -1657,11 +1727,11 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
 int64_t scan_mark_status_words(int64_t cap_nf) { return 2 * std::max<int64_t>(1, (cap_nf + kMarkTile - 1) / kMarkTile); }
 
 int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *item_tile_count,
+                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *bin_count,
                      FrameCounters *counters, uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s) {
     const int64_t words = scan_mark_status_words(cap_nf);
     k_scan_mark<<<(unsigned)(words / 2), kMarkThreads, 0, s>>>(a, skey, perm, wn, wn_scan, draw, heads, item_scene,
-                                                               item_tile_count, counters, tile_status, tile_status + words / 2,
+                                                               bin_count, counters, tile_status, tile_status + words / 2,
                                                                spin_cap);
     return 1;
 }
@@ -1680,19 +1750,21 @@ int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr,
     return 1;
 }
 
-int launch_emit_pairs(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
-                      const FrameCounters *ctr, const uint32_t *offs, uint32_t *pkey, uint32_t *pval, cudaStream_t s) {
+int launch_bin_scatter(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
+                       const FrameCounters *ctr, const uint32_t *bin_off, uint32_t *bin_fill, uint32_t *pval,
+                       cudaStream_t s) {
     if (cap_items <= 0) return 0;
-    k_emit_pairs<<<grid_for(cap_items), kThreads, 0, s>>>(a, draw, item_scene, ctr, offs, pkey, pval);
+    k_bin_scatter<<<grid_for(cap_items), kThreads, 0, s>>>(a, draw, item_scene, ctr, bin_off, bin_fill, pval);
     return 1;
 }
 
-int launch_bin_bounds(const uint32_t *key, int64_t cap_pairs, const FrameCounters *ctr, uint32_t *start,
-                      uint32_t *end, cudaStream_t s) {
-    if (cap_pairs <= 0) return 0;
-    k_bin_bounds<<<grid_for(cap_pairs), kThreads, 0, s>>>(key, ctr, start, end);
+int launch_bin_sort(const uint32_t *bin_off, int64_t nbins, uint32_t *pval, const FrameCounters *ctr, cudaStream_t s) {
+    if (nbins <= 0) return 0;
+    k_bin_sort<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), kBinSortWarps * 32, 0, s>>>(bin_off, nbins,
+                                                                                                  pval, ctr);
     return 1;
 }
+
 
 int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
                     const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
