@@ -152,7 +152,7 @@ struct spr_handle {
     int tape_depth = 128;
     // frame buffers
     DevBuf tvert, pflags, pvis, counts, offsets, scan_tmp, entries, key, pidw, wn, mask, skey[2], sval[2], sort_tmp,
-        wn_scan, draw, heads, merged, pval, bins, image, counters, dump_tmp, overflow;
+        wn_scan, draw, heads, merged, pval, rec_a, rec_m, bins, image, counters, dump_tmp, overflow;
     // look-back tile words of the frame's scans: entry offsets, scan-mark, pair offsets
     DevBuf lb_off, lb_mark, lb_pair;
     uint64_t *skey_sorted = nullptr;
@@ -213,7 +213,7 @@ std::vector<DevBuf *> handle_bufs(spr_handle *h) {
                       &h->offsets,    &h->scan_tmp, &h->entries, &h->key,       &h->pidw,    &h->wn,
                       &h->mask,       &h->skey[0], &h->skey[1],  &h->sval[0],   &h->sval[1], &h->sort_tmp,
                       &h->wn_scan,    &h->draw,    &h->heads,    &h->lb_off,    &h->merged,  &h->pval,
-                      &h->bins,
+                      &h->rec_a,      &h->rec_m,   &h->bins,
                       &h->image,      &h->counters, &h->dump_tmp, &h->overflow, &h->scenes_d, &h->path_scene,
                       &h->item_scene, &h->chord,  &h->lmask,   &h->item_path, &h->tape,  &h->tape_rec,
                       &h->grad_tvert, &h->vmap, &h->bitems, &h->vmask, &h->chain, &h->ekey[0], &h->ekey[1], &h->eval[0],
@@ -938,11 +938,16 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     }
     const int64_t cap_pairs = h->cap_pairs;
     if ((st = ensure(h->pval, 4 * (size_t)cap_pairs))) return st;
+    // resolve records of plain frames (the adjoint reads the items and masks itself)
+    if (!dc && ((st = ensure(h->rec_a, 8 * (size_t)cap_pairs)) ||
+                (st = ensure(h->rec_m, 4 * (size_t)WORDS * cap_pairs))))
+        return st;
     L += launch_admit(&ctr->need_pairs, &ctr->n_pairs, (uint32_t)std::min<int64_t>(cap_pairs, INT32_MAX),
                       &ctr->status, s);
     L += launch_bin_scatter(a, h->draw.as<int4>(), item_scene, cap_items, ctr, bin_off, bin_fill,
                             h->pval.as<uint32_t>(), s);
-    L += launch_bin_sort(bin_off, nbins, h->pval.as<uint32_t>(), ctr, s);
+    L += launch_bin_sort(bin_off, nbins, h->pval.as<uint32_t>(), ctr, a.S, h->draw.as<int4>(), h->merged.as<uint32_t>(),
+                         dc ? nullptr : h->rec_a.as<uint2>(), dc ? nullptr : h->rec_m.as<uint32_t>(), s);
     const uint32_t *pv = h->pval.as<uint32_t>();
     uint32_t *bin_start = bin_off, *bin_end = bin_off + 1;
     rec(h, 7, s);
@@ -957,7 +962,7 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     if (dc) {
         if ((st = diff_stage(h, a, *dc, pv, bin_start, bin_end, s, &L))) return st;
     } else {
-        L += launch_resolve(a, h->draw.as<int4>(), h->merged.as<uint32_t>(), pv, bin_start, bin_end,
+        L += launch_resolve(a, h->rec_a.as<uint2>(), h->rec_m.as<uint32_t>(), bin_start, bin_end,
                             h->image.as<uint32_t>(), h->overflow.as<uint32_t>(), ctr, s);
     }
     rec(h, 8, s);

@@ -199,11 +199,16 @@ int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr,
 int launch_bin_scatter(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
                        const FrameCounters *ctr, const uint32_t *bin_off, uint32_t *bin_fill, uint32_t *pval,
                        cudaStream_t s);
-int launch_bin_sort(const uint32_t *bin_off, int64_t nbins, uint32_t *pval, const FrameCounters *ctr, cudaStream_t s);
+// Sorts every bin's item indices into draw order.  With rec_a set, also
+// writes the resolve records in that order: rec_a[p] = (colour, first
+// column | width << 16) and rec_m[p] the sample mask (S / 8 words; every
+// sample for a span).
+int launch_bin_sort(const uint32_t *bin_off, int64_t nbins, uint32_t *pval, const FrameCounters *ctr, int S,
+                    const int4 *draw, const uint32_t *merged, uint2 *rec_a, uint32_t *rec_m, cudaStream_t s);
 // The resolve is persistent: resolve_warps(a) warps take bins from
-// counters->bin_queue (zeroed by launch_resolve).  overflow: 64 * 32 words
-// per warp for pixels that need explicit samples (multisample modes with
-// more than 8 samples; unused otherwise).
+// counters->bin_queue (zeroed by launch_resolve).  overflow:
+// resolve_overflow_words(a) words, the cell entries past the ones each warp
+// keeps in shared memory (multisample modes; unused otherwise).
 int64_t resolve_warps(const FrameArgs &a);
 int64_t resolve_overflow_words(const FrameArgs &a);
 // RGBA8 image of a 256-sample frame from the sums its 8 passes accumulated.
@@ -213,9 +218,9 @@ struct OutputInverse {
 };
 int launch_output_view(const uint32_t *image, uint32_t *out, int W, int H, const OutputInverse &inv, cudaStream_t s);
 int launch_encode_sums(const FrameArgs &a, const long long *sums, uint32_t *image, int64_t npix, cudaStream_t s);
-int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged_mask, const uint32_t *pair_val,
-                   const uint32_t *bin_start, const uint32_t *bin_end, uint32_t *image, uint32_t *overflow,
-                   FrameCounters *counters, cudaStream_t s);
+int launch_resolve(const FrameArgs &a, const uint2 *rec_a, const uint32_t *rec_m, const uint32_t *bin_start,
+                   const uint32_t *bin_end, uint32_t *image, uint32_t *overflow, FrameCounters *counters,
+                   cudaStream_t s);
 int launch_fill(uint32_t *image, int64_t n, uint32_t value, cudaStream_t s);
 // Scene upload on the device: validation, curve orientation (vertices
 // reversed in place), curve descriptors, the stored -> input vertex map.

@@ -945,54 +945,89 @@ __global__ void k_bin_scatter(FrameArgs a, const int4 *__restrict__ draw, const 
 // that compares in one direction only (stage k compares each element with
 // its mirror in the k-block, then the half-cleaners), so that the missing
 // elements past n behave as +infinity.  Bins of up to kBinSortSmem items are
-// sorted in shared memory, larger ones in place.
+// sorted in shared memory, larger ones in place.  With rec_a set, the bin's
+// resolve records are written in the same order: the item's colour and
+// columns (first | width << 16) and its merged sample mask (every sample for
+// a span), so that the resolve reads each bin's items and masks as one
+// contiguous run instead of gathering them.
 constexpr int kBinSortWarps = 4;
 constexpr int kBinSortSmem = 1024;
-__global__ void __launch_bounds__(kBinSortWarps * 32) k_bin_sort(const uint32_t *__restrict__ bin_off, int64_t nbins,
-                                                                 uint32_t *__restrict__ pval,
-                                                                 const FrameCounters *__restrict__ ctr) {
+template <int MW>
+struct MaskVec;
+template <>
+struct MaskVec<1> {
+    using T = uint32_t;
+    static __device__ __forceinline__ T all() { return 0xFFFFFFFFu; }
+};
+template <>
+struct MaskVec<2> {
+    using T = uint2;
+    static __device__ __forceinline__ T all() { return make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu); }
+};
+template <>
+struct MaskVec<4> {
+    using T = uint4;
+    static __device__ __forceinline__ T all() { return make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu); }
+};
+
+template <int MW>
+__global__ void __launch_bounds__(kBinSortWarps * 32)
+    k_bin_sort(const uint32_t *__restrict__ bin_off, int64_t nbins, uint32_t *__restrict__ pval,
+               const FrameCounters *__restrict__ ctr, const int4 *__restrict__ draw,
+               const uint32_t *__restrict__ merged, uint2 *__restrict__ rec_a,
+               typename MaskVec<MW>::T *__restrict__ rec_m) {
+    using MV = typename MaskVec<MW>::T;
     __shared__ uint32_t sk[kBinSortWarps][kBinSortSmem];
     if (ctr->status != 0u || ctr->n_pairs != ctr->need_pairs) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t b = (int64_t)blockIdx.x * kBinSortWarps + warp;
     if (b >= nbins) return;
     const uint32_t beg = bin_off[b], n = bin_off[b + 1] - beg;
-    if (n <= 1u) return;
+    if (n == 0u) return;
     const bool in_smem = n <= (uint32_t)kBinSortSmem;
     uint32_t *k = in_smem ? sk[warp] : pval + beg;
-    if (in_smem) {
-        for (uint32_t i = lane; i < n; i += 32) k[i] = pval[beg + i];
-        __syncwarp();
-    }
-    int lp = 1;
-    while ((1u << lp) < n) ++lp;  // 2^lp >= n
-    const uint32_t half = 1u << (lp - 1);
-    for (int lk = 1; lk <= lp; ++lk) {
-        for (int lj = lk - 1; lj >= 0; --lj) {
-            const uint32_t j = 1u << lj;
-            for (uint32_t i = lane; i < half; i += 32) {
-                uint32_t x, y;
-                if (lj == lk - 1) {  // mirror within the 2j-block
-                    const uint32_t blk = (i >> lj) << lk, off = i & (j - 1u);
-                    x = blk + off;
-                    y = blk + (2u * j - 1u) - off;
-                } else {
-                    x = ((i >> lj) << (lj + 1)) + (i & (j - 1u));
-                    y = x + j;
-                }
-                if (y < n) {
-                    const uint32_t u = k[x], v = k[y];
-                    if (u > v) {
-                        k[x] = v;
-                        k[y] = u;
-                    }
-                }
-            }
+    if (n > 1u) {
+        if (in_smem) {
+            for (uint32_t i = lane; i < n; i += 32) k[i] = pval[beg + i];
             __syncwarp();
         }
+        int lp = 1;
+        while ((1u << lp) < n) ++lp;  // 2^lp >= n
+        const uint32_t half = 1u << (lp - 1);
+        for (int lk = 1; lk <= lp; ++lk) {
+            for (int lj = lk - 1; lj >= 0; --lj) {
+                const uint32_t j = 1u << lj;
+                for (uint32_t i = lane; i < half; i += 32) {
+                    uint32_t x, y;
+                    if (lj == lk - 1) {  // mirror within the 2j-block
+                        const uint32_t blk = (i >> lj) << lk, off = i & (j - 1u);
+                        x = blk + off;
+                        y = blk + (2u * j - 1u) - off;
+                    } else {
+                        x = ((i >> lj) << (lj + 1)) + (i & (j - 1u));
+                        y = x + j;
+                    }
+                    if (y < n) {
+                        const uint32_t u = k[x], v = k[y];
+                        if (u > v) {
+                            k[x] = v;
+                            k[y] = u;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (in_smem)
+            for (uint32_t i = lane; i < n; i += 32) pval[beg + i] = k[i];
     }
-    if (in_smem)
-        for (uint32_t i = lane; i < n; i += 32) pval[beg + i] = k[i];
+    if (rec_a == nullptr) return;
+    for (uint32_t i = lane; i < n; i += 32) {
+        const uint32_t idx = n > 1u ? k[i] : pval[beg];
+        const int4 it = draw[idx];
+        rec_a[beg + i] = make_uint2((uint32_t)it.z, ((uint32_t)it.x & 0xFFFFu) | ((uint32_t)it.y << 16));
+        rec_m[beg + i] = it.w != 0 ? reinterpret_cast<const MV *>(merged)[it.w - 1] : MaskVec<MW>::all();
+    }
 }
 
 // Shared-memory tables of the resolve.  The sRGB decode table is replicated
@@ -1113,16 +1148,13 @@ __device__ __forceinline__ float4 gradient_colour(const FrameArgs &a, const Smem
 // per-sample rule gives.
 constexpr int kCellCap = 8;
 
-// Draw items staged per window: kWin batches of 32.
-constexpr int kWin = 2;
+// Draw items per window: kWin batches of 32.
+constexpr int kWin = 8;
 
 template <int MW, int CAP>
 struct CellState {
     uint32_t ent[CAP][MW + 1][32];  // entry j of lane l's cell: mask words k < MW, colour at k = MW
-    uint32_t icol[kWin * 32];       // staged items: colour,
-    uint32_t imask[kWin * 32];      // merged mask index + 1 (0: a span),
-    uint32_t ixw[kWin * 32];        // first column | width << 16
-    uint32_t mine[kWin][32];        // per batch, the staged items covering lane l's cell
+    uint32_t mine[kWin][32];        // per batch, the window's items covering lane l's cell
 };
 
 // Entry j of lane `lane`'s cell: its first word; word k is at [k * 32].
@@ -1225,20 +1257,17 @@ __device__ __forceinline__ void cell_apply(CellState<S / 8, CAP> &w, uint32_t *g
     if (changed && n > 1) cell_dedup<MW, CAP>(w, gx, lane, n);
 }
 
-// Merged sample mask m (MW words) of fragment record `idx` (merged index + 1).
+// Sample mask m (MW words) of resolve record p.
 template <int MW>
-__device__ __forceinline__ void load_mask(const uint32_t *__restrict__ merged, uint32_t idx, uint32_t (&m)[MW]) {
-    if (idx == 0u) {
-#pragma unroll
-        for (int k = 0; k < MW; ++k) m[k] = 0xFFFFFFFFu;  // a span: every sample
-    } else if constexpr (MW == 4) {
-        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(merged) + (idx - 1));
+__device__ __forceinline__ void load_mask(const uint32_t *__restrict__ rec_m, uint32_t p, uint32_t (&m)[MW]) {
+    if constexpr (MW == 4) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(rec_m) + p);
         m[0] = v.x, m[1] = v.y, m[2] = v.z, m[3] = v.w;
     } else if constexpr (MW == 2) {
-        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(merged) + (idx - 1));
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(rec_m) + p);
         m[0] = v.x, m[1] = v.y;
     } else {
-        m[0] = __ldg(merged + (idx - 1));
+        m[0] = __ldg(rec_m + p);
     }
 }
 
@@ -1262,17 +1291,17 @@ __device__ __forceinline__ uint32_t encode_mean(const SmemTables &T, const Pixel
     return enc8<SRGB>(T, ar) | (enc8<SRGB>(T, ag) << 8) | (enc8<SRGB>(T, ab) << 16) | (enc_lin(aa) << 24);
 }
 
-// One warp per bin.  Items (merged fragments and spans, in draw-list order)
-// are staged kWin x 32 at a time; a 32 x 32 ballot transpose of each batch's
-// cell sets gives every lane the staged items covering its cell, which it
-// applies in order, independently of the other lanes until the window ends
-// (a lane's work is the items over its own cell, not the most any lane has
-// in each batch).  The merged mask of the lane's next item is loaded while
-// it applies the current one.  Then every pixel is averaged over its
-// samples.
+// One warp per bin.  The bin's resolve records (merged fragments and spans
+// in draw-list order: colour, columns, sample mask) are taken kWin x 32 at a
+// time; a 32 x 32 ballot transpose of each batch's cell sets gives every
+// lane the window's items covering its cell, which it applies in order,
+// independently of the other lanes until the window ends (a lane's work is
+// the items over its own cell, not the most any lane has in each batch).
+// The record of the lane's next item is loaded while it applies the current
+// one.  Then every pixel is averaged over its samples.
 template <int S, bool MS, bool SRGB, int CAP, bool GRAD>
-__device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__restrict__ draw,
-                                            const uint32_t *__restrict__ merged, const uint32_t *__restrict__ pval,
+__device__ __forceinline__ void resolve_bin(const FrameArgs &a, const uint2 *__restrict__ rec_a,
+                                            const uint32_t *__restrict__ rec_m,
                                             const uint32_t *__restrict__ bstart, const uint32_t *__restrict__ bend,
                                             uint32_t *__restrict__ image, uint32_t *__restrict__ gx,
                                             const SmemTables &T, CellState<S / 8, CAP> &w, const int lane,
@@ -1315,19 +1344,12 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
         const int nb = (int)min((uint32_t)kWin, (fin - base + 31) / 32);  // batches in this window
         for (int c = 0; c < nb; ++c) {
             const uint32_t p = base + c * 32 + lane;
-            uint32_t cm = 0u;  // cells of this lane's staged item
+            uint32_t cm = 0u;  // cells of this lane's item (a fragment: one cell of 2 columns)
             if (p < fin) {
-                const int4 it = draw[pval[p]];
-                const int x = (int)((uint32_t)it.x & 0xFFFFu);
-                w.icol[c * 32 + lane] = (uint32_t)it.z;
-                w.imask[c * 32 + lane] = (uint32_t)it.w;
-                w.ixw[c * 32 + lane] = ((uint32_t)it.x & 0xFFFFu) | ((uint32_t)it.y << 16);
-                if (it.w != 0) {
-                    cm = x < W ? cell_bits((x - tx0) >> 1, ((x - tx0) >> 1) + 1) : 0u;
-                } else {
-                    const int xa = max(x, 0), xb = min(x + it.y, W);
-                    cm = xb > xa ? cell_bits((xa - tx0) >> 1, (xb - tx0 + 1) >> 1) : 0u;
-                }
+                const uint32_t xw = __ldg(&rec_a[p].y);
+                const int x = (int)(xw & 0xFFFFu);
+                const int xb = min(x + (int)(xw >> 16), W);
+                cm = xb > x ? cell_bits((x - tx0) >> 1, (xb - tx0 + 1) >> 1) : 0u;
             }
             // bit q of lane L's word: staged item q covers cell L (a transpose
             // of the 32 x 32 bit matrix of cell sets)
@@ -1352,12 +1374,20 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
         };
         int q = next_item();
         uint32_t m[MW];
-        if (q >= 0) load_mask<MW>(merged, w.imask[q], m);
+        uint2 r = make_uint2(0u, 0u);
+        if (q >= 0) {
+            r = __ldg(rec_a + base + q);
+            load_mask<MW>(rec_m, base + q, m);
+        }
         while (q >= 0) {
             const int qn = next_item();
             uint32_t mn[MW];
-            if (qn >= 0) load_mask<MW>(merged, w.imask[qn], mn);
-            const uint32_t c = w.icol[q];
+            uint2 rn = make_uint2(0u, 0u);
+            if (qn >= 0) {
+                rn = __ldg(rec_a + base + qn);
+                load_mask<MW>(rec_m, base + qn, mn);
+            }
+            const uint32_t c = r.x;
             if (!GRAD || c - 1u >= a.n_grad) {  // a solid colour (else a gradient paint)
                 const float sr = dec8<SRGB>(T, c & 0xFF, lane), sg = dec8<SRGB>(T, (c >> 8) & 0xFF, lane),
                             sb = dec8<SRGB>(T, (c >> 16) & 0xFF, lane), sa = lin8(c >> 24);
@@ -1377,7 +1407,7 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
                 }
             } else if constexpr (GRAD) {
                 // a colour per pixel: one application per pixel
-                const uint32_t xw = w.ixw[q];
+                const uint32_t xw = r.y;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const int X = X0 + (k >> 1), Y = y0 + (k & 1);
@@ -1400,6 +1430,7 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
                 }
             }
             q = qn;
+            r = rn;
 #pragma unroll
             for (int k = 0; k < MW; ++k) m[k] = mn[k];
         }
@@ -1453,9 +1484,8 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const int4 *__re
 // Persistent resolve: each warp takes bins from the frame's bin queue until
 // it is empty; a warp's overflow entry area is reused from bin to bin.
 template <int S, bool MS, bool SRGB, bool GRAD>
-__device__ __forceinline__ void resolve_persistent(const FrameArgs &a, const int4 *__restrict__ draw,
-                                                   const uint32_t *__restrict__ merged,
-                                                   const uint32_t *__restrict__ pval,
+__device__ __forceinline__ void resolve_persistent(const FrameArgs &a, const uint2 *__restrict__ rec_a,
+                                                   const uint32_t *__restrict__ rec_m,
                                                    const uint32_t *__restrict__ bstart,
                                                    const uint32_t *__restrict__ bend, uint32_t *__restrict__ image,
                                                    uint32_t *__restrict__ overflow, uint32_t *__restrict__ bin_queue) {
@@ -1482,32 +1512,31 @@ __device__ __forceinline__ void resolve_persistent(const FrameArgs &a, const int
         if (lane == 0) b = atomicAdd(bin_queue, 1u);
         b = __shfl_sync(0xffffffffu, b, 0);
         if ((int64_t)b >= a.n_bins) break;
-        resolve_bin<S, MS, SRGB, CAP, GRAD>(a, draw, merged, pval, bstart, bend, image, gx, T, w, lane, b);
+        resolve_bin<S, MS, SRGB, CAP, GRAD>(a, rec_a, rec_m, bstart, bend, image, gx, T, w, lane, b);
         __syncwarp();
     }
 }
 
 template <int S, bool MS, bool SRGB>
-__global__ void __launch_bounds__(kResolveWarps * 32, 4) k_resolve(FrameArgs a, const int4 *__restrict__ draw,
-                                                                 const uint32_t *__restrict__ merged,
-                                                                 const uint32_t *__restrict__ pval,
+__global__ void __launch_bounds__(kResolveWarps * 32, 4) k_resolve(FrameArgs a, const uint2 *__restrict__ rec_a,
+                                                                 const uint32_t *__restrict__ rec_m,
                                                                  const uint32_t *__restrict__ bstart,
                                                                  const uint32_t *__restrict__ bend,
                                                                  uint32_t *__restrict__ image,
                                                                  uint32_t *__restrict__ overflow,
                                                                  uint32_t *__restrict__ bin_queue) {
-    resolve_persistent<S, MS, SRGB, false>(a, draw, merged, pval, bstart, bend, image, overflow, bin_queue);
+    resolve_persistent<S, MS, SRGB, false>(a, rec_a, rec_m, bstart, bend, image, overflow, bin_queue);
 }
 
 // With gradient paints: registers capped so that two blocks stay resident
 // (the per-pixel paint would otherwise take more).
 template <int S, bool MS, bool SRGB>
 __global__ void __launch_bounds__(kResolveWarps * 32, 2)
-    k_resolve_grad(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ merged,
-                   const uint32_t *__restrict__ pval, const uint32_t *__restrict__ bstart,
+    k_resolve_grad(FrameArgs a, const uint2 *__restrict__ rec_a, const uint32_t *__restrict__ rec_m,
+                   const uint32_t *__restrict__ bstart,
                    const uint32_t *__restrict__ bend, uint32_t *__restrict__ image, uint32_t *__restrict__ overflow,
                    uint32_t *__restrict__ bin_queue) {
-    resolve_persistent<S, MS, SRGB, true>(a, draw, merged, pval, bstart, bend, image, overflow, bin_queue);
+    resolve_persistent<S, MS, SRGB, true>(a, rec_a, rec_m, bstart, bend, image, overflow, bin_queue);
 }
 
 // The image of a 256-sample frame from its passes' fixed-point sample sums
@@ -1634,7 +1663,7 @@ int sm_count() {
 // Shared memory of a resolve block: the tables and one cell state per warp.
 size_t resolve_smem(int S, bool ms) {
     const int MW = S / 8, CAP = ms ? kCellCap : 1;
-    return sizeof(SmemTables) + (size_t)kResolveWarps * ((size_t)CAP * (MW + 1) * 32 * 4 + 32 * 16 + (size_t)MW * 32 * 4);
+    return sizeof(SmemTables) + (size_t)kResolveWarps * ((size_t)CAP * (MW + 1) * 32 * 4 + (size_t)kWin * 32 * 4);
 }
 
 // Resolve blocks per SM: as many as fit in shared memory (at most 4), or
@@ -1650,8 +1679,7 @@ int64_t resolve_blocks(const FrameArgs &a) {
 }
 
 template <int S, bool MS, bool SRGB, bool GRAD>
-void resolve_variant_g(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
-                     const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
+void resolve_variant_g(const FrameArgs &a, const uint2 *rec_a, const uint32_t *rec_m, const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
                      uint32_t *queue, cudaStream_t s) {
     constexpr int CAP = MS ? kCellCap : 1;
     const size_t smem = sizeof(SmemTables) + (size_t)kResolveWarps * sizeof(CellState<S / 8, CAP>);
@@ -1664,20 +1692,18 @@ void resolve_variant_g(const FrameArgs &a, const int4 *draw, const uint32_t *mer
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, kResolveWarps * 32, smem) != cudaSuccess || fit < 1)
         fit = 1;
     const int64_t blocks = std::min<int64_t>(resolve_blocks(a), (int64_t)sm_count() * fit);
-    kern<<<(unsigned)blocks, kResolveWarps * 32, smem, s>>>(a, draw, merged, pval, bstart, bend, image, overflow,
-                                                             queue);
+    kern<<<(unsigned)blocks, kResolveWarps * 32, smem, s>>>(a, rec_a, rec_m, bstart, bend, image, overflow, queue);
 }
 
 // Gradient paints get their own instantiations: the per-pixel paint costs
 // registers that plain frames should not pay for.
 template <int S, bool MS, bool SRGB>
-void resolve_variant(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
-                     const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
+void resolve_variant(const FrameArgs &a, const uint2 *rec_a, const uint32_t *rec_m, const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
                      uint32_t *queue, cudaStream_t s) {
     if (a.grad_table != nullptr)
-        resolve_variant_g<S, MS, SRGB, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        resolve_variant_g<S, MS, SRGB, true>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
     else
-        resolve_variant_g<S, MS, SRGB, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        resolve_variant_g<S, MS, SRGB, false>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
 }
 
 }  // namespace
@@ -1758,36 +1784,43 @@ int launch_bin_scatter(const FrameArgs &a, const int4 *draw, const uint32_t *ite
     return 1;
 }
 
-int launch_bin_sort(const uint32_t *bin_off, int64_t nbins, uint32_t *pval, const FrameCounters *ctr, cudaStream_t s) {
+int launch_bin_sort(const uint32_t *bin_off, int64_t nbins, uint32_t *pval, const FrameCounters *ctr, int S,
+                    const int4 *draw, const uint32_t *merged, uint2 *rec_a, uint32_t *rec_m, cudaStream_t s) {
     if (nbins <= 0) return 0;
-    k_bin_sort<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), kBinSortWarps * 32, 0, s>>>(bin_off, nbins,
-                                                                                                  pval, ctr);
+    const unsigned g = (unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps);
+    if (S == 8)
+        k_bin_sort<1><<<g, kBinSortWarps * 32, 0, s>>>(bin_off, nbins, pval, ctr, draw, merged, rec_a, rec_m);
+    else if (S == 16)
+        k_bin_sort<2><<<g, kBinSortWarps * 32, 0, s>>>(bin_off, nbins, pval, ctr, draw, merged, rec_a,
+                                                        reinterpret_cast<uint2 *>(rec_m));
+    else
+        k_bin_sort<4><<<g, kBinSortWarps * 32, 0, s>>>(bin_off, nbins, pval, ctr, draw, merged, rec_a,
+                                                        reinterpret_cast<uint4 *>(rec_m));
     return 1;
 }
 
 
-int launch_resolve(const FrameArgs &a, const int4 *draw, const uint32_t *merged, const uint32_t *pval,
-                    const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
+int launch_resolve(const FrameArgs &a, const uint2 *rec_a, const uint32_t *rec_m, const uint32_t *bstart, const uint32_t *bend, uint32_t *image, uint32_t *overflow,
                     FrameCounters *counters, cudaStream_t s) {
     if (a.n_bins <= 0) return 0;
     uint32_t *queue = &counters->bin_queue;
     cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
     const bool ms = a.ms_output != 0, srgb = a.srgb != 0;
     if (a.S == 8) {
-        if (ms && srgb) resolve_variant<8, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else if (ms) resolve_variant<8, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else if (srgb) resolve_variant<8, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else resolve_variant<8, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        if (ms && srgb) resolve_variant<8, true, true>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else if (ms) resolve_variant<8, true, false>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else if (srgb) resolve_variant<8, false, true>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else resolve_variant<8, false, false>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
     } else if (a.S == 16) {
-        if (ms && srgb) resolve_variant<16, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else if (ms) resolve_variant<16, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else if (srgb) resolve_variant<16, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else resolve_variant<16, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        if (ms && srgb) resolve_variant<16, true, true>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else if (ms) resolve_variant<16, true, false>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else if (srgb) resolve_variant<16, false, true>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else resolve_variant<16, false, false>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
     } else {
-        if (ms && srgb) resolve_variant<32, true, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else if (ms) resolve_variant<32, true, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else if (srgb) resolve_variant<32, false, true>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
-        else resolve_variant<32, false, false>(a, draw, merged, pval, bstart, bend, image, overflow, queue, s);
+        if (ms && srgb) resolve_variant<32, true, true>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else if (ms) resolve_variant<32, true, false>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else if (srgb) resolve_variant<32, false, true>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
+        else resolve_variant<32, false, false>(a, rec_a, rec_m, bstart, bend, image, overflow, queue, s);
     }
     return 1;
 }
