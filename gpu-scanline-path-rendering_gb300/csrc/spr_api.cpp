@@ -836,13 +836,15 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     // stages 6-7: entries, fragments, boundary masks
     if ((st = ensure(h->entries, 8 * (size_t)cap_nf)) || (st = ensure(h->key, 4 * (size_t)cap_nf)) ||
         (st = ensure(h->pidw, 4 * (size_t)cap_nf)) || (st = ensure(h->wn, (size_t)cap_nf)) ||
-        (st = ensure(h->mask, 4 * (size_t)WORDS * cap_nf)) || (st = ensure(h->skey[0], 8 * (size_t)cap_nf + 64)) ||
-        (st = ensure(h->skey[1], 8 * (size_t)cap_nf + 64)) || (st = ensure(h->sval[0], 4 * (size_t)cap_nf + 64)) ||
-        (st = ensure(h->sval[1], 4 * (size_t)cap_nf + 64)) || (st = ensure(h->wn_scan, (size_t)cap_nf)) ||
+        (st = ensure(h->mask, 4 * (size_t)WORDS * cap_nf)) ||
+        // (16 entries past cap_nf of the sorted keys and positions: the
+        // merged-mask pass copies whole 16-entry blocks)
+        (st = ensure(h->skey[0], 8 * (size_t)cap_nf + 128)) || (st = ensure(h->skey[1], 8 * (size_t)cap_nf + 128)) ||
+        (st = ensure(h->sval[0], 4 * (size_t)cap_nf + 64)) || (st = ensure(h->sval[1], 4 * (size_t)cap_nf + 64)) ||
+        (st = ensure(h->wn_scan, (size_t)cap_nf)) ||
         (st = ensure(h->draw, 16 * (size_t)cap_items)) || (st = ensure(h->heads, 4 * (size_t)cap_nf)) ||
         (st = ensure(h->lb_mark, 8 * (size_t)scan_mark_status_words(cap_nf))) ||
         (st = ensure(h->merged, 4 * (size_t)WORDS * cap_nf)) ||
-
         (batch && (st = ensure(h->item_scene, 4 * (size_t)cap_items))))
         return st;
     uint32_t *item_scene = batch ? h->item_scene.as<uint32_t>() : nullptr;
@@ -910,14 +912,15 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
              *bin_fill = bin_count + bin_stride(nbins);
     cudaMemsetAsync(bin_count, 0, 8 * (size_t)bin_stride(nbins), s);
     cudaMemsetAsync(h->lb_mark.p, 0, 8 * (size_t)scan_mark_status_words(cap_nf), s);
-    L += launch_scan_mark(a, cap_nf, h->skey_sorted, h->perm_sorted, h->wn.as<int8_t>(), h->wn_scan.as<int8_t>(),
+    L += launch_scan_mark(a, cap_nf, h->skey_sorted, h->wn_scan.as<int8_t>(),
                           h->draw.as<int4>(), h->heads.as<uint32_t>(), item_scene, bin_count, ctr,
                           h->lb_mark.as<uint64_t>(),
                           h->lb_spin_cap, s);
     rec(h, 5, s);
     // stage 13: merged sample masks
-    L += launch_stencil(a, cap_nf, ctr, h->skey_sorted, h->perm_sorted, h->pidw.as<uint32_t>(), h->mask.as<uint32_t>(),
-                        h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), s);
+    L += launch_stencil(a, cap_nf, ctr, h->skey_sorted, h->perm_sorted, h->mask.as<uint32_t>(),
+                        h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), h->lb_spin_cap,
+                        s);
     rec(h, 6, s);
     // stage 15: draw items binned by (cell row, 64-column tile): bin offsets
     // from the counts, then the items placed and sorted per bin; resolve

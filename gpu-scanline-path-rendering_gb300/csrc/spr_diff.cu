@@ -254,11 +254,11 @@ __device__ void group_adjoint(const FrameArgs &a, const DiffArgs &d, int64_t h, 
     const int k4 = lane >> 3, sub = lane & 7, px = k4 >> 1, py = k4 & 1;
     const int w0 = (int)d.wn_scan[h];
     // group size: the run of equal keys from h, 32 keys per step
-    const uint64_t kh = d.skey[h];
+    const uint64_t kh = d.skey[h] & kKeyMask;
     int gs = 0;
     for (;;) {
         const int64_t j = h + gs + lane;
-        const uint32_t ends = __ballot_sync(0xffffffffu, j >= d.nf || d.skey[j] != kh);
+        const uint32_t ends = __ballot_sync(0xffffffffu, j >= d.nf || (d.skey[j] & kKeyMask) != kh);
         if (ends) {
             gs += __ffs(ends) - 1;
             break;

@@ -111,6 +111,17 @@ int64_t radix_tiles(int64_t n);
 // Reads keys (values are the positions), writes keys_out / vals_out; keys and
 // vals serve as scratch for long segments.  path_start: P + 1 words.
 // Nothing is sorted when the frame's entries were not admitted (ctr->nf 0).
+// Sort key of a fragment: path << 24 | cell key within the path (24 bits),
+// with the fragment's scan winding swn and change sign chg (each -1, 0 or
+// 1) carried in bits 60-63 (pack_fw), above every bit the sorts order by.
+// Readers that compare keys mask them with kKeyMask.
+constexpr int kFwShift = 60;
+constexpr uint64_t kKeyMask = (1ull << kFwShift) - 1ull;
+__host__ __device__ __forceinline__ uint32_t pack_fw(int swn, int chg) {
+    return (uint32_t)((swn & 3) | ((chg & 3) << 2));
+}
+__host__ __device__ __forceinline__ int fw_swn(uint32_t b) { return (int)(b << 30) >> 30; }
+__host__ __device__ __forceinline__ int fw_chg(uint32_t b) { return (int)(b << 28) >> 30; }
 int launch_segment_sort(const CurveDesc *curves, uint32_t C, uint32_t P, const uint32_t *offsets, uint64_t *keys,
                         uint32_t *vals, uint64_t *keys_out, uint32_t *vals_out, uint32_t *path_start,
                         const FrameCounters *ctr, cudaStream_t s);
@@ -187,12 +198,14 @@ int64_t scan_mark_status_words(int64_t cap_nf);
 // and adds every item's pairs to bin_count (n_bins words, zero before).
 // item_scene (batch frames only, else null) receives the scene of each draw
 // item; in batch frames the winding scan restarts at every scene.
-int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *bin_count,
-                     FrameCounters *counters, uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s);
-int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr, const uint64_t *skey,
-                   const uint32_t *perm, const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan,
-                   const uint32_t *heads, uint32_t *merged_mask, cudaStream_t s);
+int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, int8_t *wn_scan, int4 *draw,
+                     uint32_t *heads, uint32_t *item_scene, uint32_t *bin_count, FrameCounters *counters,
+                     uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s);
+// Merged masks from the sorted keys and fragment indices (perm), which hold
+// at least 16 entries past cap_nf, and the fragments' masks.
+int launch_stencil(const FrameArgs &a, int64_t cap_nf, FrameCounters *ctr, const uint64_t *skey, const uint32_t *perm,
+                   const uint32_t *mask, const int8_t *wn_scan, const uint32_t *heads, uint32_t *merged_mask,
+                   uint32_t spin_cap, cudaStream_t s);
 // The draw items of every resolve bin in draw order: bin b's are
 // pval[bin_off[b] .. bin_off[b + 1]) (bin_off: the exclusive scan of the
 // bin counts; bin_fill: n_bins words, zero before).

@@ -517,7 +517,8 @@ __global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2
         reinterpret_cast<uint4 *>(mask_out)[i] = make_uint4(mask[0], mask[1], mask[2], mask[3]);
     }
     const int nrows = (dm.H + 1) / 2;
-    sort_key[i] = ((uint64_t)pathid << 24) | (uint64_t)local_sort_key(yx, nrows);
+    sort_key[i] = ((uint64_t)pathid << 24) | (uint64_t)local_sort_key(yx, nrows) |
+                  ((uint64_t)pack_fw(swn, wnchg) << kFwShift);
     sort_val[i] = (uint32_t)i;
 }
 
@@ -657,11 +658,10 @@ __device__ __forceinline__ Mark mark_of(int64_t i, uint64_t k0, uint64_t k1, int
 // decoupled look-back (restarting at every scene of a batch, so that each
 // scene sees the scan a single-scene render gives it); then the merged and
 // span marks, scanned with a second look-back, and the draw items written.
-// The last tile writes the item counts.  Sorted keys and positions are read
-// 128 bits at a time.
+// The last tile writes the item counts.  Sorted keys are read 128 bits at a
+// time; each carries its fragment's scan winding in bits 60-63.
 __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const uint64_t *__restrict__ skey,
-                                                            const uint32_t *__restrict__ perm,
-                                                            const int8_t *__restrict__ wn, int8_t *__restrict__ wn_scan,
+                                                            int8_t *__restrict__ wn_scan,
                                                             int4 *__restrict__ draw, uint32_t *__restrict__ heads,
                                                             uint32_t *__restrict__ item_scene,
                                                             uint32_t *__restrict__ bin_count,
@@ -684,7 +684,6 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
     const int64_t left = nf - base;
     const int cnt = left <= 0 ? 0 : (left >= kMarkItems ? kMarkItems : (int)left);
     uint64_t k[kMarkItems + 1];  // sorted keys at base - 1 .. base + 7
-    uint32_t pm[kMarkItems];
     if (cnt == kMarkItems) {
         const uint4 *kp = reinterpret_cast<const uint4 *>(skey + base);
 #pragma unroll
@@ -693,17 +692,16 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
             k[1 + 2 * q] = (uint64_t)v.x | ((uint64_t)v.y << 32);
             k[2 + 2 * q] = (uint64_t)v.z | ((uint64_t)v.w << 32);
         }
-        const uint4 p0 = reinterpret_cast<const uint4 *>(perm + base)[0];
-        const uint4 p1 = reinterpret_cast<const uint4 *>(perm + base)[1];
-        pm[0] = p0.x, pm[1] = p0.y, pm[2] = p0.z, pm[3] = p0.w, pm[4] = p1.x, pm[5] = p1.y, pm[6] = p1.z, pm[7] = p1.w;
     } else {
 #pragma unroll
-        for (int j = 0; j < kMarkItems; ++j) {
-            k[1 + j] = j < cnt ? skey[base + j] : 0ull;
-            pm[j] = j < cnt ? perm[base + j] : 0u;
-        }
+        for (int j = 0; j < kMarkItems; ++j) k[1 + j] = j < cnt ? skey[base + j] : 0ull;
     }
     k[0] = (cnt > 0 && base > 0) ? skey[base - 1] : 0ull;
+    uint32_t fb[kMarkItems];  // the windings, and the keys without them
+#pragma unroll
+    for (int j = 0; j < kMarkItems; ++j) fb[j] = (uint32_t)(k[1 + j] >> kFwShift);
+#pragma unroll
+    for (int j = 0; j <= kMarkItems; ++j) k[j] &= kKeyMask;
     // windings in sorted order, and the scene starts of a batch
     const bool batch = a.scenes != nullptr && a.n_scenes > 1;
     int32_t v[kMarkItems];
@@ -711,7 +709,7 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
     SegSum agg{0u, 0u};
 #pragma unroll
     for (int j = 0; j < kMarkItems; ++j) {
-        v[j] = j < cnt ? (int32_t)wn[pm[j]] : 0;
+        v[j] = j < cnt ? fw_swn(fb[j]) : 0;
         if (batch && j < cnt &&
             (base + j == 0 || a.path_scene[(uint32_t)(k[j + 1] >> 24)] != a.path_scene[(uint32_t)(k[j] >> 24)]))
             seg |= 1u << j;
@@ -832,41 +830,114 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
 // masks of every fragment of the (path, cell) group, in 8-bit lanes per
 // mask bit (the reference's packed counters), reduced to the 7-bit winding
 // number and tested against the fill rule.
+//
+// A block takes 256 consecutive merged fragments, whose groups are one
+// contiguous run of sorted positions [heads[g0], heads[g0 + 256]).  The run
+// (up to kStencilStage positions, from a 16-entry boundary) is staged into
+// shared memory by bulk copies (cp.async.bulk, completion on an mbarrier)
+// of the sorted keys (with the change signs in bits 60-63) and fragment
+// indices; positions past the staged run are read from global memory.  The
+// sample masks are read through the fragment indices.
+constexpr int kStencilStage = 1024;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// Waits for phase 0 of mbarrier `bar`, at most `cap` polls; false if it
+// did not complete.
+__device__ __forceinline__ bool mbar_wait0(uint32_t bar, uint32_t cap) {
+    for (uint32_t it = 0; it < cap; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, "
+            "p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(0u)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+struct StencilStage {
+    uint64_t key[kStencilStage];
+    uint32_t perm[kStencilStage];
+    uint64_t bar;
+};
+
 template <int S>
-__global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, const FrameCounters *__restrict__ ctr,
+__global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, FrameCounters *__restrict__ ctr,
                                                       const uint64_t *__restrict__ skey,
                                                       const uint32_t *__restrict__ perm,
-                                                      const uint32_t *__restrict__ pidw,
                                                       const uint32_t *__restrict__ mask,
                                                       const int8_t *__restrict__ wn_scan,
                                                       const uint32_t *__restrict__ heads,
-                                                      uint32_t *__restrict__ merged) {
+                                                      uint32_t *__restrict__ merged, uint32_t spin_cap) {
     constexpr int WORDS = S / 8;
+    __shared__ __align__(16) StencilStage st;
     const int64_t nf = ctr->nf, nm = ctr->n_merged;
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nm) return;
-    const int64_t h = heads[g];
-    const uint64_t kh = skey[h];
-    const int32_t w0 = wn_scan[h];
+    const int64_t g0 = (int64_t)blockIdx.x * blockDim.x;
+    if (g0 >= nm) return;
+    // the block's run of sorted positions, from a 16-entry boundary
+    const int64_t s16 = (int64_t)heads[g0] & ~(int64_t)15;
+    const int64_t e = g0 + (int64_t)blockDim.x < nm ? (int64_t)heads[g0 + blockDim.x] : nf;
+    const int64_t e16 = (e + 15) & ~(int64_t)15;
+    const int64_t n_st = min(e16 - s16, (int64_t)kStencilStage);  // a multiple of 16
+    const uint32_t bar = smem_addr(&st.bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)n_st * (8u + 4u);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+        bulk_g2s(st.key, skey + s16, (uint32_t)n_st * 8u, bar);
+        bulk_g2s(st.perm, perm + s16, (uint32_t)n_st * 4u, bar);
+    }
+    // this thread's group head and its scanned winding, while the copies run
+    const int64_t g = g0 + threadIdx.x;
+    const bool live = g < nm;
+    const int64_t h = live ? (int64_t)heads[g] : 0;
+    const int32_t w0 = live ? (int32_t)wn_scan[h] : 0;
+    if (!mbar_wait0(bar, spin_cap)) {
+        if (threadIdx.x == 0) atomicOr(&ctr->status, kStatusTimeout);
+        mbar_wait0(bar, spin_cap);  // the copies still in flight write this block's shared memory
+        return;
+    }
+    if (!live) return;
+    auto key_at = [&](int64_t j) { return j - s16 < n_st ? st.key[j - s16] : skey[j]; };
+    const uint64_t kh = key_at(h) & kKeyMask;
     const uint32_t init = 0x01010101u * (uint32_t)w0;
     uint32_t acc[WORDS][8];
 #pragma unroll
     for (int w = 0; w < WORDS; ++w)
 #pragma unroll
         for (int b = 0; b < 8; ++b) acc[w][b] = init;
-    for (int64_t j = h; j < nf && skey[j] == kh; ++j) {
-        const uint32_t raw = perm[j];
-        const int32_t chg = (int32_t)pidw[raw] >> 30;
+    for (int64_t j = h; j < nf; ++j) {
+        const bool staged = j - s16 < n_st;
+        const uint64_t kj = staged ? st.key[j - s16] : skey[j];
+        if ((kj & kKeyMask) != kh) break;
+        const int32_t chg = fw_chg((uint32_t)(kj >> kFwShift));
         if (chg == 0) continue;
+        const uint32_t raw = staged ? st.perm[j - s16] : perm[j];
         uint32_t m[WORDS];
         if constexpr (WORDS == 1) {
-            m[0] = mask[raw];
+            m[0] = __ldg(mask + raw);
         } else if constexpr (WORDS == 2) {
-            const uint2 v = reinterpret_cast<const uint2 *>(mask)[raw];
+            const uint2 v = __ldg(reinterpret_cast<const uint2 *>(mask) + raw);
             m[0] = v.x;
             m[1] = v.y;
         } else {
-            const uint4 v = reinterpret_cast<const uint4 *>(mask)[raw];
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(mask) + raw);
             m[0] = v.x;
             m[1] = v.y;
             m[2] = v.z;
@@ -1752,27 +1823,26 @@ int launch_fragment(const FrameArgs &a, const float2 *tvert, const int2 *entries
 
 int64_t scan_mark_status_words(int64_t cap_nf) { return 2 * std::max<int64_t>(1, (cap_nf + kMarkTile - 1) / kMarkTile); }
 
-int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, const uint32_t *perm, const int8_t *wn,
-                     int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *bin_count,
+int launch_scan_mark(const FrameArgs &a, int64_t cap_nf, const uint64_t *skey, int8_t *wn_scan, int4 *draw, uint32_t *heads, uint32_t *item_scene, uint32_t *bin_count,
                      FrameCounters *counters, uint64_t *tile_status, uint32_t spin_cap, cudaStream_t s) {
     const int64_t words = scan_mark_status_words(cap_nf);
-    k_scan_mark<<<(unsigned)(words / 2), kMarkThreads, 0, s>>>(a, skey, perm, wn, wn_scan, draw, heads, item_scene,
+    k_scan_mark<<<(unsigned)(words / 2), kMarkThreads, 0, s>>>(a, skey, wn_scan, draw, heads, item_scene,
                                                                bin_count, counters, tile_status, tile_status + words / 2,
                                                                spin_cap);
     return 1;
 }
 
-int launch_stencil(const FrameArgs &a, int64_t cap_nf, const FrameCounters *ctr, const uint64_t *skey,
-                   const uint32_t *perm, const uint32_t *pidw, const uint32_t *mask, const int8_t *wn_scan,
-                   const uint32_t *heads, uint32_t *merged, cudaStream_t s) {
+int launch_stencil(const FrameArgs &a, int64_t cap_nf, FrameCounters *ctr, const uint64_t *skey, const uint32_t *perm,
+                   const uint32_t *mask, const int8_t *wn_scan, const uint32_t *heads, uint32_t *merged,
+                   uint32_t spin_cap, cudaStream_t s) {
     if (cap_nf <= 0) return 0;
     const unsigned g = grid_for(cap_nf);
     if (a.S == 8)
-        k_stencil<8><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, pidw, mask, wn_scan, heads, merged);
+        k_stencil<8><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, mask, wn_scan, heads, merged, spin_cap);
     else if (a.S == 16)
-        k_stencil<16><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, pidw, mask, wn_scan, heads, merged);
+        k_stencil<16><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, mask, wn_scan, heads, merged, spin_cap);
     else
-        k_stencil<32><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, pidw, mask, wn_scan, heads, merged);
+        k_stencil<32><<<g, kThreads, 0, s>>>(a, ctr, skey, perm, mask, wn_scan, heads, merged, spin_cap);
     return 1;
 }
 

@@ -264,6 +264,15 @@ struct SegSmem {
     uint32_t wsum[kSegWarps + 1];
 };
 
+// Shared-memory form of a sort key within its path: the 24-bit cell key
+// and, in bits 24-27, key bits 60-63 (the digit passes read bits 0-23).
+__device__ __forceinline__ uint32_t sk_pack(uint64_t k) {
+    return ((uint32_t)k & 0xFFFFFFu) | ((uint32_t)(k >> kFwShift) << 24);
+}
+__device__ __forceinline__ uint64_t sk_unpack(uint64_t hi, uint32_t k) {
+    return hi | (uint64_t)(k & 0xFFFFFFu) | ((uint64_t)(k >> 24) << kFwShift);
+}
+
 // First curve of every path (curves ascending by path); start[P] = C.
 __global__ void k_path_starts(const CurveDesc *__restrict__ curves, uint32_t C, uint32_t P, uint32_t *__restrict__ start) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -374,7 +383,7 @@ __global__ void __launch_bounds__(kSmallWarps * 32) k_segment_sort_small(const u
     const int n = (int)(e - b);
     const uint64_t hi = (uint64_t)p << 24;
     for (int i = lane; i < n; i += 32) {
-        skey[w][0][i] = (uint32_t)keys_in[b + i] & 0xFFFFFFu;
+        skey[w][0][i] = sk_pack(keys_in[b + i]);
         sval[w][0][i] = b + (uint32_t)i;
     }
     __syncwarp();
@@ -434,7 +443,7 @@ __global__ void __launch_bounds__(kSmallWarps * 32) k_segment_sort_small(const u
         cur ^= 1;
     }
     for (int i = lane; i < n; i += 32) {
-        keys_out[b + i] = hi | skey[w][cur][i];
+        keys_out[b + i] = sk_unpack(hi, skey[w][cur][i]);
         vals_out[b + i] = sval[w][cur][i];
     }
 }
@@ -460,7 +469,7 @@ __global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t 
 #pragma unroll
         for (int r = 0; r < kSegItems; ++r) {
             const uint32_t li = (uint32_t)(warp * kSegWarpSpan + r * 32 + lane);
-            kk[r] = li < n ? (uint32_t)keys_in[b + li] & 0xFFFFFFu : 0u;
+            kk[r] = li < n ? sk_pack(keys_in[b + li]) : 0u;
             vv[r] = b + li;
         }
         bool staged = false;  // the current order is in shared memory
@@ -497,14 +506,14 @@ __global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t 
             for (int r = 0; r < kSegItems; ++r) {
                 const uint32_t li = (uint32_t)(warp * kSegWarpSpan + r * 32 + lane);
                 if (li < n) {
-                    keys_out[b + li] = hi | kk[r];
+                    keys_out[b + li] = sk_unpack(hi, kk[r]);
                     vals_out[b + li] = vv[r];
                 }
             }
             return;
         }
         for (uint32_t i = threadIdx.x; i < n; i += kSegThreads) {
-            keys_out[b + i] = hi | sm.key[i];
+            keys_out[b + i] = sk_unpack(hi, sm.key[i]);
             vals_out[b + i] = sm.val[i];
         }
         return;
@@ -556,7 +565,7 @@ __global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t 
             for (int r = 0; r < kSegItems; ++r) {
                 const int li = warp * kSegWarpSpan + r * 32 + lane;
                 const bool valid = li < cnt;
-                kk[r] = valid ? (uint32_t)ksrc[b + c0 + li] & 0xFFFFFFu : 0u;
+                kk[r] = valid ? sk_pack(ksrc[b + c0 + li]) : 0u;
                 vv[r] = valid ? (cur == 0 ? b + c0 + (uint32_t)li : vsrc[b + c0 + li]) : 0u;
             }
             uint32_t tot;
@@ -565,7 +574,7 @@ __global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t 
                 const uint32_t k = sm.key[i];
                 const uint32_t d = (k >> shift) & 0xFFu;
                 const uint32_t pos = sm.dstart[d] + (uint32_t)i - sm.lstart[d];
-                kdst[pos] = hi | k;
+                kdst[pos] = sk_unpack(hi, k);
                 vdst[pos] = sm.val[i];
             }
             __syncthreads();
