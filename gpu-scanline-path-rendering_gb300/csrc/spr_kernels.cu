@@ -1413,13 +1413,21 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const uint2 *__r
     for (uint32_t base = beg; base < fin; base += kWin * 32) {
         __syncwarp();
         const int nb = (int)min((uint32_t)kWin, (fin - base + 31) / 32);  // batches in this window
-        for (int c = 0; c < nb; ++c) {
+        // the columns of the window's items (lane l: item 32 c + l of batch
+        // c), all loads issued before the first is used
+        uint32_t xws[kWin];
+#pragma unroll
+        for (int c = 0; c < kWin; ++c) {
             const uint32_t p = base + c * 32 + lane;
+            xws[c] = c < nb && p < fin ? __ldg(&rec_a[p].y) : 0u;
+        }
+#pragma unroll
+        for (int c = 0; c < kWin; ++c) {
+            if (c >= nb) break;
             uint32_t cm = 0u;  // cells of this lane's item (a fragment: one cell of 2 columns)
-            if (p < fin) {
-                const uint32_t xw = __ldg(&rec_a[p].y);
-                const int x = (int)(xw & 0xFFFFu);
-                const int xb = min(x + (int)(xw >> 16), W);
+            {
+                const int x = (int)(xws[c] & 0xFFFFu);
+                const int xb = min(x + (int)(xws[c] >> 16), W);
                 cm = xb > x ? cell_bits((x - tx0) >> 1, (xb - tx0 + 1) >> 1) : 0u;
             }
             // bit q of lane L's word: staged item q covers cell L (a transpose
