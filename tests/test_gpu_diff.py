@@ -164,12 +164,13 @@ def test_empty_scene_and_errors():
         assert e.value.status == spr.ERR_INVALID_ARG
 
 
-@pytest.mark.parametrize("samples,n_jit", [(16, 64), (256, 4)])
-def test_finite_differences_on_jittered_renders(samples, n_jit):
-    """dL/d(vertex) against central differences (h = 0.1 px) of the rendered
-    loss, both averaged over sub-pixel translations (1024 samples per pixel
-    in all: 16 spp x 64 translations, or 256 spp x 4); coincident endpoint
-    copies of a contour move together (one contour point)."""
+@pytest.mark.parametrize("samples,n_jit,h", [(16, 64, 0.1), (256, 4, 0.1), (256, 16, 0.01)])
+def test_finite_differences_on_jittered_renders(samples, n_jit, h):
+    """dL/d(vertex) against central differences (step h px: 0.1, or 0.01 on
+    256-sample renders) of the rendered loss, both averaged over sub-pixel
+    translations (16 spp x 64 translations, 256 spp x 4 or 256 spp x 16);
+    coincident endpoint copies of a contour move together (one contour
+    point)."""
     W = H = 96
     sc = spr.Scene.generate(spr.SCENE_CUBICS, seed=5, width=W, height=H, n_paths=6, seg_min=4, seg_max=6)
     fill = fills(sc.n_paths, 1)
@@ -205,9 +206,9 @@ def test_finite_differences_on_jittered_renders(samples, n_jit):
                 acc = 0.0
                 for t in jit:
                     sp, sm = sc.copy(), sc.copy()
-                    sp.vertex[grp, c] += 0.1
-                    sm.vertex[grp, c] -= 0.1
-                    acc += (loss(sp, t) - loss(sm, t)) / 0.2
+                    sp.vertex[grp, c] += h
+                    sm.vertex[grp, c] -= h
+                    acc += (loss(sp, t) - loss(sm, t)) / (2 * h)
                 an.append(gv[grp, c].sum())
                 fd.append(acc / len(jit))
     an, fd = np.array(an), np.array(fd)
