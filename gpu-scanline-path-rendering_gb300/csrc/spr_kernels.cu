@@ -874,7 +874,7 @@ struct StencilStage {
 };
 
 template <int S>
-__global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, FrameCounters *__restrict__ ctr,
+__global__ void __launch_bounds__(kThreads, 5) k_stencil(FrameArgs a, FrameCounters *__restrict__ ctr,
                                                       const uint64_t *__restrict__ skey,
                                                       const uint32_t *__restrict__ perm,
                                                       const uint32_t *__restrict__ mask,
@@ -916,33 +916,87 @@ __global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, FrameCounters
     if (!live) return;
     auto key_at = [&](int64_t j) { return j - s16 < n_st ? st.key[j - s16] : skey[j]; };
     const uint64_t kh = key_at(h) & kKeyMask;
+    // the group's fragments with a winding change: fn(change sign, mask)
+    auto walk = [&](auto &&fn) {
+        for (int64_t j = h; j < nf; ++j) {
+            const bool staged = j - s16 < n_st;
+            const uint64_t kj = staged ? st.key[j - s16] : skey[j];
+            if ((kj & kKeyMask) != kh) break;
+            const int32_t chg = fw_chg((uint32_t)(kj >> kFwShift));
+            if (chg == 0) continue;
+            const uint32_t raw = staged ? st.perm[j - s16] : perm[j];
+            uint32_t m[WORDS];
+            if constexpr (WORDS == 1) {
+                m[0] = __ldg(mask + raw);
+            } else if constexpr (WORDS == 2) {
+                const uint2 v = __ldg(reinterpret_cast<const uint2 *>(mask) + raw);
+                m[0] = v.x;
+                m[1] = v.y;
+            } else {
+                const uint4 v = __ldg(reinterpret_cast<const uint4 *>(mask) + raw);
+                m[0] = v.x;
+                m[1] = v.y;
+                m[2] = v.z;
+                m[3] = v.w;
+            }
+            fn(chg, m);
+        }
+    };
+    const int fr = a.fill_rule[(uint32_t)(kh >> 24)];
+    // Every sample's winding w0 + (sum of the changes of the fragments covering
+    // it) as a 7-bit counter, bit-sliced: plane p holds bit p of the counters of
+    // all samples, and adding a fragment is a ripple carry (or borrow) over the
+    // planes.  The packed counters below (four 8-bit counters per word, the
+    // reference's form) give each sample its winding modulo 128 as long as no
+    // winding leaves [-128, 127], where a byte's carry would reach its
+    // neighbour; with |w0| + (fragments) <= 127 that cannot happen, and the
+    // planes give the same bits.
+    uint32_t pl[7][WORDS];
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+#pragma unroll
+        for (int w = 0; w < WORDS; ++w) pl[q][w] = (((uint32_t)w0 >> q) & 1u) ? 0xFFFFFFFFu : 0u;
+    int k = 0;
+    walk([&](int32_t chg, const uint32_t (&m)[WORDS]) {
+        ++k;
+#pragma unroll
+        for (int w = 0; w < WORDS; ++w) {
+            uint32_t c = m[w];
+            if (chg > 0) {
+#pragma unroll
+                for (int q = 0; q < 7; ++q) {
+                    const uint32_t t = pl[q][w] & c;
+                    pl[q][w] ^= c;
+                    c = t;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 7; ++q) {
+                    const uint32_t t = ~pl[q][w] & c;
+                    pl[q][w] ^= c;
+                    c = t;
+                }
+            }
+        }
+    });
+    if ((w0 < 0 ? -w0 : w0) + k <= 127) {
+#pragma unroll
+        for (int w = 0; w < WORDS; ++w) {
+            // nonzero: any bit of the 7-bit winding; even-odd: its lowest bit
+            const uint32_t ret = fr == 0 ? (pl[0][w] | pl[1][w] | pl[2][w] | pl[3][w] | pl[4][w] | pl[5][w] | pl[6][w])
+                                         : pl[0][w];
+            merged[g * WORDS + w] = ret;
+        }
+        return;
+    }
+    // packed 8-bit counters per mask bit, reduced to the 7-bit winding number
     const uint32_t init = 0x01010101u * (uint32_t)w0;
     uint32_t acc[WORDS][8];
 #pragma unroll
     for (int w = 0; w < WORDS; ++w)
 #pragma unroll
         for (int b = 0; b < 8; ++b) acc[w][b] = init;
-    for (int64_t j = h; j < nf; ++j) {
-        const bool staged = j - s16 < n_st;
-        const uint64_t kj = staged ? st.key[j - s16] : skey[j];
-        if ((kj & kKeyMask) != kh) break;
-        const int32_t chg = fw_chg((uint32_t)(kj >> kFwShift));
-        if (chg == 0) continue;
-        const uint32_t raw = staged ? st.perm[j - s16] : perm[j];
-        uint32_t m[WORDS];
-        if constexpr (WORDS == 1) {
-            m[0] = __ldg(mask + raw);
-        } else if constexpr (WORDS == 2) {
-            const uint2 v = __ldg(reinterpret_cast<const uint2 *>(mask) + raw);
-            m[0] = v.x;
-            m[1] = v.y;
-        } else {
-            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(mask) + raw);
-            m[0] = v.x;
-            m[1] = v.y;
-            m[2] = v.z;
-            m[3] = v.w;
-        }
+    walk([&](int32_t chg, const uint32_t (&m)[WORDS]) {
 #pragma unroll
         for (int w = 0; w < WORDS; ++w)
 #pragma unroll
@@ -950,8 +1004,7 @@ __global__ void __launch_bounds__(kThreads) k_stencil(FrameArgs a, FrameCounters
                 const uint32_t bits = (m[w] >> b) & 0x01010101u;
                 acc[w][b] = chg > 0 ? acc[w][b] + bits : acc[w][b] - bits;
             }
-    }
-    const int fr = a.fill_rule[(uint32_t)(kh >> 24)];
+    });
 #pragma unroll
     for (int w = 0; w < WORDS; ++w) {
         uint32_t ret = 0;

@@ -493,3 +493,37 @@ def test_opaque_fills(samples, ms, srgb):
     opaque = rng.random(sc.n_paths) < 0.7
     sc.path_fill_rgba = np.where(opaque, sc.path_fill_rgba | 0xFF000000, sc.path_fill_rgba).astype(np.uint32)
     check_parity(sc, 160, 120, samples=samples, ms=ms, srgb=srgb)
+
+
+def stacked_contours(copies, reverse_every=0):
+    """One path per fill rule, each of `copies` slightly shifted copies of
+    the same 9-gon (every `reverse_every`-th copy reversed when set): the
+    boundary cells hold groups of up to `copies` fragments and the windings
+    reach +-copies."""
+    vert, vpid, cvp, ctype, cpid, cw = [], [], [], [], [], []
+    ang = np.linspace(0, 2 * np.pi, 9, endpoint=False)
+    for pid in range(2):
+        cx, cy = 40.0 + 70.0 * pid, 40.0
+        for k in range(copies):
+            pts = [(cx + 27.3 * np.cos(a) + 0.013 * k, cy + 25.1 * np.sin(a) - 0.007 * k) for a in ang]
+            if reverse_every and k % reverse_every == 0:
+                pts = pts[::-1]
+            for i in range(len(pts)):
+                cvp.append(len(vert))
+                ctype.append(spr.CURVE_LINEAR)
+                cpid.append(pid)
+                cw.append(-1.0)
+                for p in (pts[i], pts[(i + 1) % len(pts)]):
+                    vert.append(p)
+                    vpid.append(pid)
+    return spr.Scene(np.array(vert, np.float32), vpid, cvp, ctype, cpid, cw, [0, 1],
+                     [0xC04080F0, 0xB0F08040])
+
+
+@pytest.mark.parametrize("copies,reverse_every", [(100, 0), (127, 0), (128, 0), (200, 0), (300, 7)])
+@pytest.mark.parametrize("samples", [8, 32])
+def test_high_winding_numbers(copies, reverse_every, samples):
+    """Merged masks where the windings leave the int8 range (groups of up to
+    300 fragments in one cell): the bit-sliced counters and the packed 8-bit
+    counters they fall back to, exact against the oracle."""
+    check_parity(stacked_contours(copies, reverse_every), 150, 80, samples=samples)
