@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_curve_emit(FrameArgs a, con
 
 // ---------------------------------------------------------- fragments --
 template <int S>
-__global__ void __launch_bounds__(kThreads) k_fragment(FrameArgs a, const float2 *__restrict__ tv,
+__global__ void __launch_bounds__(kThreads, 8) k_fragment(FrameArgs a, const float2 *__restrict__ tv,
                                                        const int2 *__restrict__ entries,
                                                        const FrameCounters *__restrict__ ctr,
                                                        int32_t *__restrict__ key_out, uint32_t *__restrict__ pid_out,

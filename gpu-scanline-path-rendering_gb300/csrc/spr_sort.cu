@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(kSmallWarps * 32) k_segment_sort_small(const u
     }
 }
 
-__global__ void __launch_bounds__(kSegThreads, 4) k_segment_sort(const uint64_t *__restrict__ keys_in,
+__global__ void __launch_bounds__(kSegThreads, 5) k_segment_sort(const uint64_t *__restrict__ keys_in,
                                                                const uint32_t *__restrict__ start,
                                                                const uint32_t *__restrict__ offsets,
                                                                uint64_t *__restrict__ keys_out,
