@@ -532,6 +532,11 @@ extern "C" {
 int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     if (!h) return SPR_ERR_INVALID_ARG;
     drop_graph(h);
+    // the frame capacities stay when the new scene has the same element
+    // counts (the same scene again, or new geometry of the same structure);
+    // a frame that outgrows them is rendered again, sized, when read
+    const bool keep_caps = h->caps_ok && h->has_scene && h->n_scenes == 0 && v != nullptr &&
+                           v->n_paths == h->P && v->n_curves == h->C && v->n_vertices == h->V;
     h->caps_ok = false;
     int st = validate_view(v);
     if (st) return st;
@@ -581,6 +586,7 @@ int spr_set_scene(spr_handle *h, const spr_scene_view *v) {
     h->C = C;
     h->V = V;
     h->has_scene = true;
+    h->caps_ok = keep_caps;
     return SPR_OK;
 }
 

@@ -219,7 +219,8 @@ int spr_set_rev_transform(spr_handle *h, const float ctx[13]);
  * y in [y, y+1), row-major, 4*width bytes per row) in device memory.  Returns
  * after the work is enqueued.  The reference reads the fragment counts back
  * twice per frame (cu:980, 1139-1157); here only the first frame after a
- * change of scene, viewport or sample count does (to size the buffers, with
+ * change of scene (other than one with the same path, curve and vertex
+ * counts), viewport or sample count does (to size the buffers, with
  * headroom).  Later frames make no host reads: their kernels take their sizes
  * from device memory, and a frame that outgrows the buffers is rendered again
  * with larger ones when its results are first read (spr_read_image,

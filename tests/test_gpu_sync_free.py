@@ -117,3 +117,28 @@ def test_lookback_wait_gives_up():
         r.rasterize()  # and without host reads
         assert r.frame_stats()["host_syncs"] == 0
         assert np.array_equal(r.read_image().reshape(-1), ref["IMAGE"])
+
+
+def test_same_structure_scene_keeps_capacities():
+    """A new scene with the same element counts (the same scene set again, or
+    moved geometry) renders without host reads; one that outgrows the kept
+    buffers is rendered again, sized, when read, and stays exact."""
+    sc = spr.Scene.generate(spr.SCENE_MIXED, seed=63, width=320, height=256, n_paths=200, n_large=8)
+    with spr.VGRasterizer(320, 256, samples=32) as r:
+        r.add_vg(sc)
+        r.rasterize()
+        assert r.frame_stats()["host_syncs"] == 2  # the sized first frame
+        r.add_vg(sc)
+        r.rasterize()
+        assert r.frame_stats()["host_syncs"] == 0
+        ref = oracle.run(sc, 320, 256, samples=32)
+        assert np.array_equal(r.read_image().reshape(-1), ref["IMAGE"])
+        # the same structure, every path scaled up 3x about the centre: far
+        # more entries than the kept buffers hold
+        big = sc.copy()
+        big.vertex = ((big.vertex - [160.0, 128.0]) * 3.0 + [160.0, 128.0]).astype(np.float32)
+        r.add_vg(big)
+        r.rasterize()
+        ref = oracle.run(big, 320, 256, samples=32)
+        assert np.array_equal(r.read_image().reshape(-1), ref["IMAGE"])
+        assert r.element_number() == ref.counts
