@@ -122,6 +122,7 @@ struct spr_handle {
     // the scene of every path; single-scene frames use cfg and m
     int n_scenes = 0;
     std::vector<SceneInfo> scenes_h;
+    int scenes_shift = kBinShift;  // bin geometry of the scene table on the device
     DevBuf scenes_d, path_scene, item_scene;
     // differentiable frames: per-fragment chords and left masks, per-item
     // paths, the per-block tapes, the transformed-vertex gradient and the
@@ -138,7 +139,7 @@ struct spr_handle {
     // launch choices (spr_autotune; -1 / 0 = the built-in rule): fragment
     // sort (0 device-wide radix, 1 per-path segments), curve-emission order
     // (0 off, 1 on), resolve blocks per SM
-    int tune_sort = -1, tune_emit = -1, tune_bps = 0;
+    int tune_sort = -1, tune_emit = -1, tune_bps = 0, tune_bin_w = 0;
     uint32_t n_grad = 0;
     float rev[13] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
     // output view (setOutputTransform / enableOutputTransform): the inverse
@@ -262,7 +263,19 @@ int build_tables(spr_handle *h) {
     return SPR_OK;
 }
 
-FrameArgs make_args(const spr_handle *h) {
+// Bin geometry of a frame (shift: tiles of 1 << shift columns).
+int frame_bin_shift(const spr_handle *h, bool diff) {
+    if (diff) return kBinShift;
+    switch (h->tune_bin_w) {
+    case 8: return 3;
+    case 16: return 4;
+    case 32: return 5;
+    case 64: return 6;
+    default: return kPlainBinShift;
+    }
+}
+
+FrameArgs make_args(const spr_handle *h, bool diff = false) {
     FrameArgs a;
     a.W = h->cfg.width;
     a.H = h->cfg.height;
@@ -304,11 +317,13 @@ FrameArgs make_args(const spr_handle *h) {
         a.n_scenes = h->n_scenes;
         const SceneInfo &last = h->scenes_h.back();
         a.n_bins = (int64_t)last.bin_off + (int64_t)last.ntx * last.nrows;
+        a.bin_shift = h->scenes_shift;
     } else {
         a.path_scene = nullptr;
         a.scenes = nullptr;
         a.n_scenes = 0;
-        a.n_bins = (int64_t)((a.W + kBinW - 1) / kBinW) * ((a.H + 1) / 2);
+        a.bin_shift = frame_bin_shift(h, diff);
+        a.n_bins = (int64_t)bin_cols(a.W, a.bin_shift) * bin_rows(a.H, a.bin_shift);
     }
     return a;
 }
@@ -716,6 +731,27 @@ int diff_stage(spr_handle *h, const FrameArgs &a, const DiffCall &dc, const uint
 int64_t bin_stride(int64_t nbins) { return (nbins + 1 + 3) & ~int64_t(3); }
 int64_t bin_words(int64_t nbins) { return 3 * bin_stride(nbins); }
 
+// The batch scene table for bin geometry `shift` (tiles of 1 << shift
+// columns): every scene's tile and band counts and first bin, uploaded when
+// the geometry differs from the table's.
+int scene_bins(spr_handle *h, int shift, cudaStream_t s) {
+    if (h->n_scenes == 0 || h->scenes_shift == shift) return SPR_OK;
+    uint64_t bins = 0;
+    for (SceneInfo &si : h->scenes_h) {
+        si.ntx = bin_cols(si.W, shift);
+        si.nrows = bin_rows(si.H, shift);
+        si.bin_off = (uint32_t)bins;
+        bins += (uint64_t)si.ntx * (uint64_t)si.nrows;
+        if (bins > UINT32_MAX) return SPR_ERR_CAPACITY_EXCEEDED;
+    }
+    // (from pageable memory: staged before the call returns)
+    if (cudaMemcpyAsync(h->scenes_d.p, h->scenes_h.data(), sizeof(SceneInfo) * h->scenes_h.size(),
+                        cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return cuda_status();
+    h->scenes_shift = shift;
+    return SPR_OK;
+}
+
 // Headroom of the capacities a sized frame sets, so that frames whose sizes
 // drift a little (an animation, a fitting loop) keep fitting.
 int64_t with_headroom(int64_t n) { return n + n / 8 + 256; }
@@ -798,7 +834,8 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     h->diff_ready = false;
     int L = 0;  // kernels launched by this frame
     h->host_syncs = 0;
-    FrameArgs a = make_args(h);
+    if ((st = scene_bins(h, frame_bin_shift(h, dc != nullptr), s))) return st;
+    FrameArgs a = make_args(h, dc != nullptr);
     const int W = a.W, H = a.H, WORDS = a.S / 8;
     const bool batch = h->n_scenes > 0;
     const int64_t npix = frame_pixels(h);
@@ -955,8 +992,9 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
                       &ctr->status, s);
     L += launch_bin_scatter(a, h->draw.as<int4>(), item_scene, cap_items, ctr, bin_off, bin_fill,
                             h->pval.as<uint32_t>(), s);
-    L += launch_bin_sort(bin_off, nbins, h->pval.as<uint32_t>(), ctr, a.S, h->draw.as<int4>(), h->merged.as<uint32_t>(),
-                         dc ? nullptr : h->rec_a.as<uint2>(), dc ? nullptr : h->rec_m.as<uint32_t>(), s);
+    L += launch_bin_sort(bin_off, nbins, h->pval.as<uint32_t>(), ctr, a.S, a.bin_shift, h->draw.as<int4>(),
+                         h->merged.as<uint32_t>(), dc ? nullptr : h->rec_a.as<uint2>(),
+                         dc ? nullptr : h->rec_m.as<uint32_t>(), s);
     const uint32_t *pv = h->pval.as<uint32_t>();
     uint32_t *bin_start = bin_off, *bin_end = bin_off + 1;
     rec(h, 7, s);
@@ -1004,7 +1042,8 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
 int backward_of_held_frame(spr_handle *h, void *stream, const DiffCall &dc) {
     cudaSetDevice(h->cfg.device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    FrameArgs a = make_args(h);
+    if (int st = scene_bins(h, kBinShift, s)) return st;
+    FrameArgs a = make_args(h, true);
     if (h->nf > 0) {
         a.chord = h->chord.as<float4>();
         a.lmask = h->lmask.as<uint32_t>();
@@ -1191,6 +1230,9 @@ int spr_autotune(spr_handle *h, int32_t frames, void *stream, spr_tune *out) {
     h->timing = false;
     h->tune_sort = h->tune_emit = -1;
     h->tune_bps = 0;
+    const int bin_w0 = h->tune_bin_w;
+    h->tune_bin_w = 0;
+    if (bin_w0 != 0) h->caps_ok = false;  // (the pairs depend on the tile)
     float base = 0.f;
     int st = time_frames(h, stream, frames, &base);
     // one choice at a time, the others at their best so far
@@ -1217,12 +1259,24 @@ int spr_autotune(spr_handle *h, int32_t frames, void *stream, spr_tune *out) {
         if (t < best) best = t, best_bps = v;
     }
     h->tune_bps = best_bps;
+    int best_bin_w = 0;
+    for (const int v : {64, 32, 8}) {  // 16 is the default
+        if (st) break;
+        h->tune_bin_w = v;
+        h->caps_ok = false;
+        float t = 0.f;
+        if ((st = time_frames(h, stream, frames, &t))) break;
+        if (t < best) best = t, best_bin_w = v;
+    }
+    if (h->tune_bin_w != best_bin_w) h->caps_ok = false;
+    h->tune_bin_w = best_bin_w;
     h->timing = timing;
     if (st) return st;
     if (out) {
         out->sort = best_sort;
         out->emit_order = best_emit;
         out->resolve_bps = best_bps;
+        out->bin_width = best_bin_w;
         out->frame_ms = best;
         out->default_ms = base;
     }
@@ -1232,12 +1286,16 @@ int spr_autotune(spr_handle *h, int32_t frames, void *stream, spr_tune *out) {
 int spr_set_tuning(spr_handle *h, const spr_tune *t) {
     if (!h || !t) return SPR_ERR_INVALID_ARG;
     if (t->sort < -1 || t->sort > 1 || t->emit_order < -1 || t->emit_order > 1 || t->resolve_bps < 0 ||
-        t->resolve_bps > 4)
+        t->resolve_bps > 4 ||
+        (t->bin_width != 0 && t->bin_width != 64 && t->bin_width != 32 && t->bin_width != 16 && t->bin_width != 8))
         return SPR_ERR_INVALID_ARG;
     drop_graph(h, false);
     h->tune_sort = t->sort;
     h->tune_emit = t->emit_order;
     h->tune_bps = t->resolve_bps;
+    const int bw = t->bin_width == 16 ? 0 : t->bin_width;  // (0: the default, 16 columns)
+    if (bw != h->tune_bin_w) h->caps_ok = false;  // (the pairs depend on the tile)
+    h->tune_bin_w = bw;
     return SPR_OK;
 }
 
@@ -1649,6 +1707,7 @@ int upload_group(spr_handle *h, const spr_batch_scene *in, const std::vector<int
                                 gramp.empty() ? nullptr : gramp.data(), (uint32_t)gramp.size())))
         return st;
     h->scenes_h = info;
+    h->scenes_shift = kBinShift;
     h->n_scenes = (int)info.size();
     return SPR_OK;
 }

@@ -54,11 +54,22 @@ struct FrameCounters {
     uint32_t pad[3];
 };
 
-// Pixel columns of a resolve bin (one cell row high, one warp each).
+// Resolve bins: a bin is a band of 64 / bin_w cell rows x bin_w pixel
+// columns holding 32 cells (one per lane of the warp that resolves it),
+// bin_w = 1 << shift, shift 3..6 (8 x 8, 16 x 4, 32 x 2 or 64 x 1 cells).
+// Plain frames use 16 x 4 unless the tuning picks another; differentiable
+// frames use 64 x 1 (kBinW columns, one cell row).
 constexpr int kBinW = 64;
-
-// One scene of a batch frame: its viewport, its resolve bins (ntx columns of
-// kBinW pixels x nrows cell rows, numbered from bin_off) and its image (W x H
+constexpr int kBinShift = 6;
+constexpr int kPlainBinShift = 4;
+__host__ __device__ __forceinline__ int bin_cols(int W, int shift) { return (W + (1 << shift) - 1) >> shift; }
+__host__ __device__ __forceinline__ int bin_rows(int H, int shift) {
+    const int band_shift = kBinShift - shift;  // cell rows per band: 1 << band_shift
+    return (((H + 1) / 2) + (1 << band_shift) - 1) >> band_shift;
+}
+// One scene of a batch frame: its viewport, its resolve bins (ntx tiles x
+// nrows bands of the frame's bin geometry, numbered from bin_off) and its
+// image (W x H
 // pixels from image_off in the frame's image buffer), and its 4x4 input
 // transform (row-major).
 struct SceneInfo {
@@ -155,6 +166,7 @@ struct FrameArgs {
     const SceneInfo *scenes;
     int n_scenes;
     int64_t n_bins;  // resolve bins of the frame
+    int bin_shift;   // bins of 1 << bin_shift pixel columns x 64 >> bin_shift cell rows
     // Differentiable frames (else null): per fragment its chord in cell
     // units (q0, q1) and its left mask; per draw item its path.
     float4 *chord;
@@ -214,10 +226,11 @@ int launch_bin_scatter(const FrameArgs &a, const int4 *draw, const uint32_t *ite
                        cudaStream_t s);
 // Sorts every bin's item indices into draw order.  With rec_a set, also
 // writes the resolve records in that order: rec_a[p] = (colour, first
-// column | width << 16) and rec_m[p] the sample mask (S / 8 words; every
-// sample for a span).
+// column | width << 16 | cell row within the bin's band << 29) and rec_m[p]
+// the sample mask (S / 8 words; every sample for a span).
 int launch_bin_sort(const uint32_t *bin_off, int64_t nbins, uint32_t *pval, const FrameCounters *ctr, int S,
-                    const int4 *draw, const uint32_t *merged, uint2 *rec_a, uint32_t *rec_m, cudaStream_t s);
+                    int bin_shift, const int4 *draw, const uint32_t *merged, uint2 *rec_a, uint32_t *rec_m,
+                    cudaStream_t s);
 // The resolve is persistent: resolve_warps(a) warps take bins from
 // counters->bin_queue (zeroed by launch_resolve).  overflow:
 // resolve_overflow_words(a) words, the cell entries past the ones each warp

@@ -606,16 +606,17 @@ __device__ __forceinline__ void item_cols(const int4 &it, int W, int &x0, int &x
     x1 = min(x + it.y, W);
 }
 
-// Resolve bins of draw item `it` (64-column tiles of its cell row) in a
-// viewport W x H whose bins are numbered from bin0: *first and the count.
-__device__ __forceinline__ int item_bins(const int4 &it, int W, int H, uint32_t bin0, uint32_t *first) {
+// Resolve bins of draw item `it` (the tiles of 1 << shift columns of the
+// band of 64 >> shift cell rows holding its row) in a viewport W x H whose
+// bins are numbered from bin0: *first and the count (consecutive bins).
+__device__ __forceinline__ int item_bins(const int4 &it, int W, int H, int shift, uint32_t bin0, uint32_t *first) {
     int x0, x1;
     item_cols(it, W, x0, x1);
     const int row = (it.x >> 16) / 2;
     if (x1 <= x0 || row < 0 || row >= (H + 1) / 2) return 0;
-    const int ntx = (W + kBinW - 1) / kBinW;
-    *first = bin0 + (uint32_t)(row * ntx + x0 / kBinW);
-    return (x1 - 1) / kBinW - x0 / kBinW + 1;
+    const int ntx = bin_cols(W, shift);
+    *first = bin0 + (uint32_t)((row >> (kBinShift - shift)) * ntx + (x0 >> shift));
+    return ((x1 - 1) >> shift) - (x0 >> shift) + 1;
 }
 
 // Counts item `it`'s pairs in its bins.
@@ -623,7 +624,7 @@ __device__ __forceinline__ void count_bins(const FrameArgs &a, const int4 &it, c
                                            uint32_t *__restrict__ bin_count) {
     const uint32_t bin0 = a.scenes != nullptr ? a.scenes[a.path_scene[p]].bin_off : 0u;
     uint32_t b0 = 0;
-    const int nb = item_bins(it, dp.W, dp.H, bin0, &b0);
+    const int nb = item_bins(it, dp.W, dp.H, a.bin_shift, bin0, &b0);
     for (int t = 0; t < nb; ++t) atomicAdd(bin_count + b0 + t, 1u);
 }
 
@@ -1023,7 +1024,6 @@ __global__ void __launch_bounds__(kThreads, 5) k_stencil(FrameArgs a, FrameCount
 }
 
 // ------------------------------------------------------------ resolve --
-constexpr int kBinCells = kBinW / 2;  // cells per resolve bin: one lane each
 constexpr int kResolveWarps = 8;
 constexpr int kResolveMaxBlocksPerSM = 4;
 
@@ -1050,7 +1050,7 @@ __global__ void k_bin_scatter(FrameArgs a, const int4 *__restrict__ draw, const 
             H = sc->H;
             bin0 = sc->bin_off;
         }
-        nb = item_bins(it, W, H, bin0, &b0);
+        nb = item_bins(it, W, H, a.bin_shift, bin0, &b0);
     }
     const int most = __reduce_max_sync(0xffffffffu, nb);
     for (int t = 0; t < most; ++t) {
@@ -1070,10 +1070,12 @@ __global__ void k_bin_scatter(FrameArgs a, const int4 *__restrict__ draw, const 
 // its mirror in the k-block, then the half-cleaners), so that the missing
 // elements past n behave as +infinity.  Bins of up to kBinSortSmem items are
 // sorted in shared memory, larger ones in place.  With rec_a set, the bin's
-// resolve records are written in the same order: the item's colour and
-// columns (first | width << 16) and its merged sample mask (every sample for
-// a span), so that the resolve reads each bin's items and masks as one
-// contiguous run instead of gathering them.
+// resolve records are written in the same order: the item's colour, its
+// columns and cell row within the bin's band (first | width << 16 |
+// row << 29) and its merged sample mask (every sample for a span), so that
+// the resolve reads each bin's items and masks as one contiguous run
+// instead of gathering them.  (Widths stay below 2^13: viewports are at
+// most 4096 pixels wide.)
 constexpr int kBinSortWarps = 4;
 constexpr int kBinSortSmem = 1024;
 template <int MW>
@@ -1099,7 +1101,7 @@ __global__ void __launch_bounds__(kBinSortWarps * 32)
     k_bin_sort(const uint32_t *__restrict__ bin_off, int64_t nbins, uint32_t *__restrict__ pval,
                const FrameCounters *__restrict__ ctr, const int4 *__restrict__ draw,
                const uint32_t *__restrict__ merged, uint2 *__restrict__ rec_a,
-               typename MaskVec<MW>::T *__restrict__ rec_m) {
+               typename MaskVec<MW>::T *__restrict__ rec_m, int band_mask) {
     using MV = typename MaskVec<MW>::T;
     __shared__ uint32_t sk[kBinSortWarps][kBinSortSmem];
     if (ctr->status != 0u || ctr->n_pairs != ctr->need_pairs) return;
@@ -1149,7 +1151,9 @@ __global__ void __launch_bounds__(kBinSortWarps * 32)
     for (uint32_t i = lane; i < n; i += 32) {
         const uint32_t idx = n > 1u ? k[i] : pval[beg];
         const int4 it = draw[idx];
-        rec_a[beg + i] = make_uint2((uint32_t)it.z, ((uint32_t)it.x & 0xFFFFu) | ((uint32_t)it.y << 16));
+        const uint32_t ro = (uint32_t)(((it.x >> 16) / 2) & band_mask);  // the item's cell row within the band
+        rec_a[beg + i] = make_uint2((uint32_t)it.z,
+                                    ((uint32_t)it.x & 0xFFFFu) | ((uint32_t)it.y << 16) | (ro << 29));
         rec_m[beg + i] = it.w != 0 ? reinterpret_cast<const MV *>(merged)[it.w - 1] : MaskVec<MW>::all();
     }
 }
@@ -1287,13 +1291,14 @@ __device__ __forceinline__ uint32_t *entry(CellState<MW, CAP> &w, uint32_t *gx, 
     return j < CAP ? &w.ent[j][0][lane] : gx + (size_t)(j - CAP) * (MW + 1) * 32 + lane;
 }
 
-// Cells [c0, c1) of a bin as a lane mask.
-__device__ __forceinline__ uint32_t cell_bits(int c0, int c1) {
+// Cells [c0, c1) of cell row `ro` of a bin whose rows hold cpr cells (lane
+// ro * cpr + c holds cell c of row ro) as a lane mask.
+__device__ __forceinline__ uint32_t cell_bits(int c0, int c1, int cpr, int ro) {
     c0 = max(c0, 0);
-    c1 = min(c1, kBinCells);
+    c1 = min(c1, cpr);
     if (c1 <= c0) return 0u;
     const uint32_t hi = c1 >= 32 ? 0xFFFFFFFFu : ((1u << c1) - 1u);
-    return hi & ~((1u << c0) - 1u);
+    return (hi & ~((1u << c0) - 1u)) << (ro * cpr);
 }
 
 // Bits of pixel k within mask word `wd` (cell masks of S samples per pixel).
@@ -1449,11 +1454,14 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const uint2 *__r
         image_off = sc->image_off;
         image += image_off;
     }
-    const int ntx = (W + kBinW - 1) / kBinW;
-    const int row = (int)(lb / ntx), tile = (int)(lb % ntx);
-    const int tx0 = tile * kBinW;
-    const int y0 = row * 2;
-    const int X0 = tx0 + 2 * lane;  // this lane's cell: columns X0, X0 + 1, rows y0, y0 + 1
+    // the bin: band `brow` of 64 >> sh cell rows, tile `tile` of 1 << sh
+    // columns; lane l: cell l % cpr of the band's row l / cpr
+    const int sh = a.bin_shift, cs = sh - 1, cpr = 1 << cs;  // cells per row: 1 << cs
+    const int ntx = bin_cols(W, sh);
+    const int brow = (int)(lb / ntx), tile = (int)(lb % ntx);
+    const int tx0 = tile << sh;
+    const int y0 = ((brow << (kBinShift - sh)) + (lane >> cs)) * 2;
+    const int X0 = tx0 + 2 * (lane & (cpr - 1));  // this lane's cell: columns X0, X0 + 1, rows y0, y0 + 1
     // state: one white entry over every sample (multisample), or one colour
     // per pixel (single-sample output)
     int n = 1;
@@ -1480,8 +1488,8 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const uint2 *__r
             uint32_t cm = 0u;  // cells of this lane's item (a fragment: one cell of 2 columns)
             {
                 const int x = (int)(xws[c] & 0xFFFFu);
-                const int xb = min(x + (int)(xws[c] >> 16), W);
-                cm = xb > x ? cell_bits((x - tx0) >> 1, (xb - tx0 + 1) >> 1) : 0u;
+                const int xb = min(x + (int)((xws[c] >> 16) & 0x1FFFu), W);
+                cm = xb > x ? cell_bits((x - tx0) >> 1, (xb - tx0 + 1) >> 1, cpr, (int)(xws[c] >> 29)) : 0u;
             }
             // bit q of lane L's word: staged item q covers cell L (a transpose
             // of the 32 x 32 bit matrix of cell sets)
@@ -1551,7 +1559,7 @@ __device__ __forceinline__ void resolve_bin(const FrameArgs &a, const uint2 *__r
                         cov += __popc(mk[wd]);
                     }
                     if (cov == 0) continue;
-                    const float4 gc = gradient_colour<SRGB>(a, T, c - 1u, (int)(int16_t)(xw & 0xFFFFu), (int)(xw >> 16),
+                    const float4 gc = gradient_colour<SRGB>(a, T, c - 1u, (int)(int16_t)(xw & 0xFFFFu), (int)((xw >> 16) & 0x1FFFu),
                                                             X, Y, lane);
                     if constexpr (MS) {
                         cell_apply<S, SRGB, CAP>(w, gx, lane, n, mk, T, gc.x, gc.y, gc.z, gc.w);
@@ -1916,17 +1924,19 @@ int launch_bin_scatter(const FrameArgs &a, const int4 *draw, const uint32_t *ite
 }
 
 int launch_bin_sort(const uint32_t *bin_off, int64_t nbins, uint32_t *pval, const FrameCounters *ctr, int S,
-                    const int4 *draw, const uint32_t *merged, uint2 *rec_a, uint32_t *rec_m, cudaStream_t s) {
+                    int bin_shift, const int4 *draw, const uint32_t *merged, uint2 *rec_a, uint32_t *rec_m,
+                    cudaStream_t s) {
+    const int band_mask = (1 << (kBinShift - bin_shift)) - 1;  // cell rows per band - 1
     if (nbins <= 0) return 0;
     const unsigned g = (unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps);
     if (S == 8)
-        k_bin_sort<1><<<g, kBinSortWarps * 32, 0, s>>>(bin_off, nbins, pval, ctr, draw, merged, rec_a, rec_m);
+        k_bin_sort<1><<<g, kBinSortWarps * 32, 0, s>>>(bin_off, nbins, pval, ctr, draw, merged, rec_a, rec_m, band_mask);
     else if (S == 16)
         k_bin_sort<2><<<g, kBinSortWarps * 32, 0, s>>>(bin_off, nbins, pval, ctr, draw, merged, rec_a,
-                                                        reinterpret_cast<uint2 *>(rec_m));
+                                                        reinterpret_cast<uint2 *>(rec_m), band_mask);
     else
         k_bin_sort<4><<<g, kBinSortWarps * 32, 0, s>>>(bin_off, nbins, pval, ctr, draw, merged, rec_a,
-                                                        reinterpret_cast<uint4 *>(rec_m));
+                                                        reinterpret_cast<uint4 *>(rec_m), band_mask);
     return 1;
 }
 

@@ -99,7 +99,7 @@ class RvgInfo(C.Structure):
 
 class Tune(C.Structure):
     _fields_ = [("sort", C.c_int32), ("emit_order", C.c_int32), ("resolve_bps", C.c_int32),
-                ("frame_ms", C.c_float), ("default_ms", C.c_float)]
+                ("bin_width", C.c_int32), ("frame_ms", C.c_float), ("default_ms", C.c_float)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -476,8 +476,8 @@ class VGRasterizer:
         check(lib().spr_autotune(self._h, int(frames), stream, C.byref(t)), "spr_autotune")
         return t.as_dict()
 
-    def set_tuning(self, sort=-1, emit_order=-1, resolve_bps=0):
-        t = Tune(sort, emit_order, resolve_bps, 0.0, 0.0)
+    def set_tuning(self, sort=-1, emit_order=-1, resolve_bps=0, bin_width=0):
+        t = Tune(sort, emit_order, resolve_bps, bin_width, 0.0, 0.0)
         check(lib().spr_set_tuning(self._h, C.byref(t)), "spr_set_tuning")
 
     def set_rev_transform(self, ctx):

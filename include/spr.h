@@ -189,18 +189,22 @@ int spr_set_gradients(spr_handle *h, const uint32_t *table, uint32_t n_entries, 
 /* ---- launch tuning (an extension) --------------------------------------------
  * Launch choices that change speed, never results: the fragment sort (0 =
  * device-wide LSD radix, 1 = one block per path segment), the curve-emission
- * order by estimated cost (0 off, 1 on) and the resolve's blocks per SM
- * (1-4).  -1 / 0 select the built-in rule (segment sort for frames of at
- * least 1,024 paths averaging at most 2,048 entries; emission order from
- * 4,096 curves; 4 blocks per SM).  spr_autotune times `frames` frames of
- * the handle's scene under each choice, one choice at a time with the
- * others at their best so far, keeps the fastest (built-in rules on ties)
- * and reports it with the built-in rules' time.  Both drop a captured
- * graph. */
+ * order by estimated cost (0 off, 1 on), the resolve's blocks per SM (1-4)
+ * and its tile: bin_width pixel columns by 64 / bin_width cell rows (the
+ * band height; 64 x 1, 32 x 2, 16 x 4 or 8 x 8 cells of 2 x 2 pixels, 32
+ * cells: one per lane of the warp that resolves the tile).  -1 / 0 select
+ * the built-in rule (segment sort for frames of at least 1,024 paths
+ * averaging at most 2,048 entries; emission order from 4,096 curves; 4
+ * blocks per SM; tiles of 16 columns by 4 cell rows).  Differentiable
+ * frames use 64 x 1 tiles.  spr_autotune times `frames` frames of the
+ * handle's scene under each choice, one choice at a time with the others at
+ * their best so far, keeps the fastest (built-in rules on ties) and reports
+ * it with the built-in rules' time.  Both drop a captured graph. */
 typedef struct spr_tune {
     int32_t sort;
     int32_t emit_order;
     int32_t resolve_bps;
+    int32_t bin_width;
     float frame_ms;   /* spr_autotune: the kept choices' mean frame time */
     float default_ms; /* spr_autotune: the built-in rules' mean frame time */
 } spr_tune;

@@ -413,13 +413,39 @@ def test_tuning_changes_speed_not_results():
                     r.rasterize()
                     assert np.array_equal(r.read_image(), ref), (sort, emit, bps)
                     assert np.array_equal(r.dump("SORT_PERM"), perm)
+        for bw in (64, 32, 8, 16):
+            r.set_tuning(bin_width=bw)
+            r.rasterize()
+            assert np.array_equal(r.read_image(), ref), bw
         t = r.autotune(frames=2)
         assert t["sort"] in (-1, 0, 1) and t["emit_order"] in (-1, 0, 1) and t["resolve_bps"] in (0, 2, 3)
+        assert t["bin_width"] in (0, 64, 32, 8)
         assert 0 < t["frame_ms"] <= t["default_ms"]
         r.rasterize()
         assert np.array_equal(r.read_image(), ref)
         with pytest.raises(spr.SprError):
             r.set_tuning(2, 0, 0)
+        with pytest.raises(spr.SprError):
+            r.set_tuning(bin_width=48)
+
+
+@pytest.mark.parametrize("bin_width", [64, 32, 16, 8])
+@pytest.mark.parametrize("samples,ms,srgb", [(8, True, True), (32, True, False), (16, False, True), (256, True, True)])
+def test_resolve_tiles(bin_width, samples, ms, srgb):
+    """Resolve tiles of 64 x 1, 32 x 2, 16 x 4 (the default) and 8 x 8 cells
+    (tile width x band height): the image exact against the oracle on an
+    odd-sized viewport (partial tiles and bands at the right and bottom
+    edges)."""
+    W, H = 173, 131
+    sc = spr.Scene.generate(spr.SCENE_MIXED, seed=23, width=W, height=H, n_paths=80, n_large=5, with_affine=True)
+    ref = oracle.run(sc, W, H, samples=samples, ms_output=ms, srgb=srgb)
+    r = spr.VGRasterizer(W, H, samples=samples, ms_output=ms, srgb=srgb)
+    with r:
+        r.set_tuning(bin_width=bin_width)
+        r.add_vg(sc)
+        r.rasterize()
+        diff = np.abs(r.read_image().astype(np.int16) - ref["IMAGE"].reshape(H, W, 4).astype(np.int16)).max()
+        assert diff <= IMAGE_TOL
 
 
 def test_random_configurations():
