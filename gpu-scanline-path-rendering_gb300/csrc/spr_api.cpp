@@ -140,6 +140,7 @@ struct spr_handle {
     // sort (0 device-wide radix, 1 per-path segments), curve-emission order
     // (0 off, 1 on), resolve blocks per SM
     int tune_sort = -1, tune_emit = -1, tune_bps = 0, tune_bin_w = 0;
+    int auto_bin_shift = kBinShift;  // the built-in tile, from the last sized frame's spans
     uint32_t n_grad = 0;
     float rev[13] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
     // output view (setOutputTransform / enableOutputTransform): the inverse
@@ -271,7 +272,7 @@ int frame_bin_shift(const spr_handle *h, bool diff) {
     case 16: return 4;
     case 32: return 5;
     case 64: return 6;
-    default: return kPlainBinShift;
+    default: return h->auto_bin_shift;
     }
 }
 
@@ -318,11 +319,13 @@ FrameArgs make_args(const spr_handle *h, bool diff = false) {
         const SceneInfo &last = h->scenes_h.back();
         a.n_bins = (int64_t)last.bin_off + (int64_t)last.ntx * last.nrows;
         a.bin_shift = h->scenes_shift;
+        a.alt_shift = !diff && h->tune_bin_w == 0 ? kPlainBinShift + kBinShift - a.bin_shift : -1;
     } else {
         a.path_scene = nullptr;
         a.scenes = nullptr;
         a.n_scenes = 0;
         a.bin_shift = frame_bin_shift(h, diff);
+        a.alt_shift = !diff && h->tune_bin_w == 0 ? kPlainBinShift + kBinShift - a.bin_shift : -1;
         a.n_bins = (int64_t)bin_cols(a.W, a.bin_shift) * bin_rows(a.H, a.bin_shift);
     }
     return a;
@@ -841,12 +844,13 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
     const int64_t npix = frame_pixels(h);
     // (the passes of a 256-sample frame are sized: they add up into one image)
     const bool sized = (dc != nullptr || !h->caps_ok || h->cfg.samples == 256) && !h->capturing;
+    if (!sized) a.alt_shift = -1;  // (only a sized frame chooses the built-in tile)
     if (h->timing) {
         for (auto &e : h->ev)
             if (!e) cudaEventCreate(&e);
     }
     FrameCounters *ctr = h->counters.as<FrameCounters>();
-    const int64_t nbins = a.n_bins;
+    int64_t nbins = a.n_bins;
     // stage 3: transform + visibility
     if ((st = ensure(h->tvert, sizeof(float2) * h->V)) || (st = ensure(h->pflags, 4 * (size_t)h->P)) ||
         (st = ensure(h->pvis, h->P)) || (st = ensure(h->counts, 4 * (size_t)h->C + 16)) ||
@@ -981,6 +985,30 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
         h->ns = h->h_counters->n_span;
         h->npairs = h->h_counters->need_pairs;
         h->cap_pairs = dc ? std::max<int64_t>(h->npairs, 1) : with_headroom(h->npairs);
+        if (!dc) {  // the built-in tile, from this frame's spans
+            const uint64_t items = (uint64_t)h->h_counters->n_merged + h->h_counters->n_span;
+            h->auto_bin_shift = h->h_counters->span_px <= (uint64_t)kShortSpanPx * items ? kPlainBinShift : kBinShift;
+            if (frame_bin_shift(h, false) != a.bin_shift) {
+                // the bins again in that tile: counts from the draw list, offsets, pair total
+                if ((st = scene_bins(h, frame_bin_shift(h, false), s))) return st;
+                a = make_args(h, false);
+                nbins = a.n_bins;
+                if ((st = ensure(h->bins, 4 * (size_t)bin_words(nbins))) ||
+                    (st = ensure(h->lb_pair, 8 * (size_t)lookback_words(nbins))))
+                    return st;
+                bin_off = h->bins.as<uint32_t>();
+                bin_count = bin_off + bin_stride(nbins);
+                bin_fill = bin_count + bin_stride(nbins);
+                cudaMemsetAsync(bin_count, 0, 8 * (size_t)bin_stride(nbins), s);
+                L += launch_bin_count(a, h->draw.as<int4>(), item_scene, cap_items, ctr, bin_count, s);
+                cudaMemsetAsync(h->lb_pair.p, 0, 8 * (size_t)lookback_words(nbins), s);
+                cudaMemsetAsync(&ctr->tiles[2], 0, 4, s);
+                L += scan_lookback_u32(bin_count, bin_off, nullptr, nbins, h->lb_pair.as<uint64_t>(), &ctr->tiles[2],
+                                       h->lb_spin_cap, &ctr->status, &ctr->need_pairs, s);
+                h->npairs = h->h_counters->pairs_alt;  // (the total the scan-mark pass counted for this tile)
+                h->cap_pairs = with_headroom(h->npairs);
+            }
+        }
     }
     const int64_t cap_pairs = h->cap_pairs;
     if ((st = ensure(h->pval, 4 * (size_t)cap_pairs))) return st;
@@ -1260,7 +1288,7 @@ int spr_autotune(spr_handle *h, int32_t frames, void *stream, spr_tune *out) {
     }
     h->tune_bps = best_bps;
     int best_bin_w = 0;
-    for (const int v : {64, 32, 8}) {  // 16 is the default
+    for (const int v : {64, 32, 16, 8}) {
         if (st) break;
         h->tune_bin_w = v;
         h->caps_ok = false;
@@ -1293,7 +1321,7 @@ int spr_set_tuning(spr_handle *h, const spr_tune *t) {
     h->tune_sort = t->sort;
     h->tune_emit = t->emit_order;
     h->tune_bps = t->resolve_bps;
-    const int bw = t->bin_width == 16 ? 0 : t->bin_width;  // (0: the default, 16 columns)
+    const int bw = t->bin_width;  // (0: the built-in rule)
     if (bw != h->tune_bin_w) h->caps_ok = false;  // (the pairs depend on the tile)
     h->tune_bin_w = bw;
     return SPR_OK;

@@ -51,17 +51,22 @@ struct FrameCounters {
     uint32_t n_items;      // n_merged + n_span
     uint32_t tiles[3];     // look-back tile counters: entry offsets, scan-mark, pair offsets
     uint32_t diff_status;  // differentiable frames: bit 0 tape too short, bit 1 chain too short
-    uint32_t pad[3];
+    uint32_t pairs_alt;          // resolve pairs in the other built-in tile (FrameArgs::alt_shift)
+    unsigned long long span_px;  // the spans' pixels (sum of their widths)
 };
 
 // Resolve bins: a bin is a band of 64 / bin_w cell rows x bin_w pixel
 // columns holding 32 cells (one per lane of the warp that resolves it),
 // bin_w = 1 << shift, shift 3..6 (8 x 8, 16 x 4, 32 x 2 or 64 x 1 cells).
-// Plain frames use 16 x 4 unless the tuning picks another; differentiable
-// frames use 64 x 1 (kBinW columns, one cell row).
+// Plain frames use 16 x 4 when their spans are short (at most
+// kShortSpanPx pixels of span per draw item, measured by the sized frame:
+// narrower tiles cut long spans into many more pairs), else 64 x 1, unless
+// the tuning picks a tile; differentiable frames use 64 x 1 (kBinW columns,
+// one cell row).
 constexpr int kBinW = 64;
 constexpr int kBinShift = 6;
 constexpr int kPlainBinShift = 4;
+constexpr int kShortSpanPx = 8;
 __host__ __device__ __forceinline__ int bin_cols(int W, int shift) { return (W + (1 << shift) - 1) >> shift; }
 __host__ __device__ __forceinline__ int bin_rows(int H, int shift) {
     const int band_shift = kBinShift - shift;  // cell rows per band: 1 << band_shift
@@ -167,6 +172,7 @@ struct FrameArgs {
     int n_scenes;
     int64_t n_bins;  // resolve bins of the frame
     int bin_shift;   // bins of 1 << bin_shift pixel columns x 64 >> bin_shift cell rows
+    int alt_shift;   // the other built-in tile, whose pairs the scan-mark pass also counts (-1: none)
     // Differentiable frames (else null): per fragment its chord in cell
     // units (q0, q1) and its left mask; per draw item its path.
     float4 *chord;
@@ -224,6 +230,9 @@ int launch_stencil(const FrameArgs &a, int64_t cap_nf, FrameCounters *ctr, const
 int launch_bin_scatter(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
                        const FrameCounters *ctr, const uint32_t *bin_off, uint32_t *bin_fill, uint32_t *pval,
                        cudaStream_t s);
+// Pairs of every bin counted from the draw list into bin_count (zero before).
+int launch_bin_count(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
+                     const FrameCounters *ctr, uint32_t *bin_count, cudaStream_t s);
 // Sorts every bin's item indices into draw order.  With rec_a set, also
 // writes the resolve records in that order: rec_a[p] = (colour, first
 // column | width << 16 | cell row within the bin's band << 29) and rec_m[p]

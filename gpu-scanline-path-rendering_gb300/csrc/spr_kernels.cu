@@ -619,13 +619,15 @@ __device__ __forceinline__ int item_bins(const int4 &it, int W, int H, int shift
     return ((x1 - 1) >> shift) - (x0 >> shift) + 1;
 }
 
-// Counts item `it`'s pairs in its bins.
-__device__ __forceinline__ void count_bins(const FrameArgs &a, const int4 &it, const Dim &dp, uint32_t p,
-                                           uint32_t *__restrict__ bin_count) {
+// Counts item `it`'s pairs in its bins; returns its pairs in the other
+// built-in tile (0 if there is none).
+__device__ __forceinline__ uint32_t count_bins(const FrameArgs &a, const int4 &it, const Dim &dp, uint32_t p,
+                                               uint32_t *__restrict__ bin_count) {
     const uint32_t bin0 = a.scenes != nullptr ? a.scenes[a.path_scene[p]].bin_off : 0u;
     uint32_t b0 = 0;
     const int nb = item_bins(it, dp.W, dp.H, a.bin_shift, bin0, &b0);
     for (int t = 0; t < nb; ++t) atomicAdd(bin_count + b0 + t, 1u);
+    return a.alt_shift >= 0 ? (uint32_t)item_bins(it, dp.W, dp.H, a.alt_shift, 0u, &b0) : 0u;
 }
 
 // k_mark_merged_fragment_and_span (cu:462-535) on sorted position i with
@@ -783,6 +785,7 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
     __syncthreads();
     uint32_t nfb = (uint32_t)(s_pre >> 31) + (fpre & 0xFFFFu);
     uint32_t nsb = (uint32_t)(s_pre & 0x7FFFFFFFu) + (fpre >> 16);
+    uint32_t span_px = 0, pairs_alt = 0;  // this thread's span pixels and pairs in the other tile
 #pragma unroll
     for (int j = 0; j < kMarkItems; ++j) {
         const uint32_t ff = mk[j].ff, sfl = mk[j].sf;
@@ -806,7 +809,7 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
                 const int32_t pos = (int32_t)(((uint32_t)key_y(key1) << 16) | (uint32_t)key_x(key1));
                 const int4 it = make_int4(pos, 2, fill, (int)(nfb + 1));
                 draw[nfb + nsb] = it;
-                count_bins(a, it, dp, p, bin_count);
+                pairs_alt += count_bins(a, it, dp, p, bin_count);
                 heads[nfb] = (uint32_t)(base + j);
             }
             if (sfl) {
@@ -818,12 +821,17 @@ __global__ void __launch_bounds__(kMarkThreads) k_scan_mark(FrameArgs a, const u
                 const int32_t pos = (int32_t)(((uint32_t)y0 << 16) | (uint32_t)x0);
                 const int4 it = make_int4(pos, x1 - x0, fill, 0);
                 draw[nfb + nsb + ff] = it;
-                count_bins(a, it, dp, p, bin_count);
+                pairs_alt += count_bins(a, it, dp, p, bin_count);
+                span_px += (uint32_t)max(x1 - x0, 0);
             }
         }
         nfb += ff;
         nsb += sfl;
     }
+    const uint32_t wpx = __reduce_add_sync(0xffffffffu, span_px);
+    const uint32_t wpa = __reduce_add_sync(0xffffffffu, pairs_alt);
+    if ((threadIdx.x & 31) == 0 && wpx) atomicAdd(&ctr->span_px, (unsigned long long)wpx);
+    if ((threadIdx.x & 31) == 0 && wpa) atomicAdd(&ctr->pairs_alt, wpa);
 }
 
 // ------------------------------------------------------- merged masks --
@@ -1063,6 +1071,26 @@ __global__ void k_bin_scatter(FrameArgs a, const int4 *__restrict__ draw, const 
         base = __shfl_sync(0xffffffffu, base, leader);
         if (act) pval[bin_off[bin] + base + __popc(peers & ((1u << lane) - 1u))] = (uint32_t)i;
     }
+}
+
+// Pairs of every bin counted again from the draw list (a sized frame that
+// changes its resolve tile after the scan-mark pass counted them).
+__global__ void k_bin_count(FrameArgs a, const int4 *__restrict__ draw, const uint32_t *__restrict__ item_scene,
+                            const FrameCounters *__restrict__ ctr, uint32_t *__restrict__ bin_count) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ctr->status != 0u || i >= (int64_t)ctr->n_items) return;
+    const int4 it = draw[i];
+    int W = a.W, H = a.H;
+    uint32_t bin0 = 0;
+    if (item_scene != nullptr) {
+        const SceneInfo *sc = a.scenes + item_scene[i];
+        W = sc->W;
+        H = sc->H;
+        bin0 = sc->bin_off;
+    }
+    uint32_t b0 = 0;
+    const int nb = item_bins(it, W, H, a.bin_shift, bin0, &b0);
+    for (int t = 0; t < nb; ++t) atomicAdd(bin_count + b0 + t, 1u);
 }
 
 // One warp per bin: its item indices sorted ascending by a bitonic network
@@ -1920,6 +1948,13 @@ int launch_bin_scatter(const FrameArgs &a, const int4 *draw, const uint32_t *ite
                        cudaStream_t s) {
     if (cap_items <= 0) return 0;
     k_bin_scatter<<<grid_for(cap_items), kThreads, 0, s>>>(a, draw, item_scene, ctr, bin_off, bin_fill, pval);
+    return 1;
+}
+
+int launch_bin_count(const FrameArgs &a, const int4 *draw, const uint32_t *item_scene, int64_t cap_items,
+                     const FrameCounters *ctr, uint32_t *bin_count, cudaStream_t s) {
+    if (cap_items <= 0) return 0;
+    k_bin_count<<<grid_for(cap_items), kThreads, 0, s>>>(a, draw, item_scene, ctr, bin_count);
     return 1;
 }
 

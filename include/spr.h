@@ -195,7 +195,9 @@ int spr_set_gradients(spr_handle *h, const uint32_t *table, uint32_t n_entries, 
  * cells: one per lane of the warp that resolves the tile).  -1 / 0 select
  * the built-in rule (segment sort for frames of at least 1,024 paths
  * averaging at most 2,048 entries; emission order from 4,096 curves; 4
- * blocks per SM; tiles of 16 columns by 4 cell rows).  Differentiable
+ * blocks per SM; tiles of 16 x 4 cells when the spans of the handle's last
+ * sized frame covered at most 8 pixels per draw item, else 64 x 1: narrow
+ * tiles cut long spans into many more resolve pairs).  Differentiable
  * frames use 64 x 1 tiles.  spr_autotune times `frames` frames of the
  * handle's scene under each choice, one choice at a time with the others at
  * their best so far, keeps the fastest (built-in rules on ties) and reports

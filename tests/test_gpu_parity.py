@@ -419,7 +419,7 @@ def test_tuning_changes_speed_not_results():
             assert np.array_equal(r.read_image(), ref), bw
         t = r.autotune(frames=2)
         assert t["sort"] in (-1, 0, 1) and t["emit_order"] in (-1, 0, 1) and t["resolve_bps"] in (0, 2, 3)
-        assert t["bin_width"] in (0, 64, 32, 8)
+        assert t["bin_width"] in (0, 64, 32, 16, 8)
         assert 0 < t["frame_ms"] <= t["default_ms"]
         r.rasterize()
         assert np.array_equal(r.read_image(), ref)
@@ -432,7 +432,7 @@ def test_tuning_changes_speed_not_results():
 @pytest.mark.parametrize("bin_width", [64, 32, 16, 8])
 @pytest.mark.parametrize("samples,ms,srgb", [(8, True, True), (32, True, False), (16, False, True), (256, True, True)])
 def test_resolve_tiles(bin_width, samples, ms, srgb):
-    """Resolve tiles of 64 x 1, 32 x 2, 16 x 4 (the default) and 8 x 8 cells
+    """Resolve tiles of 64 x 1, 32 x 2, 16 x 4 and 8 x 8 cells
     (tile width x band height): the image exact against the oracle on an
     odd-sized viewport (partial tiles and bands at the right and bottom
     edges)."""
@@ -553,3 +553,19 @@ def test_high_winding_numbers(copies, reverse_every, samples):
     300 fragments in one cell): the bit-sliced counters and the packed 8-bit
     counters they fall back to, exact against the oracle."""
     check_parity(stacked_contours(copies, reverse_every), 150, 80, samples=samples)
+
+
+def test_built_in_tile_follows_span_lengths():
+    """The built-in resolve tile: 16 x 4 cells for scenes of short spans
+    (glyph-like paths), 64 x 1 for long spans (large paths), chosen by the
+    sized first frame (which bins again if its tile was the other one):
+    later frames read nothing back, and the images stay exact."""
+    small = spr.Scene.generate(spr.SCENE_MIXED, seed=29, width=256, height=256, n_paths=400)
+    large = spr.Scene.generate(spr.SCENE_CUBICS, seed=30, width=256, height=256, n_paths=12, seg_min=16, seg_max=32)
+    for sc in (small, large):
+        ref = oracle.run(sc, 256, 256, samples=8)
+        with render(sc, 256, 256, 8) as r:
+            for _ in range(3):
+                r.rasterize()
+                assert r.frame_stats()["host_syncs"] == 0  # (the first frame chose the tile)
+                assert np.array_equal(r.read_image().reshape(-1), ref["IMAGE"])
