@@ -969,7 +969,7 @@ int render_frame(spr_handle *h, void *stream, const DiffCall *dc) {
                         h->wn_scan.as<int8_t>(), h->heads.as<uint32_t>(), h->merged.as<uint32_t>(), h->lb_spin_cap,
                         s);
     rec(h, 6, s);
-    // stage 15: draw items binned by (cell row, 64-column tile): bin offsets
+    // stage 15: draw items binned by resolve tile (a band of cell rows x columns): bin offsets
     // from the counts, then the items placed and sorted per bin; resolve
     cudaMemsetAsync(h->lb_pair.p, 0, 8 * (size_t)lookback_words(nbins), s);
     L += scan_lookback_u32(bin_count, bin_off, nullptr, nbins, h->lb_pair.as<uint64_t>(), &ctr->tiles[2],

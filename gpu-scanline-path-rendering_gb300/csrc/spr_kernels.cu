@@ -5,10 +5,11 @@
 //   k_make_intersection_0 + escan (ras_cut.h:1254)   -> k_curve_count + scan
 //   k_make_intersection_1 (ras_cut.h:1484)           -> k_curve_emit
 //   k_gen_fragment_and_stencil_mask (cu:112-441)     -> k_fragment
-//   cuda_seg_sort_int_by_int (cuda_sort.cu:12)       -> radix_sort (spr_sort.cu)
-//   k_shuffleFragments + int8 scan (cu:444, 1099)    -> k_wn_reduce / k_wn_down
-//   k_mark_merged_fragment_and_span + scans +
-//   k_gen_gl_merged_fragment_and_span (cu:462-868)   -> k_flags_reduce / k_flags_down
+//   cuda_seg_sort_int_by_int (cuda_sort.cu:12)       -> k_segment_sort(_small), radix_sort
+//                                                       (spr_sort.cu)
+//   k_shuffleFragments + int8 scan (cu:444, 1099),
+//   k_mark_merged_fragment_and_span + scans,
+//   k_gen_gl_merged_fragment_and_span (cu:444-868)   -> k_scan_mark (one look-back pass)
 //   k_gen_stencil_cuda_sm + block boundary (cu:554)  -> k_stencil
 //   OpenGL draw + multisample resolve (cu:1312-1433) -> bin counts (k_scan_mark),
 //                                                       k_scan_lb, k_bin_scatter,
