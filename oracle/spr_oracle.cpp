@@ -1912,7 +1912,7 @@ extern "C" int orc_diff(const spr_scene_view *scene, const orc_config *cfgp, con
 }
 
 // ------------------------------------ FP64 check of the crossing points --
-// For the benchmark spec's accuracy report: how far the FP32 crossing points of
+// For the benchmark's accuracy report: how far the FP32 crossing points of
 // the intersection entries (k_make_intersection_impl_1, ras_cut.h:837-1241,
 // as emitted above) lie from the exact crossings of the same curves with the
 // same cut lines.  The curves are the FP32 transformed vertices; the exact
