@@ -8,7 +8,6 @@ import numpy as np
 import pytest
 
 
-
 def packed(w0, frags, fill_rule):
     """Merged mask word of one mask word position: frags = [(chg, mask)]."""
     init = (0x01010101 * (w0 & 0xFFFFFFFF)) & 0xFFFFFFFF
