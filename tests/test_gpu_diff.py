@@ -376,3 +376,37 @@ def test_open_contours_against_reference_gradient():
     ref_img, ref = oracle.diff(sc, W, H, fill, grad_image=G, samples=16)
     assert np.abs(img - ref_img).max() < 1e-5
     assert rel(gf, ref["fill"]) < REL_TOL and rel(gv, ref["vertex"]) < REL_TOL
+
+
+def test_batch_plain_and_differentiable_frames_alternate():
+    """A batch of glyph-like scenes rendered plain (the built-in resolve tile
+    of short spans), then differentiable (64 x 1 tiles), then plain again:
+    the scene table follows each frame's tile, the plain images equal the
+    single-scene renders both times and the differentiable image equals the
+    single-scene one."""
+    sizes = [(256, 256), (192, 160)]
+    scenes = [spr.Scene.generate(spr.SCENE_MIXED, seed=400 + i, width=W, height=H, n_paths=300)
+              for i, (W, H) in enumerate(sizes)]
+    items = [(sc, W, H, 16) for sc, (W, H) in zip(scenes, sizes)]
+    fills_all = [fills(sc.n_paths, 40 + i) for i, sc in enumerate(scenes)]
+    with spr.Batch() as b:
+        b.set_scenes(items)
+        b.render()
+        first = [b.read_image(i).copy() for i in range(len(items))]
+        off = b.image_offsets()
+        f = torch.tensor(np.concatenate(fills_all), device="cuda")
+        img = torch.empty((int(off[-1]), 4), device="cuda")
+        b.diff_render(f.data_ptr(), img.data_ptr())
+        torch.cuda.synchronize()
+        dimg = img.cpu().numpy()
+        b.render()
+        again = [b.read_image(i).copy() for i in range(len(items))]
+    for i, (sc, (W, H)) in enumerate(zip(scenes, sizes)):
+        with spr.VGRasterizer(W, H, samples=16) as r:
+            r.add_vg(sc)
+            r.rasterize()
+            single = r.read_image()
+        assert np.array_equal(first[i], single), i
+        assert np.array_equal(again[i], single), i
+        si = gpu_diff(sc, W, H, fills_all[i], np.zeros((H, W, 4), np.float32), 16)[0]
+        assert np.abs(dimg[off[i]:off[i + 1]].reshape(H, W, 4) - si).max() < 1e-6
